@@ -1,0 +1,213 @@
+/*
+ * nuto_gpu.h — C ABI of the GB300 (sm_103a) element-assembly path for NuTo.
+ *
+ * One context (nuto_gpu_ctx) holds one cell group on one GPU: the coordinate elements of a CellStorage, the
+ * DOF types with their numbering, the Dirichlet constraints, the integrand and its history, the CSR pattern of
+ * the global tangent and the solver workspace. Every call is stream-ordered on the context's stream; pointers
+ * named d_* are device pointers owned by the caller, all others are host pointers borrowed for the duration of
+ * the call. A context is externally synchronised (one host thread at a time). Every function returns a status
+ * code; NUTO_GPU_OK is 0 and nuto_gpu_last_error() gives the message of the last failure. No C++ exception
+ * crosses this boundary.
+ *
+ * Reference interfaces replaced (paths relative to the NuTo project root):
+ *   nuto_gpu_set_cells          CellStorage::AddCells                    nuto/mechanics/tools/CellStorage.cpp:6-16
+ *                               IntegrationTypeTensorProduct<D>(n, GAUSS) nuto/mechanics/integrationtypes/IntegrationTypeTensorProduct.cpp:15-39
+ *   nuto_gpu_add_dof_type       ElementFem::GetDofNumbering              nuto/mechanics/elements/ElementFem.h:58-70
+ *                               DofNumbering::Build / DofInfo            nuto/mechanics/dofs/DofNumbering.cpp:32-58
+ *   nuto_gpu_set_dirichlet      Constraint::Component + RhsRamp          nuto/mechanics/constraints/ConstraintCompanion.cpp:12-53
+ *                               Constraints::GetSparseGlobalRhs          nuto/mechanics/constraints/Constraints.cpp:37-50
+ *   nuto_gpu_build_pattern      pattern of SimpleAssembler::BuildMatrix + ToEigen
+ *                                                                        nuto/mechanics/cell/SimpleAssembler.cpp:100-156
+ *                                                                        nuto/mechanics/dofs/DofMatrixSparseConvertEigen.h:40-67
+ *   nuto_gpu_set_integrand      MomentumBalance<D> + LinearElastic<D>     nuto/mechanics/integrands/MomentumBalance.h:14-53
+ *                               MomentumBalance<D> + LocalIsotropicDamage nuto/mechanics/constitutive/LocalIsotropicDamage.h:33-143
+ *                               GradientDamage<D, Constant|Decreasing>   nuto/mechanics/integrands/GradientDamage.h:25-186
+ *   nuto_gpu_set_history        GradientDamage::mKappas / EvolutionImplicit::mKappas (public members)
+ *   nuto_gpu_build_vector       SimpleAssembler::BuildVector(cells, dofs, Bind(integrand, &Gradient))
+ *                                                                        nuto/mechanics/cell/SimpleAssembler.cpp:38-65
+ *   nuto_gpu_build_matrix       SimpleAssembler::BuildMatrix(cells, dofs, Bind(integrand, &Hessian0)) + ToEigen
+ *                                                                        nuto/mechanics/cell/SimpleAssembler.cpp:100-156
+ *   nuto_gpu_update_history     TimeDependentProblem::UpdateHistory      nuto/mechanics/tools/TimeDependentProblem.cpp:78-85
+ *   nuto_gpu_assemble_cell_vectors / _matrices
+ *                               the scatter half of SimpleAssembler::BuildVector/BuildMatrix for caller-given cell
+ *                               results (any CellInterface::VectorFunction/MatrixFunction)
+ *   nuto_gpu_solve              Solve (C^T K C u = C^T f) + EigenSparseSolve nuto/mechanics/solver/Solve.cpp:8-34,
+ *                                                                        nuto/math/EigenSparseSolve.cpp:22-73
+ *   nuto_gpu_do_step            QuasistaticSolver::DoStep (trial state, NewtonRaphson::Solve with LineSearch,
+ *                               UpdateHistory)                           nuto/mechanics/tools/QuasistaticSolver.cpp:51-147,
+ *                                                                        nuto/math/NewtonRaphson.h:62-94, nuto/math/LineSearch.h:38-63
+ *   nuto_gpu_do_step_host       the same with the state vector and history in host memory (NuTo keeps mX on the host)
+ */
+#ifndef NUTO_GPU_H
+#define NUTO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define NUTO_GPU_OK 0
+#define NUTO_GPU_EINVAL 1   /* invalid argument or unsupported combination */
+#define NUTO_GPU_ENOMEM 2   /* device allocation failed */
+#define NUTO_GPU_ENOCONV 3  /* Newton or Krylov did not converge (NewtonRaphson::NoConvergence) */
+#define NUTO_GPU_ENAN 4     /* NaN/Inf in a residual or a Krylov scalar */
+#define NUTO_GPU_ETIMEOUT 5 /* a bounded device wait gave up */
+#define NUTO_GPU_ECUDA 6    /* CUDA runtime error */
+#define NUTO_GPU_ESTATE 7   /* call out of order (e.g. build_matrix before build_pattern) */
+
+/* interpolations: InterpolationQuadLinear, InterpolationBrickLinear, InterpolationBrickQuadratic */
+#define NUTO_GPU_QUAD4 0
+#define NUTO_GPU_HEX8 1
+#define NUTO_GPU_HEX20 2
+
+/* integrands */
+#define NUTO_GPU_MB_LINEAR_ELASTIC 0 /* MomentumBalance<D> with LinearElastic<D> */
+#define NUTO_GPU_MB_LOCAL_DAMAGE 1   /* MomentumBalance<D> with LocalIsotropicDamage<D> (EvolutionImplicit) */
+#define NUTO_GPU_GRADIENT_DAMAGE 2   /* GradientDamage<D, interaction, DamageLawExponential> */
+
+#define NUTO_GPU_PLANE_STRESS 0
+#define NUTO_GPU_PLANE_STRAIN 1
+#define NUTO_GPU_DAMAGE_FULL 0
+#define NUTO_GPU_DAMAGE_UNILATERAL 1
+#define NUTO_GPU_INTERACTION_CONSTANT 0
+#define NUTO_GPU_INTERACTION_DECREASING 1
+
+/* arithmetic of the tangent values and of the Krylov iteration */
+#define NUTO_GPU_FP32 32
+#define NUTO_GPU_FP64 64
+
+/* Krylov methods */
+#define NUTO_GPU_SOLVER_AUTO 0     /* PCG for the symmetric integrands, BiCGStab otherwise */
+#define NUTO_GPU_SOLVER_PCG 1      /* Jacobi-preconditioned CG */
+#define NUTO_GPU_SOLVER_BICGSTAB 2 /* Jacobi-preconditioned BiCGStab */
+
+typedef struct nuto_gpu_ctx nuto_gpu_ctx;
+
+/* Integrand and law parameters. The plane state applies to every 2D law of the integrand. */
+typedef struct nuto_gpu_integrand
+{
+    int kind;               /* NUTO_GPU_MB_LINEAR_ELASTIC | NUTO_GPU_MB_LOCAL_DAMAGE | NUTO_GPU_GRADIENT_DAMAGE */
+    int dim;                /* 2 or 3 */
+    double E, nu;           /* LinearElastic / LinearElasticDamage */
+    int plane_state;        /* NUTO_GPU_PLANE_STRESS | NUTO_GPU_PLANE_STRAIN */
+    int damage_application; /* NUTO_GPU_DAMAGE_FULL | NUTO_GPU_DAMAGE_UNILATERAL */
+    double kappa0, beta, alpha; /* DamageLawExponential(kappa0, beta, alpha) */
+    double k;               /* ModifiedMisesStrainNorm(nu, k) */
+    double c;               /* GradientDamage nonlocal parameter */
+    int interaction;        /* NUTO_GPU_INTERACTION_CONSTANT | NUTO_GPU_INTERACTION_DECREASING */
+    double R, eta;          /* NonlocalInteraction::Decreasing(R, eta) */
+    int disp_slot;          /* DOF slot of the displacements */
+    int eeq_slot;           /* DOF slot of the nonlocal equivalent strains (GRADIENT_DAMAGE only), else -1 */
+} nuto_gpu_integrand;
+
+/* Newton / Krylov options of nuto_gpu_do_step */
+typedef struct nuto_gpu_step_options
+{
+    int precision;      /* NUTO_GPU_FP32: FP32 tangent + FP32 Krylov, FP64 residual and refinement;
+                           NUTO_GPU_FP64: everything FP64 */
+    int method;         /* NUTO_GPU_SOLVER_* */
+    double newton_rtol; /* converged when |C^T r| <= max(newton_atol, newton_rtol * |C^T (r + K db)|_trial) */
+    double newton_atol;
+    int max_newton;     /* NewtonRaphson::Solve maxIterations (the reference uses 6) */
+    int line_search;    /* 1: NuTo::NewtonRaphson::LineSearch (6 halvings), 0: plain Newton */
+    double krylov_rtol; /* inner Krylov tolerance relative to |rhs| */
+    int max_krylov;
+} nuto_gpu_step_options;
+
+/* statistics of the last nuto_gpu_do_step / nuto_gpu_solve */
+typedef struct nuto_gpu_stats
+{
+    int newton_iterations;
+    int krylov_iterations;   /* summed over the step */
+    int residual_evaluations;
+    int matrix_assemblies;
+    double final_residual;   /* |C^T r| at exit */
+    double reference_residual;
+    double ms_assemble_matrix;
+    double ms_assemble_vector;
+    double ms_krylov;
+    double ms_total;
+} nuto_gpu_stats;
+
+/* ---- context ----------------------------------------------------------------------------------------- */
+int nuto_gpu_create(nuto_gpu_ctx** ctx, int device, void* cuda_stream /* cudaStream_t or NULL */);
+int nuto_gpu_destroy(nuto_gpu_ctx* ctx);
+const char* nuto_gpu_last_error(const nuto_gpu_ctx* ctx);
+int nuto_gpu_synchronize(nuto_gpu_ctx* ctx);
+int nuto_gpu_version(void);
+
+/* ---- cells, DOF types, constraints --------------------------------------------------------------------- */
+/* Coordinate elements of the cells, cell id = row of coord_conn (CellStorage::AddCells). coords are
+   n_coord_nodes x dim, coord_conn is n_cells x nodes-per-element (local node order of the interpolation). */
+int nuto_gpu_set_cells(nuto_gpu_ctx* ctx, int dim, int geo_interp, int64_t n_coord_nodes, const double* coords,
+                       int64_t n_cells, const int32_t* coord_conn, int gauss_points_per_direction);
+
+/* A DOF type. dof_conn is n_cells x nodes-per-element of DOF-node ids, dof_numbers is n_dof_nodes x ncomp and
+   holds NodeSimple::GetDofNumber(component) (components of a node must be consecutive numbers, which
+   DofNumbering::Build guarantees). n_independent + n_dependent = n_dof_nodes * ncomp. The slot index returned
+   is the position in the combined (ToEigen) order. */
+int nuto_gpu_add_dof_type(nuto_gpu_ctx* ctx, int ncomp, int interp, int64_t n_dof_nodes, const int32_t* dof_conn,
+                          const int32_t* dof_numbers, int64_t n_independent, int64_t n_dependent, int* slot);
+
+/* Dirichlet (unit) constraints of one slot: dependent DOF numbers with rhs(t) = rhs_const + rhs_slope * t
+   (RhsConstant / RhsRamp); the value is rounded through float like Constraints::GetSparseGlobalRhs. */
+int nuto_gpu_set_dirichlet(nuto_gpu_ctx* ctx, int slot, int64_t n_equations, const int32_t* dependent_dofs,
+                           const double* rhs_const, const double* rhs_slope);
+
+/* Builds the CSR pattern of the combined matrix and the cell-to-CSR maps. Outputs the combined size and nnz. */
+int nuto_gpu_build_pattern(nuto_gpu_ctx* ctx, int64_t* n_dofs, int64_t* nnz);
+/* Copies the pattern to host arrays (row_ptr: n_dofs + 1, col_idx: nnz). The pattern is structurally
+   symmetric, so these are also the column pointers / row indices of NuTo's column-major matrix. */
+int nuto_gpu_copy_pattern(nuto_gpu_ctx* ctx, int64_t* row_ptr, int32_t* col_idx);
+/* Device pointers of the pattern (valid until the context is destroyed). */
+int nuto_gpu_pattern_device(nuto_gpu_ctx* ctx, const int64_t** d_row_ptr, const int32_t** d_col_idx);
+
+int nuto_gpu_set_integrand(nuto_gpu_ctx* ctx, const nuto_gpu_integrand* params);
+int nuto_gpu_num_integration_points(const nuto_gpu_ctx* ctx);
+/* history kappa: n_cells x n_ip doubles (host pointers) */
+int nuto_gpu_set_history(nuto_gpu_ctx* ctx, const double* kappa);
+int nuto_gpu_get_history(nuto_gpu_ctx* ctx, double* kappa);
+
+/* ---- hot path: device pointers, stream-ordered ---------------------------------------------------------- */
+/* f = sum over cells of the integrand's Gradient (combined layout, all DOFs incl. dependent ones) */
+int nuto_gpu_build_vector(nuto_gpu_ctx* ctx, const double* d_u, double* d_f);
+/* CSR values of sum over cells of the integrand's Hessian0; d_values is nnz floats (FP32) or doubles (FP64) */
+int nuto_gpu_build_matrix(nuto_gpu_ctx* ctx, const double* d_u, int precision, void* d_values);
+/* kappa <- max(kappa, kappa(u)) at every integration point */
+int nuto_gpu_update_history(nuto_gpu_ctx* ctx, const double* d_u);
+/* scatter of caller-given cell vectors (n_cells x n_local doubles, slot-major, node, component) */
+int nuto_gpu_assemble_cell_vectors(nuto_gpu_ctx* ctx, const double* d_cell_vectors, double* d_f);
+/* scatter of caller-given cell matrices (n_cells x n_local x n_local doubles, row-major) into CSR values */
+int nuto_gpu_assemble_cell_matrices(nuto_gpu_ctx* ctx, const double* d_cell_matrices, int precision,
+                                    void* d_values);
+
+/* Solves C^T K C y = C^T b for the constrained system of the CSR values d_values (Dirichlet C: the constrained
+   rows and columns are eliminated) and writes x = C y (zero at dependent DOFs). */
+int nuto_gpu_solve(nuto_gpu_ctx* ctx, int precision, int method, const void* d_values, const double* d_b,
+                   double* d_x, double rtol, int max_iterations, int* iterations, double* relative_residual);
+
+/* ---- quasistatic driver ------------------------------------------------------------------------------ */
+int nuto_gpu_default_step_options(nuto_gpu_step_options* opts);
+/* state x (combined layout, host) and the global time; resets the history to zero when reset_history != 0 */
+int nuto_gpu_set_state(nuto_gpu_ctx* ctx, const double* x, double global_time, int reset_history);
+int nuto_gpu_get_state(nuto_gpu_ctx* ctx, double* x, double* global_time);
+/* Device pointer of the resident state vector (n_dofs doubles). */
+int nuto_gpu_state_device(nuto_gpu_ctx* ctx, double** d_x);
+/* QuasistaticSolver::DoStep(newGlobalTime) on the resident state; on success the state and history advance
+   and *newton_iterations holds the iteration count. NUTO_GPU_ENOCONV leaves state and history unchanged. */
+int nuto_gpu_do_step(nuto_gpu_ctx* ctx, double new_global_time, const nuto_gpu_step_options* opts,
+                     int* newton_iterations);
+/* The same with host buffers: x_in/kappa_in are uploaded, the step runs, x_out/kappa_out are downloaded
+   (kappa pointers may be NULL to keep the resident history). */
+int nuto_gpu_do_step_host(nuto_gpu_ctx* ctx, double new_global_time, const nuto_gpu_step_options* opts,
+                          const double* x_in, const double* kappa_in, double* x_out, double* kappa_out,
+                          int* newton_iterations);
+int nuto_gpu_get_stats(const nuto_gpu_ctx* ctx, nuto_gpu_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NUTO_GPU_H */

@@ -1,0 +1,212 @@
+"""Python face of the GB300 path: one cell group on one GPU behind the C ABI.
+
+`GpuCellGroup` plays the roles of NuTo's CellStorage + SimpleAssembler + QuasistaticSolver for the supported
+integrands (see include/nuto_gpu.h for the reference interface each call replaces). Device buffers are torch
+CUDA tensors (plumbing only); all arithmetic runs in the library's CUDA kernels.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (FP32, FP64, GRADIENT_DAMAGE, Integrand, MB_LINEAR_ELASTIC, MB_LOCAL_DAMAGE, Stats, StepOptions,
+                   check, load)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return ctypes.c_void_p(a.ctypes.data)
+    return ctypes.c_void_p(a.data_ptr())
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+class GpuCellGroup:
+    def __init__(self, mesh, layers, gauss_points_per_direction=2, device=0, stream=None, dependent_counts=None):
+        self.L = load()
+        self.mesh = mesh
+        self.device = device
+        h = ctypes.c_void_p()
+        if stream is None:
+            # run on torch's current stream so that tensors produced by torch are ordered before our kernels
+            torch = _torch()
+            stream = torch.cuda.current_stream(device).cuda_stream
+        rc = self.L.nuto_gpu_create(ctypes.byref(h), device, ctypes.c_void_p(stream) if stream else None)
+        if rc != _lib.OK:
+            raise _lib.NutoGpuError(rc, "nuto_gpu_create failed (no CUDA device?)")
+        self.h = h
+        self._call("nuto_gpu_set_cells", mesh.dim, mesh.geo_interp, mesh.coords.shape[0], _ptr(mesh.coords),
+                   mesh.num_cells, _ptr(mesh.conn), gauss_points_per_direction)
+        self.slots = []
+        for k, layer in enumerate(layers):
+            L = mesh.layers[layer]
+            dep = 0 if dependent_counts is None else int(dependent_counts[k])
+            slot = ctypes.c_int()
+            dn = np.ascontiguousarray(L.dof_numbers, dtype=np.int32)
+            self._call("nuto_gpu_add_dof_type", L.ncomp, L.interp, L.num_nodes, _ptr(L.conn), _ptr(dn),
+                       L.num_dofs - dep, dep, ctypes.byref(slot))
+            self.slots.append(slot.value)
+        self.layers = list(layers)
+        self.n_dofs = None
+        self.nnz = None
+        self.n_ip = None
+        self.kind = None
+
+    def _call(self, name, *args):
+        check(self.h, getattr(self.L, name)(self.h, *args))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.nuto_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- set-up --------------------------------------------------------------------------------------------
+    def set_dirichlet(self, slot, dofs, rhs_const=None, rhs_slope=None):
+        dofs = np.ascontiguousarray(dofs, dtype=np.int32)
+        a = None if rhs_const is None else np.ascontiguousarray(rhs_const, dtype=np.float64)
+        b = None if rhs_slope is None else np.ascontiguousarray(rhs_slope, dtype=np.float64)
+        self._call("nuto_gpu_set_dirichlet", slot, dofs.size, _ptr(dofs), _ptr(a), _ptr(b))
+
+    def build_pattern(self):
+        n = ctypes.c_int64()
+        nnz = ctypes.c_int64()
+        self._call("nuto_gpu_build_pattern", ctypes.byref(n), ctypes.byref(nnz))
+        self.n_dofs, self.nnz = n.value, nnz.value
+        return self.n_dofs, self.nnz
+
+    def pattern(self):
+        rp = np.empty(self.n_dofs + 1, dtype=np.int64)
+        ci = np.empty(self.nnz, dtype=np.int32)
+        self._call("nuto_gpu_copy_pattern", _ptr(rp), _ptr(ci))
+        return rp, ci
+
+    def set_integrand(self, kind, dim, E=30000.0, nu=0.2, plane_state=_lib.PLANE_STRAIN,
+                      damage_application=_lib.DAMAGE_FULL, kappa0=1e-4, beta=100.0, alpha=0.99, k=10.0, c=0.01,
+                      interaction=_lib.INTERACTION_CONSTANT, R=0.005, eta=5.0, disp_slot=0, eeq_slot=-1):
+        p = Integrand(kind, dim, E, nu, plane_state, damage_application, kappa0, beta, alpha, k, c, interaction, R,
+                      eta, disp_slot, eeq_slot)
+        self._call("nuto_gpu_set_integrand", ctypes.byref(p))
+        self.kind = kind
+        self.n_ip = self.L.nuto_gpu_num_integration_points(self.h)
+
+    @property
+    def history(self):
+        out = np.empty((self.mesh.num_cells, self.n_ip))
+        self._call("nuto_gpu_get_history", _ptr(out))
+        return out
+
+    @history.setter
+    def history(self, kappa):
+        k = np.ascontiguousarray(np.broadcast_to(kappa, (self.mesh.num_cells, self.n_ip)), dtype=np.float64)
+        self._call("nuto_gpu_set_history", _ptr(k))
+
+    # ---- hot path (device tensors) ---------------------------------------------------------------------------
+    def _dev(self, x, dtype):
+        torch = _torch()
+        t = torch.as_tensor(x, dtype=dtype, device="cuda:%d" % self.device)
+        return t.contiguous()
+
+    def build_vector(self, u, out=None):
+        torch = _torch()
+        u = self._dev(u, torch.float64)
+        f = out if out is not None else torch.empty(self.n_dofs, dtype=torch.float64, device=u.device)
+        self._call("nuto_gpu_build_vector", _ptr(u), _ptr(f))
+        return f
+
+    def build_matrix(self, u, precision=FP64, out=None):
+        torch = _torch()
+        u = self._dev(u, torch.float64)
+        dt = torch.float32 if precision == FP32 else torch.float64
+        v = out if out is not None else torch.empty(self.nnz, dtype=dt, device=u.device)
+        self._call("nuto_gpu_build_matrix", _ptr(u), precision, _ptr(v))
+        return v
+
+    def update_history(self, u):
+        torch = _torch()
+        u = self._dev(u, torch.float64)
+        self._call("nuto_gpu_update_history", _ptr(u))
+
+    def assemble_cell_vectors(self, fe):
+        torch = _torch()
+        fe = self._dev(fe, torch.float64)
+        f = torch.empty(self.n_dofs, dtype=torch.float64, device=fe.device)
+        self._call("nuto_gpu_assemble_cell_vectors", _ptr(fe), _ptr(f))
+        return f
+
+    def assemble_cell_matrices(self, ke, precision=FP64):
+        torch = _torch()
+        ke = self._dev(ke, torch.float64)
+        dt = torch.float32 if precision == FP32 else torch.float64
+        v = torch.empty(self.nnz, dtype=dt, device=ke.device)
+        self._call("nuto_gpu_assemble_cell_matrices", _ptr(ke), precision, _ptr(v))
+        return v
+
+    def solve(self, values, b, precision=FP64, method=_lib.SOLVER_AUTO, rtol=1e-10, max_iterations=100000):
+        torch = _torch()
+        b = self._dev(b, torch.float64)
+        x = torch.empty_like(b)
+        it = ctypes.c_int()
+        rel = ctypes.c_double()
+        rc = self.L.nuto_gpu_solve(self.h, precision, method, _ptr(values), _ptr(b), _ptr(x), rtol, max_iterations,
+                                   ctypes.byref(it), ctypes.byref(rel))
+        if rc not in (_lib.OK, _lib.ENOCONV):
+            check(self.h, rc)
+        return x, it.value, rel.value, rc == _lib.OK
+
+    # ---- quasistatic driver --------------------------------------------------------------------------------
+    @staticmethod
+    def default_options(**kw):
+        o = StepOptions()
+        load().nuto_gpu_default_step_options(ctypes.byref(o))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+    def set_state(self, x=None, time=0.0, reset_history=True):
+        xa = None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        self._call("nuto_gpu_set_state", _ptr(xa), float(time), int(bool(reset_history)))
+
+    def get_state(self):
+        x = np.empty(self.n_dofs)
+        t = ctypes.c_double()
+        self._call("nuto_gpu_get_state", _ptr(x), ctypes.byref(t))
+        return x, t.value
+
+    def state_device(self):
+        p = ctypes.c_void_p()
+        self._call("nuto_gpu_state_device", ctypes.byref(p))
+        return p.value
+
+    def do_step(self, t_new, options=None):
+        o = options if options is not None else self.default_options()
+        it = ctypes.c_int()
+        self._call("nuto_gpu_do_step", float(t_new), ctypes.byref(o), ctypes.byref(it))
+        return it.value
+
+    def do_step_host(self, t_new, x_in, kappa_in, x_out, kappa_out, options=None):
+        o = options if options is not None else self.default_options()
+        it = ctypes.c_int()
+        self._call("nuto_gpu_do_step_host", float(t_new), ctypes.byref(o), _ptr(x_in), _ptr(kappa_in), _ptr(x_out),
+                   _ptr(kappa_out), ctypes.byref(it))
+        return it.value
+
+    def stats(self):
+        s = Stats()
+        check(self.h, self.L.nuto_gpu_get_stats(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def synchronize(self):
+        self._call("nuto_gpu_synchronize")

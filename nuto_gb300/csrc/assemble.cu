@@ -1,0 +1,892 @@
+// Element kernels of the GB300 assembly path: integration-point geometry cache, FP64 internal-force residual,
+// FP32/FP64 tangent scattered into CSR through the rank maps, history update, and the scatter of caller-given
+// cell vectors/matrices.
+//
+// Work decomposition (all kernels): a CTA owns CPB consecutive cells and runs in phases separated by
+// __syncthreads(): (0) gather the cells' DOF values into shared memory, (A) one thread per (cell, integration
+// point) evaluates strain, law and integrand data, (B) one thread per (cell, node) or (cell, node pair)
+// integrates over the points and scatters. Geometry (w * det J and dN/dX per integration point) is computed once
+// per mesh and cached planar ([field][cell]) so that every per-cell load is coalesced.
+#include "internal.cuh"
+
+#include <algorithm>
+
+namespace nuto_gpu
+{
+
+template <int DIM, int NG, int ND, int NIP, int KIND>
+struct Cfg
+{
+    static constexpr int dim = DIM, ng = NG, nd = ND, nip = NIP, kind = KIND;
+};
+
+// Calls f(Cfg<...>{}) for the context's configuration (cell dimension, coordinate and displacement
+// interpolation, integration points, integrand kind).
+template <typename F>
+static void DispatchCfg(const Ctx& c, F&& f)
+{
+    const int nd = c.slots[c.prm.disp_slot].nen;
+    const int nip = c.ip.nIp;
+    const int kind = c.prm.kind;
+#define NG_CASE(D, G, N, Q, K)                                                                                   \
+    if (c.dim == D && c.nge == G && nd == N && nip == Q && kind == K)                                            \
+    {                                                                                                            \
+        f(Cfg<D, G, N, Q, K>{});                                                                                 \
+        return;                                                                                                  \
+    }
+#define NG_KINDS3(D, G, N, Q) NG_CASE(D, G, N, Q, 0) NG_CASE(D, G, N, Q, 1) NG_CASE(D, G, N, Q, 2)
+#define NG_KINDS2(D, G, N, Q) NG_CASE(D, G, N, Q, 0) NG_CASE(D, G, N, Q, 1)
+    NG_KINDS3(2, 4, 4, 4)
+    NG_KINDS3(2, 4, 4, 9)
+    NG_KINDS3(3, 8, 8, 8)
+    NG_KINDS3(3, 8, 8, 27)
+    NG_KINDS2(3, 8, 20, 8)
+    NG_KINDS2(3, 8, 20, 27)
+#undef NG_KINDS2
+#undef NG_KINDS3
+#undef NG_CASE
+    throw Error{NUTO_GPU_EINVAL, "unsupported cell configuration (interpolation / integration points / integrand)"};
+}
+
+// ---- small device helpers -------------------------------------------------------------------------------
+
+// Engineering strain from the displacement gradient H[c][d] = sum_n u_nc dN_n/dx_d, Voigt order of
+// Nabla::Strain (DifferentialOperators.h:24-90): 2D xx, yy, xy; 3D xx, yy, zz, yz, zx, xy.
+template <typename T, int DIM>
+__device__ __forceinline__ void StrainFromH(const T (&H)[DIM][DIM], T* e)
+{
+    if (DIM == 2)
+    {
+        e[0] = H[0][0];
+        e[1] = H[1][1];
+        e[2] = H[0][1] + H[1][0];
+    }
+    else
+    {
+        e[0] = H[0][0];
+        e[1] = H[1][1];
+        e[2] = H[2][2];
+        e[3] = H[1][2] + H[2][1];
+        e[4] = H[0][2] + H[2][0];
+        e[5] = H[0][1] + H[1][0];
+    }
+}
+
+// B_n^T s for the node with global gradient g (columns of the Voigt strain operator)
+template <typename T, int DIM>
+__device__ __forceinline__ void BtS(const T* g, const T* s, T* out)
+{
+    if (DIM == 2)
+    {
+        out[0] = g[0] * s[0] + g[1] * s[2];
+        out[1] = g[1] * s[1] + g[0] * s[2];
+    }
+    else
+    {
+        out[0] = g[0] * s[0] + g[2] * s[4] + g[1] * s[5];
+        out[1] = g[1] * s[1] + g[2] * s[3] + g[0] * s[5];
+        out[2] = g[2] * s[2] + g[1] * s[3] + g[0] * s[4];
+    }
+}
+
+// LinearElastic stress sigma = C eps (LinearElastic.h:21-24, CalculateC :47-121)
+template <typename T, int DIM>
+__device__ __forceinline__ void ElasticStress(const LawParams& L, const T* e, T* s)
+{
+    const T c11 = T(L.C11), c12 = T(L.C12), c33 = T(L.C33);
+    if (DIM == 2)
+    {
+        s[0] = c11 * e[0] + c12 * e[1];
+        s[1] = c12 * e[0] + c11 * e[1];
+        s[2] = c33 * e[2];
+    }
+    else
+    {
+        s[0] = c11 * e[0] + c12 * (e[1] + e[2]);
+        s[1] = c11 * e[1] + c12 * (e[0] + e[2]);
+        s[2] = c11 * e[2] + c12 * (e[0] + e[1]);
+        s[3] = c33 * e[3];
+        s[4] = c33 * e[4];
+        s[5] = c33 * e[5];
+    }
+}
+
+template <int A, int B>
+struct MaxI
+{
+    static constexpr int v = A > B ? A : B;
+};
+
+// ---- integration-point geometry cache (Jacobian.h:16-48, CellIpData.h:108-113) -------------------------------
+template <int DIM, int NG, int ND, int NIP>
+__global__ void __launch_bounds__(128) k_geometry(int64_t nCells, const double* __restrict__ coords,
+                                                  const int32_t* __restrict__ geoConnT,
+                                                  const double* __restrict__ tables, int tabW, int tabDNg,
+                                                  int tabDNd, int stride, double* __restrict__ geo64,
+                                                  float* __restrict__ geo32)
+{
+    const int64_t it = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (it >= nCells * NIP)
+        return;
+    const int64_t e = it % nCells;
+    const int q = static_cast<int>(it / nCells);
+    double X[NG][DIM];
+#pragma unroll
+    for (int n = 0; n < NG; ++n)
+    {
+        const int32_t node = geoConnT[static_cast<int64_t>(n) * nCells + e];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            X[n][d] = coords[static_cast<int64_t>(node) * DIM + d];
+    }
+    const double* dNg = tables + tabDNg + q * NG * 3;
+    double J[DIM][DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int j = 0; j < DIM; ++j)
+        {
+            double s = 0;
+#pragma unroll
+            for (int n = 0; n < NG; ++n)
+                s += X[n][i] * dNg[n * 3 + j];
+            J[i][j] = s;
+        }
+    double det, inv[DIM][DIM];
+    if (DIM == 2)
+    {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        inv[0][0] = J[1][1] / det;
+        inv[0][1] = -J[0][1] / det;
+        inv[1][0] = -J[1][0] / det;
+        inv[1][1] = J[0][0] / det;
+    }
+    else
+    {
+        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c10 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const double c20 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        det = J[0][0] * c00 + J[0][1] * c10 + J[0][2] * c20;
+        const double id = 1. / det;
+        inv[0][0] = c00 * id;
+        inv[1][0] = c10 * id;
+        inv[2][0] = c20 * id;
+        inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+    }
+    const int64_t base = static_cast<int64_t>(q) * stride;
+    const double wdj = tables[tabW + q] * det;
+    geo64[base * nCells + e] = wdj;
+    geo32[base * nCells + e] = static_cast<float>(wdj);
+    const double* dNd = tables + tabDNd + q * ND * 3;
+    for (int n = 0; n < ND; ++n)
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            double s = 0;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j)
+                s += dNd[n * 3 + j] * inv[j][k];
+            const int64_t idx = (base + 1 + n * DIM + k) * nCells + e;
+            geo64[idx] = s;
+            geo32[idx] = static_cast<float>(s);
+        }
+}
+
+void BuildGeometryCache(Ctx& c)
+{
+    const Slot& D = c.slots[c.prm.disp_slot];
+    c.geoStride = 1 + D.nen * c.dim;
+    const size_t total = static_cast<size_t>(c.geoStride) * c.ip.nIp * c.nCells;
+    c.dGeo64.alloc(total);
+    c.dGeo32.alloc(total);
+    const int64_t items = c.nCells * c.ip.nIp;
+    const int blocks = static_cast<int>((items + 127) / 128);
+    DispatchCfg(c, [&](auto cfg) {
+        using C = decltype(cfg);
+        k_geometry<C::dim, C::ng, C::nd, C::nip><<<blocks, 128, 0, c.stream>>>(
+                c.nCells, c.dCoords.p, c.dGeoConnT.p, c.dTables.p, c.tabW, c.tabDN[c.geoInterp], c.tabDN[D.interp],
+                c.geoStride, c.dGeo64.p, c.dGeo32.p);
+    });
+    NG_CUDA(cudaGetLastError());
+    c.haveGeo = true;
+}
+
+static CellArgs MakeCellArgs(Ctx& c)
+{
+    CellArgs a{};
+    const Slot& D = c.slots[c.prm.disp_slot];
+    a.nCells = c.nCells;
+    a.connD = D.dConnT.p;
+    a.gdofD = D.dGdof.p;
+    a.tabN_D = c.dTables.p + c.tabN[D.interp];
+    if (c.prm.kind == NUTO_GPU_GRADIENT_DAMAGE)
+    {
+        const Slot& E = c.slots[c.prm.eeq_slot];
+        a.connE = E.dConnT.p;
+        a.gdofE = E.dGdof.p;
+        a.tabN_E = c.dTables.p + c.tabN[E.interp];
+    }
+    a.geo64 = c.dGeo64.p;
+    a.geo32 = c.dGeo32.p;
+    a.geoStride = c.geoStride;
+    a.kappa = c.dKappa.p;
+    return a;
+}
+
+// ---- FP64 internal-force residual --------------------------------------------------------------------------
+// MomentumBalance::Gradient (MomentumBalance.h:26-35) and GradientDamage::Gradient (GradientDamage.h:70-90)
+// integrated as in Cell::IntegrateGeneric (Cell.h:105-119) and scattered like SimpleAssembler::BuildVector
+// (SimpleAssembler.cpp:38-65); FP64 atomics replace the thread-local vectors.
+template <int DIM, int ND, int NIP, int KIND>
+__global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const double* __restrict__ u,
+                                                  double* __restrict__ f)
+{
+    constexpr int VD = DIM == 2 ? 3 : 6;
+    constexpr bool GD = KIND == NUTO_GPU_GRADIENT_DAMAGE;
+    constexpr int CPB = MaxI<1, 128 / MaxI<NIP, ND>::v>::v;
+    constexpr int REC = VD + (GD ? 1 + DIM : 0);
+    __shared__ double sU[CPB][ND][DIM];
+    __shared__ double sE[GD ? CPB : 1][GD ? ND : 1];
+    __shared__ double sIp[CPB][NIP][REC];
+    const int64_t n = a.nCells;
+    const int64_t cell0 = static_cast<int64_t>(blockIdx.x) * CPB;
+
+    for (int it = threadIdx.x; it < CPB * ND; it += blockDim.x)
+    {
+        const int cl = it % CPB, nd = it / CPB;
+        const int64_t e = cell0 + cl;
+        if (e >= n)
+            continue;
+        const int64_t g = a.gdofD[a.connD[static_cast<int64_t>(nd) * n + e]];
+#pragma unroll
+        for (int c = 0; c < DIM; ++c)
+            sU[cl][nd][c] = u[g + c];
+        if (GD)
+            sE[cl][nd] = u[a.gdofE[a.connE[static_cast<int64_t>(nd) * n + e]]];
+    }
+    __syncthreads();
+
+    for (int it = threadIdx.x; it < CPB * NIP; it += blockDim.x)
+    {
+        const int cl = it % CPB, q = it / CPB;
+        const int64_t e = cell0 + cl;
+        if (e >= n)
+            continue;
+        const double* G = a.geo64 + static_cast<int64_t>(q) * a.geoStride * n + e;
+        const double wdj = G[0];
+        double H[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = 0; j < DIM; ++j)
+                H[i][j] = 0;
+        double eeq = 0, ge[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            ge[d] = 0;
+#pragma unroll
+        for (int nd = 0; nd < ND; ++nd)
+        {
+            double g[DIM];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                g[d] = G[(1 + nd * DIM + d) * n];
+#pragma unroll
+            for (int c = 0; c < DIM; ++c)
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    H[c][d] += sU[cl][nd][c] * g[d];
+            if (GD)
+            {
+                const double ev = sE[cl][nd];
+                eeq += a.tabN_D[q * ND + nd] * ev;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    ge[d] += ev * g[d];
+            }
+        }
+        double eps[VD], sig[VD];
+        StrainFromH<double, DIM>(H, eps);
+        const double kh = a.kappa[e * NIP + q];
+        if (KIND == NUTO_GPU_MB_LINEAR_ELASTIC)
+            ElasticStress<double, DIM>(L, eps, sig);
+        else if (KIND == NUTO_GPU_MB_LOCAL_DAMAGE)
+        {
+            // LocalIsotropicDamage::Stress with EvolutionImplicit::Kappa (LocalIsotropicDamage.h:52-57, 110-113)
+            const double kap = fmax(MisesValue<double, DIM>(L, eps), kh);
+            LedStress<double, DIM>(L, eps, DamageOmega<double>(L, kap), sig);
+        }
+        else
+        {
+            const double kap = fmax(kh, eeq); // GradientDamage::Kappa (GradientDamage.h:127-130)
+            const double omega = DamageOmega<double>(L, kap);
+            LedStress<double, DIM>(L, eps, omega, sig);
+            const double cg = L.c * InteractionFactor<double>(L, omega) * wdj;
+            sIp[cl][q][VD] = (eeq - MisesValue<double, DIM>(L, eps)) * wdj;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                sIp[cl][q][VD + 1 + d] = cg * ge[d];
+        }
+#pragma unroll
+        for (int v = 0; v < VD; ++v)
+            sIp[cl][q][v] = sig[v] * wdj;
+    }
+    __syncthreads();
+
+    for (int it = threadIdx.x; it < CPB * ND; it += blockDim.x)
+    {
+        const int cl = it % CPB, nd = it / CPB;
+        const int64_t e = cell0 + cl;
+        if (e >= n)
+            continue;
+        double fu[DIM], fe = 0;
+#pragma unroll
+        for (int c = 0; c < DIM; ++c)
+            fu[c] = 0;
+#pragma unroll 4
+        for (int q = 0; q < NIP; ++q)
+        {
+            const double* G = a.geo64 + static_cast<int64_t>(q) * a.geoStride * n + e;
+            double g[DIM], b[DIM];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                g[d] = G[(1 + nd * DIM + d) * n];
+            BtS<double, DIM>(g, sIp[cl][q], b);
+#pragma unroll
+            for (int c = 0; c < DIM; ++c)
+                fu[c] += b[c];
+            if (GD)
+            {
+                double s = a.tabN_D[q * ND + nd] * sIp[cl][q][VD];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    s += g[d] * sIp[cl][q][VD + 1 + d];
+                fe += s;
+            }
+        }
+        const int64_t g = a.gdofD[a.connD[static_cast<int64_t>(nd) * n + e]];
+#pragma unroll
+        for (int c = 0; c < DIM; ++c)
+            atomicAdd(f + g + c, fu[c]);
+        if (GD)
+            atomicAdd(f + a.gdofE[a.connE[static_cast<int64_t>(nd) * n + e]], fe);
+    }
+}
+
+void LaunchResidual(Ctx& c, const double* u, double* f)
+{
+    NG_CUDA(cudaMemsetAsync(f, 0, c.nDofs * sizeof(double), c.stream));
+    CellArgs a = MakeCellArgs(c);
+    DispatchCfg(c, [&](auto cfg) {
+        using C = decltype(cfg);
+        constexpr int CPB = MaxI<1, 128 / MaxI<C::nip, C::nd>::v>::v;
+        const int blocks = static_cast<int>((c.nCells + CPB - 1) / CPB);
+        k_residual<C::dim, C::nd, C::nip, C::kind><<<blocks, 128, 0, c.stream>>>(a, c.law, u, f);
+    });
+    NG_CUDA(cudaGetLastError());
+}
+
+// ---- tangent: FP32 or FP64 values scattered into CSR ---------------------------------------------------------
+// MomentumBalance::Hessian0 (MomentumBalance.h:37-46) with LinearElastic / LocalIsotropicDamage::Tangent
+// (LocalIsotropicDamage.h:59-68) and GradientDamage::Hessian0 (GradientDamage.h:92-120). The isotropic part of
+// every tangent is lambda m m^T + mu diag(2..2, 1..1); for a node pair (a, b) with global gradients g_a, g_b
+// this gives K_ab(k, l) = lambda g_a[k] g_b[l] + mu (g_a[l] g_b[k] + delta_kl g_a.g_b), the same values
+// as B_a^T C B_b. Non-isotropic rank-1 parts (local damage, gradient-damage coupling) enter through
+// P_a = B_a^T s and Q_b = B_b^T t.
+template <int A, int B>
+struct MinI
+{
+    static constexpr int v = A < B ? A : B;
+};
+
+// cells per block of the tangent kernel: bounded by the node pairs (512 per block) and by the shared-memory
+// records per (cell, integration point, node) (256 per block keeps the static shared memory below 48 KB)
+template <int ND, int NIP>
+struct TangentShape
+{
+    static constexpr int threads = 256;
+    static constexpr int cpb = MaxI<1, MinI<512 / (ND * ND), 256 / (NIP * ND)>::v>::v;
+};
+
+template <typename T, int DIM, int ND, int NIP, int KIND>
+__global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, ScatterArgs S, int pUU, int pUE, int pEU,
+                                                 int pEE, const double* __restrict__ u, T* __restrict__ vals)
+{
+    constexpr int VD = DIM == 2 ? 3 : 6;
+    constexpr bool GD = KIND == NUTO_GPU_GRADIENT_DAMAGE;
+    constexpr bool LD = KIND == NUTO_GPU_MB_LOCAL_DAMAGE;
+    constexpr bool RANK1 = GD || LD;
+    constexpr int CPB = TangentShape<ND, NIP>::cpb;
+    constexpr int NREC = 2 + (GD ? 2 + DIM : 0);
+    __shared__ double sU[CPB][ND][DIM];
+    __shared__ double sE[GD ? CPB : 1][GD ? ND : 1];
+    __shared__ T sG[CPB][NIP][ND][DIM];
+    __shared__ T sRec[CPB][NIP][NREC];
+    __shared__ T sST[RANK1 ? CPB : 1][RANK1 ? NIP : 1][2][VD];
+    __shared__ T sPQ[RANK1 ? CPB : 1][RANK1 ? NIP : 1][RANK1 ? ND : 1][2][DIM];
+    __shared__ int64_t sBaseU[CPB][ND][DIM]; // row start + block offset of the (disp, disp) block
+    __shared__ int64_t sBaseUE[GD ? CPB : 1][GD ? ND : 1][DIM];
+    __shared__ int64_t sBaseEU[GD ? CPB : 1][GD ? ND : 1];
+    __shared__ int64_t sBaseEE[GD ? CPB : 1][GD ? ND : 1];
+    const int64_t n = a.nCells;
+    const int64_t cell0 = static_cast<int64_t>(blockIdx.x) * CPB;
+
+    // phase 0: DOF values, row bases, geometry
+    for (int it = threadIdx.x; it < CPB * ND; it += blockDim.x)
+    {
+        const int cl = it % CPB, nd = it / CPB;
+        const int64_t e = cell0 + cl;
+        if (e >= n)
+            continue;
+        const int32_t aD = a.connD[static_cast<int64_t>(nd) * n + e];
+        const int64_t g = a.gdofD[aD];
+        const int32_t bUU = S.blk[pUU][aD];
+#pragma unroll
+        for (int c = 0; c < DIM; ++c)
+        {
+            sU[cl][nd][c] = u[g + c];
+            const int64_t rs = S.rowPtr[g + c];
+            sBaseU[cl][nd][c] = rs + bUU;
+            if (GD)
+                sBaseUE[cl][nd][c] = rs + S.blk[pUE][aD];
+        }
+        if (GD)
+        {
+            const int32_t aE = a.connE[static_cast<int64_t>(nd) * n + e];
+            const int64_t ge = a.gdofE[aE];
+            sE[cl][nd] = u[ge];
+            const int64_t rs = S.rowPtr[ge];
+            sBaseEU[cl][nd] = rs + S.blk[pEU][aE];
+            sBaseEE[cl][nd] = rs + S.blk[pEE][aE];
+        }
+    }
+    for (int it = threadIdx.x; it < CPB * NIP * ND * DIM; it += blockDim.x)
+    {
+        const int cl = it % CPB;
+        int r = it / CPB;
+        const int d = r % DIM;
+        r /= DIM;
+        const int nd = r % ND;
+        const int q = r / ND;
+        const int64_t e = cell0 + cl;
+        if (e >= n)
+            continue;
+        const int64_t idx = (static_cast<int64_t>(q) * a.geoStride + 1 + nd * DIM + d) * n + e;
+        if (sizeof(T) == 4)
+            sG[cl][q][nd][d] = static_cast<T>(a.geo32[idx]);
+        else
+            sG[cl][q][nd][d] = static_cast<T>(a.geo64[idx]);
+    }
+    __syncthreads();
+
+    // phase A: material data per (cell, integration point)
+    for (int it = threadIdx.x; it < CPB * NIP; it += blockDim.x)
+    {
+        const int cl = it % CPB, q = it / CPB;
+        const int64_t e = cell0 + cl;
+        if (e >= n)
+            continue;
+        const int64_t widx = static_cast<int64_t>(q) * a.geoStride * n + e;
+        const T wdj = sizeof(T) == 4 ? static_cast<T>(a.geo32[widx]) : static_cast<T>(a.geo64[widx]);
+        T H[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = 0; j < DIM; ++j)
+                H[i][j] = T(0);
+        T eeq = T(0), ge[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            ge[d] = T(0);
+        for (int nd = 0; nd < ND; ++nd)
+        {
+#pragma unroll
+            for (int c = 0; c < DIM; ++c)
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    H[c][d] += static_cast<T>(sU[cl][nd][c]) * sG[cl][q][nd][d];
+            if (GD)
+            {
+                const T ev = static_cast<T>(sE[cl][nd]);
+                eeq += static_cast<T>(a.tabN_D[q * ND + nd]) * ev;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    ge[d] += ev * sG[cl][q][nd][d];
+            }
+        }
+        T eps[VD];
+        StrainFromH<T, DIM>(H, eps);
+        const T kh = static_cast<T>(a.kappa[e * NIP + q]);
+        T lam, mu;
+        if (KIND == NUTO_GPU_MB_LINEAR_ELASTIC)
+        {
+            // C11 = lambda + 2 mu, C12 = lambda, C33 = mu for every LinearElastic::CalculateC variant
+            lam = T(L.C12);
+            mu = T(L.C33);
+        }
+        else if (LD)
+        {
+            const T eqs = MisesValue<T, DIM>(L, eps);
+            const T kap = eqs > kh ? eqs : kh;
+            const T omega = DamageOmega<T>(L, kap);
+            LedTangentLameParams<T, DIM>(L, eps, omega, lam, mu);
+            // rank-1 part dsigma/domega * domega/dkappa * dkappa/deps (LocalIsotropicDamage.h:59-68, 115-122)
+            T dsdw[VD], dk[VD];
+            LedDstressDomega<T, DIM>(L, eps, dsdw);
+            const T dOdK = DamageDerivative<T>(L, kap);
+            if (eqs >= kh)
+                MisesDerivative<T, DIM>(L, eps, dk);
+            else
+#pragma unroll
+                for (int v = 0; v < VD; ++v)
+                    dk[v] = T(0);
+#pragma unroll
+            for (int v = 0; v < VD; ++v)
+            {
+                sST[cl][q][0][v] = dsdw[v] * dOdK * wdj;
+                sST[cl][q][1][v] = dk[v];
+            }
+        }
+        else
+        {
+            const T kap = kh > eeq ? kh : eeq;
+            const T omega = DamageOmega<T>(L, kap);
+            const T dKdE = eeq >= kh ? T(1) : T(0);
+            const T dOdK = DamageDerivative<T>(L, kap);
+            const T g = InteractionFactor<T>(L, omega);
+            const T dgdw = InteractionDerivative<T>(L, omega);
+            LedTangentLameParams<T, DIM>(L, eps, omega, lam, mu);
+            T dsdw[VD], dn[VD];
+            LedDstressDomega<T, DIM>(L, eps, dsdw);
+            MisesDerivative<T, DIM>(L, eps, dn);
+#pragma unroll
+            for (int v = 0; v < VD; ++v)
+            {
+                sST[cl][q][0][v] = dsdw[v] * dOdK * dKdE * wdj; // (disp, eeq): B^T (dsigma/domega w' k') N
+                sST[cl][q][1][v] = dn[v] * wdj;                 // (eeq, disp): -N^T (deps_eq/deps)^T B
+            }
+            sRec[cl][q][2] = wdj;
+            sRec[cl][q][3] = T(L.c) * g * wdj;
+            const T sc = T(L.c) * dgdw * dOdK * dKdE * wdj;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                sRec[cl][q][4 + d] = sc * ge[d];
+        }
+        sRec[cl][q][0] = lam * wdj;
+        sRec[cl][q][1] = mu * wdj;
+    }
+    __syncthreads();
+
+    if (RANK1)
+    {
+        for (int it = threadIdx.x; it < CPB * NIP * ND; it += blockDim.x)
+        {
+            const int cl = it % CPB;
+            const int r = it / CPB;
+            const int nd = r % ND, q = r / ND;
+            if (cell0 + cl >= n)
+                continue;
+            BtS<T, DIM>(sG[cl][q][nd], sST[cl][q][0], sPQ[cl][q][nd][0]);
+            BtS<T, DIM>(sG[cl][q][nd], sST[cl][q][1], sPQ[cl][q][nd][1]);
+        }
+        __syncthreads();
+    }
+
+    // phase B: one thread per (cell, node pair)
+    for (int it = threadIdx.x; it < CPB * ND * ND; it += blockDim.x)
+    {
+        const int cl = it % CPB;
+        const int pr = it / CPB;
+        const int ia = pr / ND, ib = pr % ND;
+        const int64_t e = cell0 + cl;
+        if (e >= n)
+            continue;
+        T kuu[DIM][DIM], kue[DIM], keu[DIM], kee = T(0);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            kue[k] = keu[k] = T(0);
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                kuu[k][l] = T(0);
+        }
+        for (int q = 0; q < NIP; ++q)
+        {
+            const T* ga = sG[cl][q][ia];
+            const T* gb = sG[cl][q][ib];
+            const T lam = sRec[cl][q][0], mu = sRec[cl][q][1];
+            T gab = T(0);
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                gab += ga[d] * gb[d];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k)
+            {
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    kuu[k][l] += lam * ga[k] * gb[l] + mu * ga[l] * gb[k];
+                kuu[k][k] += mu * gab;
+            }
+            if (LD)
+            {
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+#pragma unroll
+                    for (int l = 0; l < DIM; ++l)
+                        kuu[k][l] += sPQ[cl][q][ia][0][k] * sPQ[cl][q][ib][1][l];
+            }
+            if (GD)
+            {
+                const T Na = static_cast<T>(a.tabN_D[q * ND + ia]);
+                const T Nb = static_cast<T>(a.tabN_D[q * ND + ib]);
+                T gs = T(0);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    gs += ga[d] * sRec[cl][q][4 + d];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                {
+                    kue[k] += sPQ[cl][q][ia][0][k] * Nb;
+                    keu[k] -= Na * sPQ[cl][q][ib][1][k];
+                }
+                kee += sRec[cl][q][2] * Na * Nb + sRec[cl][q][3] * gab + gs * Nb;
+            }
+        }
+        const int64_t ridx = static_cast<int64_t>(ia * ND + ib) * n + e;
+        const int rUU = S.rank[pUU][ridx];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            T* row = vals + sBaseU[cl][ia][k] + DIM * rUU;
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                atomicAdd(row + l, kuu[k][l]);
+        }
+        if (GD)
+        {
+            const int rUE = S.rank[pUE][ridx];
+            const int rEU = S.rank[pEU][ridx];
+            const int rEE = S.rank[pEE][ridx];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k)
+                atomicAdd(vals + sBaseUE[cl][ia][k] + rUE, kue[k]);
+            T* rowE = vals + sBaseEU[cl][ia] + DIM * rEU;
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                atomicAdd(rowE + l, keu[l]);
+            atomicAdd(vals + sBaseEE[cl][ia] + rEE, kee);
+        }
+    }
+}
+
+static ScatterArgs MakeScatterArgs(Ctx& c)
+{
+    ScatterArgs s{};
+    s.rowPtr = c.dRowPtr.p;
+    const int ns = static_cast<int>(c.slots.size());
+    for (int p = 0; p < ns * ns; ++p)
+    {
+        s.rank[p] = c.pairs[p].rank;
+        s.blk[p] = c.pairs[p].dBlk.p;
+    }
+    return s;
+}
+
+template <typename T>
+static void LaunchTangentT(Ctx& c, const double* u, T* vals)
+{
+    NG_CUDA(cudaMemsetAsync(vals, 0, c.nnz * sizeof(T), c.stream));
+    CellArgs a = MakeCellArgs(c);
+    ScatterArgs s = MakeScatterArgs(c);
+    const int ns = static_cast<int>(c.slots.size());
+    const int dS = c.prm.disp_slot;
+    const int eS = c.prm.kind == NUTO_GPU_GRADIENT_DAMAGE ? c.prm.eeq_slot : dS;
+    DispatchCfg(c, [&](auto cfg) {
+        using C = decltype(cfg);
+        constexpr int CPB = TangentShape<C::nd, C::nip>::cpb;
+        const int blocks = static_cast<int>((c.nCells + CPB - 1) / CPB);
+        k_tangent<T, C::dim, C::nd, C::nip, C::kind><<<blocks, TangentShape<C::nd, C::nip>::threads, 0, c.stream>>>(
+                a, c.law, s, dS * ns + dS, dS * ns + eS, eS * ns + dS, eS * ns + eS, u, vals);
+    });
+    NG_CUDA(cudaGetLastError());
+}
+
+void LaunchTangent(Ctx& c, const double* u, int precision, void* values)
+{
+    if (precision == NUTO_GPU_FP32)
+        LaunchTangentT<float>(c, u, static_cast<float*>(values));
+    else
+        LaunchTangentT<double>(c, u, static_cast<double*>(values));
+}
+
+// ---- history update: GradientDamage::Update (GradientDamage.h:122-125), EvolutionImplicit::Update
+// (LocalIsotropicDamage.h:130-133) -------------------------------------------------------------------------------
+template <int DIM, int ND, int NIP, int KIND>
+__global__ void __launch_bounds__(128) k_history(CellArgs a, LawParams L, const double* __restrict__ u)
+{
+    constexpr int VD = DIM == 2 ? 3 : 6;
+    const int64_t n = a.nCells;
+    const int64_t it = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (it >= n * NIP)
+        return;
+    const int64_t e = it % n;
+    const int q = static_cast<int>(it / n);
+    double& kh = a.kappa[e * NIP + q];
+    if (KIND == NUTO_GPU_GRADIENT_DAMAGE)
+    {
+        double eeq = 0;
+        for (int nd = 0; nd < ND; ++nd)
+            eeq += a.tabN_D[q * ND + nd] * u[a.gdofE[a.connE[static_cast<int64_t>(nd) * n + e]]];
+        kh = fmax(kh, eeq);
+        return;
+    }
+    const double* G = a.geo64 + static_cast<int64_t>(q) * a.geoStride * n + e;
+    double H[DIM][DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int j = 0; j < DIM; ++j)
+            H[i][j] = 0;
+    for (int nd = 0; nd < ND; ++nd)
+    {
+        const int64_t g = a.gdofD[a.connD[static_cast<int64_t>(nd) * n + e]];
+#pragma unroll
+        for (int c = 0; c < DIM; ++c)
+        {
+            const double uc = u[g + c];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                H[c][d] += uc * G[(1 + nd * DIM + d) * n];
+        }
+    }
+    double eps[VD];
+    StrainFromH<double, DIM>(H, eps);
+    kh = fmax(MisesValue<double, DIM>(L, eps), kh);
+}
+
+void LaunchHistory(Ctx& c, const double* u)
+{
+    if (c.prm.kind == NUTO_GPU_MB_LINEAR_ELASTIC)
+        return;
+    CellArgs a = MakeCellArgs(c);
+    const int64_t items = c.nCells * c.ip.nIp;
+    const int blocks = static_cast<int>((items + 127) / 128);
+    DispatchCfg(c, [&](auto cfg) {
+        using C = decltype(cfg);
+        if constexpr (C::kind != NUTO_GPU_MB_LINEAR_ELASTIC)
+            k_history<C::dim, C::nd, C::nip, C::kind><<<blocks, 128, 0, c.stream>>>(a, c.law, u);
+    });
+    NG_CUDA(cudaGetLastError());
+}
+
+// ---- scatter of caller-given cell results (SimpleAssembler scatter, SimpleAssembler.cpp:53-59, 118-137) -----
+struct SlotView
+{
+    int ncomp, nen;
+    int64_t localOffset;
+    const int32_t* connT;
+    const int64_t* gdof;
+};
+
+struct SlotViews
+{
+    int ns;
+    int nLocal;
+    SlotView s[kMaxSlots];
+};
+
+static SlotViews MakeSlotViews(const Ctx& c)
+{
+    SlotViews v{};
+    v.ns = static_cast<int>(c.slots.size());
+    int off = 0;
+    for (int i = 0; i < v.ns; ++i)
+    {
+        v.s[i].ncomp = c.slots[i].ncomp;
+        v.s[i].nen = c.slots[i].nen;
+        v.s[i].localOffset = off;
+        v.s[i].connT = c.slots[i].dConnT.p;
+        v.s[i].gdof = c.slots[i].dGdof.p;
+        off += c.slots[i].ncomp * c.slots[i].nen;
+    }
+    v.nLocal = off;
+    return v;
+}
+
+__device__ __forceinline__ void LocalToSlot(const SlotViews& v, int i, int& slot, int& node, int& comp)
+{
+    slot = 0;
+    while (slot + 1 < v.ns && i >= v.s[slot + 1].localOffset)
+        ++slot;
+    const int r = i - static_cast<int>(v.s[slot].localOffset);
+    node = r / v.s[slot].ncomp;
+    comp = r % v.s[slot].ncomp;
+}
+
+__global__ void k_cell_vectors(int64_t nCells, SlotViews v, const double* __restrict__ fe, double* __restrict__ f)
+{
+    const int64_t it = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (it >= nCells * v.nLocal)
+        return;
+    const int64_t e = it / v.nLocal;
+    const int i = static_cast<int>(it % v.nLocal);
+    int s, node, comp;
+    LocalToSlot(v, i, s, node, comp);
+    const int64_t g = v.s[s].gdof[v.s[s].connT[static_cast<int64_t>(node) * nCells + e]] + comp;
+    atomicAdd(f + g, fe[it]);
+}
+
+template <typename T>
+__global__ void k_cell_matrices(int64_t nCells, SlotViews v, ScatterArgs S, const double* __restrict__ ke,
+                                T* __restrict__ vals)
+{
+    const int64_t nl = v.nLocal;
+    const int64_t it = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (it >= nCells * nl * nl)
+        return;
+    const int64_t e = it / (nl * nl);
+    const int i = static_cast<int>((it / nl) % nl), j = static_cast<int>(it % nl);
+    int sI, nI, cI, sJ, nJ, cJ;
+    LocalToSlot(v, i, sI, nI, cI);
+    LocalToSlot(v, j, sJ, nJ, cJ);
+    const int32_t aI = v.s[sI].connT[static_cast<int64_t>(nI) * nCells + e];
+    const int64_t row = v.s[sI].gdof[aI] + cI;
+    const int p = sI * v.ns + sJ;
+    const int rank = S.rank[p][static_cast<int64_t>(nI * v.s[sJ].nen + nJ) * nCells + e];
+    atomicAdd(vals + S.rowPtr[row] + S.blk[p][aI] + v.s[sJ].ncomp * rank + cJ, static_cast<T>(ke[it]));
+}
+
+void LaunchCellVectors(Ctx& c, const double* fe, double* f)
+{
+    NG_CUDA(cudaMemsetAsync(f, 0, c.nDofs * sizeof(double), c.stream));
+    SlotViews v = MakeSlotViews(c);
+    const int64_t items = c.nCells * v.nLocal;
+    k_cell_vectors<<<static_cast<unsigned>((items + 255) / 256), 256, 0, c.stream>>>(c.nCells, v, fe, f);
+    NG_CUDA(cudaGetLastError());
+}
+
+void LaunchCellMatrices(Ctx& c, const double* ke, int precision, void* values)
+{
+    SlotViews v = MakeSlotViews(c);
+    ScatterArgs s = MakeScatterArgs(c);
+    const int64_t items = c.nCells * v.nLocal * v.nLocal;
+    const unsigned blocks = static_cast<unsigned>((items + 255) / 256);
+    if (precision == NUTO_GPU_FP32)
+    {
+        NG_CUDA(cudaMemsetAsync(values, 0, c.nnz * sizeof(float), c.stream));
+        k_cell_matrices<float><<<blocks, 256, 0, c.stream>>>(c.nCells, v, s, ke, static_cast<float*>(values));
+    }
+    else
+    {
+        NG_CUDA(cudaMemsetAsync(values, 0, c.nnz * sizeof(double), c.stream));
+        k_cell_matrices<double><<<blocks, 256, 0, c.stream>>>(c.nCells, v, s, ke, static_cast<double*>(values));
+    }
+    NG_CUDA(cudaGetLastError());
+}
+
+} // namespace nuto_gpu

@@ -1,0 +1,434 @@
+// Internal declarations of the GB300 element-assembly library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/nuto_gpu.h"
+
+namespace nuto_gpu
+{
+
+constexpr int kMaxSlots = 2;
+constexpr int kMaxIp = 27;
+constexpr int kMaxEn = 20;
+
+// Status with message, thrown only inside the library and turned into a return code at the C boundary.
+struct Error
+{
+    int code;
+    std::string msg;
+};
+
+#define NG_CUDA(call)                                                                                            \
+    do                                                                                                           \
+    {                                                                                                            \
+        cudaError_t e_ = (call);                                                                                 \
+        if (e_ != cudaSuccess)                                                                                   \
+            throw ::nuto_gpu::Error{e_ == cudaErrorMemoryAllocation ? NUTO_GPU_ENOMEM : NUTO_GPU_ECUDA,          \
+                                    std::string(#call) + ": " + cudaGetErrorString(e_)};                          \
+    } while (0)
+
+#define NG_CHECK(cond, code, msg)                                                                                \
+    do                                                                                                           \
+    {                                                                                                            \
+        if (!(cond))                                                                                             \
+            throw ::nuto_gpu::Error{code, msg};                                                                  \
+    } while (0)
+
+inline int NumNodes(int interp)
+{
+    return interp == NUTO_GPU_QUAD4 ? 4 : (interp == NUTO_GPU_HEX8 ? 8 : (interp == NUTO_GPU_HEX20 ? 20 : -1));
+}
+inline int InterpDim(int interp)
+{
+    return interp == NUTO_GPU_QUAD4 ? 2 : 3;
+}
+
+// Device buffer owned by the context.
+template <typename T>
+struct DBuf
+{
+    T* p = nullptr;
+    size_t n = 0;
+    void alloc(size_t count)
+    {
+        free();
+        if (count == 0)
+            return;
+        NG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        n = count;
+    }
+    void free()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DBuf()
+    {
+        free();
+    }
+};
+
+struct Slot
+{
+    int ncomp = 1;
+    int interp = NUTO_GPU_HEX8;
+    int nen = 8;
+    int64_t nNodes = 0;
+    int64_t nDofs = 0; // n_independent + n_dependent
+    int64_t nIndep = 0;
+    int64_t offset = 0; // first row of this slot in the combined system
+    std::vector<int32_t> conn; // nCells x nen (host copy)
+    std::vector<int32_t> dof0; // per node: dof number of component 0
+    DBuf<int32_t> dConnT; // planar [n][cell]
+    DBuf<int64_t> dGdof; // per node: combined index of component 0
+};
+
+// Per (slot I, slot J) scatter map: rank of the J-node among the sorted J-neighbours of the I-node, per cell and
+// local node pair, plus the start of the J block inside the rows of an I-node.
+struct PairMap
+{
+    DBuf<uint8_t> dRank; // planar [i * nenJ + j][cell]
+    uint8_t* rank = nullptr; // dRank.p or a shared table of an identical pair
+    DBuf<int32_t> dBlk; // per I-node
+};
+
+// Device-side constants of one integrand (plain data passed by value to kernels).
+struct LawParams
+{
+    int kind, dim;
+    int planeState, damageApp, interaction;
+    double E, nu;
+    // LinearElastic C (Voigt)
+    double C11, C12, C33;
+    // LinearElasticDamage
+    double m3K, m2G, d2; // d2: mD2 factor of the normal components (1 or 1 + nu/(nu-1))
+    // damage law, strain norm, nonlocal interaction
+    double kappa0, beta, alpha;
+    double K1, K2, k;
+    double c, R, eta;
+};
+
+// Integration-point tables (double): weights, shape values and natural derivatives per interpolation.
+struct IpTables
+{
+    int nIp = 0;
+    std::vector<double> w; // nIp
+    std::vector<double> N[3]; // per interpolation: nIp x nen
+    std::vector<double> dN[3]; // per interpolation: nIp x nen x 3
+};
+
+struct SolverWork;
+
+struct Ctx
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+    std::string err;
+    int smCount = 0;
+
+    // cells
+    bool haveCells = false;
+    int dim = 3, geoInterp = NUTO_GPU_HEX8, nge = 8;
+    int64_t nCells = 0, nCoord = 0;
+    int gauss = 2;
+    IpTables ip;
+    DBuf<double> dCoords;
+    DBuf<int32_t> dGeoConnT; // planar [n][cell]
+    std::vector<double> hCoords;
+    std::vector<int32_t> hGeoConn;
+    DBuf<double> dTables; // w | N(interp) | dN(interp) packed, see TableOffsets
+    int tabW = 0, tabN[3] = {0, 0, 0}, tabDN[3] = {0, 0, 0};
+
+    // DOF types
+    std::vector<Slot> slots;
+    int64_t nDofs = 0;
+
+    // Dirichlet constraints (combined indices)
+    std::vector<std::vector<int32_t>> depDofs; // per slot
+    std::vector<std::vector<double>> depA, depB; // per slot
+    DBuf<uint8_t> dMask; // combined n_dofs: 1 = dependent
+    DBuf<int64_t> dDepIdx;
+    DBuf<double> dDepA, dDepB;
+    int64_t nDep = 0;
+
+    // pattern
+    bool havePattern = false;
+    int64_t nnz = 0;
+    DBuf<int64_t> dRowPtr;
+    DBuf<int32_t> dColIdx;
+    std::vector<int64_t> hRowPtr;
+    PairMap pairs[kMaxSlots * kMaxSlots];
+    double avgRowLen = 0;
+
+    // geometry caches per integration point: planar [(q * S + k)][cell], S = 1 + nen_d * dim
+    bool haveGeo = false;
+    DBuf<double> dGeo64;
+    DBuf<float> dGeo32;
+    int geoStride = 0;
+
+    // integrand
+    bool haveIntegrand = false;
+    nuto_gpu_integrand prm{};
+    LawParams law{};
+    DBuf<double> dKappa; // nCells x nIp
+
+    // quasistatic state
+    bool haveState = false;
+    double time = 0;
+    DBuf<double> dX;
+    nuto_gpu_stats stats{};
+
+    SolverWork* work = nullptr;
+
+    ~Ctx();
+};
+
+// ---- host helpers implemented in the .cu files ----
+void BuildTables(Ctx& c);
+void BuildGeometryCache(Ctx& c);
+void LaunchResidual(Ctx& c, const double* u, double* f);
+void LaunchTangent(Ctx& c, const double* u, int precision, void* values);
+void LaunchHistory(Ctx& c, const double* u);
+void LaunchCellVectors(Ctx& c, const double* fe, double* f);
+void LaunchCellMatrices(Ctx& c, const double* ke, int precision, void* values);
+int SolveLinear(Ctx& c, int precision, int method, const void* values, const double* b, double* x, double rtol,
+                int maxit, int* iters, double* relres);
+int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* iters);
+void FreeSolverWork(Ctx& c);
+
+// ---- kernel argument blocks (by value) ----
+struct CellArgs
+{
+    int64_t nCells;
+    const int32_t* connD; // planar [n][cell]
+    const int32_t* connE;
+    const int64_t* gdofD; // per node: combined index of component 0
+    const int64_t* gdofE;
+    const double* tabN_D; // nIp x nenD
+    const double* tabN_E;
+    const double* geo64;
+    const float* geo32;
+    int geoStride;
+    double* kappa;
+};
+
+struct ScatterArgs
+{
+    const int64_t* rowPtr;
+    const uint8_t* rank[kMaxSlots * kMaxSlots];
+    const int32_t* blk[kMaxSlots * kMaxSlots];
+};
+
+// ------------------------------------------------------------------------------------------------------------
+// Constitutive laws, device side, templated on the arithmetic type. Each cites the reference it restates.
+// ------------------------------------------------------------------------------------------------------------
+template <typename T>
+__host__ __device__ inline T H_unilateral(const LawParams& p, T eV)
+{
+    return (p.damageApp == NUTO_GPU_DAMAGE_UNILATERAL && eV < T(0)) ? T(0) : T(1);
+}
+
+// Volumetric strain of LinearElasticDamage: 1/3 * mD2^T eps (LinearElasticDamage.h:58-66)
+template <typename T, int DIM>
+__host__ __device__ inline T VolStrain(const LawParams& p, const T* e)
+{
+    if (DIM == 2)
+        return T(1. / 3.) * (T(p.d2) * e[0] + T(p.d2) * e[1]);
+    return T(1. / 3.) * (e[0] + e[1] + e[2]);
+}
+
+// LinearElasticDamage::Stress (LinearElasticDamage.h:58-66)
+template <typename T, int DIM>
+__host__ __device__ inline void LedStress(const LawParams& p, const T* e, T omega, T* s)
+{
+    constexpr int VD = DIM == 2 ? 3 : 6;
+    const T eV = VolStrain<T, DIM>(p, e);
+    const T sV = (T(1) - omega * H_unilateral(p, eV)) * T(p.m3K) * eV;
+    const T g = (T(1) - omega) * T(p.m2G);
+#pragma unroll
+    for (int i = 0; i < VD; ++i)
+    {
+        const bool normal = i < DIM;
+        const T dev = normal ? e[i] - eV : e[i];
+        s[i] = (normal ? sV : T(0)) + g * (normal ? dev : T(0.5) * dev);
+    }
+}
+
+// LinearElasticDamage::DstressDomega (LinearElasticDamage.h:79-87)
+template <typename T, int DIM>
+__host__ __device__ inline void LedDstressDomega(const LawParams& p, const T* e, T* s)
+{
+    constexpr int VD = DIM == 2 ? 3 : 6;
+    const T eV = VolStrain<T, DIM>(p, e);
+    const T dsV = -T(p.m3K) * eV * H_unilateral(p, eV);
+#pragma unroll
+    for (int i = 0; i < VD; ++i)
+    {
+        const bool normal = i < DIM;
+        const T dev = normal ? e[i] - eV : e[i];
+        s[i] = (normal ? dsV : T(0)) - T(p.m2G) * (normal ? dev : T(0.5) * dev);
+    }
+}
+
+// Isotropic split of LinearElasticDamage::DstressDstrain (LinearElasticDamage.h:68-77):
+// a * Iv + b * PinvId = lambda * m m^T + mu * diag(2,..,2,1,..,1) with m the normal-component indicator.
+// Iv = 1/3 mD mD2^T and Pinv m = m give lambda = d2 (a - b) / 3, mu = b / 2.
+template <typename T, int DIM>
+__host__ __device__ inline void LedTangentLameParams(const LawParams& p, const T* e, T omega, T& lam, T& mu)
+{
+    const T eV = VolStrain<T, DIM>(p, e);
+    const T a = T(p.m3K) * (T(1) - omega * H_unilateral(p, eV));
+    const T b = (T(1) - omega) * T(p.m2G);
+    lam = T(DIM == 2 ? p.d2 : 1.0) * (a - b) / T(3);
+    mu = b / T(2);
+}
+
+// ModifiedMisesStrainNorm::Value / Derivative (ModifiedMisesStrainNorm.h:139-268), plane strain/stress for 2D
+template <typename T, int DIM>
+__host__ __device__ inline T MisesValue(const LawParams& p, const T* e)
+{
+    T v0 = e[0], v1 = e[1], v2, v3, v4, v5;
+    if (DIM == 2)
+    {
+        v2 = p.planeState == NUTO_GPU_PLANE_STRESS ? T(p.nu / (p.nu - 1.)) * (e[0] + e[1]) : T(0);
+        v3 = T(0);
+        v4 = T(0);
+        v5 = e[2];
+    }
+    else
+    {
+        v2 = e[2];
+        v3 = e[3];
+        v4 = e[4];
+        v5 = e[5];
+    }
+    const T I1 = v0 + v1 + v2;
+    const T yz = T(.5) * v3, zx = T(.5) * v4, xy = T(.5) * v5;
+    const T J2 = T(1. / 6.) * ((v0 - v1) * (v0 - v1) + (v1 - v2) * (v1 - v2) + (v2 - v0) * (v2 - v0)) + xy * xy +
+                 yz * yz + zx * zx;
+    const T K1 = T(p.K1), K2 = T(p.K2);
+    const T A = sqrt(K1 * K1 * I1 * I1 + K2 * J2);
+    return K1 * I1 + A;
+}
+
+template <typename T, int DIM>
+__host__ __device__ inline void MisesDerivative(const LawParams& p, const T* s, T* d)
+{
+    const T K1 = T(p.K1), K2 = T(p.K2);
+    if (DIM == 3)
+    {
+        const T I1 = s[0] + s[1] + s[2];
+        const T yz = T(.5) * s[3], zx = T(.5) * s[4], xy = T(.5) * s[5];
+        const T J2 = T(1. / 6.) * ((s[0] - s[1]) * (s[0] - s[1]) + (s[1] - s[2]) * (s[1] - s[2]) +
+                                   (s[2] - s[0]) * (s[2] - s[0])) +
+                     xy * xy + yz * yz + zx * zx;
+        const T A = sqrt(K1 * K1 * I1 * I1 + K2 * J2);
+        if (A == T(0))
+        {
+            d[0] = d[1] = d[2] = K1;
+            d[3] = d[4] = d[5] = T(0);
+            return;
+        }
+        const T inv2A = T(1) / (T(2) * A);
+        const T dxx = T(1. / 3.) * (T(2) * s[0] - s[1] - s[2]);
+        const T dyy = T(1. / 3.) * (T(2) * s[1] - s[0] - s[2]);
+        const T dzz = T(1. / 3.) * (T(2) * s[2] - s[0] - s[1]);
+        d[0] = K1 + inv2A * (T(2) * K1 * K1 * I1 + K2 * dxx);
+        d[1] = K1 + inv2A * (T(2) * K1 * K1 * I1 + K2 * dyy);
+        d[2] = K1 + inv2A * (T(2) * K1 * K1 * I1 + K2 * dzz);
+        d[3] = inv2A * K2 * T(0.5) * s[3];
+        d[4] = inv2A * K2 * T(0.5) * s[4];
+        d[5] = inv2A * K2 * T(0.5) * s[5];
+        return;
+    }
+    const T nu = T(p.nu);
+    if (p.planeState == NUTO_GPU_PLANE_STRAIN)
+    {
+        const T I1 = s[0] + s[1];
+        const T xy = T(.5) * s[2];
+        const T J2 = T(1. / 6.) * ((s[0] - s[1]) * (s[0] - s[1]) + s[1] * s[1] + s[0] * s[0]) + xy * xy;
+        const T A = sqrt(K1 * K1 * I1 * I1 + K2 * J2);
+        if (A == T(0))
+        {
+            d[0] = K1;
+            d[1] = K1;
+            d[2] = T(0);
+            return;
+        }
+        const T inv2A = T(1) / (T(2) * A);
+        d[0] = K1 + inv2A * (T(2) * K1 * K1 * I1 + K2 * T(1. / 3.) * (T(2) * s[0] - s[1]));
+        d[1] = K1 + inv2A * (T(2) * K1 * K1 * I1 + K2 * T(1. / 3.) * (T(2) * s[1] - s[0]));
+        d[2] = inv2A * (K2 * T(0.5) * s[2]);
+        return;
+    }
+    const T f = nu / (nu - T(1));
+    const T sz = f * (s[0] + s[1]);
+    const T I1 = s[0] + s[1] + sz;
+    const T xy = T(.5) * s[2];
+    const T J2 = T(1. / 6.) * ((s[0] - s[1]) * (s[0] - s[1]) + (s[1] - sz) * (s[1] - sz) + (sz - s[0]) * (sz - s[0])) +
+                 xy * xy;
+    const T A = sqrt(K1 * K1 * I1 * I1 + K2 * J2);
+    const T dI1 = T(1) + f;
+    if (A == T(0))
+    {
+        d[0] = dI1 * K1;
+        d[1] = dI1 * K1;
+        d[2] = T(0);
+        return;
+    }
+    const T inv2A = T(1) / (T(2) * A);
+    const T dxx = T(1. / 3.) * (T(2) * s[0] - s[1] - T(2) * sz + T(2) * f * sz);
+    const T dyy = T(1. / 3.) * (T(2) * s[1] - s[0] - T(2) * sz + T(2) * f * sz);
+    d[0] = dI1 * K1 + inv2A * (T(2) * dI1 * K1 * K1 * I1 + K2 * dxx);
+    d[1] = dI1 * K1 + inv2A * (T(2) * dI1 * K1 * K1 * I1 + K2 * dyy);
+    d[2] = inv2A * (K2 * T(0.5) * s[2]);
+}
+
+// DamageLawExponential (DamageLawExponential.h:40-52)
+template <typename T>
+__host__ __device__ inline T DamageOmega(const LawParams& p, T kappa)
+{
+    const T k0 = T(p.kappa0);
+    if (kappa < k0)
+        return T(0);
+    return T(1) - k0 / kappa * (T(1) - T(p.alpha) + T(p.alpha) * exp(T(p.beta) * (k0 - kappa)));
+}
+template <typename T>
+__host__ __device__ inline T DamageDerivative(const LawParams& p, T kappa)
+{
+    const T k0 = T(p.kappa0);
+    if (kappa < k0)
+        return T(0);
+    return k0 / kappa *
+           ((T(1) / kappa + T(p.beta)) * T(p.alpha) * exp(T(p.beta) * (k0 - kappa)) + (T(1) - T(p.alpha)) / kappa);
+}
+
+// NonlocalInteraction::Constant / Decreasing (GradientDamage.h:153-184)
+template <typename T>
+__host__ __device__ inline T InteractionFactor(const LawParams& p, T omega)
+{
+    if (p.interaction == NUTO_GPU_INTERACTION_CONSTANT)
+        return T(1);
+    const T eta = T(p.eta), R = T(p.R);
+    return ((T(1) - R) * exp(-eta * omega) + R - exp(-eta)) / (T(1) - exp(-eta));
+}
+template <typename T>
+__host__ __device__ inline T InteractionDerivative(const LawParams& p, T omega)
+{
+    if (p.interaction == NUTO_GPU_INTERACTION_CONSTANT)
+        return T(0);
+    const T eta = T(p.eta), R = T(p.R);
+    return ((T(1) - R) * exp(-eta * omega)) / (T(1) - exp(-eta)) * -eta;
+}
+
+} // namespace nuto_gpu

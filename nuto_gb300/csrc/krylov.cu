@@ -1,0 +1,686 @@
+// Jacobi-preconditioned Krylov solvers (PCG for SPD tangents, BiCGStab for the non-symmetric damage tangents)
+// on the CSR tangent, replacing the sparse direct solve of the reference (Solve.cpp:8-34 with
+// EigenSparseSolve.cpp:22-73). The constrained system C^T K C y = C^T b of unit (Dirichlet) constraints is
+// solved in place: dependent rows act as identity and the iterates stay zero there, so the dependent columns
+// never contribute.
+//
+// Every reduction is fused into the kernel that produces its operands; the last block of the grid (atomic
+// ticket, no waiting) turns the sums into the iteration scalars (alpha, beta, omega) kept in device memory, so a
+// whole chunk of iterations runs without a host round trip. Dot products accumulate in FP64.
+#include "solver.cuh"
+
+namespace nuto_gpu
+{
+
+SolverWork::~SolverWork()
+{
+    if (hScal)
+        cudaFreeHost(hScal);
+    if (hStat)
+        cudaFreeHost(hStat);
+    for (cudaEvent_t& e : ev)
+        if (e)
+            cudaEventDestroy(e);
+}
+
+SolverWork& Work(Ctx& c)
+{
+    if (!c.work)
+    {
+        auto* w = new SolverWork();
+        c.work = w;
+        w->scal.alloc(SC_COUNT);
+        w->stat.alloc(ST_COUNT);
+        NG_CUDA(cudaMallocHost(&w->hScal, SC_COUNT * sizeof(double)));
+        NG_CUDA(cudaMallocHost(&w->hStat, ST_COUNT * sizeof(int)));
+        for (cudaEvent_t& e : w->ev)
+            NG_CUDA(cudaEventCreate(&e));
+    }
+    return *c.work;
+}
+
+void FreeSolverWork(Ctx& c)
+{
+    delete c.work;
+    c.work = nullptr;
+}
+
+constexpr int kBS = 256;
+
+__device__ __forceinline__ double WarpSum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sums v over the block and adds the block total to *acc (thread 0).
+__device__ __forceinline__ void BlockAccumulate(double v, double* acc, double* sh)
+{
+    v = WarpSum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        sh[wid] = v;
+    __syncthreads();
+    if (wid == 0)
+    {
+        v = lane < (blockDim.x >> 5) ? sh[lane] : 0.;
+        v = WarpSum(v);
+        if (lane == 0)
+            atomicAdd(acc, v);
+    }
+    __syncthreads();
+}
+
+// True in exactly one block: the last one to arrive (threadFenceReduction pattern, no spinning).
+__device__ __forceinline__ bool LastBlock(int* counter)
+{
+    __shared__ bool last;
+    __threadfence();
+    if (threadIdx.x == 0)
+    {
+        const unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(counter), 1u);
+        last = prev == gridDim.x - 1;
+    }
+    __syncthreads();
+    return last;
+}
+
+__device__ __forceinline__ double VRead(const double* p)
+{
+    return *reinterpret_cast<const volatile double*>(p);
+}
+
+__device__ __forceinline__ bool Finite(double v)
+{
+    return isfinite(v);
+}
+
+// finalize actions of the SpMV kernel
+enum Fin
+{
+    FIN_NONE = 0,
+    FIN_PCG_ALPHA = 1,  // alpha = rho / (p.Ap)
+    FIN_BICG_ALPHA = 2, // alpha = rho / (rhat.v)
+    FIN_BICG_OMEGA = 3  // omega = (t.s) / (t.t)
+};
+
+// y = A x on the constrained operator (dependent rows: y = x), W lanes per row; optionally acc0 += w0.y and
+// acc1 += y.y, then the last block applies a finalize action.
+template <typename TV, typename TX, int W, int NDOT>
+__global__ void __launch_bounds__(kBS) k_spmv(int64_t n, const int64_t* __restrict__ rowPtr,
+                                               const int32_t* __restrict__ col, const TV* __restrict__ val,
+                                               const uint8_t* __restrict__ mask, const TX* __restrict__ x,
+                                               TX* __restrict__ y, const TX* __restrict__ w0, double* sc, int* st,
+                                               int fin)
+{
+    __shared__ double sh[kBS / 32];
+    if (st && st[ST_STATE] != RUN)
+        return;
+    const int64_t gt = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    const int64_t row = gt / W;
+    const int lane = threadIdx.x % W;
+    TX sum = TX(0);
+    bool masked = false;
+    if (row < n)
+    {
+        masked = mask[row] != 0;
+        if (!masked)
+        {
+            const int64_t end = rowPtr[row + 1];
+            for (int64_t k = rowPtr[row] + lane; k < end; k += W)
+                sum += static_cast<TX>(val[k]) * x[col[k]];
+        }
+    }
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1)
+        sum += __shfl_down_sync(0xffffffffu, sum, o, W);
+    double d0 = 0., d1 = 0.;
+    if (row < n && lane == 0)
+    {
+        const TX yv = masked ? x[row] : sum;
+        y[row] = yv;
+        if (NDOT >= 1)
+            d0 = static_cast<double>(w0[row]) * static_cast<double>(yv);
+        if (NDOT >= 2)
+            d1 = static_cast<double>(yv) * static_cast<double>(yv);
+    }
+    if (NDOT == 0)
+        return;
+    BlockAccumulate(d0, sc + SC_ACC0, sh);
+    if (NDOT >= 2)
+        BlockAccumulate(d1, sc + SC_ACC1, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        const double a0 = VRead(sc + SC_ACC0), a1 = VRead(sc + SC_ACC1);
+        sc[SC_ACC0] = 0.;
+        sc[SC_ACC1] = 0.;
+        if (fin == FIN_PCG_ALPHA)
+        {
+            if (!Finite(a0))
+                st[ST_STATE] = NONFINITE;
+            else if (!(a0 > 0.))
+                st[ST_STATE] = BREAKDOWN;
+            else
+                sc[SC_ALPHA] = sc[SC_RHO] / a0;
+        }
+        else if (fin == FIN_BICG_ALPHA)
+        {
+            if (!Finite(a0))
+                st[ST_STATE] = NONFINITE;
+            else if (a0 == 0.)
+                st[ST_STATE] = BREAKDOWN;
+            else
+                sc[SC_ALPHA] = sc[SC_RHO] / a0;
+        }
+        else if (fin == FIN_BICG_OMEGA)
+        {
+            if (!Finite(a0) || !Finite(a1))
+                st[ST_STATE] = NONFINITE;
+            else
+                sc[SC_OMEGA] = a1 > 0. ? a0 / a1 : 0.;
+        }
+    }
+}
+
+// ---- right-hand side preparation ---------------------------------------------------------------------------
+// bb = |mask0(b)|^2; last block: scale = 1/|b| (FP32) or 1, tol2 = rtol^2 |b scale|^2
+__global__ void __launch_bounds__(kBS) k_rhs_norm(int64_t n, const uint8_t* __restrict__ mask,
+                                                   const double* __restrict__ b, double* sc, int* st, double rtol,
+                                                   int scaleToUnit)
+{
+    __shared__ double sh[kBS / 32];
+    double v = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        if (!mask[i])
+            v += b[i] * b[i];
+    BlockAccumulate(v, sc + SC_ACC0, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        const double bb = VRead(sc + SC_ACC0);
+        sc[SC_ACC0] = 0.;
+        sc[SC_BB] = bb;
+        const double scale = (scaleToUnit && bb > 0.) ? 1. / sqrt(bb) : 1.;
+        sc[SC_SCALE] = scale;
+        sc[SC_TOL2] = rtol * rtol * bb * scale * scale;
+        st[ST_ITERS] = 0;
+        st[ST_HALF] = 0;
+        st[ST_STATE] = (bb == 0.) ? CONVERGED : (isfinite(bb) ? RUN : NONFINITE);
+        sc[SC_RR] = bb * scale * scale;
+    }
+}
+
+// x = 0, r = mask0(b) * scale, z = dinv r, p = z (PCG) / rh = r, p = v = 0 (BiCGStab); acc0 += r.z (PCG) or
+// r.r (BiCGStab); last block: rho
+template <typename T, bool PCG>
+__global__ void __launch_bounds__(kBS) k_krylov_init(int64_t n, const uint8_t* __restrict__ mask,
+                                                      const double* __restrict__ b, T* x, T* r, T* rh, T* p, T* v,
+                                                      T* z, const T* __restrict__ dinv, double* sc, int* st)
+{
+    __shared__ double sh[kBS / 32];
+    const double scale = sc[SC_SCALE];
+    double acc = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        const T ri = mask[i] ? T(0) : static_cast<T>(b[i] * scale);
+        x[i] = T(0);
+        r[i] = ri;
+        if (PCG)
+        {
+            const T zi = dinv[i] * ri;
+            z[i] = zi;
+            p[i] = zi;
+            acc += static_cast<double>(ri) * static_cast<double>(zi);
+        }
+        else
+        {
+            rh[i] = ri;
+            p[i] = T(0);
+            v[i] = T(0);
+            acc += static_cast<double>(ri) * static_cast<double>(ri);
+        }
+    }
+    BlockAccumulate(acc, sc + SC_ACC0, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        const double a = VRead(sc + SC_ACC0);
+        sc[SC_ACC0] = 0.;
+        sc[SC_RHO] = a;
+        sc[SC_RHO_OLD] = 1.;
+        sc[SC_ALPHA] = 1.;
+        sc[SC_OMEGA] = 1.;
+        sc[SC_BETA] = 0.;
+    }
+}
+
+// Jacobi: dinv = 1 / K_ii for independent rows, 1 for dependent rows
+template <typename TV, typename T>
+__global__ void k_diag_inv(int64_t n, const int64_t* __restrict__ rowPtr, const int32_t* __restrict__ col,
+                           const TV* __restrict__ val, const uint8_t* __restrict__ mask, T* __restrict__ dinv)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    if (mask[i])
+    {
+        dinv[i] = T(1);
+        return;
+    }
+    int64_t lo = rowPtr[i], hi = rowPtr[i + 1] - 1;
+    while (lo < hi)
+    {
+        const int64_t mid = (lo + hi) / 2;
+        if (col[mid] < i)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    const double d = (lo < rowPtr[i + 1] && col[lo] == i) ? static_cast<double>(val[lo]) : 0.;
+    dinv[i] = d != 0. ? static_cast<T>(1. / d) : T(1);
+}
+
+// ---- PCG ------------------------------------------------------------------------------------------------------
+// x += alpha p; r -= alpha q; z = dinv r; acc0 += r.z; acc1 += r.r; last block: convergence test, beta, rho
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_pcg_update(int64_t n, T* x, T* r, const T* __restrict__ p,
+                                                     const T* __restrict__ q, T* z, const T* __restrict__ dinv,
+                                                     double* sc, int* st)
+{
+    __shared__ double sh[kBS / 32];
+    if (st[ST_STATE] != RUN)
+        return;
+    const T alpha = static_cast<T>(sc[SC_ALPHA]);
+    double rz = 0, rr = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        x[i] += alpha * p[i];
+        const T ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        const T zi = dinv[i] * ri;
+        z[i] = zi;
+        rz += static_cast<double>(ri) * static_cast<double>(zi);
+        rr += static_cast<double>(ri) * static_cast<double>(ri);
+    }
+    BlockAccumulate(rz, sc + SC_ACC0, sh);
+    BlockAccumulate(rr, sc + SC_ACC1, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        const double a0 = VRead(sc + SC_ACC0), a1 = VRead(sc + SC_ACC1);
+        sc[SC_ACC0] = 0.;
+        sc[SC_ACC1] = 0.;
+        st[ST_ITERS] += 1;
+        sc[SC_RR] = a1;
+        if (!Finite(a0) || !Finite(a1))
+            st[ST_STATE] = NONFINITE;
+        else if (a1 <= sc[SC_TOL2])
+            st[ST_STATE] = CONVERGED;
+        else
+        {
+            sc[SC_BETA] = a0 / sc[SC_RHO];
+            sc[SC_RHO] = a0;
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_pcg_dir(int64_t n, T* p, const T* __restrict__ z, const double* sc,
+                                                  const int* st)
+{
+    if (st[ST_STATE] != RUN)
+        return;
+    const T beta = static_cast<T>(sc[SC_BETA]);
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        p[i] = z[i] + beta * p[i];
+}
+
+// ---- BiCGStab (right-preconditioned with dinv) ---------------------------------------------------------------
+// beta = (rho / rho_old)(alpha / omega) computed by the previous iteration; p = r + beta (p - omega v); ph = dinv p
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_bicg_p(int64_t n, T* p, const T* __restrict__ r, const T* __restrict__ v,
+                                                 T* ph, const T* __restrict__ dinv, const double* sc, const int* st)
+{
+    if (st[ST_STATE] != RUN)
+        return;
+    const T beta = static_cast<T>(sc[SC_BETA]);
+    const T omega = static_cast<T>(sc[SC_OMEGA]);
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        const T pi = r[i] + beta * (p[i] - omega * v[i]);
+        p[i] = pi;
+        ph[i] = dinv[i] * pi;
+    }
+}
+
+// s = r - alpha v; sh = dinv s; acc0 += s.s; last block: converged on s -> half step
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_bicg_s(int64_t n, T* s, const T* __restrict__ r, const T* __restrict__ v,
+                                                 T* sh_, const T* __restrict__ dinv, double* sc, int* st)
+{
+    __shared__ double sh[kBS / 32];
+    if (st[ST_STATE] != RUN)
+        return;
+    const T alpha = static_cast<T>(sc[SC_ALPHA]);
+    double ss = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        const T si = r[i] - alpha * v[i];
+        s[i] = si;
+        sh_[i] = dinv[i] * si;
+        ss += static_cast<double>(si) * static_cast<double>(si);
+    }
+    BlockAccumulate(ss, sc + SC_ACC2, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        const double a = VRead(sc + SC_ACC2);
+        sc[SC_ACC2] = 0.;
+        if (!Finite(a))
+            st[ST_STATE] = NONFINITE;
+        else if (a <= sc[SC_TOL2])
+            st[ST_HALF] = 1;
+    }
+}
+
+// x += alpha ph + omega sh; r = s - omega t; acc0 += rh.r; acc1 += r.r; last block: convergence, beta
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_bicg_x(int64_t n, T* x, T* r, const T* __restrict__ rh,
+                                                 const T* __restrict__ ph, const T* __restrict__ s,
+                                                 const T* __restrict__ shv, const T* __restrict__ t, double* sc,
+                                                 int* st)
+{
+    __shared__ double sh[kBS / 32];
+    if (st[ST_STATE] != RUN)
+        return;
+    const bool half = st[ST_HALF] != 0;
+    const T alpha = static_cast<T>(sc[SC_ALPHA]);
+    const T omega = half ? T(0) : static_cast<T>(sc[SC_OMEGA]);
+    double rhr = 0, rr = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        x[i] += alpha * ph[i] + omega * shv[i];
+        const T ri = half ? s[i] : s[i] - omega * t[i];
+        r[i] = ri;
+        rhr += static_cast<double>(rh[i]) * static_cast<double>(ri);
+        rr += static_cast<double>(ri) * static_cast<double>(ri);
+    }
+    BlockAccumulate(rhr, sc + SC_ACC0, sh);
+    BlockAccumulate(rr, sc + SC_ACC1, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        const double a0 = VRead(sc + SC_ACC0), a1 = VRead(sc + SC_ACC1);
+        sc[SC_ACC0] = 0.;
+        sc[SC_ACC1] = 0.;
+        st[ST_ITERS] += 1;
+        sc[SC_RR] = a1;
+        const double om = sc[SC_OMEGA];
+        if (!Finite(a0) || !Finite(a1))
+            st[ST_STATE] = NONFINITE;
+        else if (half || a1 <= sc[SC_TOL2])
+            st[ST_STATE] = CONVERGED;
+        else if (a0 == 0. || om == 0.)
+            st[ST_STATE] = BREAKDOWN;
+        else
+        {
+            sc[SC_BETA] = (a0 / sc[SC_RHO]) * (sc[SC_ALPHA] / om);
+            sc[SC_RHO_OLD] = sc[SC_RHO];
+            sc[SC_RHO] = a0;
+        }
+    }
+}
+
+// out = x * (1/scale) (converts the Krylov solution back to FP64)
+template <typename T>
+__global__ void k_unscale(int64_t n, const T* __restrict__ x, const double* sc, double* __restrict__ out, int add)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    const double s = sc[SC_SCALE];
+    const double v = static_cast<double>(x[i]) / s;
+    out[i] = add ? out[i] + v : v;
+}
+
+__global__ void k_masked_sq(int64_t n, const uint8_t* __restrict__ mask, const double* __restrict__ v, double* acc)
+{
+    __shared__ double sh[kBS / 32];
+    double s = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        if (!mask[i])
+            s += v[i] * v[i];
+    BlockAccumulate(s, acc, sh);
+}
+
+// ---- host side -----------------------------------------------------------------------------------------------
+static int GridFor(const Ctx& c, int64_t n)
+{
+    const int64_t want = (n + kBS - 1) / kBS;
+    const int64_t cap = static_cast<int64_t>(c.smCount) * 8;
+    return static_cast<int>(want < cap ? want : cap);
+}
+
+template <typename TV, typename TX, int NDOT>
+static void SpmvLaunch(Ctx& c, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc, int* st, int fin,
+                       const uint8_t* mask)
+{
+    const int64_t n = c.nDofs;
+    const double avg = c.avgRowLen;
+    auto go = [&](auto wtag) {
+        constexpr int W = decltype(wtag)::value;
+        const int64_t threads = n * W;
+        const unsigned blocks = static_cast<unsigned>((threads + kBS - 1) / kBS);
+        k_spmv<TV, TX, W, NDOT><<<blocks, kBS, 0, c.stream>>>(n, c.dRowPtr.p, c.dColIdx.p, vals, mask, x, y, w0, sc,
+                                                              st, fin);
+    };
+    if (avg < 6)
+        go(std::integral_constant<int, 4>{});
+    else if (avg < 14)
+        go(std::integral_constant<int, 8>{});
+    else if (avg < 40)
+        go(std::integral_constant<int, 16>{});
+    else
+        go(std::integral_constant<int, 32>{});
+}
+
+double MaskedNorm(Ctx& c, const double* v)
+{
+    SolverWork& w = Work(c);
+    NG_CUDA(cudaMemsetAsync(w.scal.p + SC_ACC2, 0, sizeof(double), c.stream));
+    k_masked_sq<<<GridFor(c, c.nDofs), kBS, 0, c.stream>>>(c.nDofs, c.dMask.p, v, w.scal.p + SC_ACC2);
+    NG_CUDA(cudaMemcpyAsync(w.hScal + SC_ACC2, w.scal.p + SC_ACC2, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    NG_CUDA(cudaStreamSynchronize(c.stream));
+    const double r = w.hScal[SC_ACC2];
+    NG_CUDA(cudaMemsetAsync(w.scal.p + SC_ACC2, 0, sizeof(double), c.stream));
+    return std::sqrt(r);
+}
+
+void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double* y)
+{
+    SolverWork& w = Work(c);
+    if (w.zeroMask.n != static_cast<size_t>(c.nDofs))
+    {
+        w.zeroMask.alloc(c.nDofs);
+        NG_CUDA(cudaMemsetAsync(w.zeroMask.p, 0, c.nDofs, c.stream));
+    }
+    if (precision == NUTO_GPU_FP32)
+        SpmvLaunch<float, double, 0>(c, static_cast<const float*>(vals), x, y, nullptr, nullptr, nullptr, FIN_NONE,
+                                     w.zeroMask.p);
+    else
+        SpmvLaunch<double, double, 0>(c, static_cast<const double*>(vals), x, y, nullptr, nullptr, nullptr, FIN_NONE,
+                                      w.zeroMask.p);
+    NG_CUDA(cudaGetLastError());
+}
+
+// Runs one Krylov solve of the constrained system with values `vals` (type TV) in arithmetic T, right-hand side
+// b (FP64, combined layout), solution written (or added) to x64. Returns the status.
+template <typename T, typename TV>
+static int KrylovSolve(Ctx& c, bool pcg, const TV* vals, const double* b, double* x64, bool addToX, double rtol,
+                       int maxit, int* iters, double* relres)
+{
+    SolverWork& w = Work(c);
+    KVecs<T>* vp;
+    if constexpr (sizeof(T) == 4)
+        vp = &w.v32;
+    else
+        vp = &w.v64;
+    KVecs<T>& V = *vp;
+    const int64_t n = c.nDofs;
+    V.ensure(n);
+    double* sc = w.scal.p;
+    int* st = w.stat.p;
+    NG_CUDA(cudaMemsetAsync(sc, 0, SC_COUNT * sizeof(double), c.stream));
+    NG_CUDA(cudaMemsetAsync(st, 0, ST_COUNT * sizeof(int), c.stream));
+    const int grid = GridFor(c, n);
+    k_diag_inv<TV, T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, c.stream>>>(n, c.dRowPtr.p, c.dColIdx.p, vals,
+                                                                                     c.dMask.p, V.dinv.p);
+    k_rhs_norm<<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, sc, st, rtol, sizeof(T) == 4 ? 1 : 0);
+    if (pcg)
+        k_krylov_init<T, true><<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, V.x.p, V.r.p, V.rh.p, V.p.p, V.v.p,
+                                                            V.z.p, V.dinv.p, sc, st);
+    else
+        k_krylov_init<T, false><<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, V.x.p, V.r.p, V.rh.p, V.p.p, V.v.p,
+                                                             V.z.p, V.dinv.p, sc, st);
+    NG_CUDA(cudaGetLastError());
+    const int chunk = 16;
+    int done = 0;
+    int state = RUN;
+    while (done < maxit)
+    {
+        const int nIt = std::min(chunk, maxit - done);
+        for (int k = 0; k < nIt; ++k)
+        {
+            if (pcg)
+            {
+                SpmvLaunch<TV, T, 1>(c, vals, V.p.p, V.q.p, V.p.p, sc, st, FIN_PCG_ALPHA, c.dMask.p);
+                k_pcg_update<T><<<grid, kBS, 0, c.stream>>>(n, V.x.p, V.r.p, V.p.p, V.q.p, V.z.p, V.dinv.p, sc, st);
+                k_pcg_dir<T><<<grid, kBS, 0, c.stream>>>(n, V.p.p, V.z.p, sc, st);
+            }
+            else
+            {
+                k_bicg_p<T><<<grid, kBS, 0, c.stream>>>(n, V.p.p, V.r.p, V.v.p, V.ph.p, V.dinv.p, sc, st);
+                SpmvLaunch<TV, T, 1>(c, vals, V.ph.p, V.v.p, V.rh.p, sc, st, FIN_BICG_ALPHA, c.dMask.p);
+                k_bicg_s<T><<<grid, kBS, 0, c.stream>>>(n, V.s.p, V.r.p, V.v.p, V.sh.p, V.dinv.p, sc, st);
+                SpmvLaunch<TV, T, 2>(c, vals, V.sh.p, V.t.p, V.s.p, sc, st, FIN_BICG_OMEGA, c.dMask.p);
+                k_bicg_x<T><<<grid, kBS, 0, c.stream>>>(n, V.x.p, V.r.p, V.rh.p, V.ph.p, V.s.p, V.sh.p, V.t.p, sc, st);
+            }
+        }
+        NG_CUDA(cudaGetLastError());
+        done += nIt;
+        NG_CUDA(cudaMemcpyAsync(w.hStat, st, ST_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        NG_CUDA(cudaMemcpyAsync(w.hScal, sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        NG_CUDA(cudaStreamSynchronize(c.stream));
+        state = w.hStat[ST_STATE];
+        if (state != RUN)
+            break;
+    }
+    const int it = w.hStat[ST_ITERS];
+    const double bb = w.hScal[SC_BB] * w.hScal[SC_SCALE] * w.hScal[SC_SCALE];
+    const double rel = bb > 0 ? std::sqrt(w.hScal[SC_RR] / bb) : 0.;
+    if (iters)
+        *iters = it;
+    if (relres)
+        *relres = rel;
+    c.stats.krylov_iterations += it;
+    if (state == NONFINITE)
+        throw Error{NUTO_GPU_ENAN, "non-finite value in the Krylov iteration"};
+    // breakdown or iteration cap: keep the iterate (Newton refines it) but report non-convergence by the rel value
+    k_unscale<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, c.stream>>>(n, V.x.p, sc, x64, addToX ? 1 : 0);
+    NG_CUDA(cudaGetLastError());
+    return state;
+}
+
+template <typename T, typename TV>
+int KrylovSolveExport(Ctx& c, bool pcg, const TV* vals, const double* b, double* x64, bool add, double rtol,
+                      int maxit, int* iters, double* relres)
+{
+    return KrylovSolve<T, TV>(c, pcg, vals, b, x64, add, rtol, maxit, iters, relres);
+}
+template int KrylovSolveExport<float, float>(Ctx&, bool, const float*, const double*, double*, bool, double, int,
+                                             int*, double*);
+template int KrylovSolveExport<double, double>(Ctx&, bool, const double*, const double*, double*, bool, double, int,
+                                               int*, double*);
+
+__global__ void k_residual64(int64_t n, const uint8_t* __restrict__ mask, const double* __restrict__ b,
+                             const double* __restrict__ kx, double* __restrict__ r)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i < n)
+        r[i] = mask[i] ? 0. : b[i] - kx[i];
+}
+
+void Residual64(Ctx& c, const double* b, const double* kx, double* r)
+{
+    k_residual64<<<static_cast<unsigned>((c.nDofs + 255) / 256), 256, 0, c.stream>>>(c.nDofs, c.dMask.p, b, kx, r);
+    NG_CUDA(cudaGetLastError());
+}
+
+bool UsePcg(const Ctx& c, int method)
+{
+    if (method == NUTO_GPU_SOLVER_PCG)
+        return true;
+    if (method == NUTO_GPU_SOLVER_BICGSTAB)
+        return false;
+    return c.prm.kind == NUTO_GPU_MB_LINEAR_ELASTIC;
+}
+
+// nuto_gpu_solve: FP64 solve, or FP32 Krylov inside an FP64 iterative refinement (r = b - K x in FP64 with the
+// FP32 values) until |r| <= rtol |b|.
+int SolveLinear(Ctx& c, int precision, int method, const void* values, const double* b, double* x, double rtol,
+                int maxit, int* iters, double* relres)
+{
+    SolverWork& w = Work(c);
+    const bool pcg = UsePcg(c, method);
+    c.stats.krylov_iterations = 0;
+    if (precision == NUTO_GPU_FP64)
+    {
+        int it = 0;
+        double rel = 0;
+        const int st = KrylovSolve<double, double>(c, pcg, static_cast<const double*>(values), b, x, false, rtol,
+                                                   maxit, &it, &rel);
+        if (iters)
+            *iters = it;
+        if (relres)
+            *relres = rel;
+        return st == CONVERGED ? NUTO_GPU_OK : NUTO_GPU_ENOCONV;
+    }
+    const int64_t n = c.nDofs;
+    w.tmp.alloc(n);
+    w.rhs.alloc(n);
+    const double bnorm = MaskedNorm(c, b);
+    NG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), c.stream));
+    NG_CUDA(cudaMemcpyAsync(w.rhs.p, b, n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    int total = 0;
+    double rel = bnorm > 0 ? 1. : 0.;
+    for (int sweep = 0; sweep < 30 && rel > rtol && total < maxit; ++sweep)
+    {
+        const double inner = std::max(rtol / std::max(rel, 1e-300), 1e-5);
+        int it = 0;
+        KrylovSolve<float, float>(c, pcg, static_cast<const float*>(values), w.rhs.p, x, true, std::min(inner, 0.5),
+                                  maxit - total, &it, nullptr);
+        total += it;
+        // r = b - K x (FP64 vectors, FP32 values), constrained rows zero
+        SpmvFull64(c, NUTO_GPU_FP32, values, x, w.tmp.p);
+        Residual64(c, b, w.tmp.p, w.rhs.p);
+        rel = bnorm > 0 ? MaskedNorm(c, w.rhs.p) / bnorm : 0.;
+    }
+    if (iters)
+        *iters = total;
+    if (relres)
+        *relres = rel;
+    return rel <= rtol ? NUTO_GPU_OK : NUTO_GPU_ENOCONV;
+}
+
+} // namespace nuto_gpu

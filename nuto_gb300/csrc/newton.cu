@@ -1,0 +1,243 @@
+// Quasistatic load step on the GPU: QuasistaticSolver::DoStep (nuto/mechanics/tools/QuasistaticSolver.cpp:116-147)
+// with the trial state of QuasistaticSolver::TrialState / SolveTrialState (QuasistaticSolver.cpp:51-66,
+// nuto/mechanics/solver/Solve.cpp:36-81), NewtonRaphson::Solve (nuto/math/NewtonRaphson.h:62-94) and
+// LineSearch (nuto/math/LineSearch.h:38-63). The state vector, history, tangent and every residual stay in HBM;
+// the host only sees one norm per residual evaluation to steer the iteration.
+//
+// Precision: with NUTO_GPU_FP32 the tangent is assembled and the Krylov iteration runs in FP32, while the
+// residual, the history, the constraint values and the convergence test stay FP64, so Newton acts as
+// iterative refinement of the FP32 linear solves. NUTO_GPU_FP64 runs everything in FP64.
+#include "solver.cuh"
+
+#include <chrono>
+
+namespace nuto_gpu
+{
+
+// db = float(rhs(tNew)) - float(rhs(tOld)) at the dependent DOFs: Constraints::GetSparseGlobalRhs stores the
+// right-hand sides in an Eigen::SparseVector<float> (Constraints.cpp:37-50).
+__global__ void k_delta_bc(int64_t nDep, const int64_t* __restrict__ idx, const double* __restrict__ a,
+                           const double* __restrict__ b, double tOld, double tNew, double* __restrict__ db)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= nDep)
+        return;
+    const float vNew = static_cast<float>(a[i] + b[i] * tNew);
+    const float vOld = static_cast<float>(a[i] + b[i] * tOld);
+    db[idx[i]] = static_cast<double>(vNew) - static_cast<double>(vOld);
+}
+
+// out = mask0(f + kdb) (C^T (f + K db) of SolveTrialState; kdb may be null)
+__global__ void k_masked_sum(int64_t n, const uint8_t* __restrict__ mask, const double* __restrict__ f,
+                             const double* __restrict__ kdb, double* __restrict__ out)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    out[i] = mask[i] ? 0. : f[i] + (kdb ? kdb[i] : 0.);
+}
+
+// out = x0 - alpha * dx (+ db)
+__global__ void k_update(int64_t n, const double* __restrict__ x0, const double* __restrict__ dx, double alpha,
+                         const double* __restrict__ db, double* __restrict__ out)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    out[i] = x0[i] - alpha * dx[i] + (db ? db[i] : 0.);
+}
+
+namespace
+{
+struct Timers
+{
+    Ctx& c;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
+    std::vector<std::pair<int, double*>> pending; // pool index, accumulator
+    size_t next = 0;
+    explicit Timers(Ctx& ctx)
+        : c(ctx)
+    {
+    }
+    ~Timers()
+    {
+        for (auto& p : pool)
+        {
+            cudaEventDestroy(p.first);
+            cudaEventDestroy(p.second);
+        }
+    }
+    int Begin()
+    {
+        if (next == pool.size())
+        {
+            std::pair<cudaEvent_t, cudaEvent_t> p;
+            NG_CUDA(cudaEventCreate(&p.first));
+            NG_CUDA(cudaEventCreate(&p.second));
+            pool.push_back(p);
+        }
+        NG_CUDA(cudaEventRecord(pool[next].first, c.stream));
+        return static_cast<int>(next++);
+    }
+    void End(int k, double* acc)
+    {
+        NG_CUDA(cudaEventRecord(pool[k].second, c.stream));
+        pending.push_back({k, acc});
+    }
+    // after a stream synchronisation: fold the finished pairs into their accumulators
+    void Collect()
+    {
+        for (auto& p : pending)
+        {
+            float ms = 0;
+            NG_CUDA(cudaEventElapsedTime(&ms, pool[p.first].first, pool[p.first].second));
+            *p.second += ms;
+        }
+        pending.clear();
+        next = 0;
+    }
+};
+} // namespace
+
+int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    NG_CHECK(o.precision == NUTO_GPU_FP32 || o.precision == NUTO_GPU_FP64, NUTO_GPU_EINVAL, "precision 32 or 64");
+    SolverWork& w = Work(c);
+    const int64_t n = c.nDofs;
+    for (DBuf<double>* b : {&w.f, &w.rhs, &w.dx, &w.db, &w.x0, &w.xs, &w.tmp})
+        if (b->n != static_cast<size_t>(n))
+            b->alloc(n);
+    const bool fp32 = o.precision == NUTO_GPU_FP32;
+    if (fp32 && w.K32.n != static_cast<size_t>(c.nnz))
+        w.K32.alloc(c.nnz);
+    if (!fp32 && w.K64.n != static_cast<size_t>(c.nnz))
+        w.K64.alloc(c.nnz);
+    void* K = fp32 ? static_cast<void*>(w.K32.p) : static_cast<void*>(w.K64.p);
+    const bool pcg = UsePcg(c, o.method);
+    c.stats = nuto_gpu_stats{};
+    nuto_gpu_stats& S = c.stats;
+    Timers T(c);
+    const unsigned gb = static_cast<unsigned>((n + 255) / 256);
+
+    auto assembleK = [&](const double* x) {
+        const int k = T.Begin();
+        LaunchTangent(c, x, o.precision, K);
+        T.End(k, &S.ms_assemble_matrix);
+        S.matrix_assemblies++;
+    };
+    auto residual = [&](const double* x) {
+        const int k = T.Begin();
+        LaunchResidual(c, x, w.f.p);
+        T.End(k, &S.ms_assemble_vector);
+        S.residual_evaluations++;
+        const double r = MaskedNorm(c, w.f.p);
+        T.Collect();
+        if (!std::isfinite(r))
+            throw Error{NUTO_GPU_ENAN, "non-finite residual"};
+        return r;
+    };
+    auto solve = [&](const double* rhs, double* out) {
+        const auto k0 = std::chrono::steady_clock::now();
+        int it = 0;
+        if (fp32)
+            KrylovSolveExport<float, float>(c, pcg, w.K32.p, rhs, out, false, o.krylov_rtol, o.max_krylov, &it,
+                                            nullptr);
+        else
+            KrylovSolveExport<double, double>(c, pcg, w.K64.p, rhs, out, false, o.krylov_rtol, o.max_krylov, &it,
+                                              nullptr);
+        T.Collect();
+        S.ms_krylov += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - k0).count();
+    };
+
+    const double tOld = c.time;
+    double* x = c.dX.p;
+
+    // trial state: K(x_old), R(x_old, t_new), x_trial = x - C (C^T K C)^-1 C^T (R + K db) + db
+    assembleK(x);
+    {
+        const int k = T.Begin();
+        LaunchResidual(c, x, w.f.p);
+        T.End(k, &S.ms_assemble_vector);
+        S.residual_evaluations++;
+    }
+    NG_CUDA(cudaMemsetAsync(w.db.p, 0, n * sizeof(double), c.stream));
+    if (c.nDep > 0)
+        k_delta_bc<<<static_cast<unsigned>((c.nDep + 255) / 256), 256, 0, c.stream>>>(
+                c.nDep, c.dDepIdx.p, c.dDepA.p, c.dDepB.p, tOld, tNew, w.db.p);
+    SpmvFull64(c, o.precision, K, w.db.p, w.tmp.p);
+    k_masked_sum<<<gb, 256, 0, c.stream>>>(n, c.dMask.p, w.f.p, w.tmp.p, w.rhs.p);
+    NG_CUDA(cudaGetLastError());
+    const double refNorm = MaskedNorm(c, w.rhs.p);
+    S.reference_residual = refNorm;
+    const double tol = std::max(o.newton_atol, o.newton_rtol * refNorm);
+    solve(w.rhs.p, w.dx.p);
+    k_update<<<gb, 256, 0, c.stream>>>(n, x, w.dx.p, 1.0, w.db.p, w.xs.p);
+    NG_CUDA(cudaGetLastError());
+
+    // Newton-Raphson with line search on the trial state
+    double nr = residual(w.xs.p);
+    int it = 0;
+    bool conv = nr < tol || refNorm == 0.;
+    while (!conv && it < o.max_newton)
+    {
+        assembleK(w.xs.p);
+        k_masked_sum<<<gb, 256, 0, c.stream>>>(n, c.dMask.p, w.f.p, nullptr, w.rhs.p);
+        solve(w.rhs.p, w.dx.p);
+        ++it;
+        if (o.line_search)
+        {
+            NG_CUDA(cudaMemcpyAsync(w.x0.p, w.xs.p, n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+            const double prev = nr;
+            double alpha = 1.;
+            for (int step = 0; step < 6; ++step)
+            {
+                k_update<<<gb, 256, 0, c.stream>>>(n, w.x0.p, w.dx.p, alpha, nullptr, w.xs.p);
+                const double trial = residual(w.xs.p);
+                nr = trial;
+                if (trial < tol)
+                {
+                    conv = true;
+                    break;
+                }
+                alpha *= 0.5;
+                if (trial < (1. - alpha) * prev)
+                    break;
+            }
+        }
+        else
+        {
+            k_update<<<gb, 256, 0, c.stream>>>(n, w.xs.p, w.dx.p, 1.0, nullptr, w.xs.p);
+            nr = residual(w.xs.p);
+            conv = nr < tol;
+        }
+    }
+    S.newton_iterations = it;
+    S.final_residual = nr;
+    if (itersOut)
+        *itersOut = it;
+    auto finish = [&]() {
+        T.Collect();
+        S.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    };
+    if (!conv)
+    {
+        finish();
+        c.err = "No convergence after " + std::to_string(it) + " iterations.";
+        return NUTO_GPU_ENOCONV;
+    }
+    if (MaskedNorm(c, w.xs.p) > 1.e10)
+    {
+        finish();
+        c.err = "floating point exception";
+        return NUTO_GPU_ENOCONV;
+    }
+    LaunchHistory(c, w.xs.p);
+    NG_CUDA(cudaMemcpyAsync(x, w.xs.p, n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    NG_CUDA(cudaStreamSynchronize(c.stream));
+    c.time = tNew;
+    finish();
+    return NUTO_GPU_OK;
+}
+
+} // namespace nuto_gpu

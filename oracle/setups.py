@@ -1,0 +1,54 @@
+"""TEST INFRASTRUCTURE ONLY — the benchmark set-ups rebuilt with the oracle's restatement of NuTo's mesh code.
+
+Mirrors nuto_gb300.configs but takes every array from the C++ restatement (UnitMeshFem generators,
+AddDofInterpolation with the SubBoxes coordinate search, MeshFem::NodesAtAxis, DofNumbering::Build), so that
+the tests can compare numbering and patterns bit for bit.
+"""
+
+import numpy as np
+
+from . import core
+
+
+def _component(mesh, layer, ncomp, nodes, directions, const, slope):
+    dn = mesh.layer_dof_numbers(layer, ncomp)
+    dofs = dn[np.asarray(nodes)[:, None], np.asarray(directions)[None, :]].ravel()
+    return dofs, np.full(dofs.size, float(const)), np.full(dofs.size, float(slope))
+
+
+def _cat(*parts):
+    return (np.concatenate([p[0] for p in parts]), np.concatenate([p[1] for p in parts]),
+            np.concatenate([p[2] for p in parts]))
+
+
+def quad4_elastic(n, u_right=0.01):
+    m = core.Mesh.quads(n, n)
+    d = m.add_dof(2)
+    integ = core.Integrand.make(core.MB_LINEAR_ELASTIC, 2, E=30000.0, nu=0.2, plane_state=core.PLANE_STRAIN)
+    P = core.Problem(m, 2, [d], integ)
+    cons = _cat(_component(m, d, 2, m.nodes_at_axis(d, 0, 0.0), [0, 1], 0.0, 0.0),
+                _component(m, d, 2, m.nodes_at_axis(d, 0, 1.0), [0], 0.0, u_right))
+    return m, [d], P, cons
+
+
+def hex8_gradient_damage(n, length=4.0, u_end=2e-3):
+    m = core.Mesh.bricks(n, n, n).scale(1.0, 1.0, length)
+    d = m.add_dof(3)
+    e = m.add_dof(1)
+    integ = core.Integrand.make(core.GRADIENT_DAMAGE, 3, E=30000.0, nu=0.2, damage_application=core.FULL,
+                                kappa0=1e-4, beta=100.0, alpha=0.99, k=10.0, c=0.01)
+    P = core.Problem(m, 2, [d, e], integ)
+    cons = _cat(_component(m, d, 3, m.nodes_at_axis(d, 2, 0.0), [0, 1, 2], 0.0, 0.0),
+                _component(m, d, 3, m.nodes_at_axis(d, 2, length), [2], 0.0, u_end))
+    return m, [d, e], P, cons
+
+
+def hex20_local_damage(n, u_end=3e-4):
+    m = core.Mesh.bricks(n, n, n)
+    d = m.add_dof(3, core.HEX20)
+    integ = core.Integrand.make(core.MB_LOCAL_DAMAGE, 3, E=30000.0, nu=0.2, damage_application=core.FULL,
+                                kappa0=1e-4, beta=100.0, alpha=0.99, k=10.0)
+    P = core.Problem(m, 3, [d], integ)
+    cons = _cat(_component(m, d, 3, m.nodes_at_axis(d, 2, 0.0), [0, 1, 2], 0.0, 0.0),
+                _component(m, d, 3, m.nodes_at_axis(d, 2, 1.0), [2], 0.0, u_end))
+    return m, [d], P, cons

@@ -1,0 +1,252 @@
+"""GPU parity of the CUDA path against the oracle (CPU restatement of NuTo), through the C ABI.
+
+Tolerances: CSR pattern and DOF numbering bit-exact; FP64 residual and FP64 tangent values <= 1e-12 relative to
+the largest entry; FP32 tangent values <= 2e-6 relative to the largest entry; displacements of converged
+load steps <= 1e-8 (FP64 path) and <= 1e-6 (FP32 tangent / FP32 Krylov path) relative to the largest
+displacement.
+"""
+
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+from oracle import setups as osetups
+from oracle.quasistatic import QuasistaticOracle
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FP64_REL = 1e-12
+FP32_REL = 2e-6
+
+
+def _torch():
+    import torch
+
+    assert torch.cuda.is_available(), "these tests need a CUDA GPU"
+    return torch
+
+
+def _build(kind, n):
+    from nuto_gb300 import configs
+
+    if kind == "quad4":
+        s = configs.quad4_elastic(n)
+        o = osetups.quad4_elastic(n)
+    elif kind == "hex8gd":
+        s = configs.hex8_gradient_damage(n)
+        o = osetups.hex8_gradient_damage(n)
+    else:
+        s = configs.hex20_local_damage(n)
+        o = osetups.hex20_local_damage(n)
+    g = s.build_gpu()
+    return s, g, o
+
+
+def _state(P, rng, scale):
+    u = rng.uniform(-1.0, 1.0, P.n_dofs) * scale
+    return u
+
+
+def _oracle_csr(P, u):
+    K = P.build_matrix_scipy(u).tocsr()
+    K.sort_indices()
+    return K
+
+
+CASES = [("quad4", 5), ("hex8gd", 3), ("hex20", 2)]
+
+
+@pytest.mark.parametrize("kind,n", CASES)
+def test_pattern_bit_exact(kind, n):
+    _torch()
+    s, g, (om, layers, P, cons) = _build(kind, n)
+    rp, ci = g.pattern()
+    cp, ri, _ = P.build_matrix_csc(np.zeros(P.n_dofs))
+    assert g.n_dofs == P.n_dofs
+    assert np.array_equal(rp, cp)
+    assert np.array_equal(ci, ri)
+
+
+def _damage_state(kind, P, rng):
+    if kind == "hex8gd":
+        u = _state(P, rng, 2e-4)
+        nd = 3 * P.mesh.layer_num_nodes(0)
+        u[nd:] = rng.uniform(0.0, 4e-4, P.n_dofs - nd)  # eeq around and above kappa0
+        kappa = rng.uniform(0.0, 3e-4, (P.n_el, P.n_ip))
+    elif kind == "hex20":
+        u = _state(P, rng, 3e-4)
+        kappa = rng.uniform(0.0, 3e-4, (P.n_el, P.n_ip))
+    else:
+        u = _state(P, rng, 1e-3)
+        kappa = None
+    return u, kappa
+
+
+@pytest.mark.parametrize("kind,n", CASES)
+def test_build_vector_fp64(kind, n):
+    torch = _torch()
+    s, g, (om, layers, P, cons) = _build(kind, n)
+    rng = np.random.default_rng(7)
+    u, kappa = _damage_state(kind, P, rng)
+    if kappa is not None:
+        P.kappa = kappa
+        g.history = kappa
+    f_ref = P.build_vector(u)
+    f = g.build_vector(u).cpu().numpy()
+    assert np.abs(f - f_ref).max() <= FP64_REL * np.abs(f_ref).max()
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("kind,n", CASES)
+@pytest.mark.parametrize("precision", [64, 32])
+def test_build_matrix(kind, n, precision):
+    torch = _torch()
+    s, g, (om, layers, P, cons) = _build(kind, n)
+    rng = np.random.default_rng(11)
+    u, kappa = _damage_state(kind, P, rng)
+    if kappa is not None:
+        P.kappa = kappa
+        g.history = kappa
+    K = _oracle_csr(P, u)
+    v = g.build_matrix(u, precision).double().cpu().numpy()
+    rp, ci = g.pattern()
+    assert np.array_equal(rp, K.indptr) and np.array_equal(ci, K.indices)
+    tol = FP64_REL if precision == 64 else FP32_REL
+    assert np.abs(v - K.data).max() <= tol * np.abs(K.data).max()
+    torch.cuda.synchronize()
+
+
+def test_brick8n_golden_on_gpu():
+    """applications/integrationtests/mechanics/results/Brick8N*.txt through the GPU kernels."""
+    _torch()
+    from nuto_gb300 import mesh as M
+    from nuto_gb300._lib import MB_LINEAR_ELASTIC
+
+    gold = json.load(open(os.path.join(HERE, "golden", "brick8n.json")))
+    st = gold["setup"]
+    m = M.MeshFem(3, M.HEX8, np.array(st["coords"], float), np.arange(8)[None, :])
+    d = M.add_dof_interpolation(m, 3)
+    from nuto_gb300 import GpuCellGroup
+
+    g = GpuCellGroup(m, [d], 2)
+    g.build_pattern()
+    g.set_integrand(kind=MB_LINEAR_ELASTIC, dim=3, E=st["E"], nu=st["nu"])
+    u = np.zeros(24)
+    for nd in st["displaced_nodes"]:
+        u[3 * nd:3 * nd + 3] = st["displacement"]
+    f = g.build_vector(u).cpu().numpy()
+    v = g.build_matrix(u, 64).cpu().numpy()
+    rp, ci = g.pattern()
+    K = sp.csr_matrix((v, ci, rp), shape=(24, 24)).toarray()
+    Kg = np.array(gold["K_e"])
+    fg = np.array(gold["f_e"])
+    assert np.abs(K - Kg).max() <= 1e-11 * np.abs(Kg).max()
+    assert np.abs(f - fg).max() <= 1e-11 * np.abs(fg).max()
+
+
+def test_cell_scatter_known_answer():
+    """test/mechanics/cell/SimpleAssembler.cpp:57-114 idea: two cells sharing DOFs, caller-given cell results."""
+    _torch()
+    from nuto_gb300 import GpuCellGroup
+    from nuto_gb300 import mesh as M
+
+    m = M.create_quads(2, 1)
+    d = M.add_dof_interpolation(m, 1)
+    g = GpuCellGroup(m, [d], 2)
+    n, nnz = g.build_pattern()
+    conn = m.layers[d].conn
+    fe = np.array([[11.0, 22.0, 33.0, 44.0], [11.0, 22.0, 33.0, 44.0]])
+    f = g.assemble_cell_vectors(fe).cpu().numpy()
+    ref = np.zeros(n)
+    for c in range(2):
+        np.add.at(ref, conn[c], fe[c])
+    assert np.array_equal(f, ref)
+    ke = np.array([[[10 * i + j for j in range(1, 5)] for i in range(1, 5)]] * 2, dtype=float)
+    v = g.assemble_cell_matrices(ke).cpu().numpy()
+    rp, ci = g.pattern()
+    K = sp.csr_matrix((v, ci, rp), shape=(n, n)).toarray()
+    Kref = np.zeros((n, n))
+    for c in range(2):
+        Kref[np.ix_(conn[c], conn[c])] += ke[c]
+    assert np.array_equal(K, Kref)
+    assert nnz == 4 * 4 * 2 - 4  # shared edge: 2 x 2 entries counted once
+
+
+@pytest.mark.parametrize("kind,n", [("hex8gd", 3), ("hex20", 2)])
+def test_update_history(kind, n):
+    _torch()
+    s, g, (om, layers, P, cons) = _build(kind, n)
+    rng = np.random.default_rng(5)
+    u, kappa = _damage_state(kind, P, rng)
+    P.kappa = kappa
+    g.history = kappa
+    P.update_history(u)
+    g.update_history(u)
+    assert np.abs(g.history - P.kappa).max() <= 1e-15 + 1e-13 * np.abs(P.kappa).max()
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_linear_solve_quad4(precision):
+    _torch()
+    s, g, (om, layers, P, cons) = _build("quad4", 12)
+    u0 = np.zeros(P.n_dofs)
+    K = _oracle_csr(P, u0)
+    vals = g.build_matrix(u0, precision)
+    rng = np.random.default_rng(3)
+    b = rng.uniform(-1, 1, P.n_dofs)
+    dep = cons[0]
+    indep = np.setdiff1d(np.arange(P.n_dofs), dep)
+    x, it, rel, ok = g.solve(vals, b, precision=precision, rtol=1e-10)
+    assert ok, (it, rel)
+    import scipy.sparse.linalg as spla
+
+    y = spla.spsolve(K[indep][:, indep].tocsc(), b[indep])
+    xr = np.zeros(P.n_dofs)
+    xr[indep] = y
+    xg = x.cpu().numpy()
+    assert np.abs(xg[dep]).max() == 0.0
+    assert np.abs(xg - xr).max() <= 1e-8 * np.abs(xr).max()
+
+
+def _run_steps(kind, n, precision, steps, t_end, tol=1e-10):
+    s, g, (om, layers, P, cons) = _build(kind, n)
+    Q = QuasistaticOracle(P, cons[0], cons[1], cons[2], tolerance=tol, max_iterations=20)
+    g.set_state(None, 0.0, True)
+    opts = g.default_options(precision=precision, newton_rtol=0.0, newton_atol=tol,
+                             krylov_rtol=1e-12 if precision == 64 else 1e-5, max_newton=30, max_krylov=50000)
+    out = []
+    for k in range(1, steps + 1):
+        t = t_end * k / steps
+        Q.do_step(t)
+        g.do_step(t, opts)
+        x, tg = g.get_state()
+        out.append((Q.x.copy(), x.copy(), Q.P.kappa.copy(), g.history.copy(), g.stats()))
+        assert tg == t
+    return out
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_quasistatic_quad4_elastic(precision):
+    _torch()
+    res = _run_steps("quad4", 10, precision, 1, 1.0, tol=1e-9)
+    xo, xg, _, _, st = res[-1]
+    rel = np.abs(xg - xo).max() / np.abs(xo).max()
+    assert rel <= (1e-8 if precision == 64 else 1e-6), (rel, st)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_quasistatic_hex8_gradient_damage(precision):
+    """Eight load steps of the gradient-damage beam (damage starts after step 4); displacement, eeq and the
+    kappa history follow the oracle's direct-solve Newton."""
+    _torch()
+    res = _run_steps("hex8gd", 3, precision, 8, 0.4)
+    for k, (xo, xg, ko, kg, st) in enumerate(res):
+        rel = np.abs(xg - xo).max() / np.abs(xo).max()
+        assert rel <= (1e-8 if precision == 64 else 1e-6), (k, rel, st)
+        assert np.abs(kg - ko).max() <= (1e-8 if precision == 64 else 1e-6) * max(np.abs(ko).max(), 1e-4)
+    assert res[-1][2].max() > 1e-4  # the last steps are in the damaged regime
