@@ -36,9 +36,10 @@ class GpuCellGroup:
         h = ctypes.c_void_p()
         if stream is None:
             # run on torch's current stream so that tensors produced by torch are ordered before our kernels
+            # (handle 0 is the legacy default stream, passed as cudaStreamLegacy == 1)
             torch = _torch()
-            stream = torch.cuda.current_stream(device).cuda_stream
-        rc = self.L.nuto_gpu_create(ctypes.byref(h), device, ctypes.c_void_p(stream) if stream else None)
+            stream = torch.cuda.current_stream(device).cuda_stream or 1
+        rc = self.L.nuto_gpu_create(ctypes.byref(h), device, ctypes.c_void_p(stream))
         if rc != _lib.OK:
             raise _lib.NutoGpuError(rc, "nuto_gpu_create failed (no CUDA device?)")
         self.h = h
