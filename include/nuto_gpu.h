@@ -134,6 +134,7 @@ typedef struct nuto_gpu_stats
 /* ---- context ----------------------------------------------------------------------------------------- */
 int nuto_gpu_create(nuto_gpu_ctx** ctx, int device, void* cuda_stream /* cudaStream_t or NULL */);
 int nuto_gpu_destroy(nuto_gpu_ctx* ctx);
+/* message of the last failure of ctx; with ctx == NULL the last failed nuto_gpu_create of this thread */
 const char* nuto_gpu_last_error(const nuto_gpu_ctx* ctx);
 int nuto_gpu_synchronize(nuto_gpu_ctx* ctx);
 int nuto_gpu_version(void);

@@ -102,18 +102,24 @@ _lock = threading.Lock()
 _lib = None
 
 
+def variant():
+    """NUTO_GPU_VARIANT=checked selects the range-checked debugging build of the same library."""
+    return os.environ.get("NUTO_GPU_VARIANT", "release")
+
+
 def load(build_if_missing=True):
     """Loads libnuto_gb300.so (building it with nvcc first if it is missing or stale)."""
     global _lib
     with _lock:
         if _lib is None:
-            if build_if_missing:
-                from . import build as _build
+            from . import build as _build
 
-                _build.build()
-            if not os.path.exists(LIB_PATH):
-                raise RuntimeError("libnuto_gb300.so is missing: run nuto_gb300/build.py")
-            L = ctypes.CDLL(LIB_PATH)
+            path = _build.lib_path(variant())
+            if build_if_missing:
+                _build.build(variant=variant())
+            if not os.path.exists(path):
+                raise RuntimeError("%s is missing: run nuto_gb300/build.py" % os.path.basename(path))
+            L = ctypes.CDLL(path)
             for name, (res, args) in SIGNATURES.items():
                 fn = getattr(L, name)
                 fn.restype = res

@@ -41,7 +41,8 @@ class GpuCellGroup:
             stream = torch.cuda.current_stream(device).cuda_stream or 1
         rc = self.L.nuto_gpu_create(ctypes.byref(h), device, ctypes.c_void_p(stream))
         if rc != _lib.OK:
-            raise _lib.NutoGpuError(rc, "nuto_gpu_create failed (no CUDA device?)")
+            msg = self.L.nuto_gpu_last_error(None)
+            raise _lib.NutoGpuError(rc, "nuto_gpu_create: " + (msg.decode() if msg else ""))
         self.h = h
         self._call("nuto_gpu_set_cells", mesh.dim, mesh.geo_interp, mesh.coords.shape[0], _ptr(mesh.coords),
                    mesh.num_cells, _ptr(mesh.conn), gauss_points_per_direction)

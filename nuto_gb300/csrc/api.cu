@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <array>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <omp.h>
@@ -19,6 +20,16 @@ namespace nuto_gpu
 Ctx::~Ctx()
 {
     FreeSolverWork(*this);
+}
+
+bool SyncCheck(const Ctx& c)
+{
+    return c.syncCheck;
+}
+
+cudaStream_t StreamOf(const Ctx& c)
+{
+    return c.stream;
 }
 
 // Gauss points: Legendre roots by Newton iteration from cos guesses and weights 2 / ((1 - x^2) P_n'(x)^2)
@@ -447,6 +458,9 @@ static void RebuildConstraints(Ctx& c)
 // ------------------------------------------------------------------------------------------------------------
 // C ABI
 // ------------------------------------------------------------------------------------------------------------
+// message of the last failure that had no context to hold it (nuto_gpu_create)
+static thread_local std::string tlsError;
+
 template <typename F>
 static int Guard(nuto_gpu_ctx* ctx, F&& f)
 {
@@ -455,17 +469,12 @@ static int Guard(nuto_gpu_ctx* ctx, F&& f)
     try
     {
         int dev = -1;
-        cudaGetDevice(&dev);
+        NG_CUDA(cudaGetDevice(&dev));
         if (dev != ctx->device)
             NG_CUDA(cudaSetDevice(ctx->device));
-        const int rc = f();
-        if (rc == NUTO_GPU_OK)
-        {
-            const cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess)
-                throw Error{NUTO_GPU_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e)};
-        }
-        return rc;
+        // a pending (non-sticky) error of an earlier call must not be reported as ours
+        cudaGetLastError();
+        return f();
     }
     catch (const Error& e)
     {
@@ -497,13 +506,22 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
         return NUTO_GPU_EINVAL;
     *out = nullptr;
     int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n)
+    const cudaError_t ce = cudaGetDeviceCount(&n);
+    if (ce != cudaSuccess || device < 0 || device >= n)
     {
+        tlsError = ce != cudaSuccess ? std::string("cudaGetDeviceCount: ") + cudaGetErrorString(ce)
+                                     : "device " + std::to_string(device) + " out of range";
         cudaGetLastError();
         return NUTO_GPU_ECUDA;
     }
     auto* c = new nuto_gpu_ctx();
     c->device = device;
+#ifdef NUTO_GPU_CHECKED
+    c->syncCheck = true;
+#else
+    const char* sc = std::getenv("NUTO_GPU_SYNC_CHECK");
+    c->syncCheck = sc && sc[0] == '1';
+#endif
     const int rc = Guard(c, [&] {
         NG_CUDA(cudaSetDevice(device));
         NG_CUDA(cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device));
@@ -518,6 +536,7 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
     });
     if (rc != NUTO_GPU_OK)
     {
+        tlsError = c->err;
         delete c;
         return rc;
     }
@@ -529,19 +548,23 @@ int nuto_gpu_destroy(nuto_gpu_ctx* ctx)
 {
     if (!ctx)
         return NUTO_GPU_OK;
-    cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    int rc = NUTO_GPU_OK;
+    if (cudaSetDevice(ctx->device) != cudaSuccess || cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        rc = NUTO_GPU_ECUDA;
     const bool own = ctx->ownStream;
     cudaStream_t s = ctx->stream;
     delete ctx;
-    if (own)
-        cudaStreamDestroy(s);
-    return NUTO_GPU_OK;
+    if (own && cudaStreamDestroy(s) != cudaSuccess)
+        rc = NUTO_GPU_ECUDA;
+    if (rc != NUTO_GPU_OK)
+        tlsError = std::string("nuto_gpu_destroy: ") + cudaGetErrorString(cudaGetLastError());
+    cudaGetLastError();
+    return rc;
 }
 
 const char* nuto_gpu_last_error(const nuto_gpu_ctx* ctx)
 {
-    return ctx ? ctx->err.c_str() : "null context";
+    return ctx ? ctx->err.c_str() : tlsError.c_str();
 }
 
 int nuto_gpu_synchronize(nuto_gpu_ctx* ctx)

@@ -119,7 +119,7 @@ struct MaxI
 
 // ---- integration-point geometry cache (Jacobian.h:16-48, CellIpData.h:108-113) -------------------------------
 template <int DIM, int NG, int ND, int NIP>
-__global__ void __launch_bounds__(128) k_geometry(int64_t nCells, const double* __restrict__ coords,
+__global__ void __launch_bounds__(128) k_geometry(int64_t nCells, int64_t nCoordValues, const double* __restrict__ coords,
                                                   const int32_t* __restrict__ geoConnT,
                                                   const double* __restrict__ tables, int tabW, int tabDNg,
                                                   int tabDNd, int stride, double* __restrict__ geo64,
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(128) k_geometry(int64_t nCells, const double* 
         const int32_t node = geoConnT[static_cast<int64_t>(n) * nCells + e];
 #pragma unroll
         for (int d = 0; d < DIM; ++d)
-            X[n][d] = coords[static_cast<int64_t>(node) * DIM + d];
+            X[n][d] = coords[NG_IDX(static_cast<int64_t>(node) * DIM + d, nCoordValues, 1)];
     }
     const double* dNg = tables + tabDNg + q * NG * 3;
     double J[DIM][DIM];
@@ -209,10 +209,10 @@ void BuildGeometryCache(Ctx& c)
     DispatchCfg(c, [&](auto cfg) {
         using C = decltype(cfg);
         k_geometry<C::dim, C::ng, C::nd, C::nip><<<blocks, 128, 0, c.stream>>>(
-                c.nCells, c.dCoords.p, c.dGeoConnT.p, c.dTables.p, c.tabW, c.tabDN[c.geoInterp], c.tabDN[D.interp],
+                c.nCells, static_cast<int64_t>(c.dCoords.n), c.dCoords.p, c.dGeoConnT.p, c.dTables.p, c.tabW, c.tabDN[c.geoInterp], c.tabDN[D.interp],
                 c.geoStride, c.dGeo64.p, c.dGeo32.p);
     });
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "k_geometry");
     c.haveGeo = true;
 }
 
@@ -221,12 +221,16 @@ static CellArgs MakeCellArgs(Ctx& c)
     CellArgs a{};
     const Slot& D = c.slots[c.prm.disp_slot];
     a.nCells = c.nCells;
+    a.nNodesD = D.nNodes;
+    a.nDofs = c.nDofs;
+    a.geoSize = static_cast<int64_t>(c.dGeo64.n);
     a.connD = D.dConnT.p;
     a.gdofD = D.dGdof.p;
     a.tabN_D = c.dTables.p + c.tabN[D.interp];
     if (c.prm.kind == NUTO_GPU_GRADIENT_DAMAGE)
     {
         const Slot& E = c.slots[c.prm.eeq_slot];
+        a.nNodesE = E.nNodes;
         a.connE = E.dConnT.p;
         a.gdofE = E.dGdof.p;
         a.tabN_E = c.dTables.p + c.tabN[E.interp];
@@ -262,12 +266,12 @@ __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const
         const int64_t e = cell0 + cl;
         if (e >= n)
             continue;
-        const int64_t g = a.gdofD[a.connD[static_cast<int64_t>(nd) * n + e]];
+        const int64_t g = a.gdofD[NG_IDX(a.connD[static_cast<int64_t>(nd) * n + e], a.nNodesD, 2)];
 #pragma unroll
         for (int c = 0; c < DIM; ++c)
-            sU[cl][nd][c] = u[g + c];
+            sU[cl][nd][c] = u[NG_IDX(g + c, a.nDofs, 3)];
         if (GD)
-            sE[cl][nd] = u[a.gdofE[a.connE[static_cast<int64_t>(nd) * n + e]]];
+            sE[cl][nd] = u[NG_IDX(a.gdofE[NG_IDX(a.connE[static_cast<int64_t>(nd) * n + e], a.nNodesE, 4)], a.nDofs, 5)];
     }
     __syncthreads();
 
@@ -277,7 +281,8 @@ __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const
         const int64_t e = cell0 + cl;
         if (e >= n)
             continue;
-        const double* G = a.geo64 + static_cast<int64_t>(q) * a.geoStride * n + e;
+        const int64_t G0 = static_cast<int64_t>(q) * a.geoStride * n + e;
+        const double* G = a.geo64 + NG_IDX(G0, a.geoSize, 6);
         const double wdj = G[0];
         double H[DIM][DIM];
 #pragma unroll
@@ -312,7 +317,7 @@ __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const
         }
         double eps[VD], sig[VD];
         StrainFromH<double, DIM>(H, eps);
-        const double kh = a.kappa[e * NIP + q];
+        const double kh = a.kappa[NG_IDX(e * NIP + q, n * NIP, 7)];
         if (KIND == NUTO_GPU_MB_LINEAR_ELASTIC)
             ElasticStress<double, DIM>(L, eps, sig);
         else if (KIND == NUTO_GPU_MB_LOCAL_DAMAGE)
@@ -351,7 +356,7 @@ __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const
 #pragma unroll 4
         for (int q = 0; q < NIP; ++q)
         {
-            const double* G = a.geo64 + static_cast<int64_t>(q) * a.geoStride * n + e;
+            const double* G = a.geo64 + NG_IDX(static_cast<int64_t>(q) * a.geoStride * n + e, a.geoSize, 6);
             double g[DIM], b[DIM];
 #pragma unroll
             for (int d = 0; d < DIM; ++d)
@@ -369,12 +374,12 @@ __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const
                 fe += s;
             }
         }
-        const int64_t g = a.gdofD[a.connD[static_cast<int64_t>(nd) * n + e]];
+        const int64_t g = a.gdofD[NG_IDX(a.connD[static_cast<int64_t>(nd) * n + e], a.nNodesD, 2)];
 #pragma unroll
         for (int c = 0; c < DIM; ++c)
-            atomicAdd(f + g + c, fu[c]);
+            atomicAdd(f + NG_IDX(g + c, a.nDofs, 8), fu[c]);
         if (GD)
-            atomicAdd(f + a.gdofE[a.connE[static_cast<int64_t>(nd) * n + e]], fe);
+            atomicAdd(f + NG_IDX(a.gdofE[NG_IDX(a.connE[static_cast<int64_t>(nd) * n + e], a.nNodesE, 4)], a.nDofs, 8), fe);
     }
 }
 
@@ -388,7 +393,7 @@ void LaunchResidual(Ctx& c, const double* u, double* f)
         const int blocks = static_cast<int>((c.nCells + CPB - 1) / CPB);
         k_residual<C::dim, C::nd, C::nip, C::kind><<<blocks, 128, 0, c.stream>>>(a, c.law, u, f);
     });
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "k_residual");
 }
 
 // ---- tangent: FP32 or FP64 values scattered into CSR ---------------------------------------------------------
@@ -443,24 +448,24 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
         const int64_t e = cell0 + cl;
         if (e >= n)
             continue;
-        const int32_t aD = a.connD[static_cast<int64_t>(nd) * n + e];
+        const int32_t aD = static_cast<int32_t>(NG_IDX(a.connD[static_cast<int64_t>(nd) * n + e], a.nNodesD, 2));
         const int64_t g = a.gdofD[aD];
         const int32_t bUU = S.blk[pUU][aD];
 #pragma unroll
         for (int c = 0; c < DIM; ++c)
         {
-            sU[cl][nd][c] = u[g + c];
-            const int64_t rs = S.rowPtr[g + c];
+            sU[cl][nd][c] = u[NG_IDX(g + c, a.nDofs, 3)];
+            const int64_t rs = S.rowPtr[NG_IDX(g + c, S.nRows, 9)];
             sBaseU[cl][nd][c] = rs + bUU;
             if (GD)
                 sBaseUE[cl][nd][c] = rs + S.blk[pUE][aD];
         }
         if (GD)
         {
-            const int32_t aE = a.connE[static_cast<int64_t>(nd) * n + e];
+            const int32_t aE = static_cast<int32_t>(NG_IDX(a.connE[static_cast<int64_t>(nd) * n + e], a.nNodesE, 4));
             const int64_t ge = a.gdofE[aE];
-            sE[cl][nd] = u[ge];
-            const int64_t rs = S.rowPtr[ge];
+            sE[cl][nd] = u[NG_IDX(ge, a.nDofs, 5)];
+            const int64_t rs = S.rowPtr[NG_IDX(ge, S.nRows, 9)];
             sBaseEU[cl][nd] = rs + S.blk[pEU][aE];
             sBaseEE[cl][nd] = rs + S.blk[pEE][aE];
         }
@@ -476,7 +481,7 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
         const int64_t e = cell0 + cl;
         if (e >= n)
             continue;
-        const int64_t idx = (static_cast<int64_t>(q) * a.geoStride + 1 + nd * DIM + d) * n + e;
+        const int64_t idx = NG_IDX((static_cast<int64_t>(q) * a.geoStride + 1 + nd * DIM + d) * n + e, a.geoSize, 6);
         if (sizeof(T) == 4)
             sG[cl][q][nd][d] = static_cast<T>(a.geo32[idx]);
         else
@@ -491,7 +496,7 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
         const int64_t e = cell0 + cl;
         if (e >= n)
             continue;
-        const int64_t widx = static_cast<int64_t>(q) * a.geoStride * n + e;
+        const int64_t widx = NG_IDX(static_cast<int64_t>(q) * a.geoStride * n + e, a.geoSize, 6);
         const T wdj = sizeof(T) == 4 ? static_cast<T>(a.geo32[widx]) : static_cast<T>(a.geo64[widx]);
         T H[DIM][DIM];
 #pragma unroll
@@ -521,7 +526,7 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
         }
         T eps[VD];
         StrainFromH<T, DIM>(H, eps);
-        const T kh = static_cast<T>(a.kappa[e * NIP + q]);
+        const T kh = static_cast<T>(a.kappa[NG_IDX(e * NIP + q, n * NIP, 7)]);
         T lam, mu;
         if (KIND == NUTO_GPU_MB_LINEAR_ELASTIC)
         {
@@ -662,10 +667,10 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
 #pragma unroll
         for (int k = 0; k < DIM; ++k)
         {
-            T* row = vals + sBaseU[cl][ia][k] + DIM * rUU;
+            const int64_t row = sBaseU[cl][ia][k] + DIM * rUU;
 #pragma unroll
             for (int l = 0; l < DIM; ++l)
-                atomicAdd(row + l, kuu[k][l]);
+                atomicAdd(vals + NG_IDX(row + l, S.nnz, 10), kuu[k][l]);
         }
         if (GD)
         {
@@ -674,12 +679,12 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
             const int rEE = S.rank[pEE][ridx];
 #pragma unroll
             for (int k = 0; k < DIM; ++k)
-                atomicAdd(vals + sBaseUE[cl][ia][k] + rUE, kue[k]);
-            T* rowE = vals + sBaseEU[cl][ia] + DIM * rEU;
+                atomicAdd(vals + NG_IDX(sBaseUE[cl][ia][k] + rUE, S.nnz, 10), kue[k]);
+            const int64_t rowE = sBaseEU[cl][ia] + DIM * rEU;
 #pragma unroll
             for (int l = 0; l < DIM; ++l)
-                atomicAdd(rowE + l, keu[l]);
-            atomicAdd(vals + sBaseEE[cl][ia] + rEE, kee);
+                atomicAdd(vals + NG_IDX(rowE + l, S.nnz, 10), keu[l]);
+            atomicAdd(vals + NG_IDX(sBaseEE[cl][ia] + rEE, S.nnz, 10), kee);
         }
     }
 }
@@ -687,6 +692,8 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
 static ScatterArgs MakeScatterArgs(Ctx& c)
 {
     ScatterArgs s{};
+    s.nnz = c.nnz;
+    s.nRows = c.nDofs;
     s.rowPtr = c.dRowPtr.p;
     const int ns = static_cast<int>(c.slots.size());
     for (int p = 0; p < ns * ns; ++p)
@@ -713,7 +720,7 @@ static void LaunchTangentT(Ctx& c, const double* u, T* vals)
         k_tangent<T, C::dim, C::nd, C::nip, C::kind><<<blocks, TangentShape<C::nd, C::nip>::threads, 0, c.stream>>>(
                 a, c.law, s, dS * ns + dS, dS * ns + eS, eS * ns + dS, eS * ns + eS, u, vals);
     });
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "k_tangent");
 }
 
 void LaunchTangent(Ctx& c, const double* u, int precision, void* values)
@@ -736,16 +743,17 @@ __global__ void __launch_bounds__(128) k_history(CellArgs a, LawParams L, const 
         return;
     const int64_t e = it % n;
     const int q = static_cast<int>(it / n);
-    double& kh = a.kappa[e * NIP + q];
+    double& kh = a.kappa[NG_IDX(e * NIP + q, n * NIP, 7)];
     if (KIND == NUTO_GPU_GRADIENT_DAMAGE)
     {
         double eeq = 0;
         for (int nd = 0; nd < ND; ++nd)
-            eeq += a.tabN_D[q * ND + nd] * u[a.gdofE[a.connE[static_cast<int64_t>(nd) * n + e]]];
+            eeq += a.tabN_D[q * ND + nd] *
+                   u[NG_IDX(a.gdofE[NG_IDX(a.connE[static_cast<int64_t>(nd) * n + e], a.nNodesE, 4)], a.nDofs, 5)];
         kh = fmax(kh, eeq);
         return;
     }
-    const double* G = a.geo64 + static_cast<int64_t>(q) * a.geoStride * n + e;
+    const double* G = a.geo64 + NG_IDX(static_cast<int64_t>(q) * a.geoStride * n + e, a.geoSize, 6);
     double H[DIM][DIM];
 #pragma unroll
     for (int i = 0; i < DIM; ++i)
@@ -754,11 +762,11 @@ __global__ void __launch_bounds__(128) k_history(CellArgs a, LawParams L, const 
             H[i][j] = 0;
     for (int nd = 0; nd < ND; ++nd)
     {
-        const int64_t g = a.gdofD[a.connD[static_cast<int64_t>(nd) * n + e]];
+        const int64_t g = a.gdofD[NG_IDX(a.connD[static_cast<int64_t>(nd) * n + e], a.nNodesD, 2)];
 #pragma unroll
         for (int c = 0; c < DIM; ++c)
         {
-            const double uc = u[g + c];
+            const double uc = u[NG_IDX(g + c, a.nDofs, 3)];
 #pragma unroll
             for (int d = 0; d < DIM; ++d)
                 H[c][d] += uc * G[(1 + nd * DIM + d) * n];
@@ -781,7 +789,7 @@ void LaunchHistory(Ctx& c, const double* u)
         if constexpr (C::kind != NUTO_GPU_MB_LINEAR_ELASTIC)
             k_history<C::dim, C::nd, C::nip, C::kind><<<blocks, 128, 0, c.stream>>>(a, c.law, u);
     });
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "k_history");
 }
 
 // ---- scatter of caller-given cell results (SimpleAssembler scatter, SimpleAssembler.cpp:53-59, 118-137) -----
@@ -797,6 +805,7 @@ struct SlotViews
 {
     int ns;
     int nLocal;
+    int64_t nDofs;
     SlotView s[kMaxSlots];
 };
 
@@ -804,6 +813,7 @@ static SlotViews MakeSlotViews(const Ctx& c)
 {
     SlotViews v{};
     v.ns = static_cast<int>(c.slots.size());
+    v.nDofs = c.nDofs;
     int off = 0;
     for (int i = 0; i < v.ns; ++i)
     {
@@ -838,7 +848,7 @@ __global__ void k_cell_vectors(int64_t nCells, SlotViews v, const double* __rest
     int s, node, comp;
     LocalToSlot(v, i, s, node, comp);
     const int64_t g = v.s[s].gdof[v.s[s].connT[static_cast<int64_t>(node) * nCells + e]] + comp;
-    atomicAdd(f + g, fe[it]);
+    atomicAdd(f + NG_IDX(g, v.nDofs, 14), fe[it]);
 }
 
 template <typename T>
@@ -858,7 +868,8 @@ __global__ void k_cell_matrices(int64_t nCells, SlotViews v, ScatterArgs S, cons
     const int64_t row = v.s[sI].gdof[aI] + cI;
     const int p = sI * v.ns + sJ;
     const int rank = S.rank[p][static_cast<int64_t>(nI * v.s[sJ].nen + nJ) * nCells + e];
-    atomicAdd(vals + S.rowPtr[row] + S.blk[p][aI] + v.s[sJ].ncomp * rank + cJ, static_cast<T>(ke[it]));
+    const int64_t pos = S.rowPtr[NG_IDX(row, S.nRows, 9)] + S.blk[p][aI] + v.s[sJ].ncomp * rank + cJ;
+    atomicAdd(vals + NG_IDX(pos, S.nnz, 15), static_cast<T>(ke[it]));
 }
 
 void LaunchCellVectors(Ctx& c, const double* fe, double* f)
@@ -867,7 +878,7 @@ void LaunchCellVectors(Ctx& c, const double* fe, double* f)
     SlotViews v = MakeSlotViews(c);
     const int64_t items = c.nCells * v.nLocal;
     k_cell_vectors<<<static_cast<unsigned>((items + 255) / 256), 256, 0, c.stream>>>(c.nCells, v, fe, f);
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "k_cell_vectors");
 }
 
 void LaunchCellMatrices(Ctx& c, const double* ke, int precision, void* values)
@@ -886,7 +897,7 @@ void LaunchCellMatrices(Ctx& c, const double* ke, int precision, void* values)
         NG_CUDA(cudaMemsetAsync(values, 0, c.nnz * sizeof(double), c.stream));
         k_cell_matrices<double><<<blocks, 256, 0, c.stream>>>(c.nCells, v, s, ke, static_cast<double*>(values));
     }
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "k_cell_matrices");
 }
 
 } // namespace nuto_gpu

@@ -41,6 +41,64 @@ struct Error
             throw ::nuto_gpu::Error{code, msg};                                                                  \
     } while (0)
 
+// ---- checked builds ------------------------------------------------------------------------------------------
+// Compiled with -DNUTO_GPU_CHECKED, every kernel index into a caller or library buffer goes through NG_IDX: an
+// index outside [0, n) is recorded in a device flag (first violation wins) and replaced by 0, so the access
+// stays inside the buffer. The host reads the flag after every launch (AfterLaunch) and reports the site.
+struct CheckFlag
+{
+    int site;
+    long long index;
+    long long limit;
+};
+#ifdef NUTO_GPU_CHECKED
+static __device__ CheckFlag g_check; // one per translation unit (no relocatable device code)
+__device__ __forceinline__ long long CheckedIndex(long long i, long long n, int site)
+{
+    if (i >= 0 && i < n)
+        return i;
+    if (atomicCAS(&g_check.site, 0, site) == 0)
+    {
+        g_check.index = i;
+        g_check.limit = n;
+    }
+    return 0;
+}
+#define NG_IDX(i, n, site) ::nuto_gpu::CheckedIndex(static_cast<long long>(i), static_cast<long long>(n), site)
+#else
+#define NG_IDX(i, n, site) (i)
+#endif
+
+struct Ctx;
+bool SyncCheck(const Ctx& c);
+cudaStream_t StreamOf(const Ctx& c);
+
+// Checks the launch; with NUTO_GPU_SYNC_CHECK=1 in the environment (or a checked build) also synchronises the
+// stream and reports faults and index violations with the kernel name.
+static inline void AfterLaunch(Ctx& c, const char* kernel)
+{
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        throw Error{NUTO_GPU_ECUDA, std::string("launch of ") + kernel + ": " + cudaGetErrorString(e)};
+    if (!SyncCheck(c))
+        return;
+    const cudaError_t s = cudaStreamSynchronize(StreamOf(c));
+    if (s != cudaSuccess)
+        throw Error{NUTO_GPU_ECUDA, std::string("after ") + kernel + ": " + cudaGetErrorString(s)};
+#ifdef NUTO_GPU_CHECKED
+    CheckFlag f{};
+    NG_CUDA(cudaMemcpyFromSymbol(&f, g_check, sizeof(f)));
+    if (f.site != 0)
+    {
+        const CheckFlag zero{};
+        NG_CUDA(cudaMemcpyToSymbol(g_check, &zero, sizeof(zero)));
+        throw Error{NUTO_GPU_ECUDA, std::string("index check failed in ") + kernel + " at site " +
+                                        std::to_string(f.site) + ": index " + std::to_string(f.index) +
+                                        " outside [0, " + std::to_string(f.limit) + ")"};
+    }
+#endif
+}
+
 inline int NumNodes(int interp)
 {
     return interp == NUTO_GPU_QUAD4 ? 4 : (interp == NUTO_GPU_HEX8 ? 8 : (interp == NUTO_GPU_HEX20 ? 20 : -1));
@@ -50,12 +108,34 @@ inline int InterpDim(int interp)
     return interp == NUTO_GPU_QUAD4 ? 2 : 3;
 }
 
-// Device buffer owned by the context.
+// Device buffer owned by the context. Move-only: a copy would share the pointer and free it twice.
 template <typename T>
 struct DBuf
 {
     T* p = nullptr;
     size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept
+        : p(o.p)
+        , n(o.n)
+    {
+        o.p = nullptr;
+        o.n = 0;
+    }
+    DBuf& operator=(DBuf&& o) noexcept
+    {
+        if (this != &o)
+        {
+            free();
+            p = o.p;
+            n = o.n;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
     void alloc(size_t count)
     {
         free();
@@ -189,6 +269,7 @@ struct Ctx
     nuto_gpu_stats stats{};
 
     SolverWork* work = nullptr;
+    bool syncCheck = false; // NUTO_GPU_SYNC_CHECK=1 or a checked build
 
     ~Ctx();
 };
@@ -210,6 +291,7 @@ void FreeSolverWork(Ctx& c);
 struct CellArgs
 {
     int64_t nCells;
+    int64_t nNodesD, nNodesE, nDofs, geoSize; // buffer extents for checked builds
     const int32_t* connD; // planar [n][cell]
     const int32_t* connE;
     const int64_t* gdofD; // per node: combined index of component 0
@@ -224,6 +306,7 @@ struct CellArgs
 
 struct ScatterArgs
 {
+    int64_t nnz, nRows; // buffer extents for checked builds
     const int64_t* rowPtr;
     const uint8_t* rank[kMaxSlots * kMaxSlots];
     const int32_t* blk[kMaxSlots * kMaxSlots];

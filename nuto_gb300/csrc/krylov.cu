@@ -109,7 +109,7 @@ enum Fin
 // y = A x on the constrained operator (dependent rows: y = x), W lanes per row; optionally acc0 += w0.y and
 // acc1 += y.y, then the last block applies a finalize action.
 template <typename TV, typename TX, int W, int NDOT>
-__global__ void __launch_bounds__(kBS) k_spmv(int64_t n, const int64_t* __restrict__ rowPtr,
+__global__ void __launch_bounds__(kBS) k_spmv(int64_t n, int64_t nnz, const int64_t* __restrict__ rowPtr,
                                                const int32_t* __restrict__ col, const TV* __restrict__ val,
                                                const uint8_t* __restrict__ mask, const TX* __restrict__ x,
                                                TX* __restrict__ y, const TX* __restrict__ w0, double* sc, int* st,
@@ -130,7 +130,10 @@ __global__ void __launch_bounds__(kBS) k_spmv(int64_t n, const int64_t* __restri
         {
             const int64_t end = rowPtr[row + 1];
             for (int64_t k = rowPtr[row] + lane; k < end; k += W)
-                sum += static_cast<TX>(val[k]) * x[col[k]];
+            {
+                const int64_t kk = NG_IDX(k, nnz, 12);
+                sum += static_cast<TX>(val[kk]) * x[NG_IDX(col[kk], n, 13)];
+            }
         }
     }
 #pragma unroll
@@ -482,8 +485,8 @@ static void SpmvLaunch(Ctx& c, const TV* vals, const TX* x, TX* y, const TX* w0,
         constexpr int W = decltype(wtag)::value;
         const int64_t threads = n * W;
         const unsigned blocks = static_cast<unsigned>((threads + kBS - 1) / kBS);
-        k_spmv<TV, TX, W, NDOT><<<blocks, kBS, 0, c.stream>>>(n, c.dRowPtr.p, c.dColIdx.p, vals, mask, x, y, w0, sc,
-                                                              st, fin);
+        k_spmv<TV, TX, W, NDOT><<<blocks, kBS, 0, c.stream>>>(n, c.nnz, c.dRowPtr.p, c.dColIdx.p, vals, mask, x, y,
+                                                              w0, sc, st, fin);
     };
     if (avg < 6)
         go(std::integral_constant<int, 4>{});
@@ -521,7 +524,7 @@ void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double
     else
         SpmvLaunch<double, double, 0>(c, static_cast<const double*>(vals), x, y, nullptr, nullptr, nullptr, FIN_NONE,
                                       w.zeroMask.p);
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "krylov");
 }
 
 // Runs one Krylov solve of the constrained system with values `vals` (type TV) in arithmetic T, right-hand side
@@ -553,7 +556,7 @@ static int KrylovSolve(Ctx& c, bool pcg, const TV* vals, const double* b, double
     else
         k_krylov_init<T, false><<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, V.x.p, V.r.p, V.rh.p, V.p.p, V.v.p,
                                                              V.z.p, V.dinv.p, sc, st);
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "krylov");
     const int chunk = 16;
     int done = 0;
     int state = RUN;
@@ -577,7 +580,7 @@ static int KrylovSolve(Ctx& c, bool pcg, const TV* vals, const double* b, double
                 k_bicg_x<T><<<grid, kBS, 0, c.stream>>>(n, V.x.p, V.r.p, V.rh.p, V.ph.p, V.s.p, V.sh.p, V.t.p, sc, st);
             }
         }
-        NG_CUDA(cudaGetLastError());
+        AfterLaunch(c, "krylov");
         done += nIt;
         NG_CUDA(cudaMemcpyAsync(w.hStat, st, ST_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         NG_CUDA(cudaMemcpyAsync(w.hScal, sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -598,7 +601,7 @@ static int KrylovSolve(Ctx& c, bool pcg, const TV* vals, const double* b, double
         throw Error{NUTO_GPU_ENAN, "non-finite value in the Krylov iteration"};
     // breakdown or iteration cap: keep the iterate (Newton refines it) but report non-convergence by the rel value
     k_unscale<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, c.stream>>>(n, V.x.p, sc, x64, addToX ? 1 : 0);
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "krylov");
     return state;
 }
 
@@ -624,7 +627,7 @@ __global__ void k_residual64(int64_t n, const uint8_t* __restrict__ mask, const 
 void Residual64(Ctx& c, const double* b, const double* kx, double* r)
 {
     k_residual64<<<static_cast<unsigned>((c.nDofs + 255) / 256), 256, 0, c.stream>>>(c.nDofs, c.dMask.p, b, kx, r);
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "krylov");
 }
 
 bool UsePcg(const Ctx& c, int method)

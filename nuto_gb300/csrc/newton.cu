@@ -167,13 +167,13 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
                 c.nDep, c.dDepIdx.p, c.dDepA.p, c.dDepB.p, tOld, tNew, w.db.p);
     SpmvFull64(c, o.precision, K, w.db.p, w.tmp.p);
     k_masked_sum<<<gb, 256, 0, c.stream>>>(n, c.dMask.p, w.f.p, w.tmp.p, w.rhs.p);
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "newton vector kernels");
     const double refNorm = MaskedNorm(c, w.rhs.p);
     S.reference_residual = refNorm;
     const double tol = std::max(o.newton_atol, o.newton_rtol * refNorm);
     solve(w.rhs.p, w.dx.p);
     k_update<<<gb, 256, 0, c.stream>>>(n, x, w.dx.p, 1.0, w.db.p, w.xs.p);
-    NG_CUDA(cudaGetLastError());
+    AfterLaunch(c, "newton vector kernels");
 
     // Newton-Raphson with line search on the trial state
     double nr = residual(w.xs.p);

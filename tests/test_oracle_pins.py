@@ -377,11 +377,12 @@ def test_build_vector_matches_cellwise_scatter(oracle_lib):
     for c in range(P.n_el):
         fe, _ = P.cell_integrate(c, u)
         np.add.at(ref, P.cell_dofs(c), fe)
-    assert np.allclose(f, ref, rtol=1e-13, atol=1e-18)
+    # thread-order summation (SimpleAssembler.cpp:61-62): compare relative to the largest entry
+    assert np.abs(f - ref).max() <= 1e-13 * np.abs(ref).max()
     K = P.build_matrix_scipy(u).toarray()
     Kref = np.zeros((P.n_dofs, P.n_dofs))
     for c in range(P.n_el):
         _, Ke = P.cell_integrate(c, u)
         idx = P.cell_dofs(c)
         Kref[np.ix_(idx, idx)] += Ke
-    assert np.allclose(K, Kref, rtol=1e-13, atol=1e-18)
+    assert np.abs(K - Kref).max() <= 1e-13 * np.abs(Kref).max()
