@@ -598,7 +598,15 @@ static int KrylovSolve(Ctx& c, bool pcg, const TV* vals, const double* b, double
         *relres = rel;
     c.stats.krylov_iterations += it;
     if (state == NONFINITE)
-        throw Error{NUTO_GPU_ENAN, "non-finite value in the Krylov iteration"};
+    {
+        char buf[256];
+        std::snprintf(buf, sizeof(buf),
+                      "non-finite value in the Krylov iteration (%s, iteration %d, rho %.3e, alpha %.3e, omega %.3e, "
+                      "beta %.3e, |r|^2 %.3e)",
+                      pcg ? "PCG" : "BiCGStab", it, w.hScal[SC_RHO], w.hScal[SC_ALPHA], w.hScal[SC_OMEGA],
+                      w.hScal[SC_BETA], w.hScal[SC_RR]);
+        throw Error{NUTO_GPU_ENAN, buf};
+    }
     // breakdown or iteration cap: keep the iterate (Newton refines it) but report non-convergence by the rel value
     k_unscale<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, c.stream>>>(n, V.x.p, sc, x64, addToX ? 1 : 0);
     AfterLaunch(c, "krylov");
