@@ -1,0 +1,381 @@
+"""Benchmark: quasistatic load steps of the 3D implicit gradient-damage beam (Hex8, 64^3 cells, 1.1 M DOFs) on GB300.
+
+A step is one load step of the 20-step schedule to u_z = 2e-3 m (QuasistaticSolver::DoStep: trial state, Newton
+with line search to |C^T r| <= 1e-8 |C^T (r + K db)|, history update), run through the C ABI with the state and
+history resident in HBM. W warm-up load steps from rest come first, then exactly K timed load steps.
+
+value      DOFs x tangent solves / s of the mixed-precision path (FP32 tangent + FP32 GMRES, FP64 residual): the
+           assembled-and-solved DOFs per second; ms_per_step is the time of one load step and newton_step_ms the
+           time of one tangent assembly + Krylov solve + residual update.
+fp64       the same K load steps on the plain FP64 GPU path, from the same warm state, and the speed-up.
+e2e        the same metric through nuto_gpu_do_step_host with the state vector and history in pinned host memory
+           (copied in and out every step).
+roofline   the Krylov SpMV (dominant kernel): algorithmic bytes per launch / mean CUDA-event duration.
+cpu_baseline / --impl reference
+           the oracle (CPU restatement of NuTo's assembly, OpenMP) plus scipy SuperLU as the stand-in for
+           Eigen::SparseLU, timed on a bounded sample of the same problem on the host cores.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton-step time & assembled DOFs/s, FP32-tangent vs FP64 GPU at 1e-8 residual"
+LOAD_STEPS = 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--size", type=int, default=64)
+    p.add_argument("--skip-fp64", action="store_true")
+    p.add_argument("--skip-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.idx)], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names[1:], f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gpu_index(local_rank):
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        ids = [v for v in vis.split(",") if v.strip()]
+        if local_rank < len(ids) and ids[local_rank].strip().isdigit():
+            return int(ids[local_rank])
+    return local_rank
+
+
+def spmv_bytes(n_dofs, nnz, value_bytes):
+    # values + column indices + row pointers + mask + x gather (compulsory once) + y write
+    return nnz * (value_bytes + 4) + (n_dofs + 1) * 8 + n_dofs * (1 + 2 * value_bytes)
+
+
+def tangent_bytes(setup, nnz, value_bytes):
+    """Compulsory traffic of one tangent assembly: values written once, connectivity, coordinates, DOF values and
+    history read once."""
+    m = setup.mesh
+    conn = sum(m.layers[l].conn.size for l in setup.layers) * 4 + m.conn.size * 4
+    n_ip = setup.gauss ** m.dim
+    return nnz * value_bytes + conn + m.coords.size * 8 + setup.n_dofs * 8 + m.num_cells * n_ip * 8
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        return json.load(open(path))
+    return {}
+
+
+def run_steps(g, opts, t_values, torch):
+    agg = {"matrix_assemblies": 0, "newton_iterations": 0, "krylov_iterations": 0, "ms_spmv": 0.0,
+           "spmv_launches": 0, "kernel_launches": 0, "ms_assemble_matrix": 0.0, "ms_assemble_vector": 0.0,
+           "ms_krylov": 0.0, "residual_evaluations": 0}
+    for t in t_values:
+        g.do_step(t, opts)
+        st = g.stats()
+        for k in agg:
+            agg[k] += st[k]
+    return agg
+
+
+def cpu_sample(n_s, threads):
+    """One Newton iteration of the oracle (BuildMatrix + BuildVector + SuperLU solve of C^T K C) on an n_s^3 beam of
+    the same problem, after two elastic load steps. Returns (seconds, n_dofs)."""
+    import scipy.sparse.linalg as spla
+
+    from oracle import setups
+    from oracle.core import lib
+    from oracle.quasistatic import QuasistaticOracle
+
+    lib().oracle_set_threads(threads)
+    om, layers, P, cons = setups.hex8_gradient_damage(n_s)
+    Q = QuasistaticOracle(P, cons[0], cons[1], cons[2], tolerance=1e-10, max_iterations=20)
+    x = np.zeros(P.n_dofs)
+    t0 = time.perf_counter()
+    K = Q.derivative(x)
+    r = Q.residual(x)
+    t1 = time.perf_counter()
+    db = Q.global_rhs(1.0 / LOAD_STEPS) - Q.global_rhs(0.0)
+    rhs = r + K @ db
+    Kr = K[Q.indep][:, Q.indep].tocsc()
+    spla.spsolve(Kr, rhs[Q.indep])
+    t2 = time.perf_counter()
+    cpu_sample.last = (t1 - t0, t2 - t1)
+    return t2 - t0, P.n_dofs
+
+
+def cpu_baseline(steps=1, n_s=16):
+    from oracle.core import lib
+
+    threads = lib().oracle_max_threads()
+    times = []
+    for _ in range(steps):
+        dt, n = cpu_sample(n_s, threads)
+        times.append(dt)
+    t = float(np.median(times))
+    return {"value": n / t, "unit": "DOF/s", "cores": threads, "kind": "port",
+            "sample": "one Newton iteration (oracle BuildMatrix + BuildVector with OpenMP, SuperLU solve of C^T K C) "
+                      "of the same gradient-damage beam at %d^3 cells (%d DOFs); %.2f s, of which assembly %.2f s "
+                      "and SuperLU %.2f s" % (n_s, n, t, cpu_sample.last[0], cpu_sample.last[1]),
+            "assembly_dofs_per_s": n / cpu_sample.last[0],
+            "ms_per_newton_step": 1e3 * t}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+
+    oracle.build()
+    for _ in range(args.warmup):
+        cpu_sample(16, oracle.lib().oracle_max_threads())
+    times = []
+    n = None
+    for _ in range(args.steps):
+        dt, n = cpu_sample(16, oracle.lib().oracle_max_threads())
+        times.append(dt)
+    total = float(sum(times))
+    value = n * args.steps / total
+    cores = oracle.lib().oracle_max_threads()
+    out = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+           "config": {"workload": "hex8_gradient_damage beam 1x1x4, 16^3 cells sample of the 64^3 workload",
+                      "n_dofs": n, "parallelism": "host OpenMP"},
+           "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": cores, "kind": "port",
+                            "sample": "one Newton iteration per step (oracle assembly + SuperLU) on a 16^3 cell "
+                                      "sample; the reference itself cannot be built (Eigen/Boost absent)"},
+           "e2e": {"value": value, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import nuto_gb300
+    from nuto_gb300 import configs
+
+    nuto_gb300.load()
+    s = configs.hex8_gradient_damage(args.size, load_steps=LOAD_STEPS)
+    g = s.build_gpu(device=local)
+    n_dofs, nnz = g.n_dofs, g.nnz
+    opts32 = g.default_options(precision=nuto_gb300.FP32, newton_rtol=1e-8, krylov_rtol=1e-4, max_newton=20,
+                               max_krylov=20000)
+    opts64 = g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-8, krylov_rtol=1e-4, max_newton=20,
+                               max_krylov=20000)
+    dt = 1.0 / LOAD_STEPS
+    g.set_state(None, 0.0, True)
+    for k in range(1, args.warmup + 1):
+        g.do_step(k * dt, opts32)
+    x_w, t_w = g.get_state()
+    kappa_w = g.history
+    t_values = [(args.warmup + k) * dt for k in range(1, args.steps + 1)]
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as tdist
+
+            tdist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(opts):
+        g.set_state(x_w, t_w, False)
+        g.history = kappa_w
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        agg = run_steps(g, opts, t_values, torch)
+        e1.record()
+        barrier()
+        return e0.elapsed_time(e1) / 1e3, agg
+
+    clocks = ClockSampler(gpu_index(local))
+    clocks.start()
+    sec32, agg32 = timed(opts32)
+    clk = clocks.stop()
+    x32, _ = g.get_state()
+    if world > 1:
+        import torch.distributed as tdist
+
+        tt = torch.tensor([sec32], device="cuda")
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        sec32 = float(tt.item())
+    value = world * n_dofs * agg32["matrix_assemblies"] / sec32
+
+    fp64 = None
+    if not args.skip_fp64:
+        sec64, agg64 = timed(opts64)
+        x64, _ = g.get_state()
+        err = float(np.abs(x32 - x64).max() / max(np.abs(x64).max(), 1e-300))
+        fp64 = {"value": n_dofs * agg64["matrix_assemblies"] / sec64, "unit": "DOF/s",
+                "ms_per_step": 1e3 * sec64 / args.steps,
+                "newton_step_ms": 1e3 * sec64 / max(agg64["matrix_assemblies"], 1),
+                "newton_iterations": agg64["newton_iterations"], "krylov_iterations": agg64["krylov_iterations"],
+                "ms_assemble_matrix_per_launch": agg64["ms_assemble_matrix"] / max(agg64["matrix_assemblies"], 1),
+                "speedup_mixed_vs_fp64_newton_step": (sec64 / max(agg64["matrix_assemblies"], 1))
+                / (sec32 / max(agg32["matrix_assemblies"], 1)),
+                "speedup_mixed_vs_fp64_load_step": sec64 / sec32,
+                "max_rel_displacement_error_mixed_vs_fp64": err}
+
+    # end to end through the C ABI with pinned host buffers (state + history copied in and out every step)
+    n_hist = s.mesh.num_cells * g.n_ip
+    xa = torch.empty(n_dofs, dtype=torch.float64, pin_memory=True)
+    xb = torch.empty(n_dofs, dtype=torch.float64, pin_memory=True)
+    ka = torch.empty(n_hist, dtype=torch.float64, pin_memory=True)
+    kb = torch.empty(n_hist, dtype=torch.float64, pin_memory=True)
+    xa.numpy()[:] = x_w
+    ka.numpy()[:] = kappa_w.ravel()
+    g.set_state(x_w, t_w, False)
+    barrier()
+    h0 = time.perf_counter()
+    assemblies = 0
+    for t in t_values:
+        g.do_step_host(t, xa, ka, xb, kb, opts32)
+        assemblies += g.stats()["matrix_assemblies"]
+        xa, xb = xb, xa
+        ka, kb = kb, ka
+    barrier()
+    sec_e2e = time.perf_counter() - h0
+    e2e = {"value": world * n_dofs * assemblies / sec_e2e, "unit": "DOF/s",
+           "h2d_bytes_per_step": int((n_dofs + n_hist) * 8), "d2h_bytes_per_step": int((n_dofs + n_hist) * 8),
+           "ms_per_step": 1e3 * sec_e2e / args.steps}
+
+    peak, peak_kind = load_peaks()
+    traffic = load_traffic()
+    per_launch = agg32["ms_spmv"] / max(agg32["spmv_launches"], 1) / 1e3
+    sb = spmv_bytes(n_dofs, nnz, 4)
+    achieved = sb / per_launch / 1e9
+    roof = {"kernel": "k_spmv<float,float,32,*> (Krylov SpMV, FP32 CSR)", "bound": "hbm", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "traffic": traffic.get("k_spmv_fp32_bytes_per_launch"), "algorithmic_bytes_per_launch": sb,
+            "mean_launch_us": per_launch * 1e6, "launches": agg32["spmv_launches"]}
+    tb = tangent_bytes(s, nnz, 4)
+    asm_launch = agg32["ms_assemble_matrix"] / max(agg32["matrix_assemblies"], 1) / 1e3
+    assembly = {"kernel": "k_tangent<float> (FP32 tangent assembly incl. value reset)", "bound": "hbm",
+                "achieved": tb / asm_launch / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": tb / asm_launch / 1e9 / peak, "algorithmic_bytes_per_launch": tb,
+                "mean_launch_ms": asm_launch * 1e3, "assembled_dofs_per_s": n_dofs / asm_launch,
+                "traffic": traffic.get("k_tangent_fp32_bytes_per_launch")}
+
+    out = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * sec32 / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+           "config": {"workload": "hex8_gradient_damage_%d^3: Hex8 2x2x2 Gauss, beam 1x1x4 m, u + eeq, "
+                                  "GradientDamage(c=0.01, LinearElasticDamage(30000, 0.2, FULL), "
+                                  "DamageLawExponential(1e-4, 100, 0.99), ModifiedMises(k=10)), 20 load steps to "
+                                  "u_z=2e-3; timed load steps %d..%d" % (args.size, args.warmup + 1,
+                                                                        args.warmup + args.steps),
+                      "n_dofs": n_dofs, "nnz": nnz, "precision": "FP32 tangent + FP32 GMRES(40), FP64 residual, "
+                                                                "history and Newton test",
+                      "newton_tolerance": "|C^T r| <= 1e-8 |C^T (r + K db)| of the load step",
+                      "krylov_rtol": 1e-4, "l2": "inputs larger than L2 (FP32 tangent %.0f MB)" % (nnz * 4 / 1e6),
+                      "parallelism": "replicas" if world > 1 else "single GPU"},
+           "newton_step_ms": 1e3 * sec32 / max(agg32["matrix_assemblies"], 1),
+           "newton_iterations": agg32["newton_iterations"], "tangent_solves": agg32["matrix_assemblies"],
+           "krylov_iterations": agg32["krylov_iterations"],
+           "roofline": roof, "roofline_assembly": assembly, "fp64": fp64, "e2e": e2e,
+           "gpu_launches": int(agg32["kernel_launches"]), "clocks": clk}
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        try:
+            out["cpu_baseline"] = cpu_baseline()
+        except Exception as exc:  # the CPU leg must not hide the GPU result
+            out["cpu_baseline"] = {"value": None, "error": str(exc)}
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

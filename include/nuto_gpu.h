@@ -79,9 +79,10 @@ extern "C" {
 #define NUTO_GPU_FP64 64
 
 /* Krylov methods */
-#define NUTO_GPU_SOLVER_AUTO 0     /* PCG for the symmetric integrands, BiCGStab otherwise */
+#define NUTO_GPU_SOLVER_AUTO 0     /* PCG for the symmetric integrands, GMRES otherwise */
 #define NUTO_GPU_SOLVER_PCG 1      /* Jacobi-preconditioned CG */
 #define NUTO_GPU_SOLVER_BICGSTAB 2 /* Jacobi-preconditioned BiCGStab */
+#define NUTO_GPU_SOLVER_GMRES 3    /* Jacobi-preconditioned restarted GMRES(40) */
 
 typedef struct nuto_gpu_ctx nuto_gpu_ctx;
 
@@ -129,6 +130,9 @@ typedef struct nuto_gpu_stats
     double ms_assemble_vector;
     double ms_krylov;
     double ms_total;
+    double ms_spmv;          /* device time of the Krylov sparse matrix-vector products (CUDA events) */
+    int64_t spmv_launches;
+    int64_t kernel_launches; /* kernels launched by the step */
 } nuto_gpu_stats;
 
 /* ---- context ----------------------------------------------------------------------------------------- */

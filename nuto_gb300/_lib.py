@@ -57,7 +57,8 @@ class Stats(ctypes.Structure):
         ("residual_evaluations", ctypes.c_int), ("matrix_assemblies", ctypes.c_int),
         ("final_residual", ctypes.c_double), ("reference_residual", ctypes.c_double),
         ("ms_assemble_matrix", ctypes.c_double), ("ms_assemble_vector", ctypes.c_double),
-        ("ms_krylov", ctypes.c_double), ("ms_total", ctypes.c_double),
+        ("ms_krylov", ctypes.c_double), ("ms_total", ctypes.c_double), ("ms_spmv", ctypes.c_double),
+        ("spmv_launches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
     ]
 
     def as_dict(self):

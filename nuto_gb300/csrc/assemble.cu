@@ -394,6 +394,7 @@ void LaunchResidual(Ctx& c, const double* u, double* f)
         k_residual<C::dim, C::nd, C::nip, C::kind><<<blocks, 128, 0, c.stream>>>(a, c.law, u, f);
     });
     AfterLaunch(c, "k_residual");
+    c.stats.kernel_launches += 1;
 }
 
 // ---- tangent: FP32 or FP64 values scattered into CSR ---------------------------------------------------------
@@ -721,6 +722,7 @@ static void LaunchTangentT(Ctx& c, const double* u, T* vals)
                 a, c.law, s, dS * ns + dS, dS * ns + eS, eS * ns + dS, eS * ns + eS, u, vals);
     });
     AfterLaunch(c, "k_tangent");
+    c.stats.kernel_launches += 1;
 }
 
 void LaunchTangent(Ctx& c, const double* u, int precision, void* values)
@@ -790,6 +792,7 @@ void LaunchHistory(Ctx& c, const double* u)
             k_history<C::dim, C::nd, C::nip, C::kind><<<blocks, 128, 0, c.stream>>>(a, c.law, u);
     });
     AfterLaunch(c, "k_history");
+    c.stats.kernel_launches += 1;
 }
 
 // ---- scatter of caller-given cell results (SimpleAssembler scatter, SimpleAssembler.cpp:53-59, 118-137) -----

@@ -14,6 +14,13 @@ namespace nuto_gpu
 
 SolverWork::~SolverWork()
 {
+    for (auto& p : spmvEv)
+    {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+    }
+    if (hG)
+        cudaFreeHost(hG);
     if (hScal)
         cudaFreeHost(hScal);
     if (hStat)
@@ -498,11 +505,46 @@ static void SpmvLaunch(Ctx& c, const TV* vals, const TX* x, TX* y, const TX* w0,
         go(std::integral_constant<int, 32>{});
 }
 
+// Krylov SpMV with a CUDA-event pair around it (device time of the dominant kernel, collected by SpmvCollect)
+template <typename TV, typename TX, int NDOT>
+static void SpmvTimed(Ctx& c, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc, int* st, int fin,
+                      const uint8_t* mask)
+{
+    SolverWork& w = Work(c);
+    if (w.spmvNext == w.spmvEv.size())
+    {
+        std::pair<cudaEvent_t, cudaEvent_t> p;
+        NG_CUDA(cudaEventCreate(&p.first));
+        NG_CUDA(cudaEventCreate(&p.second));
+        w.spmvEv.push_back(p);
+    }
+    auto& ev = w.spmvEv[w.spmvNext++];
+    NG_CUDA(cudaEventRecord(ev.first, c.stream));
+    SpmvLaunch<TV, TX, NDOT>(c, vals, x, y, w0, sc, st, fin, mask);
+    NG_CUDA(cudaEventRecord(ev.second, c.stream));
+    c.stats.kernel_launches += 1;
+}
+
+// after a stream synchronisation: add the recorded SpMV times to the statistics
+static void SpmvCollect(Ctx& c)
+{
+    SolverWork& w = Work(c);
+    for (size_t i = 0; i < w.spmvNext; ++i)
+    {
+        float ms = 0;
+        NG_CUDA(cudaEventElapsedTime(&ms, w.spmvEv[i].first, w.spmvEv[i].second));
+        c.stats.ms_spmv += ms;
+    }
+    c.stats.spmv_launches += static_cast<int64_t>(w.spmvNext);
+    w.spmvNext = 0;
+}
+
 double MaskedNorm(Ctx& c, const double* v)
 {
     SolverWork& w = Work(c);
     NG_CUDA(cudaMemsetAsync(w.scal.p + SC_ACC2, 0, sizeof(double), c.stream));
     k_masked_sq<<<GridFor(c, c.nDofs), kBS, 0, c.stream>>>(c.nDofs, c.dMask.p, v, w.scal.p + SC_ACC2);
+    c.stats.kernel_launches += 1;
     NG_CUDA(cudaMemcpyAsync(w.hScal + SC_ACC2, w.scal.p + SC_ACC2, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     NG_CUDA(cudaStreamSynchronize(c.stream));
     const double r = w.hScal[SC_ACC2];
@@ -518,6 +560,7 @@ void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double
         w.zeroMask.alloc(c.nDofs);
         NG_CUDA(cudaMemsetAsync(w.zeroMask.p, 0, c.nDofs, c.stream));
     }
+    c.stats.kernel_launches += 1;
     if (precision == NUTO_GPU_FP32)
         SpmvLaunch<float, double, 0>(c, static_cast<const float*>(vals), x, y, nullptr, nullptr, nullptr, FIN_NONE,
                                      w.zeroMask.p);
@@ -527,12 +570,313 @@ void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double
     AfterLaunch(c, "krylov");
 }
 
+
+// ---- restarted GMRES(m), right Jacobi preconditioning ----------------------------------------------------------
+// Arnoldi with classical Gram-Schmidt and one re-orthogonalisation (CGS2); the FP64 Hessenberg column, its Givens
+// rotation and the residual estimate are formed by the last block of the second projection, so a whole cycle is
+// enqueued without a host round trip. The basis is stored in T (FP32 or FP64).
+using GL = GmresLayout;
+
+// acc[i] += V_i . w for i < nv (grid-stride dot per basis vector)
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_gm_dots(int64_t n, const T* __restrict__ V, int nv, const T* __restrict__ w,
+                                                  double* acc, const int* st)
+{
+    __shared__ double sh[kBS / 32];
+    if (st[ST_STATE] != RUN)
+        return;
+    for (int i = 0; i < nv; ++i)
+    {
+        const T* v = V + static_cast<int64_t>(i) * n;
+        double s = 0;
+        for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < n;
+             r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+            s += static_cast<double>(v[r]) * static_cast<double>(w[r]);
+        BlockAccumulate(s, acc + i, sh);
+    }
+}
+
+// w -= sum_i h_i V_i. With finalize: also |w|^2, and the last block completes Arnoldi column j: H(:, j) = h1 + h2,
+// H(j+1, j) = |w|, earlier rotations applied, new rotation formed, residual estimate |g(j+1)| tested.
+template <typename T, bool FINAL>
+__global__ void __launch_bounds__(kBS) k_gm_update(int64_t n, const T* __restrict__ V, int nv, double* gs, T* w,
+                                                    int* st, int j)
+{
+    __shared__ double sh[kBS / 32];
+    __shared__ T hs[GL::m + 1];
+    if (st[ST_STATE] != RUN)
+        return;
+    const double* h = gs + (FINAL ? GL::H2 : GL::H1);
+    for (int i = threadIdx.x; i < nv; i += blockDim.x)
+        hs[i] = static_cast<T>(h[i]);
+    __syncthreads();
+    double nrm = 0;
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < n;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        T a = w[r];
+        for (int i = 0; i < nv; ++i)
+            a -= hs[i] * V[static_cast<int64_t>(i) * n + r];
+        w[r] = a;
+        if (FINAL)
+            nrm += static_cast<double>(a) * static_cast<double>(a);
+    }
+    if (!FINAL)
+        return;
+    BlockAccumulate(nrm, gs + GL::ACC, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        double* H = gs + GL::H + static_cast<int64_t>(j) * (GL::m + 1);
+        for (int i = 0; i <= j; ++i)
+        {
+            H[i] = VRead(gs + GL::H1 + i) + VRead(gs + GL::H2 + i);
+            gs[GL::H1 + i] = 0.;
+            gs[GL::H2 + i] = 0.;
+        }
+        const double hn = sqrt(VRead(gs + GL::ACC));
+        gs[GL::ACC] = 0.;
+        // earlier rotations
+        for (int i = 0; i < j; ++i)
+        {
+            const double c = gs[GL::CS + i], s = gs[GL::SN + i];
+            const double a = H[i], b = H[i + 1];
+            H[i] = c * a + s * b;
+            H[i + 1] = -s * a + c * b;
+        }
+        const double a = H[j], b = hn;
+        const double r = hypot(a, b);
+        const double c = r > 0. ? a / r : 1., s = r > 0. ? b / r : 0.;
+        gs[GL::CS + j] = c;
+        gs[GL::SN + j] = s;
+        H[j] = r;
+        H[j + 1] = 0.;
+        const double gj = gs[GL::G + j];
+        gs[GL::G + j] = c * gj;
+        gs[GL::G + j + 1] = -s * gj;
+        gs[GL::NRM] = hn;
+        st[ST_ITERS] += 1;
+        st[ST_JDONE] = j + 1;
+        const double res = fabs(gs[GL::G + j + 1]);
+        if (!isfinite(res) || !isfinite(hn))
+            st[ST_STATE] = NONFINITE;
+        else if (res * res <= gs[GL::TOL2] || hn == 0.)
+            st[ST_STATE] = CONVERGED;
+    }
+}
+
+// v_j = w / nrm; z = dinv v_j
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_gm_normalize(int64_t n, const T* __restrict__ w, T* vj, T* z,
+                                                       const T* __restrict__ dinv, const double* gs, const int* st)
+{
+    if (st[ST_STATE] != RUN)
+        return;
+    const T inv = static_cast<T>(1. / gs[GL::NRM]);
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < n;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        const T v = w[r] * inv;
+        vj[r] = v;
+        z[r] = dinv[r] * v;
+    }
+}
+
+// w = rhs - w (w holds A x) or w = rhs (first cycle); |w|^2; last block: beta, g, state
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_gm_start(int64_t n, const T* __restrict__ rhs, T* w, int subtract, double* gs,
+                                                   int* st)
+{
+    __shared__ double sh[kBS / 32];
+    double nrm = 0;
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < n;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        const T a = subtract ? rhs[r] - w[r] : rhs[r];
+        w[r] = a;
+        nrm += static_cast<double>(a) * static_cast<double>(a);
+    }
+    BlockAccumulate(nrm, gs + GL::ACC, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        const double beta = sqrt(VRead(gs + GL::ACC));
+        gs[GL::ACC] = 0.;
+        gs[GL::BETA] = beta;
+        gs[GL::NRM] = beta;
+        gs[GL::G] = beta;
+        for (int i = 1; i <= GL::m; ++i)
+            gs[GL::G + i] = 0.;
+        st[ST_JDONE] = 0;
+        if (!isfinite(beta))
+            st[ST_STATE] = NONFINITE;
+        else if (beta * beta <= gs[GL::TOL2])
+            st[ST_STATE] = CONVERGED;
+        else
+            st[ST_STATE] = RUN;
+    }
+}
+
+// x += dinv (sum_i y_i V_i)
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_gm_solution(int64_t n, const T* __restrict__ V, int k, const double* gs,
+                                                      const T* __restrict__ dinv, T* x)
+{
+    __shared__ T ys[GL::m];
+    for (int i = threadIdx.x; i < k; i += blockDim.x)
+        ys[i] = static_cast<T>(gs[GL::Y + i]);
+    __syncthreads();
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < n;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        T a = T(0);
+        for (int i = 0; i < k; ++i)
+            a += ys[i] * V[static_cast<int64_t>(i) * n + r];
+        x[r] += dinv[r] * a;
+    }
+}
+
+// rhs in T: mask0(b) * scale (scale from k_rhs_norm)
+template <typename T>
+__global__ void k_gm_rhs(int64_t n, const uint8_t* __restrict__ mask, const double* __restrict__ b, const double* sc,
+                         T* rhs, T* x)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    rhs[i] = mask[i] ? T(0) : static_cast<T>(b[i] * sc[SC_SCALE]);
+    x[i] = T(0);
+}
+
+template <typename T, typename TV>
+static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool addToX, double rtol, int maxit,
+                      int* iters, double* relres)
+{
+    SolverWork& w = Work(c);
+    KVecs<T>* kp;
+    GVecs<T>* gp;
+    if constexpr (sizeof(T) == 4)
+    {
+        kp = &w.v32;
+        gp = &w.g32;
+    }
+    else
+    {
+        kp = &w.v64;
+        gp = &w.g64;
+    }
+    KVecs<T>& K = *kp;
+    GVecs<T>& G = *gp;
+    const int64_t n = c.nDofs;
+    K.ensure(n);
+    G.ensure(n);
+    if (w.gsc.n != static_cast<size_t>(GL::SIZE))
+    {
+        w.gsc.alloc(GL::SIZE);
+        if (!w.hG)
+            NG_CUDA(cudaMallocHost(&w.hG, GL::SIZE * sizeof(double)));
+    }
+    double* sc = w.scal.p;
+    int* st = w.stat.p;
+    double* gs = w.gsc.p;
+    NG_CUDA(cudaMemsetAsync(sc, 0, SC_COUNT * sizeof(double), c.stream));
+    NG_CUDA(cudaMemsetAsync(st, 0, ST_COUNT * sizeof(int), c.stream));
+    NG_CUDA(cudaMemsetAsync(gs, 0, GL::SIZE * sizeof(double), c.stream));
+    const int grid = GridFor(c, n);
+    const unsigned g256 = static_cast<unsigned>((n + 255) / 256);
+    k_diag_inv<TV, T><<<g256, 256, 0, c.stream>>>(n, c.dRowPtr.p, c.dColIdx.p, vals, c.dMask.p, K.dinv.p);
+    k_rhs_norm<<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, sc, st, rtol, sizeof(T) == 4 ? 1 : 0);
+    // rhs (scaled) in K.r, solution in K.x; tolerance (rtol relative to the scaled rhs) to the GMRES block
+    k_gm_rhs<T><<<g256, 256, 0, c.stream>>>(n, c.dMask.p, b, sc, K.r.p, K.x.p);
+    AfterLaunch(c, "gmres set-up");
+    c.stats.kernel_launches += 3;
+    NG_CUDA(cudaMemcpyAsync(gs + GL::TOL2, sc + SC_TOL2, sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    int total = 0;
+    int state = RUN;
+    double relEst = 1.;
+    double beta0 = -1.;
+    bool first = true;
+    const int m = GL::m;
+    while (total < maxit)
+    {
+        // r = rhs - A x, v_0 = r / |r|
+        if (!first)
+            SpmvTimed<TV, T, 0>(c, vals, K.x.p, G.w.p, nullptr, nullptr, nullptr, FIN_NONE, c.dMask.p);
+        c.stats.kernel_launches += 2;
+        k_gm_start<T><<<grid, kBS, 0, c.stream>>>(n, K.r.p, G.w.p, first ? 0 : 1, gs, st);
+        first = false;
+        k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, G.V.p, G.z.p, K.dinv.p, gs, st);
+        const int cols = std::min(m, maxit - total);
+        for (int j = 0; j < cols; ++j)
+        {
+            T* vj1 = G.V.p + static_cast<int64_t>(j + 1) * n;
+            SpmvTimed<TV, T, 0>(c, vals, G.z.p, G.w.p, nullptr, nullptr, st, FIN_NONE, c.dMask.p);
+            c.stats.kernel_launches += 4 + (j + 1 < cols ? 1 : 0);
+            k_gm_dots<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, G.w.p, gs + GL::H1, st);
+            k_gm_update<T, false><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, gs, G.w.p, st, j);
+            k_gm_dots<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, G.w.p, gs + GL::H2, st);
+            k_gm_update<T, true><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, gs, G.w.p, st, j);
+            if (j + 1 < cols)
+                k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, vj1, G.z.p, K.dinv.p, gs, st);
+        }
+        AfterLaunch(c, "gmres cycle");
+        NG_CUDA(cudaMemcpyAsync(w.hG, gs, GL::SIZE * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        NG_CUDA(cudaMemcpyAsync(w.hStat, st, ST_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        NG_CUDA(cudaStreamSynchronize(c.stream));
+        SpmvCollect(c);
+        state = w.hStat[ST_STATE];
+        const int k = w.hStat[ST_JDONE];
+        total = w.hStat[ST_ITERS];
+        if (beta0 < 0.)
+            beta0 = w.hG[GL::BETA];
+        if (state == NONFINITE)
+            break;
+        if (k > 0)
+        {
+            // back substitution R y = g on the host (k <= m)
+            double* y = w.hG + GL::Y;
+            for (int i = k - 1; i >= 0; --i)
+            {
+                double s = w.hG[GL::G + i];
+                for (int l = i + 1; l < k; ++l)
+                    s -= w.hG[GL::H + l * (m + 1) + i] * y[l];
+                const double d = w.hG[GL::H + i * (m + 1) + i];
+                y[i] = d != 0. ? s / d : 0.;
+            }
+            NG_CUDA(cudaMemcpyAsync(gs + GL::Y, y, k * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+            k_gm_solution<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, k, gs, K.dinv.p, K.x.p);
+            AfterLaunch(c, "gmres solution");
+            c.stats.kernel_launches += 1;
+            relEst = beta0 > 0. ? std::fabs(w.hG[GL::G + k]) / beta0 : 0.;
+        }
+        if (state != RUN)
+            break;
+        // restart: the state flag is reset by k_gm_start
+    }
+    if (state == CONVERGED && beta0 == 0.)
+        relEst = 0.;
+    if (iters)
+        *iters = total;
+    if (relres)
+        *relres = relEst;
+    c.stats.krylov_iterations += total;
+    if (state == NONFINITE)
+        throw Error{NUTO_GPU_ENAN, "non-finite value in the GMRES iteration (iteration " + std::to_string(total) + ")"};
+    k_unscale<T><<<g256, 256, 0, c.stream>>>(n, K.x.p, sc, x64, addToX ? 1 : 0);
+    AfterLaunch(c, "gmres unscale");
+    c.stats.kernel_launches += 1;
+    return state == CONVERGED ? CONVERGED : (state == RUN ? RUN : state);
+}
+
 // Runs one Krylov solve of the constrained system with values `vals` (type TV) in arithmetic T, right-hand side
 // b (FP64, combined layout), solution written (or added) to x64. Returns the status.
 template <typename T, typename TV>
-static int KrylovSolve(Ctx& c, bool pcg, const TV* vals, const double* b, double* x64, bool addToX, double rtol,
+static int KrylovSolve(Ctx& c, int method, const TV* vals, const double* b, double* x64, bool addToX, double rtol,
                        int maxit, int* iters, double* relres)
 {
+    if (method == NUTO_GPU_SOLVER_GMRES)
+        return GmresSolve<T, TV>(c, vals, b, x64, addToX, rtol, maxit, iters, relres);
+    const bool pcg = method == NUTO_GPU_SOLVER_PCG;
     SolverWork& w = Work(c);
     KVecs<T>* vp;
     if constexpr (sizeof(T) == 4)
@@ -567,16 +911,18 @@ static int KrylovSolve(Ctx& c, bool pcg, const TV* vals, const double* b, double
         {
             if (pcg)
             {
-                SpmvLaunch<TV, T, 1>(c, vals, V.p.p, V.q.p, V.p.p, sc, st, FIN_PCG_ALPHA, c.dMask.p);
+                SpmvTimed<TV, T, 1>(c, vals, V.p.p, V.q.p, V.p.p, sc, st, FIN_PCG_ALPHA, c.dMask.p);
+                c.stats.kernel_launches += 2;
                 k_pcg_update<T><<<grid, kBS, 0, c.stream>>>(n, V.x.p, V.r.p, V.p.p, V.q.p, V.z.p, V.dinv.p, sc, st);
                 k_pcg_dir<T><<<grid, kBS, 0, c.stream>>>(n, V.p.p, V.z.p, sc, st);
             }
             else
             {
                 k_bicg_p<T><<<grid, kBS, 0, c.stream>>>(n, V.p.p, V.r.p, V.v.p, V.ph.p, V.dinv.p, sc, st);
-                SpmvLaunch<TV, T, 1>(c, vals, V.ph.p, V.v.p, V.rh.p, sc, st, FIN_BICG_ALPHA, c.dMask.p);
+                SpmvTimed<TV, T, 1>(c, vals, V.ph.p, V.v.p, V.rh.p, sc, st, FIN_BICG_ALPHA, c.dMask.p);
+                c.stats.kernel_launches += 3;
                 k_bicg_s<T><<<grid, kBS, 0, c.stream>>>(n, V.s.p, V.r.p, V.v.p, V.sh.p, V.dinv.p, sc, st);
-                SpmvLaunch<TV, T, 2>(c, vals, V.sh.p, V.t.p, V.s.p, sc, st, FIN_BICG_OMEGA, c.dMask.p);
+                SpmvTimed<TV, T, 2>(c, vals, V.sh.p, V.t.p, V.s.p, sc, st, FIN_BICG_OMEGA, c.dMask.p);
                 k_bicg_x<T><<<grid, kBS, 0, c.stream>>>(n, V.x.p, V.r.p, V.rh.p, V.ph.p, V.s.p, V.sh.p, V.t.p, sc, st);
             }
         }
@@ -585,6 +931,7 @@ static int KrylovSolve(Ctx& c, bool pcg, const TV* vals, const double* b, double
         NG_CUDA(cudaMemcpyAsync(w.hStat, st, ST_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         NG_CUDA(cudaMemcpyAsync(w.hScal, sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         NG_CUDA(cudaStreamSynchronize(c.stream));
+        SpmvCollect(c);
         state = w.hStat[ST_STATE];
         if (state != RUN)
             break;
@@ -609,19 +956,20 @@ static int KrylovSolve(Ctx& c, bool pcg, const TV* vals, const double* b, double
     }
     // breakdown or iteration cap: keep the iterate (Newton refines it) but report non-convergence by the rel value
     k_unscale<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, c.stream>>>(n, V.x.p, sc, x64, addToX ? 1 : 0);
+    c.stats.kernel_launches += 4; // diagonal, rhs norm, init, unscale
     AfterLaunch(c, "krylov");
     return state;
 }
 
 template <typename T, typename TV>
-int KrylovSolveExport(Ctx& c, bool pcg, const TV* vals, const double* b, double* x64, bool add, double rtol,
+int KrylovSolveExport(Ctx& c, int method, const TV* vals, const double* b, double* x64, bool add, double rtol,
                       int maxit, int* iters, double* relres)
 {
-    return KrylovSolve<T, TV>(c, pcg, vals, b, x64, add, rtol, maxit, iters, relres);
+    return KrylovSolve<T, TV>(c, ResolveMethod(c, method), vals, b, x64, add, rtol, maxit, iters, relres);
 }
-template int KrylovSolveExport<float, float>(Ctx&, bool, const float*, const double*, double*, bool, double, int,
+template int KrylovSolveExport<float, float>(Ctx&, int, const float*, const double*, double*, bool, double, int,
                                              int*, double*);
-template int KrylovSolveExport<double, double>(Ctx&, bool, const double*, const double*, double*, bool, double, int,
+template int KrylovSolveExport<double, double>(Ctx&, int, const double*, const double*, double*, bool, double, int,
                                                int*, double*);
 
 __global__ void k_residual64(int64_t n, const uint8_t* __restrict__ mask, const double* __restrict__ b,
@@ -638,13 +986,11 @@ void Residual64(Ctx& c, const double* b, const double* kx, double* r)
     AfterLaunch(c, "krylov");
 }
 
-bool UsePcg(const Ctx& c, int method)
+int ResolveMethod(const Ctx& c, int method)
 {
-    if (method == NUTO_GPU_SOLVER_PCG)
-        return true;
-    if (method == NUTO_GPU_SOLVER_BICGSTAB)
-        return false;
-    return c.prm.kind == NUTO_GPU_MB_LINEAR_ELASTIC;
+    if (method == NUTO_GPU_SOLVER_PCG || method == NUTO_GPU_SOLVER_BICGSTAB || method == NUTO_GPU_SOLVER_GMRES)
+        return method;
+    return c.prm.kind == NUTO_GPU_MB_LINEAR_ELASTIC ? NUTO_GPU_SOLVER_PCG : NUTO_GPU_SOLVER_GMRES;
 }
 
 // nuto_gpu_solve: FP64 solve, or FP32 Krylov inside an FP64 iterative refinement (r = b - K x in FP64 with the
@@ -653,13 +999,13 @@ int SolveLinear(Ctx& c, int precision, int method, const void* values, const dou
                 int maxit, int* iters, double* relres)
 {
     SolverWork& w = Work(c);
-    const bool pcg = UsePcg(c, method);
+    const int meth = ResolveMethod(c, method);
     c.stats.krylov_iterations = 0;
     if (precision == NUTO_GPU_FP64)
     {
         int it = 0;
         double rel = 0;
-        const int st = KrylovSolve<double, double>(c, pcg, static_cast<const double*>(values), b, x, false, rtol,
+        const int st = KrylovSolve<double, double>(c, meth, static_cast<const double*>(values), b, x, false, rtol,
                                                    maxit, &it, &rel);
         if (iters)
             *iters = it;
@@ -679,8 +1025,8 @@ int SolveLinear(Ctx& c, int precision, int method, const void* values, const dou
     {
         const double inner = std::max(rtol / std::max(rel, 1e-300), 1e-5);
         int it = 0;
-        KrylovSolve<float, float>(c, pcg, static_cast<const float*>(values), w.rhs.p, x, true, std::min(inner, 0.5),
-                                  maxit - total, &it, nullptr);
+        KrylovSolve<float, float>(c, meth, static_cast<const float*>(values), w.rhs.p, x, true,
+                                  std::min(inner, 0.5), maxit - total, &it, nullptr);
         total += it;
         // r = b - K x (FP64 vectors, FP32 values), constrained rows zero
         SpmvFull64(c, NUTO_GPU_FP32, values, x, w.tmp.p);

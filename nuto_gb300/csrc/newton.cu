@@ -114,7 +114,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     if (!fp32 && w.K64.n != static_cast<size_t>(c.nnz))
         w.K64.alloc(c.nnz);
     void* K = fp32 ? static_cast<void*>(w.K32.p) : static_cast<void*>(w.K64.p);
-    const bool pcg = UsePcg(c, o.method);
+    const int method = ResolveMethod(c, o.method);
     c.stats = nuto_gpu_stats{};
     nuto_gpu_stats& S = c.stats;
     Timers T(c);
@@ -141,11 +141,11 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
         const auto k0 = std::chrono::steady_clock::now();
         int it = 0;
         if (fp32)
-            KrylovSolveExport<float, float>(c, pcg, w.K32.p, rhs, out, false, o.krylov_rtol, o.max_krylov, &it,
+            KrylovSolveExport<float, float>(c, method, w.K32.p, rhs, out, false, o.krylov_rtol, o.max_krylov, &it,
                                             nullptr);
         else
-            KrylovSolveExport<double, double>(c, pcg, w.K64.p, rhs, out, false, o.krylov_rtol, o.max_krylov, &it,
-                                              nullptr);
+            KrylovSolveExport<double, double>(c, method, w.K64.p, rhs, out, false, o.krylov_rtol, o.max_krylov,
+                                              &it, nullptr);
         T.Collect();
         S.ms_krylov += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - k0).count();
     };
@@ -168,12 +168,14 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     SpmvFull64(c, o.precision, K, w.db.p, w.tmp.p);
     k_masked_sum<<<gb, 256, 0, c.stream>>>(n, c.dMask.p, w.f.p, w.tmp.p, w.rhs.p);
     AfterLaunch(c, "newton vector kernels");
+    S.kernel_launches += c.nDep > 0 ? 2 : 1;
     const double refNorm = MaskedNorm(c, w.rhs.p);
     S.reference_residual = refNorm;
     const double tol = std::max(o.newton_atol, o.newton_rtol * refNorm);
     solve(w.rhs.p, w.dx.p);
     k_update<<<gb, 256, 0, c.stream>>>(n, x, w.dx.p, 1.0, w.db.p, w.xs.p);
     AfterLaunch(c, "newton vector kernels");
+    S.kernel_launches += 1;
 
     // Newton-Raphson with line search on the trial state
     double nr = residual(w.xs.p);
@@ -183,6 +185,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     {
         assembleK(w.xs.p);
         k_masked_sum<<<gb, 256, 0, c.stream>>>(n, c.dMask.p, w.f.p, nullptr, w.rhs.p);
+        S.kernel_launches += 1;
         solve(w.rhs.p, w.dx.p);
         ++it;
         if (o.line_search)
@@ -193,6 +196,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
             for (int step = 0; step < 6; ++step)
             {
                 k_update<<<gb, 256, 0, c.stream>>>(n, w.x0.p, w.dx.p, alpha, nullptr, w.xs.p);
+                S.kernel_launches += 1;
                 const double trial = residual(w.xs.p);
                 nr = trial;
                 if (trial < tol)
@@ -208,6 +212,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
         else
         {
             k_update<<<gb, 256, 0, c.stream>>>(n, w.xs.p, w.dx.p, 1.0, nullptr, w.xs.p);
+            S.kernel_launches += 1;
             nr = residual(w.xs.p);
             conv = nr < tol;
         }

@@ -31,6 +31,7 @@ enum Stat
     ST_ITERS,
     ST_COUNTER,   // last-block counter of the fused reductions
     ST_HALF,      // BiCGStab: converged on s
+    ST_JDONE,     // GMRES: Arnoldi columns completed in the current cycle
     ST_COUNT
 };
 
@@ -57,6 +58,43 @@ struct KVecs
     }
 };
 
+constexpr int kGmresRestart = 40;
+
+// GMRES workspace: Krylov basis V (m + 1 vectors of n), work vectors and the FP64 Arnoldi scalars.
+template <typename T>
+struct GVecs
+{
+    DBuf<T> V, w, z;
+    int64_t n = 0;
+    void ensure(int64_t count)
+    {
+        if (n == count)
+            return;
+        V.alloc(static_cast<size_t>(count) * (kGmresRestart + 1));
+        w.alloc(count);
+        z.alloc(count);
+        n = count;
+    }
+};
+
+// offsets into the GMRES scalar block (doubles)
+struct GmresLayout
+{
+    static constexpr int m = kGmresRestart;
+    static constexpr int H = 0;                  // (m + 1) x m, column-major
+    static constexpr int G = H + (m + 1) * m;    // m + 1: rotated right-hand side
+    static constexpr int CS = G + m + 1;         // m: Givens cosines
+    static constexpr int SN = CS + m;            // m: Givens sines
+    static constexpr int H1 = SN + m;            // m + 1: first projection accumulators
+    static constexpr int H2 = H1 + m + 1;        // m + 1: second projection accumulators
+    static constexpr int Y = H2 + m + 1;         // m: least-squares solution
+    static constexpr int ACC = Y + m;            // norm accumulator
+    static constexpr int NRM = ACC + 1;          // normalisation of the next basis vector
+    static constexpr int BETA = NRM + 1;         // |r| at the start of the cycle
+    static constexpr int TOL2 = BETA + 1;        // rtol^2 (right-hand side scaled to unit norm)
+    static constexpr int SIZE = TOL2 + 1;
+};
+
 struct SolverWork
 {
     DBuf<double> scal;
@@ -65,12 +103,19 @@ struct SolverWork
     int* hStat = nullptr;    // pinned
     KVecs<float> v32;
     KVecs<double> v64;
+    GVecs<float> g32;
+    GVecs<double> g64;
+    DBuf<double> gsc; // GmresLayout
+    double* hG = nullptr; // pinned copy of the GMRES scalars
     // Newton buffers
     DBuf<float> K32;
     DBuf<double> K64;
     DBuf<double> f, rhs, dx, db, x0, xs, tmp;
     DBuf<uint8_t> zeroMask;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // CUDA-event pairs around the Krylov SpMV launches, folded into stats at synchronisation points
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spmvEv;
+    size_t spmvNext = 0;
     ~SolverWork();
 };
 
@@ -82,11 +127,11 @@ double MaskedNorm(Ctx& c, const double* v);
 void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double* y);
 // r = mask0(b - kx)
 void Residual64(Ctx& c, const double* b, const double* kx, double* r);
-// PCG for the symmetric integrands (or when asked), BiCGStab otherwise
-bool UsePcg(const Ctx& c, int method);
+// NUTO_GPU_SOLVER_AUTO resolves to PCG for the symmetric integrands and GMRES otherwise
+int ResolveMethod(const Ctx& c, int method);
 // one Krylov solve in arithmetic T on values of type TV; adds to (add) or overwrites x64; returns SolverState
 template <typename T, typename TV>
-int KrylovSolveExport(Ctx& c, bool pcg, const TV* vals, const double* b, double* x64, bool add, double rtol,
+int KrylovSolveExport(Ctx& c, int method, const TV* vals, const double* b, double* x64, bool add, double rtol,
                       int maxit, int* iters, double* relres);
 
 } // namespace nuto_gpu

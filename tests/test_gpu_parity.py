@@ -190,8 +190,10 @@ def test_update_history(kind, n):
     assert np.abs(g.history - P.kappa).max() <= 1e-15 + 1e-13 * np.abs(P.kappa).max()
 
 
+@pytest.mark.parametrize("method", [1, 2, 3])
 @pytest.mark.parametrize("precision", [64, 32])
-def test_linear_solve_quad4(precision):
+def test_linear_solve_quad4(precision, method):
+    """Jacobi PCG (1), BiCGStab (2) and GMRES (3) against a direct solve of the reduced system C^T K C."""
     _torch()
     s, g, (om, layers, P, cons) = _build("quad4", 12)
     u0 = np.zeros(P.n_dofs)
@@ -201,7 +203,7 @@ def test_linear_solve_quad4(precision):
     b = rng.uniform(-1, 1, P.n_dofs)
     dep = cons[0]
     indep = np.setdiff1d(np.arange(P.n_dofs), dep)
-    x, it, rel, ok = g.solve(vals, b, precision=precision, rtol=1e-10)
+    x, it, rel, ok = g.solve(vals, b, precision=precision, method=method, rtol=1e-10)
     assert ok, (it, rel)
     import scipy.sparse.linalg as spla
 
@@ -240,6 +242,30 @@ def test_quasistatic_quad4_elastic(precision):
     xo, xg, _, _, st = res[-1]
     rel = np.abs(xg - xo).max() / np.abs(xo).max()
     assert rel <= (1e-8 if precision == 64 else 1e-6), (rel, st)
+
+
+def test_gmres_nonsymmetric_gradient_damage_tangent():
+    """GMRES on the non-symmetric gradient-damage tangent in the damaged regime, FP64 and FP32 values."""
+    _torch()
+    s, g, (om, layers, P, cons) = _build("hex8gd", 3)
+    rng = np.random.default_rng(2)
+    u, kappa = _damage_state("hex8gd", P, rng)
+    P.kappa = kappa
+    g.history = kappa
+    K = _oracle_csr(P, u)
+    b = rng.uniform(-1, 1, P.n_dofs)
+    dep = cons[0]
+    indep = np.setdiff1d(np.arange(P.n_dofs), dep)
+    import scipy.sparse.linalg as spla
+
+    for precision in (64, 32):
+        vals = g.build_matrix(u, precision)
+        x, it, rel, ok = g.solve(vals, b, precision=precision, method=3, rtol=1e-9, max_iterations=20000)
+        assert ok, (precision, it, rel)
+        Kp = K.astype(np.float32).astype(np.float64) if precision == 32 else K
+        y = spla.spsolve(Kp[indep][:, indep].tocsc(), b[indep])
+        xg = x.cpu().numpy()
+        assert np.abs(xg[indep] - y).max() <= 1e-6 * np.abs(y).max(), precision
 
 
 @pytest.mark.parametrize("precision", [64, 32])
