@@ -10,6 +10,7 @@
 #include "solver.cuh"
 
 #include <chrono>
+#include <cstdlib>
 
 namespace nuto_gpu
 {
@@ -118,6 +119,8 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     c.stats = nuto_gpu_stats{};
     nuto_gpu_stats& S = c.stats;
     Timers T(c);
+    int lastKrylov = 0;
+    double lastRel = 0;
     const unsigned gb = static_cast<unsigned>((n + 255) / 256);
 
     auto assembleK = [&](const double* x) {
@@ -140,18 +143,23 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     auto solve = [&](const double* rhs, double* out) {
         const auto k0 = std::chrono::steady_clock::now();
         int it = 0;
+        double* relp = &lastRel;
         if (fp32)
             KrylovSolveExport<float, float>(c, method, w.K32.p, rhs, out, false, o.krylov_rtol, o.max_krylov, &it,
-                                            nullptr);
+                                            relp);
         else
             KrylovSolveExport<double, double>(c, method, w.K64.p, rhs, out, false, o.krylov_rtol, o.max_krylov,
-                                              &it, nullptr);
+                                              &it, relp);
+        lastKrylov = it;
         T.Collect();
         S.ms_krylov += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - k0).count();
     };
 
     const double tOld = c.time;
     double* x = c.dX.p;
+    // NUTO_GPU_VERBOSE=1: one line per Newton iteration on stderr, like QuasistaticSolver::Info
+    const char* vb = std::getenv("NUTO_GPU_VERBOSE");
+    const bool verbose = vb && vb[0] == '1';
 
     // trial state: K(x_old), R(x_old, t_new), x_trial = x - C (C^T K C)^-1 C^T (R + K db) + db
     assembleK(x);
@@ -181,6 +189,9 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     double nr = residual(w.xs.p);
     int it = 0;
     bool conv = nr < tol || refNorm == 0.;
+    if (verbose)
+        std::fprintf(stderr, "[nuto_gpu] t = %g: trial |C^T r| = %.3e (ref %.3e, tol %.3e), krylov %d (rel %.2e)\n", tNew,
+                     nr, refNorm, tol, lastKrylov, lastRel);
     while (!conv && it < o.max_newton)
     {
         assembleK(w.xs.p);
@@ -208,6 +219,9 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
                 if (trial < (1. - alpha) * prev)
                     break;
             }
+            if (verbose)
+                std::fprintf(stderr, "[nuto_gpu] iteration %d: |C^T r| = %.3e, krylov %d (rel %.2e), alpha %g\n", it, nr,
+                             lastKrylov, lastRel, conv ? alpha : 2 * alpha);
         }
         else
         {

@@ -207,9 +207,10 @@ def test_linear_solve_quad4(precision, method):
     assert ok, (it, rel)
     import scipy.sparse.linalg as spla
 
-    # FP32 values: the FP64 refinement converges to the solution of the float-rounded operator (removing the
-    # rounding of the tangent itself is the job of Newton with the FP64 residual)
-    Kp = K.astype(np.float32).astype(np.float64) if precision == 32 else K
+    # FP32 values: the FP64 refinement converges to the solution of the FP32 operator the GPU assembled (removing
+    # the rounding of the tangent itself is the job of Newton with the FP64 residual)
+    rp, ci = g.pattern()
+    Kp = sp.csr_matrix((vals.double().cpu().numpy(), ci, rp), shape=K.shape) if precision == 32 else K
     y = spla.spsolve(Kp[indep][:, indep].tocsc(), b[indep])
     xr = np.zeros(P.n_dofs)
     xr[indep] = y
@@ -238,7 +239,7 @@ def _run_steps(kind, n, precision, steps, t_end, tol=1e-10):
 @pytest.mark.parametrize("precision", [64, 32])
 def test_quasistatic_quad4_elastic(precision):
     _torch()
-    res = _run_steps("quad4", 10, precision, 1, 1.0, tol=1e-9)
+    res = _run_steps("quad4", 10, precision, 1, 1.0, tol=1e-11)
     xo, xg, _, _, st = res[-1]
     rel = np.abs(xg - xo).max() / np.abs(xo).max()
     assert rel <= (1e-8 if precision == 64 else 1e-6), (rel, st)
@@ -262,7 +263,8 @@ def test_gmres_nonsymmetric_gradient_damage_tangent():
         vals = g.build_matrix(u, precision)
         x, it, rel, ok = g.solve(vals, b, precision=precision, method=3, rtol=1e-9, max_iterations=20000)
         assert ok, (precision, it, rel)
-        Kp = K.astype(np.float32).astype(np.float64) if precision == 32 else K
+        rp, ci = g.pattern()
+        Kp = sp.csr_matrix((vals.double().cpu().numpy(), ci, rp), shape=K.shape)
         y = spla.spsolve(Kp[indep][:, indep].tocsc(), b[indep])
         xg = x.cpu().numpy()
         assert np.abs(xg[indep] - y).max() <= 1e-6 * np.abs(y).max(), precision
@@ -273,7 +275,7 @@ def test_quasistatic_hex8_gradient_damage(precision):
     """Eight load steps of the gradient-damage beam (damage starts after step 4); displacement, eeq and the
     kappa history follow the oracle's direct-solve Newton."""
     _torch()
-    res = _run_steps("hex8gd", 3, precision, 8, 0.4)
+    res = _run_steps("hex8gd", 3, precision, 8, 0.4, tol=1e-12)
     for k, (xo, xg, ko, kg, st) in enumerate(res):
         rel = np.abs(xg - xo).max() / np.abs(xo).max()
         assert rel <= (1e-8 if precision == 64 else 1e-6), (k, rel, st)
