@@ -32,6 +32,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Newton-step time & assembled DOFs/s, FP32-tangent vs FP64 GPU at 1e-8 residual"
 LOAD_STEPS = 20
+# inexact Newton: each inner Krylov solve (both precisions) reduces its residual by 1e3; Newton on the FP64 residual
+# then converges linearly at about max(1e-3, rounding of the FP32 tangent) per iteration
+KRYLOV_RTOL = 1e-3
 
 
 def parse():
@@ -239,9 +242,9 @@ def run_ours(args):
     s = configs.hex8_gradient_damage(args.size, load_steps=LOAD_STEPS)
     g = s.build_gpu(device=local)
     n_dofs, nnz = g.n_dofs, g.nnz
-    opts32 = g.default_options(precision=nuto_gb300.FP32, newton_rtol=1e-8, krylov_rtol=1e-4, max_newton=20,
+    opts32 = g.default_options(precision=nuto_gb300.FP32, newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20,
                                max_krylov=20000)
-    opts64 = g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-8, krylov_rtol=1e-4, max_newton=20,
+    opts64 = g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20,
                                max_krylov=20000)
     dt = 1.0 / LOAD_STEPS
     g.set_state(None, 0.0, True)
@@ -349,7 +352,7 @@ def run_ours(args):
                       "n_dofs": n_dofs, "nnz": nnz, "precision": "FP32 tangent + FP32 GMRES(40), FP64 residual, "
                                                                 "history and Newton test",
                       "newton_tolerance": "|C^T r| <= 1e-8 |C^T (r + K db)| of the load step",
-                      "krylov_rtol": 1e-4, "l2": "inputs larger than L2 (FP32 tangent %.0f MB)" % (nnz * 4 / 1e6),
+                      "krylov_rtol": KRYLOV_RTOL, "l2": "inputs larger than L2 (FP32 tangent %.0f MB)" % (nnz * 4 / 1e6),
                       "parallelism": "replicas" if world > 1 else "single GPU"},
            "newton_step_ms": 1e3 * sec32 / max(agg32["matrix_assemblies"], 1),
            "newton_iterations": agg32["newton_iterations"], "tangent_solves": agg32["matrix_assemblies"],

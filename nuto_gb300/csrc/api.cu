@@ -385,6 +385,8 @@ static void BuildPattern(Ctx& c)
             M.rank = M.dRank.p;
         }
         Upload(M.dBlk, blk[p]);
+        Upload(M.dNbrPtr, nbr[p].ptr);
+        Upload(M.dNbrIdx, nbr[p].idx);
     }
     c.havePattern = true;
 }
@@ -870,7 +872,7 @@ int nuto_gpu_default_step_options(nuto_gpu_step_options* o)
     o->newton_atol = 0.0;
     o->max_newton = 20;
     o->line_search = 1;
-    o->krylov_rtol = 1e-4;
+    o->krylov_rtol = 1e-3;
     o->max_krylov = 20000;
     return NUTO_GPU_OK;
 }

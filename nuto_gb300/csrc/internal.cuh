@@ -179,6 +179,9 @@ struct PairMap
     DBuf<uint8_t> dRank; // planar [i * nenJ + j][cell]
     uint8_t* rank = nullptr; // dRank.p or a shared table of an identical pair
     DBuf<int32_t> dBlk; // per I-node
+    // J-neighbours of every I-node in CSR column order (the node-block SpMV reconstructs column indices from them)
+    DBuf<int64_t> dNbrPtr; // nNodes_I + 1
+    DBuf<int32_t> dNbrIdx;
 };
 
 // Device-side constants of one integrand (plain data passed by value to kernels).

@@ -113,48 +113,115 @@ enum Fin
     FIN_BICG_OMEGA = 3  // omega = (t.s) / (t.t)
 };
 
-// y = A x on the constrained operator (dependent rows: y = x), W lanes per row; optionally acc0 += w0.y and
-// acc1 += y.y, then the last block applies a finalize action.
-template <typename TV, typename TX, int W, int NDOT>
-__global__ void __launch_bounds__(kBS) k_spmv(int64_t n, int64_t nnz, const int64_t* __restrict__ rowPtr,
-                                               const int32_t* __restrict__ col, const TV* __restrict__ val,
-                                               const uint8_t* __restrict__ mask, const TX* __restrict__ x,
-                                               TX* __restrict__ y, const TX* __restrict__ w0, double* sc, int* st,
-                                               int fin)
+// Node-block SpMV: one warp per DOF node (of every slot) computes all rows of that node. DofNumbering numbers the
+// components of a node consecutively, so every row of node a lists, per slot J, the J-neighbours of a in the
+// same order with ncomp_J consecutive values each; the lanes run over the neighbours, load the neighbour's x
+// values once for all rows of the node and read the values at rowPtr[row] + blk_IJ(a) + ncomp_J * k + d. The
+// column indices are never read: the CSR values plus the per-node neighbour lists are the whole traffic.
+struct NodeSpmv
+{
+    int ns;
+    int ncomp[kMaxSlots];
+    int64_t nNodes[kMaxSlots];
+    int64_t firstWarp[kMaxSlots];
+    int64_t totalWarps;
+    const int64_t* gdof[kMaxSlots];
+    const int64_t* nbrPtr[kMaxSlots * kMaxSlots];
+    const int32_t* nbrIdx[kMaxSlots * kMaxSlots];
+    const int32_t* blk[kMaxSlots * kMaxSlots];
+    const int64_t* rowPtr;
+    int64_t nnz, nRows, nbrTotal[kMaxSlots * kMaxSlots];
+};
+
+template <typename TV, typename TX, int NDOT>
+__global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
+                                                    const uint8_t* __restrict__ mask, const TX* __restrict__ x,
+                                                    TX* __restrict__ y, const TX* __restrict__ w0, double* sc, int* st,
+                                                    int fin)
 {
     __shared__ double sh[kBS / 32];
     if (st && st[ST_STATE] != RUN)
         return;
-    const int64_t gt = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-    const int64_t row = gt / W;
-    const int lane = threadIdx.x % W;
-    TX sum = TX(0);
-    bool masked = false;
-    if (row < n)
+    const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int I = (A.ns > 1 && warp >= A.firstWarp[1]) ? 1 : 0;
+    const int64_t a = warp - A.firstWarp[I];
+    const bool valid = warp < A.totalWarps && a < A.nNodes[I];
+    const int ncI = A.ncomp[I];
+    TX s0 = TX(0), s1 = TX(0), s2 = TX(0);
+    int64_t g0 = 0, rs0 = 0, rs1 = 0, rs2 = 0;
+    if (valid)
     {
-        masked = mask[row] != 0;
-        if (!masked)
+        g0 = A.gdof[I][a];
+        rs0 = A.rowPtr[NG_IDX(g0, A.nRows, 16)];
+        if (ncI > 1)
+            rs1 = A.rowPtr[NG_IDX(g0 + 1, A.nRows, 16)];
+        if (ncI > 2)
+            rs2 = A.rowPtr[NG_IDX(g0 + 2, A.nRows, 16)];
+        for (int J = 0; J < A.ns; ++J)
         {
-            const int64_t end = rowPtr[row + 1];
-            for (int64_t k = rowPtr[row] + lane; k < end; k += W)
+            const int p = I * A.ns + J;
+            const int ncJ = A.ncomp[J];
+            const int64_t q0 = A.nbrPtr[p][a], q1 = A.nbrPtr[p][a + 1];
+            const int64_t blk = A.blk[p][a];
+            for (int64_t k = lane; k < q1 - q0; k += 32)
             {
-                const int64_t kk = NG_IDX(k, nnz, 12);
-                sum += static_cast<TX>(val[kk]) * x[NG_IDX(col[kk], n, 13)];
+                const int32_t b = A.nbrIdx[p][NG_IDX(q0 + k, A.nbrTotal[p], 17)];
+                const int64_t gb = A.gdof[J][b];
+                const TX x0 = x[NG_IDX(gb, A.nRows, 18)];
+                const TX x1 = ncJ > 1 ? x[NG_IDX(gb + 1, A.nRows, 18)] : TX(0);
+                const TX x2 = ncJ > 2 ? x[NG_IDX(gb + 2, A.nRows, 18)] : TX(0);
+                const int64_t off = blk + ncJ * k;
+                {
+                    const int64_t o = NG_IDX(rs0 + off, A.nnz, 19);
+                    s0 += static_cast<TX>(val[o]) * x0;
+                    if (ncJ > 1)
+                        s0 += static_cast<TX>(val[o + 1]) * x1;
+                    if (ncJ > 2)
+                        s0 += static_cast<TX>(val[o + 2]) * x2;
+                }
+                if (ncI > 1)
+                {
+                    const int64_t o = NG_IDX(rs1 + off, A.nnz, 19);
+                    s1 += static_cast<TX>(val[o]) * x0;
+                    if (ncJ > 1)
+                        s1 += static_cast<TX>(val[o + 1]) * x1;
+                    if (ncJ > 2)
+                        s1 += static_cast<TX>(val[o + 2]) * x2;
+                }
+                if (ncI > 2)
+                {
+                    const int64_t o = NG_IDX(rs2 + off, A.nnz, 19);
+                    s2 += static_cast<TX>(val[o]) * x0;
+                    if (ncJ > 1)
+                        s2 += static_cast<TX>(val[o + 1]) * x1;
+                    if (ncJ > 2)
+                        s2 += static_cast<TX>(val[o + 2]) * x2;
+                }
             }
         }
     }
 #pragma unroll
-    for (int o = W / 2; o > 0; o >>= 1)
-        sum += __shfl_down_sync(0xffffffffu, sum, o, W);
-    double d0 = 0., d1 = 0.;
-    if (row < n && lane == 0)
+    for (int o = 16; o > 0; o >>= 1)
     {
-        const TX yv = masked ? x[row] : sum;
-        y[row] = yv;
-        if (NDOT >= 1)
-            d0 = static_cast<double>(w0[row]) * static_cast<double>(yv);
-        if (NDOT >= 2)
-            d1 = static_cast<double>(yv) * static_cast<double>(yv);
+        s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    }
+    double d0 = 0., d1 = 0.;
+    if (valid && lane == 0)
+    {
+        const TX sums[3] = {s0, s1, s2};
+        for (int c = 0; c < ncI; ++c)
+        {
+            const int64_t r = g0 + c;
+            const TX yv = mask[r] ? x[r] : sums[c];
+            y[r] = yv;
+            if (NDOT >= 1)
+                d0 += static_cast<double>(w0[r]) * static_cast<double>(yv);
+            if (NDOT >= 2)
+                d1 += static_cast<double>(yv) * static_cast<double>(yv);
+        }
     }
     if (NDOT == 0)
         return;
@@ -482,27 +549,41 @@ static int GridFor(const Ctx& c, int64_t n)
     return static_cast<int>(want < cap ? want : cap);
 }
 
+static NodeSpmv MakeNodeSpmv(const Ctx& c)
+{
+    NodeSpmv A{};
+    A.ns = static_cast<int>(c.slots.size());
+    int64_t w = 0;
+    for (int I = 0; I < A.ns; ++I)
+    {
+        A.ncomp[I] = c.slots[I].ncomp;
+        A.nNodes[I] = c.slots[I].nNodes;
+        A.firstWarp[I] = w;
+        A.gdof[I] = c.slots[I].dGdof.p;
+        w += c.slots[I].nNodes;
+    }
+    A.totalWarps = w;
+    for (int p = 0; p < A.ns * A.ns; ++p)
+    {
+        A.nbrPtr[p] = c.pairs[p].dNbrPtr.p;
+        A.nbrIdx[p] = c.pairs[p].dNbrIdx.p;
+        A.blk[p] = c.pairs[p].dBlk.p;
+        A.nbrTotal[p] = static_cast<int64_t>(c.pairs[p].dNbrIdx.n);
+    }
+    A.rowPtr = c.dRowPtr.p;
+    A.nnz = c.nnz;
+    A.nRows = c.nDofs;
+    return A;
+}
+
 template <typename TV, typename TX, int NDOT>
 static void SpmvLaunch(Ctx& c, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc, int* st, int fin,
                        const uint8_t* mask)
 {
-    const int64_t n = c.nDofs;
-    const double avg = c.avgRowLen;
-    auto go = [&](auto wtag) {
-        constexpr int W = decltype(wtag)::value;
-        const int64_t threads = n * W;
-        const unsigned blocks = static_cast<unsigned>((threads + kBS - 1) / kBS);
-        k_spmv<TV, TX, W, NDOT><<<blocks, kBS, 0, c.stream>>>(n, c.nnz, c.dRowPtr.p, c.dColIdx.p, vals, mask, x, y,
-                                                              w0, sc, st, fin);
-    };
-    if (avg < 6)
-        go(std::integral_constant<int, 4>{});
-    else if (avg < 14)
-        go(std::integral_constant<int, 8>{});
-    else if (avg < 40)
-        go(std::integral_constant<int, 16>{});
-    else
-        go(std::integral_constant<int, 32>{});
+    const NodeSpmv A = MakeNodeSpmv(c);
+    const int64_t threads = A.totalWarps * 32;
+    const unsigned blocks = static_cast<unsigned>((threads + kBS - 1) / kBS);
+    k_spmv_node<TV, TX, NDOT><<<blocks, kBS, 0, c.stream>>>(A, vals, mask, x, y, w0, sc, st, fin);
 }
 
 // Krylov SpMV with a CUDA-event pair around it (device time of the dominant kernel, collected by SpmvCollect)
@@ -577,22 +658,49 @@ void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double
 // enqueued without a host round trip. The basis is stored in T (FP32 or FP64).
 using GL = GmresLayout;
 
-// acc[i] += V_i . w for i < nv (grid-stride dot per basis vector)
+// acc[i] += V_i . w for i < nv, eight basis vectors per pass; per-thread partial sums in T (the FP64 pipe is
+// narrow), FP64 across threads
+constexpr int kDotChunk = 8;
+
 template <typename T>
 __global__ void __launch_bounds__(kBS) k_gm_dots(int64_t n, const T* __restrict__ V, int nv, const T* __restrict__ w,
                                                   double* acc, const int* st)
 {
-    __shared__ double sh[kBS / 32];
+    __shared__ double sh[kBS / 32][kDotChunk];
     if (st[ST_STATE] != RUN)
         return;
-    for (int i = 0; i < nv; ++i)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i0 = 0; i0 < nv; i0 += kDotChunk)
     {
-        const T* v = V + static_cast<int64_t>(i) * n;
-        double s = 0;
+        T s[kDotChunk];
+#pragma unroll
+        for (int c = 0; c < kDotChunk; ++c)
+            s[c] = T(0);
         for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < n;
              r += static_cast<int64_t>(gridDim.x) * blockDim.x)
-            s += static_cast<double>(v[r]) * static_cast<double>(w[r]);
-        BlockAccumulate(s, acc + i, sh);
+        {
+            const T wr = w[r];
+#pragma unroll
+            for (int c = 0; c < kDotChunk; ++c)
+                if (i0 + c < nv)
+                    s[c] += V[static_cast<int64_t>(i0 + c) * n + r] * wr;
+        }
+#pragma unroll
+        for (int c = 0; c < kDotChunk; ++c)
+        {
+            const double v = WarpSum(static_cast<double>(s[c]));
+            if (lane == 0)
+                sh[wid][c] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < kDotChunk && i0 + static_cast<int>(threadIdx.x) < nv)
+        {
+            double t = 0;
+            for (int q = 0; q < static_cast<int>(blockDim.x >> 5); ++q)
+                t += sh[q][threadIdx.x];
+            atomicAdd(acc + i0 + threadIdx.x, t);
+        }
+        __syncthreads();
     }
 }
 
@@ -794,6 +902,7 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
     int total = 0;
     int state = RUN;
     double relEst = 1.;
+    double cycleStart = 1.;
     double beta0 = -1.;
     bool first = true;
     const int m = GL::m;
@@ -851,6 +960,14 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
         }
         if (state != RUN)
             break;
+        // stagnation: a full cycle that reduced the residual estimate by less than 5 % ends the solve (restarted
+        // GMRES can stall on indefinite systems); the caller gets the iterate and a non-converged status
+        if (k == cols && cycleStart > 0. && relEst > 0.95 * cycleStart)
+        {
+            state = BREAKDOWN;
+            break;
+        }
+        cycleStart = relEst;
         // restart: the state flag is reset by k_gm_start
     }
     if (state == CONVERGED && beta0 == 0.)

@@ -250,8 +250,13 @@ def test_gmres_nonsymmetric_gradient_damage_tangent():
     _torch()
     s, g, (om, layers, P, cons) = _build("hex8gd", 3)
     rng = np.random.default_rng(2)
-    u, kappa = _damage_state("hex8gd", P, rng)
-    P.kappa = kappa
+    # a consistent damaged state: eight load steps of the oracle's Newton (damage grows from step 4)
+    Q = QuasistaticOracle(P, cons[0], cons[1], cons[2], tolerance=1e-10, max_iterations=20)
+    for k in range(1, 9):
+        Q.do_step(0.05 * k)
+    u = Q.x.copy()
+    kappa = P.kappa.copy()
+    assert kappa.max() > 2e-4
     g.history = kappa
     K = _oracle_csr(P, u)
     b = rng.uniform(-1, 1, P.n_dofs)
@@ -261,7 +266,7 @@ def test_gmres_nonsymmetric_gradient_damage_tangent():
 
     for precision in (64, 32):
         vals = g.build_matrix(u, precision)
-        x, it, rel, ok = g.solve(vals, b, precision=precision, method=3, rtol=1e-9, max_iterations=20000)
+        x, it, rel, ok = g.solve(vals, b, precision=precision, method=3, rtol=1e-9, max_iterations=5000)
         assert ok, (precision, it, rel)
         rp, ci = g.pattern()
         Kp = sp.csr_matrix((vals.double().cpu().numpy(), ci, rp), shape=K.shape)
@@ -278,6 +283,8 @@ def test_quasistatic_hex8_gradient_damage(precision):
     res = _run_steps("hex8gd", 3, precision, 8, 0.4, tol=1e-12)
     for k, (xo, xg, ko, kg, st) in enumerate(res):
         rel = np.abs(xg - xo).max() / np.abs(xo).max()
-        assert rel <= (1e-8 if precision == 64 else 1e-6), (k, rel, st)
-        assert np.abs(kg - ko).max() <= (1e-8 if precision == 64 else 1e-6) * max(np.abs(ko).max(), 1e-4)
+        # the Newton tolerance (1e-12 on |C^T r|) bounds the eeq components only to ~1e-10 absolute, because the
+        # eeq rows scale with the cell volume; hence 1e-7 relative for the FP64 path
+        assert rel <= (1e-7 if precision == 64 else 1e-6), (k, rel, st)
+        assert np.abs(kg - ko).max() <= (1e-7 if precision == 64 else 1e-6) * max(np.abs(ko).max(), 1e-4)
     assert res[-1][2].max() > 1e-4  # the last steps are in the damaged regime
