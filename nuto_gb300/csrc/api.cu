@@ -305,6 +305,8 @@ static void BuildPattern(Ctx& c)
         c.hRowPtr[r + 1] = c.hRowPtr[r] + rowLen[r];
     c.nnz = c.hRowPtr.back();
     NG_CHECK(c.nnz < (int64_t(1) << 40), NUTO_GPU_EINVAL, "pattern too large");
+    NG_CHECK(*std::max_element(rowLen.begin(), rowLen.end()) <= 256, NUTO_GPU_EINVAL,
+             "a row has more than 256 entries (unsupported element family)");
     c.avgRowLen = c.nDofs ? double(c.nnz) / double(c.nDofs) : 0;
 
     std::vector<int32_t> colIdx(c.nnz);

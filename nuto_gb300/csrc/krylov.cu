@@ -133,6 +133,8 @@ struct NodeSpmv
     int64_t nnz, nRows, nbrTotal[kMaxSlots * kMaxSlots];
 };
 
+constexpr int kMaxRowLen = 256; // longest row of a node (Hex20 displacements: 3 x 81)
+
 template <typename TV, typename TX, int NDOT>
 __global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
                                                     const uint8_t* __restrict__ mask, const TX* __restrict__ x,
@@ -140,87 +142,56 @@ __global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restr
                                                     int fin)
 {
     __shared__ double sh[kBS / 32];
+    __shared__ TX xs[kBS / 32][kMaxRowLen];
     if (st && st[ST_STATE] != RUN)
         return;
     const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int I = (A.ns > 1 && warp >= A.firstWarp[1]) ? 1 : 0;
     const int64_t a = warp - A.firstWarp[I];
     const bool valid = warp < A.totalWarps && a < A.nNodes[I];
     const int ncI = A.ncomp[I];
-    TX s0 = TX(0), s1 = TX(0), s2 = TX(0);
-    int64_t g0 = 0, rs0 = 0, rs1 = 0, rs2 = 0;
+    double d0 = 0., d1 = 0.;
     if (valid)
     {
-        g0 = A.gdof[I][a];
-        rs0 = A.rowPtr[NG_IDX(g0, A.nRows, 16)];
-        if (ncI > 1)
-            rs1 = A.rowPtr[NG_IDX(g0 + 1, A.nRows, 16)];
-        if (ncI > 2)
-            rs2 = A.rowPtr[NG_IDX(g0 + 2, A.nRows, 16)];
+        // x of the node's neighbours in the column order of its rows
+        int len = 0;
         for (int J = 0; J < A.ns; ++J)
         {
             const int p = I * A.ns + J;
             const int ncJ = A.ncomp[J];
-            const int64_t q0 = A.nbrPtr[p][a], q1 = A.nbrPtr[p][a + 1];
-            const int64_t blk = A.blk[p][a];
-            for (int64_t k = lane; k < q1 - q0; k += 32)
+            const int64_t q0 = A.nbrPtr[p][a];
+            const int nn = static_cast<int>(A.nbrPtr[p][a + 1] - q0);
+            for (int kk = lane; kk < nn; kk += 32)
             {
-                const int32_t b = A.nbrIdx[p][NG_IDX(q0 + k, A.nbrTotal[p], 17)];
-                const int64_t gb = A.gdof[J][b];
-                const TX x0 = x[NG_IDX(gb, A.nRows, 18)];
-                const TX x1 = ncJ > 1 ? x[NG_IDX(gb + 1, A.nRows, 18)] : TX(0);
-                const TX x2 = ncJ > 2 ? x[NG_IDX(gb + 2, A.nRows, 18)] : TX(0);
-                const int64_t off = blk + ncJ * k;
-                {
-                    const int64_t o = NG_IDX(rs0 + off, A.nnz, 19);
-                    s0 += static_cast<TX>(val[o]) * x0;
-                    if (ncJ > 1)
-                        s0 += static_cast<TX>(val[o + 1]) * x1;
-                    if (ncJ > 2)
-                        s0 += static_cast<TX>(val[o + 2]) * x2;
-                }
-                if (ncI > 1)
-                {
-                    const int64_t o = NG_IDX(rs1 + off, A.nnz, 19);
-                    s1 += static_cast<TX>(val[o]) * x0;
-                    if (ncJ > 1)
-                        s1 += static_cast<TX>(val[o + 1]) * x1;
-                    if (ncJ > 2)
-                        s1 += static_cast<TX>(val[o + 2]) * x2;
-                }
-                if (ncI > 2)
-                {
-                    const int64_t o = NG_IDX(rs2 + off, A.nnz, 19);
-                    s2 += static_cast<TX>(val[o]) * x0;
-                    if (ncJ > 1)
-                        s2 += static_cast<TX>(val[o + 1]) * x1;
-                    if (ncJ > 2)
-                        s2 += static_cast<TX>(val[o + 2]) * x2;
-                }
+                const int64_t gb = A.gdof[J][A.nbrIdx[p][NG_IDX(q0 + kk, A.nbrTotal[p], 17)]];
+                for (int d = 0; d < ncJ; ++d)
+                    xs[wid][NG_IDX(len + ncJ * kk + d, kMaxRowLen, 20)] = x[NG_IDX(gb + d, A.nRows, 18)];
             }
+            len += ncJ * nn;
         }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        s0 += __shfl_down_sync(0xffffffffu, s0, o);
-        s1 += __shfl_down_sync(0xffffffffu, s1, o);
-        s2 += __shfl_down_sync(0xffffffffu, s2, o);
-    }
-    double d0 = 0., d1 = 0.;
-    if (valid && lane == 0)
-    {
-        const TX sums[3] = {s0, s1, s2};
+        __syncwarp();
+        const int64_t g0 = A.gdof[I][a];
         for (int c = 0; c < ncI; ++c)
         {
             const int64_t r = g0 + c;
-            const TX yv = mask[r] ? x[r] : sums[c];
-            y[r] = yv;
-            if (NDOT >= 1)
-                d0 += static_cast<double>(w0[r]) * static_cast<double>(yv);
-            if (NDOT >= 2)
-                d1 += static_cast<double>(yv) * static_cast<double>(yv);
+            const int64_t rs = A.rowPtr[NG_IDX(r, A.nRows, 16)];
+            TX s = TX(0);
+#pragma unroll 4
+            for (int q = lane; q < len; q += 32)
+                s += static_cast<TX>(val[NG_IDX(rs + q, A.nnz, 19)]) * xs[wid][q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                s += __shfl_down_sync(0xffffffffu, s, o);
+            if (lane == 0)
+            {
+                const TX yv = mask[r] ? x[r] : s;
+                y[r] = yv;
+                if (NDOT >= 1)
+                    d0 += static_cast<double>(w0[r]) * static_cast<double>(yv);
+                if (NDOT >= 2)
+                    d1 += static_cast<double>(yv) * static_cast<double>(yv);
+            }
         }
     }
     if (NDOT == 0)
@@ -902,7 +873,7 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
     int total = 0;
     int state = RUN;
     double relEst = 1.;
-    double cycleStart = 1.;
+    std::vector<double> history;
     double beta0 = -1.;
     bool first = true;
     const int m = GL::m;
@@ -960,14 +931,14 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
         }
         if (state != RUN)
             break;
-        // stagnation: a full cycle that reduced the residual estimate by less than 5 % ends the solve (restarted
-        // GMRES can stall on indefinite systems); the caller gets the iterate and a non-converged status
-        if (k == cols && cycleStart > 0. && relEst > 0.95 * cycleStart)
+        // stagnation: eight full cycles that together reduced the residual estimate by less than 10 % end the solve
+        // (restarted GMRES can stall on indefinite systems); the caller gets the iterate and a non-converged status
+        history.push_back(relEst);
+        if (k == cols && history.size() > 8 && relEst > 0.9 * history[history.size() - 9])
         {
             state = BREAKDOWN;
             break;
         }
-        cycleStart = relEst;
         // restart: the state flag is reset by k_gm_start
     }
     if (state == CONVERGED && beta0 == 0.)
