@@ -33,6 +33,7 @@
  *                               results (any CellInterface::VectorFunction/MatrixFunction)
  *   nuto_gpu_solve              Solve (C^T K C u = C^T f) + EigenSparseSolve nuto/mechanics/solver/Solve.cpp:8-34,
  *                                                                        nuto/math/EigenSparseSolve.cpp:22-73
+ *   nuto_gpu_set_preconditioner (none: the reference factorises the matrix)
  *   nuto_gpu_do_step            QuasistaticSolver::DoStep (trial state, NewtonRaphson::Solve with LineSearch,
  *                               UpdateHistory)                           nuto/mechanics/tools/QuasistaticSolver.cpp:51-147,
  *                                                                        nuto/math/NewtonRaphson.h:62-94, nuto/math/LineSearch.h:38-63
@@ -80,9 +81,13 @@ extern "C" {
 
 /* Krylov methods */
 #define NUTO_GPU_SOLVER_AUTO 0     /* PCG for the symmetric integrands, GMRES otherwise */
-#define NUTO_GPU_SOLVER_PCG 1      /* Jacobi-preconditioned CG */
-#define NUTO_GPU_SOLVER_BICGSTAB 2 /* Jacobi-preconditioned BiCGStab */
-#define NUTO_GPU_SOLVER_GMRES 3    /* Jacobi-preconditioned restarted GMRES(40) */
+#define NUTO_GPU_SOLVER_PCG 1      /* preconditioned CG */
+#define NUTO_GPU_SOLVER_BICGSTAB 2 /* Jacobi-preconditioned BiCGStab (always Jacobi) */
+#define NUTO_GPU_SOLVER_GMRES 3    /* restarted GMRES(40), right-preconditioned (flexible form) */
+
+/* preconditioners of PCG and GMRES (nuto_gpu_set_preconditioner) */
+#define NUTO_GPU_PRECOND_JACOBI 1 /* diagonal */
+#define NUTO_GPU_PRECOND_AMG 2    /* aggregation multigrid V-cycle in FP32 (default) */
 
 typedef struct nuto_gpu_ctx nuto_gpu_ctx;
 
@@ -192,6 +197,11 @@ int nuto_gpu_assemble_cell_matrices(nuto_gpu_ctx* ctx, const double* d_cell_matr
    rows and columns are eliminated) and writes x = C y (zero at dependent DOFs). */
 int nuto_gpu_solve(nuto_gpu_ctx* ctx, int precision, int method, const void* d_values, const double* d_b,
                    double* d_x, double rtol, int max_iterations, int* iterations, double* relative_residual);
+/* Preconditioner of the PCG and GMRES solves of nuto_gpu_solve and nuto_gpu_do_step (NUTO_GPU_PRECOND_*). The
+   multigrid hierarchy (spatial aggregates of the DOF nodes, piecewise-constant transfer per component) is built
+   on the first solve after build_pattern; its coarse operators are rebuilt once per tangent. No counterpart in
+   the reference, which factorises the matrix (EigenSparseSolve.cpp:22-73). */
+int nuto_gpu_set_preconditioner(nuto_gpu_ctx* ctx, int preconditioner);
 
 /* ---- quasistatic driver ------------------------------------------------------------------------------ */
 int nuto_gpu_default_step_options(nuto_gpu_step_options* opts);

@@ -17,7 +17,8 @@ PLANE_STRESS, PLANE_STRAIN = 0, 1
 DAMAGE_FULL, DAMAGE_UNILATERAL = 0, 1
 INTERACTION_CONSTANT, INTERACTION_DECREASING = 0, 1
 FP32, FP64 = 32, 64
-SOLVER_AUTO, SOLVER_PCG, SOLVER_BICGSTAB = 0, 1, 2
+SOLVER_AUTO, SOLVER_PCG, SOLVER_BICGSTAB, SOLVER_GMRES = 0, 1, 2, 3
+PRECOND_JACOBI, PRECOND_AMG = 1, 2
 
 _ERRNAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ENOCONV: "ENOCONV", ENAN: "ENAN", ETIMEOUT: "ETIMEOUT",
              ECUDA: "ECUDA", ESTATE: "ESTATE"}
@@ -90,6 +91,7 @@ SIGNATURES = {
     "nuto_gpu_assemble_cell_vectors": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_assemble_cell_matrices": (_i, [_vp, _vp, _i, _vp]),
     "nuto_gpu_solve": (_i, [_vp, _i, _i, _vp, _vp, _vp, _d, _i, _P(_i), _P(_d)]),
+    "nuto_gpu_set_preconditioner": (_i, [_vp, _i]),
     "nuto_gpu_default_step_options": (_i, [_P(StepOptions)]),
     "nuto_gpu_set_state": (_i, [_vp, _vp, _d, _i]),
     "nuto_gpu_get_state": (_i, [_vp, _vp, _P(_d)]),

@@ -168,6 +168,10 @@ class GpuCellGroup:
             check(self.h, rc)
         return x, it.value, rel.value, rc == _lib.OK
 
+    def set_preconditioner(self, kind):
+        """PRECOND_JACOBI or PRECOND_AMG (default) for the PCG and GMRES solves of solve() and do_step()."""
+        self._call("nuto_gpu_set_preconditioner", int(kind))
+
     # ---- quasistatic driver --------------------------------------------------------------------------------
     @staticmethod
     def default_options(**kw):

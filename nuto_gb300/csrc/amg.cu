@@ -1,0 +1,752 @@
+// Aggregation multigrid preconditioner for the Krylov solvers. The reference has no iterative solver on this
+// path (it factorises the matrix, EigenSparseSolve.cpp:22-73); this is the GB300-side replacement of that
+// factorisation inside the Newton loop.
+//
+// Structure: one hierarchy per DOF slot (displacements, nonlocal equivalent strains), applied as one block
+// Gauss-Seidel sweep in slot order: z_0 = V_0(v_0), z_1 = V_1(v_1 - K_10 z_0). For gradient damage K_10 (the
+// dependence of the eeq equation on the local strain) is the strong coupling and K_01 vanishes outside the
+// damaging zone, so the sweep is exact there up to the V-cycles.
+//
+// Hierarchy (host, once per pattern): the DOF nodes of a slot are grouped into aggregates by spatial binning.
+// The bins start at one cell extent per axis and grow per level by doubling the axes that are shorter than the
+// longest by more than half (all axes when none is), so stretched cells (the 1 x 1 x 4 beam) first coarsen across
+// their short sides. Levels stop at kCoarsest nodes. Transfer is piecewise constant per component; constrained
+// DOFs take part in neither restriction nor prolongation. Coarse operators keep the node-block CSR layout, so the
+// node SpMV serves every level; level 0 is a diagonal-block view of the tangent itself.
+//
+// Per tangent (device, FP32): Galerkin coarse values A_c = P^T A P by one pass over the finer values with
+// atomics; Jacobi diagonals and Gershgorin bounds of D^-1 A per level. Cycle: V(2,2) with Chebyshev-Jacobi
+// smoothing on [lmax / 10, lmax] and a degree-6 Chebyshev solve on the coarsest level. The sweep is a fixed
+// linear operator; GMRES uses it in flexible form (stored preconditioned basis) so FP32 rounding inside the cycle
+// does not limit the attainable residual.
+#include "spmv.cuh"
+
+#include <algorithm>
+#include <numeric>
+#include <unordered_map>
+
+namespace nuto_gpu
+{
+
+constexpr int kCoarsest = 64; // nodes on the coarsest level
+constexpr int kMaxLevels = 12;
+constexpr int kPreDegree = 2;
+constexpr int kPostDegree = 2;
+constexpr int kCoarseDegree = 6;
+constexpr float kSmoothRatio = 10.f; // smoothing interval [lmax / ratio, lmax]
+constexpr float kCoarseRatio = 30.f;
+
+struct AmgLevel
+{
+    int ncomp = 1;
+    int64_t nNodes = 0;
+    int64_t nDofs = 0, nnz = 0;
+    // level-0 views address the combined vectors: rows [off, off + nDofs) of the slot
+    int64_t off = 0;
+    std::vector<int64_t> hNbrPtr;
+    std::vector<int32_t> hNbrIdx;
+    std::vector<double> hCoords; // 3 per node
+    // device structure of coarse levels (level 0 uses the context's pattern)
+    DBuf<int64_t> gdof, rowPtr, nbrPtr;
+    DBuf<int32_t> nbrIdx, blk;
+    DBuf<int32_t> diagOff;  // per node: offset of the diagonal block in the node's row segment
+    DBuf<uint8_t> zeroMask; // coarse levels have no constrained rows
+    // transfer from the finer level
+    DBuf<int32_t> aggOf;   // finer node -> node of this level
+    DBuf<uint16_t> cRank;  // finer neighbour entry -> rank in this level's neighbour list
+    // numerics
+    DBuf<float> vals, dinv, e, b, t, d;
+    float lmax = 1.f;
+    NodeSpmv spmv{};
+};
+
+struct Amg
+{
+    int ns = 0;
+    std::vector<AmgLevel> h[kMaxSlots];
+    DBuf<float> lmaxDev; // all levels of all hierarchies
+    std::vector<float> lmaxHost;
+    DBuf<float> fine32; // FP32 copy of an FP64 tangent
+    DBuf<float> in32, out32, res32; // combined-length work vectors of the sweep
+    const float* fine = nullptr;
+    const void* setupVals = nullptr;
+    uint64_t setupVersion = 0;
+    bool built = false;
+};
+
+void FreeAmg(Ctx& c)
+{
+    delete c.amg;
+    c.amg = nullptr;
+}
+
+// ---- host: hierarchy -------------------------------------------------------------------------------------------
+// natural coordinates of the local nodes (InterpolationQuadLinear / BrickLinear / BrickQuadratic order)
+static void LocalNodeCoords(int interp, int n, double* xi)
+{
+    static const double h20[20][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, 1}, {1, -1, 1},
+                                      {1, 1, 1},    {-1, 1, 1},  {0, -1, -1}, {1, 0, -1},  {0, 1, -1},  {-1, 0, -1},
+                                      {-1, -1, 0},  {1, -1, 0},  {1, 1, 0},   {-1, 1, 0},  {0, -1, 1},  {1, 0, 1},
+                                      {0, 1, 1},    {-1, 0, 1}};
+    static const double q4[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+    if (interp == NUTO_GPU_QUAD4)
+    {
+        xi[0] = q4[n][0];
+        xi[1] = q4[n][1];
+        xi[2] = 0;
+        return;
+    }
+    for (int d = 0; d < 3; ++d)
+        xi[d] = h20[n][d];
+}
+
+// shape functions of the coordinate element (Quad4 / Hex8) at a natural point
+static void GeoShape(int geo, const double* xi, double* N)
+{
+    if (geo == NUTO_GPU_QUAD4)
+    {
+        const double r = xi[0], s = xi[1];
+        N[0] = 0.25 * (1 - r) * (1 - s);
+        N[1] = 0.25 * (1 + r) * (1 - s);
+        N[2] = 0.25 * (1 + r) * (1 + s);
+        N[3] = 0.25 * (1 - r) * (1 + s);
+        return;
+    }
+    const int sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                          {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+    for (int i = 0; i < 8; ++i)
+        N[i] = 0.125 * (1 + sg[i][0] * xi[0]) * (1 + sg[i][1] * xi[1]) * (1 + sg[i][2] * xi[2]);
+}
+
+// per node: offset of the node's own block inside its neighbour segment
+static std::vector<int32_t> DiagOffsets(const std::vector<int64_t>& ptr, const std::vector<int32_t>& idx, int ncomp)
+{
+    const int64_t n = static_cast<int64_t>(ptr.size()) - 1;
+    std::vector<int32_t> off(n, 0);
+    for (int64_t a = 0; a < n; ++a)
+    {
+        const int32_t* first = idx.data() + ptr[a];
+        const int32_t* last = idx.data() + ptr[a + 1];
+        const int32_t* it = std::find(first, last, static_cast<int32_t>(a));
+        NG_CHECK(it != last, NUTO_GPU_EINVAL, "a node is missing from its own neighbour list");
+        off[a] = static_cast<int32_t>(ncomp * (it - first));
+    }
+    return off;
+}
+
+template <typename T>
+static void UploadV(DBuf<T>& buf, const std::vector<T>& h)
+{
+    buf.alloc(h.size());
+    if (!h.empty())
+        NG_CUDA(cudaMemcpy(buf.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+// single-slot NodeSpmv of a coarse level
+static void FillSpmv(AmgLevel& L)
+{
+    NodeSpmv& A = L.spmv;
+    A = NodeSpmv{};
+    A.ns = 1;
+    A.ncomp[0] = L.ncomp;
+    A.nNodes[0] = L.nNodes;
+    A.firstWarp[0] = 0;
+    A.totalWarps = L.nNodes;
+    A.gdof[0] = L.gdof.p;
+    A.nbrPtr[0] = L.nbrPtr.p;
+    A.nbrIdx[0] = L.nbrIdx.p;
+    A.blk[0] = L.blk.p;
+    A.nbrTotal[0] = static_cast<int64_t>(L.nbrIdx.n);
+    A.rowPtr = L.rowPtr.p;
+    A.nnz = L.nnz;
+    A.nRows = L.nDofs;
+}
+
+// diagonal-block view of slot I of the context's tangent
+static NodeSpmv SlotView(const Ctx& c, int I)
+{
+    const int ns = static_cast<int>(c.slots.size());
+    const PairMap& M = c.pairs[I * ns + I];
+    NodeSpmv A{};
+    A.ns = 1;
+    A.ncomp[0] = c.slots[I].ncomp;
+    A.nNodes[0] = c.slots[I].nNodes;
+    A.firstWarp[0] = 0;
+    A.totalWarps = c.slots[I].nNodes;
+    A.gdof[0] = c.slots[I].dGdof.p;
+    A.nbrPtr[0] = M.dNbrPtr.p;
+    A.nbrIdx[0] = M.dNbrIdx.p;
+    A.blk[0] = M.dBlk.p;
+    A.nbrTotal[0] = static_cast<int64_t>(M.dNbrIdx.n);
+    A.rowPtr = c.dRowPtr.p;
+    A.nnz = c.nnz;
+    A.nRows = c.nDofs;
+    return A;
+}
+
+// whole-row operator restricted to the rows of slot I (K_I0 z_0 + K_II z_I, used with z_I = 0)
+static NodeSpmv RowsView(const Ctx& c, int I)
+{
+    NodeSpmv A = MakeNodeSpmv(c);
+    if (I == 1)
+    {
+        A.firstWarp[1] = 0;
+        A.totalWarps = A.nNodes[1];
+    }
+    else
+        A.totalWarps = A.nNodes[0];
+    return A;
+}
+
+static void GrowBins(double* bin, int dim)
+{
+    double mx = 0;
+    for (int d = 0; d < dim; ++d)
+        mx = std::max(mx, bin[d]);
+    bool any = false;
+    for (int d = 0; d < dim; ++d)
+        any = any || bin[d] * 1.5 < mx;
+    for (int d = 0; d < dim; ++d)
+        if (!any || bin[d] * 1.5 < mx)
+            bin[d] *= 2.0;
+}
+
+static void BuildSlotHierarchy(Ctx& c, int I, const double* ext, std::vector<AmgLevel>& H)
+{
+    const int ns = static_cast<int>(c.slots.size());
+    const Slot& S = c.slots[I];
+    H.clear();
+    H.emplace_back();
+    {
+        AmgLevel& F = H[0];
+        F.ncomp = S.ncomp;
+        F.nNodes = S.nNodes;
+        F.nDofs = S.nDofs;
+        F.off = S.offset;
+        F.hNbrPtr = c.pairs[I * ns + I].hNbrPtr;
+        F.hNbrIdx = c.pairs[I * ns + I].hNbrIdx;
+        // DOF-node coordinates: the coordinate element interpolated at the node's natural coordinates
+        F.hCoords.assign(S.nNodes * 3, 0.);
+        std::vector<char> done(S.nNodes, 0);
+        for (int64_t e = 0; e < c.nCells; ++e)
+            for (int n = 0; n < S.nen; ++n)
+            {
+                const int32_t node = S.conn[e * S.nen + n];
+                if (done[node])
+                    continue;
+                done[node] = 1;
+                double xi[3], N[8];
+                LocalNodeCoords(S.interp, n, xi);
+                GeoShape(c.geoInterp, xi, N);
+                for (int d = 0; d < c.dim; ++d)
+                {
+                    double v = 0;
+                    for (int g = 0; g < c.nge; ++g)
+                        v += N[g] * c.hCoords[static_cast<size_t>(c.hGeoConn[e * c.nge + g]) * c.dim + d];
+                    F.hCoords[node * 3 + d] = v;
+                }
+            }
+        UploadV(F.diagOff, DiagOffsets(F.hNbrPtr, F.hNbrIdx, F.ncomp));
+        F.spmv = SlotView(c, I);
+    }
+    double lo[3] = {1e300, 1e300, 1e300};
+    for (int64_t a = 0; a < H[0].nNodes; ++a)
+        for (int d = 0; d < 3; ++d)
+            lo[d] = std::min(lo[d], H[0].hCoords[a * 3 + d]);
+    double bin[3] = {ext[0], ext[1], ext[2]};
+    GrowBins(bin, c.dim);
+
+    for (int level = 1; level < kMaxLevels; ++level)
+    {
+        AmgLevel& Fi = H[level - 1];
+        if (Fi.nNodes <= kCoarsest)
+            break;
+        AmgLevel C;
+        C.ncomp = Fi.ncomp;
+        std::unordered_map<int64_t, int32_t> keyToAgg;
+        keyToAgg.reserve(Fi.nNodes / 4 + 16);
+        std::vector<int32_t> agg(Fi.nNodes, -1);
+        std::vector<double> sum;
+        std::vector<int64_t> cnt;
+        for (int64_t a = 0; a < Fi.nNodes; ++a)
+        {
+            int64_t key = 0;
+            for (int d = 0; d < 3; ++d)
+            {
+                const double x = (Fi.hCoords[a * 3 + d] - lo[d]) / (d < c.dim ? bin[d] : 1.0);
+                key = key * 2097152 + static_cast<int64_t>(std::floor(x + 1e-9));
+            }
+            auto it = keyToAgg.find(key);
+            int32_t A;
+            if (it == keyToAgg.end())
+            {
+                A = static_cast<int32_t>(keyToAgg.size());
+                keyToAgg.emplace(key, A);
+                sum.insert(sum.end(), {0., 0., 0.});
+                cnt.push_back(0);
+            }
+            else
+                A = it->second;
+            agg[a] = A;
+            for (int d = 0; d < 3; ++d)
+                sum[A * 3 + d] += Fi.hCoords[a * 3 + d];
+            cnt[A]++;
+        }
+        C.nNodes = static_cast<int64_t>(cnt.size());
+        if (C.nNodes * 5 >= Fi.nNodes * 4)
+            break; // the bins no longer merge nodes
+        C.hCoords.resize(cnt.size() * 3);
+        for (size_t A = 0; A < cnt.size(); ++A)
+            for (int d = 0; d < 3; ++d)
+                C.hCoords[A * 3 + d] = sum[A * 3 + d] / cnt[A];
+        // members of every aggregate
+        std::vector<int64_t> mptr(C.nNodes + 1, 0);
+        for (int64_t a = 0; a < Fi.nNodes; ++a)
+            mptr[agg[a] + 1]++;
+        for (int64_t A = 0; A < C.nNodes; ++A)
+            mptr[A + 1] += mptr[A];
+        std::vector<int64_t> fill(mptr.begin(), mptr.end() - 1);
+        std::vector<int32_t> mem(Fi.nNodes);
+        for (int64_t a = 0; a < Fi.nNodes; ++a)
+            mem[fill[agg[a]]++] = static_cast<int32_t>(a);
+        // coarse neighbour lists (sorted by node index = DOF order on coarse levels)
+        std::vector<std::vector<int32_t>> lists(C.nNodes);
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int64_t A = 0; A < C.nNodes; ++A)
+        {
+            auto& v = lists[A];
+            for (int64_t m = mptr[A]; m < mptr[A + 1]; ++m)
+            {
+                const int32_t a = mem[m];
+                for (int64_t q = Fi.hNbrPtr[a]; q < Fi.hNbrPtr[a + 1]; ++q)
+                    v.push_back(agg[Fi.hNbrIdx[q]]);
+            }
+            std::sort(v.begin(), v.end());
+            v.erase(std::unique(v.begin(), v.end()), v.end());
+        }
+        C.hNbrPtr.assign(C.nNodes + 1, 0);
+        int64_t maxLen = 0;
+        for (int64_t A = 0; A < C.nNodes; ++A)
+        {
+            C.hNbrPtr[A + 1] = C.hNbrPtr[A] + static_cast<int64_t>(lists[A].size());
+            maxLen = std::max(maxLen, static_cast<int64_t>(lists[A].size()) * C.ncomp);
+        }
+        if (maxLen > kMaxRowLen)
+            break; // a denser coarse stencil than the SpMV supports: keep the finer level as the coarsest
+        C.hNbrIdx.resize(C.hNbrPtr.back());
+        for (int64_t A = 0; A < C.nNodes; ++A)
+            std::copy(lists[A].begin(), lists[A].end(), C.hNbrIdx.begin() + C.hNbrPtr[A]);
+        // rank of every finer neighbour entry in the coarse list of its aggregate
+        std::vector<uint16_t> cr(Fi.hNbrIdx.size());
+#pragma omp parallel for schedule(static)
+        for (int64_t a = 0; a < Fi.nNodes; ++a)
+        {
+            const int32_t A = agg[a];
+            const int32_t* first = C.hNbrIdx.data() + C.hNbrPtr[A];
+            const int32_t* last = C.hNbrIdx.data() + C.hNbrPtr[A + 1];
+            for (int64_t q = Fi.hNbrPtr[a]; q < Fi.hNbrPtr[a + 1]; ++q)
+                cr[q] = static_cast<uint16_t>(std::lower_bound(first, last, agg[Fi.hNbrIdx[q]]) - first);
+        }
+        // node-block CSR of the coarse level
+        C.nDofs = C.nNodes * C.ncomp;
+        std::vector<int64_t> rowPtr(C.nDofs + 1, 0), gdof(C.nNodes);
+        std::vector<int32_t> blk(C.nNodes, 0);
+        for (int64_t A = 0; A < C.nNodes; ++A)
+        {
+            gdof[A] = A * C.ncomp;
+            const int64_t len = C.ncomp * (C.hNbrPtr[A + 1] - C.hNbrPtr[A]);
+            for (int k = 0; k < C.ncomp; ++k)
+                rowPtr[A * C.ncomp + k + 1] = len;
+        }
+        for (int64_t r = 0; r < C.nDofs; ++r)
+            rowPtr[r + 1] += rowPtr[r];
+        C.nnz = rowPtr.back();
+        UploadV(C.rowPtr, rowPtr);
+        UploadV(C.gdof, gdof);
+        UploadV(C.blk, blk);
+        UploadV(C.nbrPtr, C.hNbrPtr);
+        UploadV(C.nbrIdx, C.hNbrIdx);
+        UploadV(C.diagOff, DiagOffsets(C.hNbrPtr, C.hNbrIdx, C.ncomp));
+        UploadV(C.aggOf, agg);
+        UploadV(C.cRank, cr);
+        C.zeroMask.alloc(C.nDofs);
+        NG_CUDA(cudaMemset(C.zeroMask.p, 0, C.nDofs));
+        C.vals.alloc(C.nnz);
+        for (DBuf<float>* b : {&C.dinv, &C.e, &C.b, &C.t, &C.d})
+            b->alloc(C.nDofs);
+        FillSpmv(C);
+        H.push_back(std::move(C));
+        GrowBins(bin, c.dim);
+    }
+    // level-0 work vectors span the combined system (the view writes rows of this slot only)
+    for (DBuf<float>* b : {&H[0].dinv, &H[0].t, &H[0].d})
+        b->alloc(c.nDofs);
+    H[0].nnz = c.nnz;
+}
+
+static void BuildHierarchy(Ctx& c)
+{
+    Amg& M = *c.amg;
+    M.ns = static_cast<int>(c.slots.size());
+    // median cell extent per axis (every 7th cell)
+    double ext[3] = {1, 1, 1};
+    for (int d = 0; d < c.dim; ++d)
+    {
+        std::vector<double> v;
+        for (int64_t e = 0; e < c.nCells; e += 7)
+        {
+            double lo = 1e300, hi = -1e300;
+            for (int g = 0; g < c.nge; ++g)
+            {
+                const double x = c.hCoords[static_cast<size_t>(c.hGeoConn[e * c.nge + g]) * c.dim + d];
+                lo = std::min(lo, x);
+                hi = std::max(hi, x);
+            }
+            v.push_back(hi - lo);
+        }
+        std::nth_element(v.begin(), v.begin() + v.size() / 2, v.end());
+        ext[d] = v[v.size() / 2];
+        NG_CHECK(ext[d] > 0, NUTO_GPU_EINVAL, "degenerate cells");
+    }
+    size_t total = 0;
+    for (int I = 0; I < M.ns; ++I)
+    {
+        BuildSlotHierarchy(c, I, ext, M.h[I]);
+        total += M.h[I].size();
+    }
+    M.lmaxDev.alloc(total);
+    M.lmaxHost.assign(total, 0.f);
+    for (DBuf<float>* b : {&M.in32, &M.out32, &M.res32})
+        b->alloc(c.nDofs);
+    M.setupVals = nullptr;
+    M.built = true;
+}
+
+// ---- device: per-tangent set-up -----------------------------------------------------------------------------------
+// Galerkin coarse values: one warp per finer node adds its (unconstrained) rows into the aggregate's rows
+__global__ void __launch_bounds__(kBS) k_amg_coarsen(NodeSpmv F, const uint8_t* __restrict__ fmask,
+                                                      const float* __restrict__ fv, NodeSpmv C,
+                                                      const int32_t* __restrict__ agg, const uint16_t* __restrict__ cr,
+                                                      float* cv)
+{
+    const int64_t a = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (a >= F.totalWarps)
+        return;
+    const int32_t A = agg[a];
+    const int nc = F.ncomp[0];
+    const int64_t g0 = F.gdof[0][a];
+    const int64_t G0 = C.gdof[0][NG_IDX(A, C.nNodes[0], 31)];
+    const int64_t q0 = F.nbrPtr[0][a];
+    const int nn = static_cast<int>(F.nbrPtr[0][a + 1] - q0);
+    for (int c = 0; c < nc; ++c)
+    {
+        if (fmask[g0 + c])
+            continue;
+        const int64_t off = F.rowPtr[g0 + c] + F.blk[0][a];
+        const int64_t OFF = C.rowPtr[G0 + c];
+        for (int k = lane; k < nn; k += 32)
+        {
+            const int64_t gb = F.gdof[0][F.nbrIdx[0][q0 + k]];
+            const int64_t base = OFF + static_cast<int64_t>(nc) * cr[q0 + k];
+            for (int d = 0; d < nc; ++d)
+                if (!fmask[gb + d])
+                    atomicAdd(cv + NG_IDX(base + d, C.nnz, 30), fv[off + nc * k + d]);
+        }
+    }
+}
+
+// Jacobi diagonal (0 where the DOF is constrained or the diagonal is not positive) and the Gershgorin bound
+// max_r sum_j |a_rj| / a_rr of the spectral radius of D^-1 A (positive floats order like their bit patterns)
+__global__ void __launch_bounds__(kBS) k_amg_diag(NodeSpmv A, const uint8_t* __restrict__ mask,
+                                                   const float* __restrict__ v, const int32_t* __restrict__ diagOff,
+                                                   float* dinv, float* lmax)
+{
+    const int64_t a = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (a >= A.totalWarps)
+        return;
+    const int nc = A.ncomp[0];
+    const int64_t g0 = A.gdof[0][a];
+    const int len = nc * static_cast<int>(A.nbrPtr[0][a + 1] - A.nbrPtr[0][a]);
+    for (int c = 0; c < nc; ++c)
+    {
+        const int64_t r = g0 + c;
+        const int64_t rs = A.rowPtr[r] + A.blk[0][a];
+        float s = 0.f;
+        for (int q = lane; q < len; q += 32)
+            s += fabsf(v[NG_IDX(rs + q, A.nnz, 32)]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0)
+        {
+            const float dg = v[NG_IDX(rs + diagOff[a] + c, A.nnz, 35)];
+            const bool use = !mask[r] && dg > 0.f;
+            dinv[r] = use ? 1.f / dg : 0.f;
+            if (use)
+                atomicMax(reinterpret_cast<int*>(lmax), __float_as_int(s / dg));
+        }
+    }
+}
+
+// ---- device: cycle kernels (each returns at once when the Krylov state is no longer RUN) ------------------------
+__device__ __forceinline__ bool Idle(const int* st)
+{
+    return st && st[ST_STATE] != RUN;
+}
+
+// first Chebyshev step from zero: d = dinv b / theta; e = d
+__global__ void k_cheb0(int64_t n, const float* __restrict__ dinv, const float* __restrict__ b, float* d, float* e,
+                        float invTheta, const int* st)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n || Idle(st))
+        return;
+    const float v = dinv[i] * b[i] * invTheta;
+    d[i] = v;
+    e[i] = v;
+}
+
+// first Chebyshev step from a nonzero e (t = A e): d = dinv (b - t) / theta; e += d
+__global__ void k_cheb1(int64_t n, const float* __restrict__ dinv, const float* __restrict__ b,
+                        const float* __restrict__ t, float* d, float* e, float invTheta, const int* st)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n || Idle(st))
+        return;
+    const float v = dinv[i] * (b[i] - t[i]) * invTheta;
+    d[i] = v;
+    e[i] += v;
+}
+
+// later Chebyshev steps (t = A e): d = c1 d + c2 dinv (b - t); e += d
+__global__ void k_chebk(int64_t n, const float* __restrict__ dinv, const float* __restrict__ b,
+                        const float* __restrict__ t, float* d, float* e, float c1, float c2, const int* st)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n || Idle(st))
+        return;
+    const float v = c1 * d[i] + c2 * dinv[i] * (b[i] - t[i]);
+    d[i] = v;
+    e[i] += v;
+}
+
+// coarse b = P^T (b - t) with t = A e (cb zeroed before); constrained finer DOFs are skipped
+__global__ void k_restrict(NodeSpmv F, const uint8_t* __restrict__ fmask, const float* __restrict__ b,
+                           const float* __restrict__ t, const int32_t* __restrict__ agg, NodeSpmv C, float* cb,
+                           const int* st)
+{
+    const int64_t a = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (a >= F.totalWarps || Idle(st))
+        return;
+    const int64_t g0 = F.gdof[0][a];
+    const int64_t G0 = C.gdof[0][agg[a]];
+    for (int c = 0; c < F.ncomp[0]; ++c)
+        if (!fmask[g0 + c])
+            atomicAdd(cb + NG_IDX(G0 + c, C.nRows, 33), b[g0 + c] - t[g0 + c]);
+}
+
+// e += P ce
+__global__ void k_prolong(NodeSpmv F, const uint8_t* __restrict__ fmask, const int32_t* __restrict__ agg, NodeSpmv C,
+                          const float* __restrict__ ce, float* e, const int* st)
+{
+    const int64_t a = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (a >= F.totalWarps || Idle(st))
+        return;
+    const int64_t g0 = F.gdof[0][a];
+    const int64_t G0 = C.gdof[0][agg[a]];
+    for (int c = 0; c < F.ncomp[0]; ++c)
+        if (!fmask[g0 + c])
+            e[g0 + c] += ce[NG_IDX(G0 + c, C.nRows, 34)];
+}
+
+// y = a - b (elementwise); a == nullptr gives y = 0
+__global__ void k_sub(int64_t n, const float* a, const float* b, float* y, const int* st)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n || Idle(st))
+        return;
+    y[i] = a ? a[i] - b[i] : 0.f;
+}
+
+template <typename TA, typename TB>
+__global__ void k_convert(int64_t n, const TA* __restrict__ a, TB* __restrict__ b, const int* st)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i < n && !Idle(st))
+        b[i] = static_cast<TB>(a[i]);
+}
+
+// ---- host: set-up and application ------------------------------------------------------------------------------
+static unsigned Blocks(int64_t n, int bs = 256)
+{
+    return static_cast<unsigned>((n + bs - 1) / bs);
+}
+
+// Builds the hierarchy on first use and the coarse operators for the tangent `vals` unless they were built for
+// the same values already (same pointer and tangent version).
+template <typename TV>
+void AmgSetup(Ctx& c, const TV* vals)
+{
+    if (!c.amg)
+        c.amg = new Amg();
+    Amg& M = *c.amg;
+    if (!M.built)
+        BuildHierarchy(c);
+    if (M.setupVals == static_cast<const void*>(vals) && M.setupVersion == c.valsVersion)
+        return;
+    const float* fine;
+    if constexpr (sizeof(TV) == 4)
+        fine = vals;
+    else
+    {
+        if (M.fine32.n != static_cast<size_t>(c.nnz))
+            M.fine32.alloc(c.nnz);
+        k_convert<double, float><<<Blocks(c.nnz), 256, 0, c.stream>>>(c.nnz, vals, M.fine32.p, nullptr);
+        c.stats.kernel_launches += 1;
+        fine = M.fine32.p;
+    }
+    M.fine = fine;
+    NG_CUDA(cudaMemsetAsync(M.lmaxDev.p, 0, M.lmaxHost.size() * sizeof(float), c.stream));
+    size_t slot = 0;
+    for (int I = 0; I < M.ns; ++I)
+    {
+        std::vector<AmgLevel>& H = M.h[I];
+        H[0].spmv = SlotView(c, I);
+        k_amg_diag<<<Blocks(H[0].nNodes * 32), kBS, 0, c.stream>>>(H[0].spmv, c.dMask.p, fine, H[0].diagOff.p,
+                                                                    H[0].dinv.p, M.lmaxDev.p + slot);
+        c.stats.kernel_launches += 1;
+        for (size_t l = 1; l < H.size(); ++l)
+        {
+            AmgLevel& Fi = H[l - 1];
+            AmgLevel& C = H[l];
+            NG_CUDA(cudaMemsetAsync(C.vals.p, 0, C.nnz * sizeof(float), c.stream));
+            k_amg_coarsen<<<Blocks(Fi.nNodes * 32), kBS, 0, c.stream>>>(
+                    Fi.spmv, l == 1 ? c.dMask.p : Fi.zeroMask.p, l == 1 ? fine : Fi.vals.p, C.spmv, C.aggOf.p,
+                    C.cRank.p, C.vals.p);
+            k_amg_diag<<<Blocks(C.nNodes * 32), kBS, 0, c.stream>>>(C.spmv, C.zeroMask.p, C.vals.p, C.diagOff.p,
+                                                                     C.dinv.p, M.lmaxDev.p + slot + l);
+            c.stats.kernel_launches += 2;
+        }
+        slot += H.size();
+    }
+    AfterLaunch(c, "multigrid set-up");
+    NG_CUDA(cudaMemcpyAsync(M.lmaxHost.data(), M.lmaxDev.p, M.lmaxHost.size() * sizeof(float),
+                            cudaMemcpyDeviceToHost, c.stream));
+    NG_CUDA(cudaStreamSynchronize(c.stream));
+    slot = 0;
+    for (int I = 0; I < M.ns; ++I)
+        for (AmgLevel& L : M.h[I])
+        {
+            const float v = M.lmaxHost[slot++];
+            L.lmax = v > 0.f ? v : 1.f;
+        }
+    M.setupVals = vals;
+    M.setupVersion = c.valsVersion;
+}
+template void AmgSetup<float>(Ctx&, const float*);
+template void AmgSetup<double>(Ctx&, const double*);
+
+// Chebyshev smoothing of A e = b on [lmax / ratio, lmax]. Vectors are base pointers of the level (combined
+// length on level 0); elementwise work runs over rows [off, off + n). fromZero starts at e = 0 (no product).
+static void Chebyshev(Ctx& c, AmgLevel& L, const float* vals, const uint8_t* mask, const float* b, float* e,
+                      int degree, bool fromZero, float ratio, const int* st)
+{
+    const int64_t n = L.nDofs, o = L.off;
+    const float lmax = L.lmax, lmin = L.lmax / ratio;
+    const float theta = 0.5f * (lmax + lmin), delta = 0.5f * (lmax - lmin);
+    const float sigma = theta / delta;
+    int* stw = const_cast<int*>(st); // the SpMV only reads the state when it computes no dot products
+    float rho = 1.f / sigma;
+    if (fromZero)
+        k_cheb0<<<Blocks(n), 256, 0, c.stream>>>(n, L.dinv.p + o, b + o, L.d.p + o, e + o, 1.f / theta, st);
+    else
+    {
+        SpmvNode<float, float, 0>(c.stream, L.spmv, vals, e, L.t.p, nullptr, nullptr, stw, 0, mask);
+        k_cheb1<<<Blocks(n), 256, 0, c.stream>>>(n, L.dinv.p + o, b + o, L.t.p + o, L.d.p + o, e + o, 1.f / theta,
+                                                 st);
+        c.stats.kernel_launches += 1;
+    }
+    c.stats.kernel_launches += 1;
+    for (int k = 1; k < degree; ++k)
+    {
+        const float rhoNew = 1.f / (2.f * sigma - rho);
+        SpmvNode<float, float, 0>(c.stream, L.spmv, vals, e, L.t.p, nullptr, nullptr, stw, 0, mask);
+        k_chebk<<<Blocks(n), 256, 0, c.stream>>>(n, L.dinv.p + o, b + o, L.t.p + o, L.d.p + o, e + o, rhoNew * rho,
+                                                 2.f * rhoNew / delta, st);
+        c.stats.kernel_launches += 2;
+        rho = rhoNew;
+    }
+}
+
+// e = V-cycle(b) on level l of hierarchy H
+static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const float* b, float* e, const int* st)
+{
+    Amg& M = *c.amg;
+    AmgLevel& L = H[l];
+    const float* vals = l == 0 ? M.fine : L.vals.p;
+    const uint8_t* mask = l == 0 ? c.dMask.p : L.zeroMask.p;
+    if (l + 1 == H.size())
+    {
+        Chebyshev(c, L, vals, mask, b, e, kCoarseDegree, true, kCoarseRatio, st);
+        return;
+    }
+    AmgLevel& C = H[l + 1];
+    int* stw = const_cast<int*>(st);
+    Chebyshev(c, L, vals, mask, b, e, kPreDegree, true, kSmoothRatio, st);
+    SpmvNode<float, float, 0>(c.stream, L.spmv, vals, e, L.t.p, nullptr, nullptr, stw, 0, mask);
+    k_sub<<<Blocks(C.nDofs), 256, 0, c.stream>>>(C.nDofs, nullptr, nullptr, C.b.p, st);
+    k_restrict<<<Blocks(L.nNodes), 256, 0, c.stream>>>(L.spmv, mask, b, L.t.p, C.aggOf.p, C.spmv, C.b.p, st);
+    c.stats.kernel_launches += 3;
+    VCycle(c, H, l + 1, C.b.p, C.e.p, st);
+    k_prolong<<<Blocks(L.nNodes), 256, 0, c.stream>>>(L.spmv, mask, C.aggOf.p, C.spmv, C.e.p, e, st);
+    c.stats.kernel_launches += 1;
+    Chebyshev(c, L, vals, mask, b, e, kPostDegree, false, kSmoothRatio, st);
+}
+
+// block Gauss-Seidel sweep in slot order on combined FP32 vectors: z_0 = V_0(v_0), z_1 = V_1(v_1 - K_10 z_0)
+static void Sweep(Ctx& c, const float* v, float* z, const int* st)
+{
+    Amg& M = *c.amg;
+    VCycle(c, M.h[0], 0, v, z, st);
+    for (int I = 1; I < M.ns; ++I)
+    {
+        AmgLevel& L = M.h[I][0];
+        const int64_t o = L.off, n = L.nDofs;
+        // z_I = 0, res = K z on the rows of slot I, res = v_I - res
+        k_sub<<<Blocks(n), 256, 0, c.stream>>>(n, nullptr, nullptr, z + o, st);
+        SpmvNode<float, float, 0>(c.stream, RowsView(c, I), M.fine, z, M.res32.p, nullptr, nullptr,
+                                  const_cast<int*>(st), 0, c.dMask.p);
+        k_sub<<<Blocks(n), 256, 0, c.stream>>>(n, v + o, M.res32.p + o, M.res32.p + o, st);
+        c.stats.kernel_launches += 3;
+        VCycle(c, M.h[I], 0, M.res32.p, z, st);
+    }
+}
+
+// z = M^-1 v for the tangent of the last AmgSetup (FP32 cycle; FP64 vectors are converted). With st given,
+// every kernel returns at once when the Krylov state is not RUN.
+template <typename T>
+void AmgApply(Ctx& c, const T* v, T* z, const int* st)
+{
+    Amg& M = *c.amg;
+    const int64_t n = c.nDofs;
+    if constexpr (sizeof(T) == 4)
+        Sweep(c, v, z, st);
+    else
+    {
+        k_convert<double, float><<<Blocks(n), 256, 0, c.stream>>>(n, v, M.in32.p, st);
+        Sweep(c, M.in32.p, M.out32.p, st);
+        k_convert<float, double><<<Blocks(n), 256, 0, c.stream>>>(n, M.out32.p, z, st);
+        c.stats.kernel_launches += 2;
+    }
+}
+template void AmgApply<float>(Ctx&, const float*, float*, const int*);
+template void AmgApply<double>(Ctx&, const double*, double*, const int*);
+
+int AmgLevels(const Ctx& c)
+{
+    return c.amg ? static_cast<int>(c.amg->h[0].size()) : 0;
+}
+
+} // namespace nuto_gpu

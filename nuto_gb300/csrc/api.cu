@@ -20,6 +20,7 @@ namespace nuto_gpu
 Ctx::~Ctx()
 {
     FreeSolverWork(*this);
+    FreeAmg(*this);
 }
 
 bool SyncCheck(const Ctx& c)
@@ -389,7 +390,10 @@ static void BuildPattern(Ctx& c)
         Upload(M.dBlk, blk[p]);
         Upload(M.dNbrPtr, nbr[p].ptr);
         Upload(M.dNbrIdx, nbr[p].idx);
+        M.hNbrPtr = std::move(nbr[p].ptr);
+        M.hNbrIdx = std::move(nbr[p].idx);
     }
+    FreeAmg(c);
     c.havePattern = true;
 }
 
@@ -860,7 +864,18 @@ int nuto_gpu_solve(nuto_gpu_ctx* ctx, int precision, int method, const void* val
     return Guard(ctx, [&] {
         NG_CHECK(ctx->havePattern, NUTO_GPU_ESTATE, "build_pattern first");
         NG_CHECK(precision == NUTO_GPU_FP32 || precision == NUTO_GPU_FP64, NUTO_GPU_EINVAL, "precision 32 or 64");
+        ctx->valsVersion++; // caller-supplied values may have changed behind the same pointer
         return SolveLinear(*ctx, precision, method, values, b, x, rtol, maxit, iters, relres);
+    });
+}
+
+int nuto_gpu_set_preconditioner(nuto_gpu_ctx* ctx, int preconditioner)
+{
+    return Guard(ctx, [&] {
+        NG_CHECK(preconditioner == NUTO_GPU_PRECOND_JACOBI || preconditioner == NUTO_GPU_PRECOND_AMG, NUTO_GPU_EINVAL,
+                 "unknown preconditioner");
+        ctx->precond = preconditioner;
+        return NUTO_GPU_OK;
     });
 }
 

@@ -727,6 +727,7 @@ static void LaunchTangentT(Ctx& c, const double* u, T* vals)
 
 void LaunchTangent(Ctx& c, const double* u, int precision, void* values)
 {
+    c.valsVersion++;
     if (precision == NUTO_GPU_FP32)
         LaunchTangentT<float>(c, u, static_cast<float*>(values));
     else
@@ -886,6 +887,7 @@ void LaunchCellVectors(Ctx& c, const double* fe, double* f)
 
 void LaunchCellMatrices(Ctx& c, const double* ke, int precision, void* values)
 {
+    c.valsVersion++;
     SlotViews v = MakeSlotViews(c);
     ScatterArgs s = MakeScatterArgs(c);
     const int64_t items = c.nCells * v.nLocal * v.nLocal;

@@ -182,6 +182,8 @@ struct PairMap
     // J-neighbours of every I-node in CSR column order (the node-block SpMV reconstructs column indices from them)
     DBuf<int64_t> dNbrPtr; // nNodes_I + 1
     DBuf<int32_t> dNbrIdx;
+    std::vector<int64_t> hNbrPtr; // host copies (multigrid hierarchy set-up)
+    std::vector<int32_t> hNbrIdx;
 };
 
 // Device-side constants of one integrand (plain data passed by value to kernels).
@@ -210,6 +212,7 @@ struct IpTables
 };
 
 struct SolverWork;
+struct Amg;
 
 struct Ctx
 {
@@ -272,6 +275,9 @@ struct Ctx
     nuto_gpu_stats stats{};
 
     SolverWork* work = nullptr;
+    Amg* amg = nullptr;
+    int precond = NUTO_GPU_PRECOND_AMG;
+    uint64_t valsVersion = 1; // bumped by every tangent assembly and every caller-supplied solve
     bool syncCheck = false; // NUTO_GPU_SYNC_CHECK=1 or a checked build
 
     ~Ctx();
@@ -289,6 +295,12 @@ int SolveLinear(Ctx& c, int precision, int method, const void* values, const dou
                 int maxit, int* iters, double* relres);
 int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* iters);
 void FreeSolverWork(Ctx& c);
+void FreeAmg(Ctx& c);
+template <typename TV>
+void AmgSetup(Ctx& c, const TV* vals);
+template <typename T>
+void AmgApply(Ctx& c, const T* v, T* z, const int* st);
+int AmgLevels(const Ctx& c);
 
 // ---- kernel argument blocks (by value) ----
 struct CellArgs

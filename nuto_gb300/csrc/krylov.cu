@@ -1,5 +1,5 @@
-// Jacobi-preconditioned Krylov solvers (PCG for SPD tangents, BiCGStab for the non-symmetric damage tangents)
-// on the CSR tangent, replacing the sparse direct solve of the reference (Solve.cpp:8-34 with
+// Preconditioned Krylov solvers (PCG for SPD tangents; GMRES and BiCGStab for the non-symmetric damage tangents;
+// Jacobi or the aggregation multigrid cycle of amg.cu) on the CSR tangent, replacing the sparse direct solve of the reference (Solve.cpp:8-34 with
 // EigenSparseSolve.cpp:22-73). The constrained system C^T K C y = C^T b of unit (Dirichlet) constraints is
 // solved in place: dependent rows act as identity and the iterates stay zero there, so the dependent columns
 // never contribute.
@@ -7,7 +7,7 @@
 // Every reduction is fused into the kernel that produces its operands; the last block of the grid (atomic
 // ticket, no waiting) turns the sums into the iteration scalars (alpha, beta, omega) kept in device memory, so a
 // whole chunk of iterations runs without a host round trip. Dot products accumulate in FP64.
-#include "solver.cuh"
+#include "spmv.cuh"
 
 namespace nuto_gpu
 {
@@ -50,187 +50,6 @@ void FreeSolverWork(Ctx& c)
 {
     delete c.work;
     c.work = nullptr;
-}
-
-constexpr int kBS = 256;
-
-__device__ __forceinline__ double WarpSum(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Sums v over the block and adds the block total to *acc (thread 0).
-__device__ __forceinline__ void BlockAccumulate(double v, double* acc, double* sh)
-{
-    v = WarpSum(v);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0)
-        sh[wid] = v;
-    __syncthreads();
-    if (wid == 0)
-    {
-        v = lane < (blockDim.x >> 5) ? sh[lane] : 0.;
-        v = WarpSum(v);
-        if (lane == 0)
-            atomicAdd(acc, v);
-    }
-    __syncthreads();
-}
-
-// True in exactly one block: the last one to arrive (threadFenceReduction pattern, no spinning).
-__device__ __forceinline__ bool LastBlock(int* counter)
-{
-    __shared__ bool last;
-    __threadfence();
-    if (threadIdx.x == 0)
-    {
-        const unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(counter), 1u);
-        last = prev == gridDim.x - 1;
-    }
-    __syncthreads();
-    return last;
-}
-
-__device__ __forceinline__ double VRead(const double* p)
-{
-    return *reinterpret_cast<const volatile double*>(p);
-}
-
-__device__ __forceinline__ bool Finite(double v)
-{
-    return isfinite(v);
-}
-
-// finalize actions of the SpMV kernel
-enum Fin
-{
-    FIN_NONE = 0,
-    FIN_PCG_ALPHA = 1,  // alpha = rho / (p.Ap)
-    FIN_BICG_ALPHA = 2, // alpha = rho / (rhat.v)
-    FIN_BICG_OMEGA = 3  // omega = (t.s) / (t.t)
-};
-
-// Node-block SpMV: one warp per DOF node (of every slot) computes all rows of that node. DofNumbering numbers the
-// components of a node consecutively, so every row of node a lists, per slot J, the J-neighbours of a in the
-// same order with ncomp_J consecutive values each; the lanes run over the neighbours, load the neighbour's x
-// values once for all rows of the node and read the values at rowPtr[row] + blk_IJ(a) + ncomp_J * k + d. The
-// column indices are never read: the CSR values plus the per-node neighbour lists are the whole traffic.
-struct NodeSpmv
-{
-    int ns;
-    int ncomp[kMaxSlots];
-    int64_t nNodes[kMaxSlots];
-    int64_t firstWarp[kMaxSlots];
-    int64_t totalWarps;
-    const int64_t* gdof[kMaxSlots];
-    const int64_t* nbrPtr[kMaxSlots * kMaxSlots];
-    const int32_t* nbrIdx[kMaxSlots * kMaxSlots];
-    const int32_t* blk[kMaxSlots * kMaxSlots];
-    const int64_t* rowPtr;
-    int64_t nnz, nRows, nbrTotal[kMaxSlots * kMaxSlots];
-};
-
-constexpr int kMaxRowLen = 256; // longest row of a node (Hex20 displacements: 3 x 81)
-
-template <typename TV, typename TX, int NDOT>
-__global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
-                                                    const uint8_t* __restrict__ mask, const TX* __restrict__ x,
-                                                    TX* __restrict__ y, const TX* __restrict__ w0, double* sc, int* st,
-                                                    int fin)
-{
-    __shared__ double sh[kBS / 32];
-    __shared__ TX xs[kBS / 32][kMaxRowLen];
-    if (st && st[ST_STATE] != RUN)
-        return;
-    const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int I = (A.ns > 1 && warp >= A.firstWarp[1]) ? 1 : 0;
-    const int64_t a = warp - A.firstWarp[I];
-    const bool valid = warp < A.totalWarps && a < A.nNodes[I];
-    const int ncI = A.ncomp[I];
-    double d0 = 0., d1 = 0.;
-    if (valid)
-    {
-        // x of the node's neighbours in the column order of its rows
-        int len = 0;
-        for (int J = 0; J < A.ns; ++J)
-        {
-            const int p = I * A.ns + J;
-            const int ncJ = A.ncomp[J];
-            const int64_t q0 = A.nbrPtr[p][a];
-            const int nn = static_cast<int>(A.nbrPtr[p][a + 1] - q0);
-            for (int kk = lane; kk < nn; kk += 32)
-            {
-                const int64_t gb = A.gdof[J][A.nbrIdx[p][NG_IDX(q0 + kk, A.nbrTotal[p], 17)]];
-                for (int d = 0; d < ncJ; ++d)
-                    xs[wid][NG_IDX(len + ncJ * kk + d, kMaxRowLen, 20)] = x[NG_IDX(gb + d, A.nRows, 18)];
-            }
-            len += ncJ * nn;
-        }
-        __syncwarp();
-        const int64_t g0 = A.gdof[I][a];
-        for (int c = 0; c < ncI; ++c)
-        {
-            const int64_t r = g0 + c;
-            const int64_t rs = A.rowPtr[NG_IDX(r, A.nRows, 16)];
-            TX s = TX(0);
-#pragma unroll 4
-            for (int q = lane; q < len; q += 32)
-                s += static_cast<TX>(val[NG_IDX(rs + q, A.nnz, 19)]) * xs[wid][q];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                s += __shfl_down_sync(0xffffffffu, s, o);
-            if (lane == 0)
-            {
-                const TX yv = mask[r] ? x[r] : s;
-                y[r] = yv;
-                if (NDOT >= 1)
-                    d0 += static_cast<double>(w0[r]) * static_cast<double>(yv);
-                if (NDOT >= 2)
-                    d1 += static_cast<double>(yv) * static_cast<double>(yv);
-            }
-        }
-    }
-    if (NDOT == 0)
-        return;
-    BlockAccumulate(d0, sc + SC_ACC0, sh);
-    if (NDOT >= 2)
-        BlockAccumulate(d1, sc + SC_ACC1, sh);
-    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
-    {
-        st[ST_COUNTER] = 0;
-        const double a0 = VRead(sc + SC_ACC0), a1 = VRead(sc + SC_ACC1);
-        sc[SC_ACC0] = 0.;
-        sc[SC_ACC1] = 0.;
-        if (fin == FIN_PCG_ALPHA)
-        {
-            if (!Finite(a0))
-                st[ST_STATE] = NONFINITE;
-            else if (!(a0 > 0.))
-                st[ST_STATE] = BREAKDOWN;
-            else
-                sc[SC_ALPHA] = sc[SC_RHO] / a0;
-        }
-        else if (fin == FIN_BICG_ALPHA)
-        {
-            if (!Finite(a0))
-                st[ST_STATE] = NONFINITE;
-            else if (a0 == 0.)
-                st[ST_STATE] = BREAKDOWN;
-            else
-                sc[SC_ALPHA] = sc[SC_RHO] / a0;
-        }
-        else if (fin == FIN_BICG_OMEGA)
-        {
-            if (!Finite(a0) || !Finite(a1))
-                st[ST_STATE] = NONFINITE;
-            else
-                sc[SC_OMEGA] = a1 > 0. ? a0 / a1 : 0.;
-        }
-    }
 }
 
 // ---- right-hand side preparation ---------------------------------------------------------------------------
@@ -334,7 +153,8 @@ __global__ void k_diag_inv(int64_t n, const int64_t* __restrict__ rowPtr, const 
 }
 
 // ---- PCG ------------------------------------------------------------------------------------------------------
-// x += alpha p; r -= alpha q; z = dinv r; acc0 += r.z; acc1 += r.r; last block: convergence test, beta, rho
+// x += alpha p; r -= alpha q; z = dinv r; acc0 += r.z; acc1 += r.r; last block: convergence test, beta, rho.
+// With dinv == nullptr (multigrid) z, beta and rho are left to k_pcg_rz after the cycle.
 template <typename T>
 __global__ void __launch_bounds__(kBS) k_pcg_update(int64_t n, T* x, T* r, const T* __restrict__ p,
                                                      const T* __restrict__ q, T* z, const T* __restrict__ dinv,
@@ -351,9 +171,12 @@ __global__ void __launch_bounds__(kBS) k_pcg_update(int64_t n, T* x, T* r, const
         x[i] += alpha * p[i];
         const T ri = r[i] - alpha * q[i];
         r[i] = ri;
-        const T zi = dinv[i] * ri;
-        z[i] = zi;
-        rz += static_cast<double>(ri) * static_cast<double>(zi);
+        if (dinv)
+        {
+            const T zi = dinv[i] * ri;
+            z[i] = zi;
+            rz += static_cast<double>(ri) * static_cast<double>(zi);
+        }
         rr += static_cast<double>(ri) * static_cast<double>(ri);
     }
     BlockAccumulate(rz, sc + SC_ACC0, sh);
@@ -370,9 +193,39 @@ __global__ void __launch_bounds__(kBS) k_pcg_update(int64_t n, T* x, T* r, const
             st[ST_STATE] = NONFINITE;
         else if (a1 <= sc[SC_TOL2])
             st[ST_STATE] = CONVERGED;
-        else
+        else if (dinv)
         {
             sc[SC_BETA] = a0 / sc[SC_RHO];
+            sc[SC_RHO] = a0;
+        }
+    }
+}
+
+// acc0 += r.z for z = M^-1 r of the multigrid cycle; last block: rho (init) or beta and rho
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_pcg_rz(int64_t n, const T* __restrict__ r, const T* __restrict__ z,
+                                                 double* sc, int* st, int init)
+{
+    __shared__ double sh[kBS / 32];
+    if (st[ST_STATE] != RUN)
+        return;
+    double rz = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        rz += static_cast<double>(r[i]) * static_cast<double>(z[i]);
+    BlockAccumulate(rz, sc + SC_ACC0, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        const double a0 = VRead(sc + SC_ACC0);
+        sc[SC_ACC0] = 0.;
+        if (!Finite(a0))
+            st[ST_STATE] = NONFINITE;
+        else if (!(a0 > 0.))
+            st[ST_STATE] = BREAKDOWN; // the preconditioner is not positive definite for this matrix
+        else
+        {
+            sc[SC_BETA] = init ? 0. : a0 / sc[SC_RHO];
             sc[SC_RHO] = a0;
         }
     }
@@ -520,7 +373,7 @@ static int GridFor(const Ctx& c, int64_t n)
     return static_cast<int>(want < cap ? want : cap);
 }
 
-static NodeSpmv MakeNodeSpmv(const Ctx& c)
+NodeSpmv MakeNodeSpmv(const Ctx& c)
 {
     NodeSpmv A{};
     A.ns = static_cast<int>(c.slots.size());
@@ -551,10 +404,7 @@ template <typename TV, typename TX, int NDOT>
 static void SpmvLaunch(Ctx& c, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc, int* st, int fin,
                        const uint8_t* mask)
 {
-    const NodeSpmv A = MakeNodeSpmv(c);
-    const int64_t threads = A.totalWarps * 32;
-    const unsigned blocks = static_cast<unsigned>((threads + kBS - 1) / kBS);
-    k_spmv_node<TV, TX, NDOT><<<blocks, kBS, 0, c.stream>>>(A, vals, mask, x, y, w0, sc, st, fin);
+    SpmvNode<TV, TX, NDOT>(c.stream, MakeNodeSpmv(c), vals, x, y, w0, sc, st, fin, mask);
 }
 
 // Krylov SpMV with a CUDA-event pair around it (device time of the dominant kernel, collected by SpmvCollect)
@@ -744,7 +594,7 @@ __global__ void __launch_bounds__(kBS) k_gm_update(int64_t n, const T* __restric
     }
 }
 
-// v_j = w / nrm; z = dinv v_j
+// v_j = w / nrm; z = dinv v_j (Jacobi; z == nullptr when the multigrid cycle computes z)
 template <typename T>
 __global__ void __launch_bounds__(kBS) k_gm_normalize(int64_t n, const T* __restrict__ w, T* vj, T* z,
                                                        const T* __restrict__ dinv, const double* gs, const int* st)
@@ -757,7 +607,8 @@ __global__ void __launch_bounds__(kBS) k_gm_normalize(int64_t n, const T* __rest
     {
         const T v = w[r] * inv;
         vj[r] = v;
-        z[r] = dinv[r] * v;
+        if (z)
+            z[r] = dinv[r] * v;
     }
 }
 
@@ -796,7 +647,7 @@ __global__ void __launch_bounds__(kBS) k_gm_start(int64_t n, const T* __restrict
     }
 }
 
-// x += dinv (sum_i y_i V_i)
+// x += dinv (sum_i y_i V_i) (Jacobi) or x += sum_i y_i Z_i (flexible form, dinv == nullptr)
 template <typename T>
 __global__ void __launch_bounds__(kBS) k_gm_solution(int64_t n, const T* __restrict__ V, int k, const double* gs,
                                                       const T* __restrict__ dinv, T* x)
@@ -811,7 +662,7 @@ __global__ void __launch_bounds__(kBS) k_gm_solution(int64_t n, const T* __restr
         T a = T(0);
         for (int i = 0; i < k; ++i)
             a += ys[i] * V[static_cast<int64_t>(i) * n + r];
-        x[r] += dinv[r] * a;
+        x[r] += dinv ? dinv[r] * a : a;
     }
 }
 
@@ -863,7 +714,14 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
     NG_CUDA(cudaMemsetAsync(gs, 0, GL::SIZE * sizeof(double), c.stream));
     const int grid = GridFor(c, n);
     const unsigned g256 = static_cast<unsigned>((n + 255) / 256);
-    k_diag_inv<TV, T><<<g256, 256, 0, c.stream>>>(n, c.dRowPtr.p, c.dColIdx.p, vals, c.dMask.p, K.dinv.p);
+    const bool amg = c.precond == NUTO_GPU_PRECOND_AMG;
+    if (amg)
+    {
+        AmgSetup<TV>(c, vals);
+        G.ensureZ();
+    }
+    else
+        k_diag_inv<TV, T><<<g256, 256, 0, c.stream>>>(n, c.dRowPtr.p, c.dColIdx.p, vals, c.dMask.p, K.dinv.p);
     k_rhs_norm<<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, sc, st, rtol, sizeof(T) == 4 ? 1 : 0);
     // rhs (scaled) in K.r, solution in K.x; tolerance (rtol relative to the scaled rhs) to the GMRES block
     k_gm_rhs<T><<<g256, 256, 0, c.stream>>>(n, c.dMask.p, b, sc, K.r.p, K.x.p);
@@ -885,19 +743,23 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
         c.stats.kernel_launches += 2;
         k_gm_start<T><<<grid, kBS, 0, c.stream>>>(n, K.r.p, G.w.p, first ? 0 : 1, gs, st);
         first = false;
-        k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, G.V.p, G.z.p, K.dinv.p, gs, st);
+        k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, G.V.p, amg ? nullptr : G.z.p, K.dinv.p, gs, st);
         const int cols = std::min(m, maxit - total);
         for (int j = 0; j < cols; ++j)
         {
             T* vj1 = G.V.p + static_cast<int64_t>(j + 1) * n;
-            SpmvTimed<TV, T, 0>(c, vals, G.z.p, G.w.p, nullptr, nullptr, st, FIN_NONE, c.dMask.p);
+            T* zj = amg ? G.Z.p + static_cast<int64_t>(j) * n : G.z.p;
+            if (amg)
+                AmgApply<T>(c, G.V.p + static_cast<int64_t>(j) * n, zj, st);
+            SpmvTimed<TV, T, 0>(c, vals, zj, G.w.p, nullptr, nullptr, st, FIN_NONE, c.dMask.p);
             c.stats.kernel_launches += 4 + (j + 1 < cols ? 1 : 0);
             k_gm_dots<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, G.w.p, gs + GL::H1, st);
             k_gm_update<T, false><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, gs, G.w.p, st, j);
             k_gm_dots<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, G.w.p, gs + GL::H2, st);
             k_gm_update<T, true><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, gs, G.w.p, st, j);
             if (j + 1 < cols)
-                k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, vj1, G.z.p, K.dinv.p, gs, st);
+                k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, vj1, amg ? nullptr : G.z.p, K.dinv.p, gs,
+                                                              st);
         }
         AfterLaunch(c, "gmres cycle");
         NG_CUDA(cudaMemcpyAsync(w.hG, gs, GL::SIZE * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -924,7 +786,8 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
                 y[i] = d != 0. ? s / d : 0.;
             }
             NG_CUDA(cudaMemcpyAsync(gs + GL::Y, y, k * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-            k_gm_solution<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, k, gs, K.dinv.p, K.x.p);
+            k_gm_solution<T><<<grid, kBS, 0, c.stream>>>(n, amg ? G.Z.p : G.V.p, k, gs, amg ? nullptr : K.dinv.p,
+                                                         K.x.p);
             AfterLaunch(c, "gmres solution");
             c.stats.kernel_launches += 1;
             relEst = beta0 > 0. ? std::fabs(w.hG[GL::G + k]) / beta0 : 0.;
@@ -979,10 +842,24 @@ static int KrylovSolve(Ctx& c, int method, const TV* vals, const double* b, doub
     NG_CUDA(cudaMemsetAsync(sc, 0, SC_COUNT * sizeof(double), c.stream));
     NG_CUDA(cudaMemsetAsync(st, 0, ST_COUNT * sizeof(int), c.stream));
     const int grid = GridFor(c, n);
-    k_diag_inv<TV, T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, c.stream>>>(n, c.dRowPtr.p, c.dColIdx.p, vals,
-                                                                                     c.dMask.p, V.dinv.p);
+    const bool amg = pcg && c.precond == NUTO_GPU_PRECOND_AMG;
+    if (amg)
+        AmgSetup<TV>(c, vals);
+    else
+        k_diag_inv<TV, T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, c.stream>>>(
+                n, c.dRowPtr.p, c.dColIdx.p, vals, c.dMask.p, V.dinv.p);
     k_rhs_norm<<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, sc, st, rtol, sizeof(T) == 4 ? 1 : 0);
-    if (pcg)
+    if (amg)
+    {
+        // x = 0, r = b, p = 0; z = M^-1 r; rho = r.z; p = z
+        k_krylov_init<T, false><<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, V.x.p, V.r.p, V.rh.p, V.p.p, V.v.p,
+                                                             V.z.p, V.dinv.p, sc, st);
+        AmgApply<T>(c, V.r.p, V.z.p, st);
+        k_pcg_rz<T><<<grid, kBS, 0, c.stream>>>(n, V.r.p, V.z.p, sc, st, 1);
+        k_pcg_dir<T><<<grid, kBS, 0, c.stream>>>(n, V.p.p, V.z.p, sc, st);
+        c.stats.kernel_launches += 2;
+    }
+    else if (pcg)
         k_krylov_init<T, true><<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, V.x.p, V.r.p, V.rh.p, V.p.p, V.v.p,
                                                             V.z.p, V.dinv.p, sc, st);
     else
@@ -1001,7 +878,14 @@ static int KrylovSolve(Ctx& c, int method, const TV* vals, const double* b, doub
             {
                 SpmvTimed<TV, T, 1>(c, vals, V.p.p, V.q.p, V.p.p, sc, st, FIN_PCG_ALPHA, c.dMask.p);
                 c.stats.kernel_launches += 2;
-                k_pcg_update<T><<<grid, kBS, 0, c.stream>>>(n, V.x.p, V.r.p, V.p.p, V.q.p, V.z.p, V.dinv.p, sc, st);
+                k_pcg_update<T><<<grid, kBS, 0, c.stream>>>(n, V.x.p, V.r.p, V.p.p, V.q.p, V.z.p,
+                                                            amg ? nullptr : V.dinv.p, sc, st);
+                if (amg)
+                {
+                    AmgApply<T>(c, V.r.p, V.z.p, st);
+                    k_pcg_rz<T><<<grid, kBS, 0, c.stream>>>(n, V.r.p, V.z.p, sc, st, 0);
+                    c.stats.kernel_launches += 1;
+                }
                 k_pcg_dir<T><<<grid, kBS, 0, c.stream>>>(n, V.p.p, V.z.p, sc, st);
             }
             else

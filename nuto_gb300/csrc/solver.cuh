@@ -65,6 +65,7 @@ template <typename T>
 struct GVecs
 {
     DBuf<T> V, w, z;
+    DBuf<T> Z; // preconditioned basis of the flexible form (m vectors), allocated on first use
     int64_t n = 0;
     void ensure(int64_t count)
     {
@@ -73,7 +74,13 @@ struct GVecs
         V.alloc(static_cast<size_t>(count) * (kGmresRestart + 1));
         w.alloc(count);
         z.alloc(count);
+        Z.free();
         n = count;
+    }
+    void ensureZ()
+    {
+        if (Z.n != static_cast<size_t>(n) * kGmresRestart)
+            Z.alloc(static_cast<size_t>(n) * kGmresRestart);
     }
 };
 

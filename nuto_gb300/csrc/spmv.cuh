@@ -1,0 +1,205 @@
+// Shared device pieces of the solver kernels: block reductions, the last-block ticket and the node-block SpMV.
+#pragma once
+
+#include "solver.cuh"
+
+namespace nuto_gpu
+{
+
+constexpr int kBS = 256;
+
+__device__ __forceinline__ double WarpSum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sums v over the block and adds the block total to *acc (thread 0).
+__device__ __forceinline__ void BlockAccumulate(double v, double* acc, double* sh)
+{
+    v = WarpSum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        sh[wid] = v;
+    __syncthreads();
+    if (wid == 0)
+    {
+        v = lane < (blockDim.x >> 5) ? sh[lane] : 0.;
+        v = WarpSum(v);
+        if (lane == 0)
+            atomicAdd(acc, v);
+    }
+    __syncthreads();
+}
+
+// True in exactly one block: the last one to arrive (threadFenceReduction pattern, no spinning).
+__device__ __forceinline__ bool LastBlock(int* counter)
+{
+    __shared__ bool last;
+    __threadfence();
+    if (threadIdx.x == 0)
+    {
+        const unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(counter), 1u);
+        last = prev == gridDim.x - 1;
+    }
+    __syncthreads();
+    return last;
+}
+
+__device__ __forceinline__ double VRead(const double* p)
+{
+    return *reinterpret_cast<const volatile double*>(p);
+}
+
+__device__ __forceinline__ bool Finite(double v)
+{
+    return isfinite(v);
+}
+
+// finalize actions of the SpMV kernel
+enum Fin
+{
+    FIN_NONE = 0,
+    FIN_PCG_ALPHA = 1,  // alpha = rho / (p.Ap)
+    FIN_BICG_ALPHA = 2, // alpha = rho / (rhat.v)
+    FIN_BICG_OMEGA = 3  // omega = (t.s) / (t.t)
+};
+
+// Node-block SpMV: one warp per DOF node (of every slot) computes all rows of that node. DofNumbering numbers the
+// components of a node consecutively, so every row of node a lists, per slot J, the J-neighbours of a in the
+// same order with ncomp_J consecutive values each; the lanes run over the neighbours, load the neighbour's x
+// values once for all rows of the node and read the values at rowPtr[row] + blk_IJ(a) + ncomp_J * k + d. The
+// column indices are never read: the CSR values plus the per-node neighbour lists are the whole traffic.
+// The row segment of node a starts at rowPtr[row] + blk[I * ns][a]: zero for the whole operator; a diagonal-block
+// view (ns = 1, the lists and block offsets of the pair (I, I)) covers only the I-columns of the I-rows.
+struct NodeSpmv
+{
+    int ns;
+    int ncomp[kMaxSlots];
+    int64_t nNodes[kMaxSlots];
+    int64_t firstWarp[kMaxSlots];
+    int64_t totalWarps;
+    const int64_t* gdof[kMaxSlots];
+    const int64_t* nbrPtr[kMaxSlots * kMaxSlots];
+    const int32_t* nbrIdx[kMaxSlots * kMaxSlots];
+    const int32_t* blk[kMaxSlots * kMaxSlots];
+    const int64_t* rowPtr;
+    int64_t nnz, nRows, nbrTotal[kMaxSlots * kMaxSlots];
+};
+
+constexpr int kMaxRowLen = 256; // longest row of a node (Hex20 displacements: 3 x 81)
+
+template <typename TV, typename TX, int NDOT>
+__global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
+                                                    const uint8_t* __restrict__ mask, const TX* __restrict__ x,
+                                                    TX* __restrict__ y, const TX* __restrict__ w0, double* sc, int* st,
+                                                    int fin)
+{
+    __shared__ double sh[kBS / 32];
+    __shared__ TX xs[kBS / 32][kMaxRowLen];
+    if (st && st[ST_STATE] != RUN)
+        return;
+    const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int I = (A.ns > 1 && warp >= A.firstWarp[1]) ? 1 : 0;
+    const int64_t a = warp - A.firstWarp[I];
+    const bool valid = warp < A.totalWarps && a < A.nNodes[I];
+    const int ncI = A.ncomp[I];
+    double d0 = 0., d1 = 0.;
+    if (valid)
+    {
+        // x of the node's neighbours in the column order of its rows
+        int len = 0;
+        for (int J = 0; J < A.ns; ++J)
+        {
+            const int p = I * A.ns + J;
+            const int ncJ = A.ncomp[J];
+            const int64_t q0 = A.nbrPtr[p][a];
+            const int nn = static_cast<int>(A.nbrPtr[p][a + 1] - q0);
+            for (int kk = lane; kk < nn; kk += 32)
+            {
+                const int64_t gb = A.gdof[J][A.nbrIdx[p][NG_IDX(q0 + kk, A.nbrTotal[p], 17)]];
+                for (int d = 0; d < ncJ; ++d)
+                    xs[wid][NG_IDX(len + ncJ * kk + d, kMaxRowLen, 20)] = x[NG_IDX(gb + d, A.nRows, 18)];
+            }
+            len += ncJ * nn;
+        }
+        __syncwarp();
+        const int64_t g0 = A.gdof[I][a];
+        const int32_t seg = A.blk[I * A.ns][a]; // 0 for a whole-row operator, the block start for a block view
+        for (int c = 0; c < ncI; ++c)
+        {
+            const int64_t r = g0 + c;
+            const int64_t rs = A.rowPtr[NG_IDX(r, A.nRows, 16)] + seg;
+            TX s = TX(0);
+#pragma unroll 4
+            for (int q = lane; q < len; q += 32)
+                s += static_cast<TX>(val[NG_IDX(rs + q, A.nnz, 19)]) * xs[wid][q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                s += __shfl_down_sync(0xffffffffu, s, o);
+            if (lane == 0)
+            {
+                const TX yv = mask[r] ? x[r] : s;
+                y[r] = yv;
+                if (NDOT >= 1)
+                    d0 += static_cast<double>(w0[r]) * static_cast<double>(yv);
+                if (NDOT >= 2)
+                    d1 += static_cast<double>(yv) * static_cast<double>(yv);
+            }
+        }
+    }
+    if (NDOT == 0)
+        return;
+    BlockAccumulate(d0, sc + SC_ACC0, sh);
+    if (NDOT >= 2)
+        BlockAccumulate(d1, sc + SC_ACC1, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        const double a0 = VRead(sc + SC_ACC0), a1 = VRead(sc + SC_ACC1);
+        sc[SC_ACC0] = 0.;
+        sc[SC_ACC1] = 0.;
+        if (fin == FIN_PCG_ALPHA)
+        {
+            if (!Finite(a0))
+                st[ST_STATE] = NONFINITE;
+            else if (!(a0 > 0.))
+                st[ST_STATE] = BREAKDOWN;
+            else
+                sc[SC_ALPHA] = sc[SC_RHO] / a0;
+        }
+        else if (fin == FIN_BICG_ALPHA)
+        {
+            if (!Finite(a0))
+                st[ST_STATE] = NONFINITE;
+            else if (a0 == 0.)
+                st[ST_STATE] = BREAKDOWN;
+            else
+                sc[SC_ALPHA] = sc[SC_RHO] / a0;
+        }
+        else if (fin == FIN_BICG_OMEGA)
+        {
+            if (!Finite(a0) || !Finite(a1))
+                st[ST_STATE] = NONFINITE;
+            else
+                sc[SC_OMEGA] = a1 > 0. ? a0 / a1 : 0.;
+        }
+    }
+}
+
+// NodeSpmv of the context's fine-level pattern
+NodeSpmv MakeNodeSpmv(const Ctx& c);
+
+template <typename TV, typename TX, int NDOT>
+void SpmvNode(cudaStream_t stream, const NodeSpmv& A, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc,
+              int* st, int fin, const uint8_t* mask)
+{
+    const int64_t threads = A.totalWarps * 32;
+    const unsigned blocks = static_cast<unsigned>((threads + kBS - 1) / kBS);
+    k_spmv_node<TV, TX, NDOT><<<blocks, kBS, 0, stream>>>(A, vals, mask, x, y, w0, sc, st, fin);
+}
+
+} // namespace nuto_gpu

@@ -190,12 +190,14 @@ def test_update_history(kind, n):
     assert np.abs(g.history - P.kappa).max() <= 1e-15 + 1e-13 * np.abs(P.kappa).max()
 
 
-@pytest.mark.parametrize("method", [1, 2, 3])
+@pytest.mark.parametrize("method,precond", [(1, 1), (1, 2), (2, 1), (3, 1), (3, 2)])
 @pytest.mark.parametrize("precision", [64, 32])
-def test_linear_solve_quad4(precision, method):
-    """Jacobi PCG (1), BiCGStab (2) and GMRES (3) against a direct solve of the reduced system C^T K C."""
+def test_linear_solve_quad4(precision, method, precond):
+    """PCG (1), BiCGStab (2) and GMRES (3) with the Jacobi (1) or multigrid (2) preconditioner against a direct
+    solve of the reduced system C^T K C."""
     _torch()
     s, g, (om, layers, P, cons) = _build("quad4", 12)
+    g.set_preconditioner(precond)
     u0 = np.zeros(P.n_dofs)
     K = _oracle_csr(P, u0)
     vals = g.build_matrix(u0, precision)
@@ -245,10 +247,13 @@ def test_quasistatic_quad4_elastic(precision):
     assert rel <= (1e-8 if precision == 64 else 1e-6), (rel, st)
 
 
-def test_gmres_nonsymmetric_gradient_damage_tangent():
-    """GMRES on the non-symmetric gradient-damage tangent in the damaged regime, FP64 and FP32 values."""
+@pytest.mark.parametrize("precond", [1, 2])
+def test_gmres_nonsymmetric_gradient_damage_tangent(precond):
+    """GMRES on the non-symmetric gradient-damage tangent in the damaged regime, FP64 and FP32 values, Jacobi (1)
+    and multigrid (2) preconditioning."""
     _torch()
     s, g, (om, layers, P, cons) = _build("hex8gd", 3)
+    g.set_preconditioner(precond)
     rng = np.random.default_rng(2)
     # a consistent damaged state: eight load steps of the oracle's Newton (damage grows from step 4)
     Q = QuasistaticOracle(P, cons[0], cons[1], cons[2], tolerance=1e-10, max_iterations=20)
@@ -288,3 +293,42 @@ def test_quasistatic_hex8_gradient_damage(precision):
         assert rel <= (1e-7 if precision == 64 else 1e-6), (k, rel, st)
         assert np.abs(kg - ko).max() <= (1e-7 if precision == 64 else 1e-6) * max(np.abs(ko).max(), 1e-4)
     assert res[-1][2].max() > 1e-4  # the last steps are in the damaged regime
+
+
+@pytest.mark.parametrize("kind,n,steps", [("hex8gd", 8, 0), ("hex8gd", 8, 6), ("hex20", 4, 0), ("quad4", 40, 0)])
+def test_multigrid_levels_solve(kind, n, steps):
+    """Multigrid-preconditioned solves on meshes large enough for several levels: GMRES (FP64 and FP32 values)
+    on the gradient-damage tangent, undamaged and after damaging load steps of the oracle, and PCG on the
+    symmetric Hex20 and Quad4 tangents, each against a direct solve; the multigrid solve needs fewer iterations
+    than the Jacobi one."""
+    _torch()
+    import scipy.sparse.linalg as spla
+
+    s, g, (om, layers, P, cons) = _build(kind, n)
+    u = np.zeros(P.n_dofs)
+    if steps:
+        Q = QuasistaticOracle(P, cons[0], cons[1], cons[2], tolerance=1e-10, max_iterations=20)
+        for k in range(1, steps + 1):
+            Q.do_step(0.05 * k)
+        u = Q.x.copy()
+        g.history = P.kappa.copy()
+    dep = cons[0]
+    indep = np.setdiff1d(np.arange(P.n_dofs), dep)
+    b = np.random.default_rng(5).uniform(-1, 1, P.n_dofs)
+    rp, ci = g.pattern()
+    for precision in (64, 32):
+        vals = g.build_matrix(u, precision)
+        its = {}
+        for precond in (2, 1):
+            g.set_preconditioner(precond)
+            x, it, rel, ok = g.solve(vals, b, precision=precision, method=0, rtol=1e-9, max_iterations=20000)
+            if precond == 1 and not ok:
+                its[1] = np.inf  # Jacobi may stall on the damaged tangent; the multigrid solve must not
+                continue
+            assert ok, (precision, precond, it, rel)
+            its[precond] = it
+            Kp = sp.csr_matrix((vals.double().cpu().numpy(), ci, rp), shape=(P.n_dofs, P.n_dofs))
+            y = spla.spsolve(Kp[indep][:, indep].tocsc(), b[indep])
+            xg = x.cpu().numpy()
+            assert np.abs(xg[indep] - y).max() <= 1e-6 * np.abs(y).max(), (precision, precond)
+        assert its[2] < its[1], its
