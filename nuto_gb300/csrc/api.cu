@@ -253,7 +253,21 @@ static void BuildPattern(Ctx& c)
         for (int64_t e = 0; e < nCells; ++e)
             for (int i = 0; i < S.nen; ++i)
                 L.idx[fill[S.conn[e * S.nen + i]]++] = static_cast<int32_t>(e);
+        std::vector<uint8_t> loc(L.idx.size());
+        for (int64_t a = 0; a < S.nNodes; ++a)
+            for (int64_t k = L.ptr[a]; k < L.ptr[a + 1]; ++k)
+            {
+                const int64_t e = L.idx[k];
+                int i = 0;
+                while (S.conn[e * S.nen + i] != a)
+                    ++i;
+                loc[k] = static_cast<uint8_t>(i);
+            }
+        Upload(c.slots[I].dCellPtr, L.ptr);
+        Upload(c.slots[I].dCellIdx, L.idx);
+        Upload(c.slots[I].dCellLoc, loc);
     }
+    c.rowsMode = -1;
 
     // neighbour lists per (I, J): J-nodes of all cells around an I-node, sorted by DOF number
     std::vector<NodeLists> nbr(ns * ns);
@@ -530,6 +544,8 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
     const char* sc = std::getenv("NUTO_GPU_SYNC_CHECK");
     c->syncCheck = sc && sc[0] == '1';
 #endif
+    const char* tk = std::getenv("NUTO_GPU_TANGENT");
+    c->forceAtomicTangent = tk && std::string(tk) == "atomic";
     const int rc = Guard(c, [&] {
         NG_CUDA(cudaSetDevice(device));
         NG_CUDA(cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device));
@@ -771,6 +787,7 @@ int nuto_gpu_set_integrand(nuto_gpu_ctx* ctx, const nuto_gpu_integrand* p)
         ctx->dKappa.alloc(static_cast<size_t>(ctx->nCells) * ctx->ip.nIp);
         NG_CUDA(cudaMemsetAsync(ctx->dKappa.p, 0, ctx->dKappa.n * sizeof(double), ctx->stream));
         ctx->haveIntegrand = true;
+        ctx->rowsMode = -1;
         ctx->haveGeo = false;
         return NUTO_GPU_OK;
     });

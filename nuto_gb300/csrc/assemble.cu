@@ -419,7 +419,25 @@ struct TangentShape
     static constexpr int cpb = MaxI<1, MinI<512 / (ND * ND), 256 / (NIP * ND)>::v>::v;
 };
 
-template <typename T, int DIM, int ND, int NIP, int KIND>
+// Integration-point record of the row-gather tangent (per cell and point, contiguous): the node gradients
+// G[ND][DIM], the integrand scalars (lambda w, mu w; gradient damage: w, c g w, c g' w' k' w grad eeq) and the
+// two Voigt vectors of the rank-1 parts (local / gradient damage).
+template <int DIM, int ND, int KIND>
+struct IpRecord
+{
+    static constexpr bool GD = KIND == NUTO_GPU_GRADIENT_DAMAGE;
+    static constexpr bool RANK1 = GD || KIND == NUTO_GPU_MB_LOCAL_DAMAGE;
+    static constexpr int VD = DIM == 2 ? 3 : 6;
+    static constexpr int nrec = 2 + (GD ? 2 + DIM : 0);
+    static constexpr int g = 0;
+    static constexpr int rec = ND * DIM;
+    static constexpr int st = rec + nrec;
+    static constexpr int size = st + (RANK1 ? 2 * VD : 0);
+};
+
+// REC = false: element-wise tangent, node-pair blocks added into the CSR values with atomics.
+// REC = true: phases 0 and A only; the integration-point records are written for k_tangent_rows.
+template <typename T, int DIM, int ND, int NIP, int KIND, bool REC>
 __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, ScatterArgs S, int pUU, int pUE, int pEU,
                                                  int pEE, const double* __restrict__ u, T* __restrict__ vals)
 {
@@ -451,24 +469,29 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
             continue;
         const int32_t aD = static_cast<int32_t>(NG_IDX(a.connD[static_cast<int64_t>(nd) * n + e], a.nNodesD, 2));
         const int64_t g = a.gdofD[aD];
-        const int32_t bUU = S.blk[pUU][aD];
 #pragma unroll
         for (int c = 0; c < DIM; ++c)
         {
             sU[cl][nd][c] = u[NG_IDX(g + c, a.nDofs, 3)];
-            const int64_t rs = S.rowPtr[NG_IDX(g + c, S.nRows, 9)];
-            sBaseU[cl][nd][c] = rs + bUU;
-            if (GD)
-                sBaseUE[cl][nd][c] = rs + S.blk[pUE][aD];
+            if (!REC)
+            {
+                const int64_t rs = S.rowPtr[NG_IDX(g + c, S.nRows, 9)];
+                sBaseU[cl][nd][c] = rs + S.blk[pUU][aD];
+                if (GD)
+                    sBaseUE[cl][nd][c] = rs + S.blk[pUE][aD];
+            }
         }
         if (GD)
         {
             const int32_t aE = static_cast<int32_t>(NG_IDX(a.connE[static_cast<int64_t>(nd) * n + e], a.nNodesE, 4));
             const int64_t ge = a.gdofE[aE];
             sE[cl][nd] = u[NG_IDX(ge, a.nDofs, 5)];
-            const int64_t rs = S.rowPtr[NG_IDX(ge, S.nRows, 9)];
-            sBaseEU[cl][nd] = rs + S.blk[pEU][aE];
-            sBaseEE[cl][nd] = rs + S.blk[pEE][aE];
+            if (!REC)
+            {
+                const int64_t rs = S.rowPtr[NG_IDX(ge, S.nRows, 9)];
+                sBaseEU[cl][nd] = rs + S.blk[pEU][aE];
+                sBaseEE[cl][nd] = rs + S.blk[pEE][aE];
+            }
         }
     }
     for (int it = threadIdx.x; it < CPB * NIP * ND * DIM; it += blockDim.x)
@@ -588,6 +611,29 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
     }
     __syncthreads();
 
+    if (REC)
+    {
+        // records of the block's cells are one contiguous range: coalesced stores
+        using R = IpRecord<DIM, ND, KIND>;
+        const int cells = static_cast<int>(n - cell0 < CPB ? n - cell0 : CPB);
+        T* out = vals + cell0 * NIP * R::size;
+        for (int it = threadIdx.x; it < cells * NIP * R::size; it += blockDim.x)
+        {
+            const int f = it % R::size;
+            const int r = it / R::size;
+            const int q = r % NIP, cl = r / NIP;
+            T v;
+            if (f < R::rec)
+                v = sG[cl][q][f / DIM][f % DIM];
+            else if (f < R::st)
+                v = sRec[cl][q][f - R::rec];
+            else
+                v = sST[cl][q][(f - R::st) / VD][(f - R::st) % VD];
+            out[it] = v;
+        }
+        return;
+    }
+
     if (RANK1)
     {
         for (int it = threadIdx.x; it < CPB * NIP * ND; it += blockDim.x)
@@ -705,9 +751,309 @@ static ScatterArgs MakeScatterArgs(Ctx& c)
     return s;
 }
 
+// ---- row-gather tangent ------------------------------------------------------------------------------------
+// One warp per displacement node a assembles the complete CSR rows of a (and, for gradient damage, of its eeq
+// node): for every cell around a it reads the cell's integration-point records once (contiguous), each lane
+// integrates one (neighbour b, row) item of the node-pair block over the points, and the sums are added into a
+// shared-memory copy of the rows at the ranks of b. Cells are visited one after another, so the row buffer
+// needs no atomics; at the end the rows are stored once, coalesced, and no value array reset is needed.
+struct RowArgs
+{
+    int64_t nNodes, nCells, nnz, nRows;
+    const int64_t* gdofD;
+    const int64_t* gdofE;
+    const int32_t* eOf;
+    const int64_t* cellPtr;
+    const int32_t* cellIdx;
+    const uint8_t* cellLoc;
+    const int64_t* rowPtr;
+    const uint8_t* rank[4]; // UU, UE, EU, EE
+    const int32_t* blk[4];
+    const double* tabN; // nIp x nd
+};
+
+constexpr int kRowCap = 256;
+
+template <typename T, int DIM, int ND, int NIP, int KIND>
+struct RowShape
+{
+    using R = IpRecord<DIM, ND, KIND>;
+    static constexpr int nrows = DIM + (R::GD ? 1 : 0);
+    static constexpr int warps = sizeof(T) == 4 ? 4 : 2;
+    static constexpr int perWarp = NIP * R::size + nrows * kRowCap; // elements of T
+    static constexpr size_t smem = static_cast<size_t>(warps) * perWarp * sizeof(T);
+};
+
+template <typename T, int DIM, int ND, int NIP, int KIND>
+__global__ void __launch_bounds__(RowShape<T, DIM, ND, NIP, KIND>::warps * 32)
+        k_tangent_rows(RowArgs r, const T* __restrict__ recs, T* __restrict__ vals)
+{
+    using R = IpRecord<DIM, ND, KIND>;
+    using Sh = RowShape<T, DIM, ND, NIP, KIND>;
+    constexpr bool GD = R::GD;
+    constexpr bool LD = KIND == NUTO_GPU_MB_LOCAL_DAMAGE;
+    constexpr int VD = R::VD;
+    constexpr int NJ = DIM + (GD ? 1 : 0); // items per neighbour: the DIM displacement rows (+ the eeq row)
+    constexpr int NITEM = ND * NJ;
+    constexpr int MAXIT = (NITEM + 31) / 32;
+    constexpr int NROWS = Sh::nrows;
+    extern __shared__ __align__(16) unsigned char smRaw[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T* rec = reinterpret_cast<T*>(smRaw) + wid * Sh::perWarp;
+    T* row = rec + NIP * R::size;
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * Sh::warps + wid;
+    if (a >= r.nNodes)
+        return; // the whole warp leaves; only warp-level synchronisation follows
+    int64_t rs[NROWS];
+    int len[NROWS];
+    const int64_t g = r.gdofD[a];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+    {
+        rs[k] = r.rowPtr[NG_IDX(g + k, r.nRows, 40)];
+        len[k] = static_cast<int>(r.rowPtr[g + k + 1] - rs[k]);
+    }
+    int32_t ae = 0;
+    if (GD)
+    {
+        ae = r.eOf[a];
+        const int64_t ge = r.gdofE[ae];
+        rs[DIM] = r.rowPtr[NG_IDX(ge, r.nRows, 40)];
+        len[DIM] = static_cast<int>(r.rowPtr[ge + 1] - rs[DIM]);
+    }
+    const int32_t bUU = r.blk[0][a];
+    const int32_t bUE = GD ? r.blk[1][a] : 0;
+    const int32_t bEU = GD ? r.blk[2][ae] : 0;
+    const int32_t bEE = GD ? r.blk[3][ae] : 0;
+#pragma unroll
+    for (int k = 0; k < NROWS; ++k)
+        for (int q = lane; q < len[k]; q += 32)
+            row[k * kRowCap + q] = T(0);
+    __syncwarp();
+
+    for (int64_t kc = r.cellPtr[a]; kc < r.cellPtr[a + 1]; ++kc)
+    {
+        const int64_t e = r.cellIdx[kc];
+        const int ia = r.cellLoc[kc];
+        const T* src = recs + NG_IDX(e, r.nCells, 41) * (NIP * R::size);
+        for (int i = lane; i < NIP * R::size; i += 32)
+            rec[i] = src[i];
+        __syncwarp();
+        T acc[MAXIT][DIM + 1];
+#pragma unroll
+        for (int m = 0; m < MAXIT; ++m)
+#pragma unroll
+            for (int l = 0; l <= DIM; ++l)
+                acc[m][l] = T(0);
+        for (int q = 0; q < NIP; ++q)
+        {
+            const T* Rq = rec + q * R::size;
+            const T* ga = Rq + R::g + ia * DIM;
+            const T lamw = Rq[R::rec + 0], muw = Rq[R::rec + 1];
+            T Pa[DIM];
+            if (LD || GD)
+                BtS<T, DIM>(ga, Rq + R::st, Pa);
+            const T Na = GD ? static_cast<T>(r.tabN[q * ND + ia]) : T(0);
+#pragma unroll
+            for (int m = 0; m < MAXIT; ++m)
+            {
+                const int item = lane + 32 * m;
+                if (item >= NITEM)
+                    continue;
+                const int ib = item / NJ, j = item % NJ;
+                const T* gb = Rq + R::g + ib * DIM;
+                T gab = T(0);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    gab += ga[d] * gb[d];
+                T Qb[DIM];
+                if (LD || (GD && j == DIM))
+                    BtS<T, DIM>(gb, Rq + R::st + VD, Qb);
+                if (j < DIM)
+                {
+                    T gaj = T(0), gbj = T(0);
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                        if (d == j)
+                        {
+                            gaj = ga[d];
+                            gbj = gb[d];
+                        }
+#pragma unroll
+                    for (int l = 0; l < DIM; ++l)
+                        acc[m][l] += lamw * gaj * gb[l] + muw * ga[l] * gbj;
+                    T paj = T(0);
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                        if (d == j)
+                        {
+                            acc[m][d] += muw * gab;
+                            if (LD || GD)
+                                paj = Pa[d];
+                        }
+                    if (LD)
+                    {
+#pragma unroll
+                        for (int l = 0; l < DIM; ++l)
+                            acc[m][l] += paj * Qb[l];
+                    }
+                    if (GD)
+                        acc[m][DIM] += paj * static_cast<T>(r.tabN[q * ND + ib]);
+                }
+                else if (GD)
+                {
+                    const T Nb = static_cast<T>(r.tabN[q * ND + ib]);
+                    T gs = T(0);
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                        gs += ga[d] * Rq[R::rec + 4 + d];
+#pragma unroll
+                    for (int l = 0; l < DIM; ++l)
+                        acc[m][l] -= Na * Qb[l];
+                    acc[m][DIM] += Rq[R::rec + 2] * Na * Nb + Rq[R::rec + 3] * gab + gs * Nb;
+                }
+            }
+        }
+        // add the items into the row buffer at the ranks of b (distinct positions: no conflicts)
+#pragma unroll
+        for (int m = 0; m < MAXIT; ++m)
+        {
+            const int item = lane + 32 * m;
+            if (item >= NITEM)
+                continue;
+            const int ib = item / NJ, j = item % NJ;
+            const int64_t ridx = static_cast<int64_t>(ia * ND + ib) * r.nCells + e;
+            if (j < DIM)
+            {
+                T* rw = row + j * kRowCap;
+                const int pos = bUU + DIM * r.rank[0][ridx];
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    rw[NG_IDX(pos + l, kRowCap, 42)] += acc[m][l];
+                if (GD)
+                    rw[NG_IDX(bUE + r.rank[1][ridx], kRowCap, 42)] += acc[m][DIM];
+            }
+            else
+            {
+                T* rw = row + DIM * kRowCap;
+                const int pos = bEU + DIM * r.rank[2][ridx];
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    rw[NG_IDX(pos + l, kRowCap, 42)] += acc[m][l];
+                rw[NG_IDX(bEE + r.rank[3][ridx], kRowCap, 42)] += acc[m][DIM];
+            }
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int k = 0; k < NROWS; ++k)
+        for (int q = lane; q < len[k]; q += 32)
+            vals[NG_IDX(rs[k] + q, r.nnz, 43)] = row[k * kRowCap + q];
+}
+
+// Row gather applies when every displacement node has one eeq node with the same local index in all its cells
+// (same interpolation for both fields, as in every gradient-damage set-up here) and the rows fit the buffer.
+static bool RowsSupported(Ctx& c)
+{
+    if (c.rowsMode >= 0)
+        return c.rowsMode == 1;
+    c.rowsMode = 0;
+    const int dS = c.prm.disp_slot;
+    const Slot& D = c.slots[dS];
+    if (c.prm.kind == NUTO_GPU_GRADIENT_DAMAGE)
+    {
+        const Slot& E = c.slots[c.prm.eeq_slot];
+        if (E.nen != D.nen || E.nNodes != D.nNodes)
+            return false;
+        std::vector<int32_t> eOf(D.nNodes, -1);
+        std::vector<char> seen(E.nNodes, 0);
+        for (size_t i = 0; i < D.conn.size(); ++i)
+        {
+            int32_t& m = eOf[D.conn[i]];
+            if (m < 0)
+            {
+                m = E.conn[i];
+                if (seen[m])
+                    return false;
+                seen[m] = 1;
+            }
+            else if (m != E.conn[i])
+                return false;
+        }
+        c.dEOf.alloc(eOf.size());
+        NG_CUDA(cudaMemcpy(c.dEOf.p, eOf.data(), eOf.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    }
+    c.rowsMode = 1;
+    return true;
+}
+
+static RowArgs MakeRowArgs(Ctx& c)
+{
+    const int ns = static_cast<int>(c.slots.size());
+    const int dS = c.prm.disp_slot;
+    const bool gd = c.prm.kind == NUTO_GPU_GRADIENT_DAMAGE;
+    const int eS = gd ? c.prm.eeq_slot : dS;
+    const Slot& D = c.slots[dS];
+    RowArgs r{};
+    r.nNodes = D.nNodes;
+    r.nCells = c.nCells;
+    r.nnz = c.nnz;
+    r.nRows = c.nDofs;
+    r.gdofD = D.dGdof.p;
+    r.gdofE = c.slots[eS].dGdof.p;
+    r.eOf = gd ? c.dEOf.p : nullptr;
+    r.cellPtr = D.dCellPtr.p;
+    r.cellIdx = D.dCellIdx.p;
+    r.cellLoc = D.dCellLoc.p;
+    r.rowPtr = c.dRowPtr.p;
+    const int pr[4] = {dS * ns + dS, dS * ns + eS, eS * ns + dS, eS * ns + eS};
+    for (int k = 0; k < 4; ++k)
+    {
+        r.rank[k] = c.pairs[pr[k]].rank;
+        r.blk[k] = c.pairs[pr[k]].dBlk.p;
+    }
+    r.tabN = c.dTables.p + c.tabN[D.interp];
+    return r;
+}
+
+template <typename T>
+static void LaunchTangentRows(Ctx& c, const double* u, T* vals)
+{
+    CellArgs a = MakeCellArgs(c);
+    ScatterArgs s = MakeScatterArgs(c);
+    RowArgs r = MakeRowArgs(c);
+    DispatchCfg(c, [&](auto cfg) {
+        using C = decltype(cfg);
+        using R = IpRecord<C::dim, C::nd, C::kind>;
+        using Sh = RowShape<T, C::dim, C::nd, C::nip, C::kind>;
+        const size_t recBytes = static_cast<size_t>(c.nCells) * C::nip * R::size * sizeof(T);
+        if (c.dRecords.n < recBytes)
+            c.dRecords.alloc(recBytes);
+        T* recs = reinterpret_cast<T*>(c.dRecords.p);
+        constexpr int CPB = TangentShape<C::nd, C::nip>::cpb;
+        const int blocks = static_cast<int>((c.nCells + CPB - 1) / CPB);
+        k_tangent<T, C::dim, C::nd, C::nip, C::kind, true><<<blocks, TangentShape<C::nd, C::nip>::threads, 0,
+                                                               c.stream>>>(a, c.law, s, 0, 0, 0, 0, u, recs);
+        AfterLaunch(c, "k_tangent (records)");
+        auto kern = k_tangent_rows<T, C::dim, C::nd, C::nip, C::kind>;
+        if (Sh::smem > 48 * 1024)
+            NG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(Sh::smem)));
+        const int64_t rowBlocks = (r.nNodes + Sh::warps - 1) / Sh::warps;
+        kern<<<static_cast<unsigned>(rowBlocks), Sh::warps * 32, Sh::smem, c.stream>>>(r, recs, vals);
+        AfterLaunch(c, "k_tangent_rows");
+    });
+    c.stats.kernel_launches += 2;
+}
+
 template <typename T>
 static void LaunchTangentT(Ctx& c, const double* u, T* vals)
 {
+    if (RowsSupported(c) && !c.forceAtomicTangent)
+    {
+        LaunchTangentRows<T>(c, u, vals);
+        return;
+    }
     NG_CUDA(cudaMemsetAsync(vals, 0, c.nnz * sizeof(T), c.stream));
     CellArgs a = MakeCellArgs(c);
     ScatterArgs s = MakeScatterArgs(c);
@@ -718,7 +1064,7 @@ static void LaunchTangentT(Ctx& c, const double* u, T* vals)
         using C = decltype(cfg);
         constexpr int CPB = TangentShape<C::nd, C::nip>::cpb;
         const int blocks = static_cast<int>((c.nCells + CPB - 1) / CPB);
-        k_tangent<T, C::dim, C::nd, C::nip, C::kind><<<blocks, TangentShape<C::nd, C::nip>::threads, 0, c.stream>>>(
+        k_tangent<T, C::dim, C::nd, C::nip, C::kind, false><<<blocks, TangentShape<C::nd, C::nip>::threads, 0, c.stream>>>(
                 a, c.law, s, dS * ns + dS, dS * ns + eS, eS * ns + dS, eS * ns + eS, u, vals);
     });
     AfterLaunch(c, "k_tangent");

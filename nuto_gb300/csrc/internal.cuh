@@ -170,6 +170,10 @@ struct Slot
     std::vector<int32_t> dof0; // per node: dof number of component 0
     DBuf<int32_t> dConnT; // planar [n][cell]
     DBuf<int64_t> dGdof; // per node: combined index of component 0
+    // node -> cells adjacency (cells in ascending order) with the node's local index in each cell
+    DBuf<int64_t> dCellPtr;
+    DBuf<int32_t> dCellIdx;
+    DBuf<uint8_t> dCellLoc;
 };
 
 // Per (slot I, slot J) scatter map: rank of the J-node among the sorted J-neighbours of the I-node, per cell and
@@ -261,6 +265,12 @@ struct Ctx
     DBuf<double> dGeo64;
     DBuf<float> dGeo32;
     int geoStride = 0;
+
+    // row-gather tangent: integration-point records and the displacement-node -> eeq-node map
+    int rowsMode = -1; // -1 not decided, 0 element-wise atomics, 1 row gather
+    bool forceAtomicTangent = false; // NUTO_GPU_TANGENT=atomic selects the element-wise kernel
+    DBuf<int32_t> dEOf;
+    DBuf<unsigned char> dRecords;
 
     // integrand
     bool haveIntegrand = false;
