@@ -106,7 +106,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     NG_CHECK(o.precision == NUTO_GPU_FP32 || o.precision == NUTO_GPU_FP64, NUTO_GPU_EINVAL, "precision 32 or 64");
     SolverWork& w = Work(c);
     const int64_t n = c.nDofs;
-    for (DBuf<double>* b : {&w.f, &w.rhs, &w.dx, &w.db, &w.x0, &w.xs, &w.tmp})
+    for (DBuf<double>* b : {&w.f, &w.rhs, &w.dx, &w.db, &w.x0, &w.xs, &w.tmp, &w.refR, &w.refKx})
         if (b->n != static_cast<size_t>(n))
             b->alloc(n);
     const bool fp32 = o.precision == NUTO_GPU_FP32;
@@ -140,13 +140,32 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
             throw Error{NUTO_GPU_ENAN, "non-finite residual"};
         return r;
     };
+    // FP64: one Krylov solve to krylov_rtol. FP32: FP32 Krylov sweeps inside an FP64 refinement on the FP32
+    // tangent (r = rhs - K32 dx accumulated in FP64) until the true relative residual reaches krylov_rtol: the
+    // FP32 iteration's own residual estimate is not trusted for the Newton direction.
     auto solve = [&](const double* rhs, double* out) {
         const auto k0 = std::chrono::steady_clock::now();
         int it = 0;
         double* relp = &lastRel;
         if (fp32)
-            KrylovSolveExport<float, float>(c, method, w.K32.p, rhs, out, false, o.krylov_rtol, o.max_krylov, &it,
-                                            relp);
+        {
+            const double bn = MaskedNorm(c, rhs);
+            NG_CUDA(cudaMemsetAsync(out, 0, n * sizeof(double), c.stream));
+            NG_CUDA(cudaMemcpyAsync(w.refR.p, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+            double rel = bn > 0. ? 1. : 0.;
+            for (int sweep = 0; sweep < 4 && rel > o.krylov_rtol && it < o.max_krylov; ++sweep)
+            {
+                const double inner = std::min(0.5, std::max(o.krylov_rtol / rel, 1e-5));
+                int its = 0;
+                KrylovSolveExport<float, float>(c, method, w.K32.p, w.refR.p, out, true, inner, o.max_krylov - it,
+                                                &its, nullptr);
+                it += its;
+                SpmvFull64(c, NUTO_GPU_FP32, w.K32.p, out, w.refKx.p);
+                Residual64(c, rhs, w.refKx.p, w.refR.p);
+                rel = bn > 0. ? MaskedNorm(c, w.refR.p) / bn : 0.;
+            }
+            lastRel = rel;
+        }
         else
             KrylovSolveExport<double, double>(c, method, w.K64.p, rhs, out, false, o.krylov_rtol, o.max_krylov,
                                               &it, relp);

@@ -118,6 +118,7 @@ struct SolverWork
     DBuf<float> K32;
     DBuf<double> K64;
     DBuf<double> f, rhs, dx, db, x0, xs, tmp;
+    DBuf<double> refR, refKx; // FP64 refinement of the FP32 Newton solves
     DBuf<uint8_t> zeroMask;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // CUDA-event pairs around the Krylov SpMV launches, folded into stats at synchronisation points

@@ -90,6 +90,7 @@ struct NodeSpmv
 };
 
 constexpr int kMaxRowLen = 256; // longest row of a node (Hex20 displacements: 3 x 81)
+constexpr int kMaxComp = 3;     // components per DOF node
 
 template <typename TV, typename TX, int NDOT>
 __global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
@@ -129,20 +130,38 @@ __global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restr
         __syncwarp();
         const int64_t g0 = A.gdof[I][a];
         const int32_t seg = A.blk[I * A.ns][a]; // 0 for a whole-row operator, the block start for a block view
-        for (int c = 0; c < ncI; ++c)
-        {
-            const int64_t r = g0 + c;
-            const int64_t rs = A.rowPtr[NG_IDX(r, A.nRows, 16)] + seg;
-            TX s = TX(0);
-#pragma unroll 4
-            for (int q = lane; q < len; q += 32)
-                s += static_cast<TX>(val[NG_IDX(rs + q, A.nnz, 19)]) * xs[wid][q];
+        // all rows of the node stream together (ncI independent loads per step keep more bytes in flight)
+        int64_t rs[kMaxComp];
+        TX s[kMaxComp];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                s += __shfl_down_sync(0xffffffffu, s, o);
-            if (lane == 0)
+        for (int c = 0; c < kMaxComp; ++c)
+        {
+            rs[c] = c < ncI ? A.rowPtr[NG_IDX(g0 + c, A.nRows, 16)] + seg : 0;
+            s[c] = TX(0);
+        }
+#pragma unroll 4
+        for (int q = lane; q < len; q += 32)
+        {
+            const TX xv = xs[wid][q];
+#pragma unroll
+            for (int c = 0; c < kMaxComp; ++c)
+                if (c < ncI)
+                    s[c] += static_cast<TX>(val[NG_IDX(rs[c] + q, A.nnz, 19)]) * xv;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < kMaxComp; ++c)
+                s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
+        if (lane == 0)
+        {
+#pragma unroll
+            for (int c = 0; c < kMaxComp; ++c)
             {
-                const TX yv = mask[r] ? x[r] : s;
+                if (c >= ncI)
+                    break;
+                const int64_t r = g0 + c;
+                const TX yv = mask[r] ? x[r] : s[c];
                 y[r] = yv;
                 if (NDOT >= 1)
                     d0 += static_cast<double>(w0[r]) * static_cast<double>(yv);
