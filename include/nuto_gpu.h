@@ -78,6 +78,7 @@ extern "C" {
 /* arithmetic of the tangent values and of the Krylov iteration */
 #define NUTO_GPU_FP32 32
 #define NUTO_GPU_FP64 64
+#define NUTO_GPU_MIXED 48 /* nuto_gpu_do_step only: FP32 tangent and preconditioner, FP64 Krylov vectors */
 
 /* Krylov methods */
 #define NUTO_GPU_SOLVER_AUTO 0     /* PCG for the symmetric integrands, GMRES otherwise */
@@ -112,6 +113,7 @@ typedef struct nuto_gpu_integrand
 typedef struct nuto_gpu_step_options
 {
     int precision;      /* NUTO_GPU_FP32: FP32 tangent + FP32 Krylov, FP64 residual and refinement;
+                           NUTO_GPU_MIXED: FP32 tangent + preconditioner, FP64 Krylov vectors and accumulation;
                            NUTO_GPU_FP64: everything FP64 */
     int method;         /* NUTO_GPU_SOLVER_* */
     double newton_rtol; /* converged when |C^T r| <= max(newton_atol, newton_rtol * |C^T (r + K db)|_trial) */

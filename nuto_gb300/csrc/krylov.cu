@@ -943,6 +943,8 @@ template int KrylovSolveExport<float, float>(Ctx&, int, const float*, const doub
                                              int*, double*);
 template int KrylovSolveExport<double, double>(Ctx&, int, const double*, const double*, double*, bool, double, int,
                                                int*, double*);
+template int KrylovSolveExport<double, float>(Ctx&, int, const float*, const double*, double*, bool, double, int,
+                                              int*, double*);
 
 __global__ void k_residual64(int64_t n, const uint8_t* __restrict__ mask, const double* __restrict__ b,
                              const double* __restrict__ kx, double* __restrict__ r)

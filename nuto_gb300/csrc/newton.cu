@@ -6,7 +6,8 @@
 //
 // Precision: with NUTO_GPU_FP32 the tangent is assembled and the Krylov iteration runs in FP32, while the
 // residual, the history, the constraint values and the convergence test stay FP64, so Newton acts as
-// iterative refinement of the FP32 linear solves. NUTO_GPU_FP64 runs everything in FP64.
+// iterative refinement of the FP32 linear solves. NUTO_GPU_MIXED keeps the FP32 tangent and preconditioner but runs
+// the Krylov vectors and the products' accumulation in FP64. NUTO_GPU_FP64 runs everything in FP64.
 #include "solver.cuh"
 
 #include <chrono>
@@ -103,13 +104,16 @@ struct Timers
 int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
 {
     const auto t0 = std::chrono::steady_clock::now();
-    NG_CHECK(o.precision == NUTO_GPU_FP32 || o.precision == NUTO_GPU_FP64, NUTO_GPU_EINVAL, "precision 32 or 64");
+    NG_CHECK(o.precision == NUTO_GPU_FP32 || o.precision == NUTO_GPU_FP64 || o.precision == NUTO_GPU_MIXED,
+             NUTO_GPU_EINVAL, "precision NUTO_GPU_FP32, NUTO_GPU_FP64 or NUTO_GPU_MIXED");
     SolverWork& w = Work(c);
     const int64_t n = c.nDofs;
     for (DBuf<double>* b : {&w.f, &w.rhs, &w.dx, &w.db, &w.x0, &w.xs, &w.tmp, &w.refR, &w.refKx})
         if (b->n != static_cast<size_t>(n))
             b->alloc(n);
-    const bool fp32 = o.precision == NUTO_GPU_FP32;
+    const bool mixed = o.precision == NUTO_GPU_MIXED;
+    const bool fp32 = o.precision == NUTO_GPU_FP32 || mixed; // FP32 tangent values
+    const int valPrec = fp32 ? NUTO_GPU_FP32 : NUTO_GPU_FP64;
     if (fp32 && w.K32.n != static_cast<size_t>(c.nnz))
         w.K32.alloc(c.nnz);
     if (!fp32 && w.K64.n != static_cast<size_t>(c.nnz))
@@ -125,7 +129,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
 
     auto assembleK = [&](const double* x) {
         const int k = T.Begin();
-        LaunchTangent(c, x, o.precision, K);
+        LaunchTangent(c, x, valPrec, K);
         T.End(k, &S.ms_assemble_matrix);
         S.matrix_assemblies++;
     };
@@ -147,7 +151,10 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
         const auto k0 = std::chrono::steady_clock::now();
         int it = 0;
         double* relp = &lastRel;
-        if (fp32)
+        if (mixed)
+            KrylovSolveExport<double, float>(c, method, w.K32.p, rhs, out, false, o.krylov_rtol, o.max_krylov, &it,
+                                             relp);
+        else if (fp32)
         {
             const double bn = MaskedNorm(c, rhs);
             NG_CUDA(cudaMemsetAsync(out, 0, n * sizeof(double), c.stream));
@@ -192,7 +199,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     if (c.nDep > 0)
         k_delta_bc<<<static_cast<unsigned>((c.nDep + 255) / 256), 256, 0, c.stream>>>(
                 c.nDep, c.dDepIdx.p, c.dDepA.p, c.dDepB.p, tOld, tNew, w.db.p);
-    SpmvFull64(c, o.precision, K, w.db.p, w.tmp.p);
+    SpmvFull64(c, valPrec, K, w.db.p, w.tmp.p);
     k_masked_sum<<<gb, 256, 0, c.stream>>>(n, c.dMask.p, w.f.p, w.tmp.p, w.rhs.p);
     AfterLaunch(c, "newton vector kernels");
     S.kernel_launches += c.nDep > 0 ? 2 : 1;
