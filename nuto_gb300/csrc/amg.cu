@@ -48,7 +48,7 @@ struct AmgLevel
     std::vector<double> hCoords; // 3 per node
     // device structure of coarse levels (level 0 uses the context's pattern)
     DBuf<int64_t> gdof, rowPtr, nbrPtr;
-    DBuf<int32_t> nbrIdx, blk;
+    DBuf<int32_t> nbrIdx, nbrCol, blk;
     DBuf<int32_t> diagOff;  // per node: offset of the diagonal block in the node's row segment
     DBuf<uint8_t> zeroMask; // coarse levels have no constrained rows
     // transfer from the finer level
@@ -155,6 +155,7 @@ static void FillSpmv(AmgLevel& L)
     A.gdof[0] = L.gdof.p;
     A.nbrPtr[0] = L.nbrPtr.p;
     A.nbrIdx[0] = L.nbrIdx.p;
+    A.nbrCol[0] = L.nbrCol.p;
     A.blk[0] = L.blk.p;
     A.nbrTotal[0] = static_cast<int64_t>(L.nbrIdx.n);
     A.rowPtr = L.rowPtr.p;
@@ -176,6 +177,7 @@ static NodeSpmv SlotView(const Ctx& c, int I)
     A.gdof[0] = c.slots[I].dGdof.p;
     A.nbrPtr[0] = M.dNbrPtr.p;
     A.nbrIdx[0] = M.dNbrIdx.p;
+    A.nbrCol[0] = M.dNbrCol.p;
     A.blk[0] = M.dBlk.p;
     A.nbrTotal[0] = static_cast<int64_t>(M.dNbrIdx.n);
     A.rowPtr = c.dRowPtr.p;
@@ -366,6 +368,12 @@ static void BuildSlotHierarchy(Ctx& c, int I, const double* ext, std::vector<Amg
         UploadV(C.blk, blk);
         UploadV(C.nbrPtr, C.hNbrPtr);
         UploadV(C.nbrIdx, C.hNbrIdx);
+        {
+            std::vector<int32_t> col(C.hNbrIdx.size());
+            for (size_t q = 0; q < col.size(); ++q)
+                col[q] = C.hNbrIdx[q] * C.ncomp;
+            UploadV(C.nbrCol, col);
+        }
         UploadV(C.diagOff, DiagOffsets(C.hNbrPtr, C.hNbrIdx, C.ncomp));
         UploadV(C.aggOf, agg);
         UploadV(C.cRank, cr);

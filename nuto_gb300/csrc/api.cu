@@ -404,6 +404,13 @@ static void BuildPattern(Ctx& c)
         Upload(M.dBlk, blk[p]);
         Upload(M.dNbrPtr, nbr[p].ptr);
         Upload(M.dNbrIdx, nbr[p].idx);
+        {
+            const Slot& SJ = c.slots[p % ns];
+            std::vector<int32_t> col(nbr[p].idx.size());
+            for (size_t q = 0; q < col.size(); ++q)
+                col[q] = static_cast<int32_t>(SJ.offset + SJ.dof0[nbr[p].idx[q]]);
+            Upload(M.dNbrCol, col);
+        }
         M.hNbrPtr = std::move(nbr[p].ptr);
         M.hNbrIdx = std::move(nbr[p].idx);
     }

@@ -780,9 +780,30 @@ struct RowShape
     using R = IpRecord<DIM, ND, KIND>;
     static constexpr int nrows = DIM + (R::GD ? 1 : 0);
     static constexpr int warps = sizeof(T) == 4 ? 4 : 2;
-    static constexpr int perWarp = NIP * R::size + nrows * kRowCap; // elements of T
+    static constexpr int recs = NIP * R::size;                         // one cell's records
+    static constexpr int perWarp = 2 * recs + nrows * kRowCap;          // double-buffered records + rows (T)
     static constexpr size_t smem = static_cast<size_t>(warps) * perWarp * sizeof(T);
 };
+
+// asynchronous global -> shared copies (cp.async, 4 or 8 bytes), committed and awaited in groups
+template <typename T>
+__device__ __forceinline__ void AsyncCopy(T* dst, const T* src)
+{
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(src) : "memory");
+}
+__device__ __forceinline__ void AsyncCommit()
+{
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void AsyncWait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 template <typename T, int DIM, int ND, int NIP, int KIND>
 __global__ void __launch_bounds__(RowShape<T, DIM, ND, NIP, KIND>::warps * 32)
@@ -799,8 +820,8 @@ __global__ void __launch_bounds__(RowShape<T, DIM, ND, NIP, KIND>::warps * 32)
     constexpr int NROWS = Sh::nrows;
     extern __shared__ __align__(16) unsigned char smRaw[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    T* rec = reinterpret_cast<T*>(smRaw) + wid * Sh::perWarp;
-    T* row = rec + NIP * R::size;
+    T* recBuf = reinterpret_cast<T*>(smRaw) + wid * Sh::perWarp;
+    T* row = recBuf + 2 * Sh::recs;
     const int64_t a = static_cast<int64_t>(blockIdx.x) * Sh::warps + wid;
     if (a >= r.nNodes)
         return; // the whole warp leaves; only warp-level synchronisation follows
@@ -831,13 +852,48 @@ __global__ void __launch_bounds__(RowShape<T, DIM, ND, NIP, KIND>::warps * 32)
             row[k * kRowCap + q] = T(0);
     __syncwarp();
 
-    for (int64_t kc = r.cellPtr[a]; kc < r.cellPtr[a + 1]; ++kc)
+    // the next cell's records stream into the other buffer while the current cell is integrated
+    const int64_t k0 = r.cellPtr[a], k1 = r.cellPtr[a + 1];
+    auto issue = [&](int64_t kc, T* buf) {
+        const T* src = recs + NG_IDX(r.cellIdx[kc], r.nCells, 41) * Sh::recs;
+        for (int i = lane; i < Sh::recs; i += 32)
+            AsyncCopy(buf + i, src + i);
+    };
+    if (k0 < k1)
+        issue(k0, recBuf);
+    AsyncCommit();
+    for (int64_t kc = k0; kc < k1; ++kc)
     {
         const int64_t e = r.cellIdx[kc];
         const int ia = r.cellLoc[kc];
-        const T* src = recs + NG_IDX(e, r.nCells, 41) * (NIP * R::size);
-        for (int i = lane; i < NIP * R::size; i += 32)
-            rec[i] = src[i];
+        T* rec = recBuf + ((kc - k0) & 1) * Sh::recs;
+        if (kc + 1 < k1)
+            issue(kc + 1, recBuf + ((kc + 1 - k0) & 1) * Sh::recs);
+        AsyncCommit();
+        // ranks of this lane's neighbours (independent of the records: loaded while the copies complete)
+        int rk0[MAXIT], rk1[MAXIT];
+#pragma unroll
+        for (int m = 0; m < MAXIT; ++m)
+        {
+            const int item = lane + 32 * m;
+            rk0[m] = rk1[m] = 0;
+            if (item >= NITEM)
+                continue;
+            const int ib = item / NJ, j = item % NJ;
+            const int64_t ridx = static_cast<int64_t>(ia * ND + ib) * r.nCells + e;
+            if (j < DIM)
+            {
+                rk0[m] = r.rank[0][ridx];
+                if (GD)
+                    rk1[m] = r.rank[1][ridx];
+            }
+            else
+            {
+                rk0[m] = r.rank[2][ridx];
+                rk1[m] = r.rank[3][ridx];
+            }
+        }
+        AsyncWait<1>();
         __syncwarp();
         T acc[MAXIT][DIM + 1];
 #pragma unroll
@@ -921,26 +977,25 @@ __global__ void __launch_bounds__(RowShape<T, DIM, ND, NIP, KIND>::warps * 32)
             const int item = lane + 32 * m;
             if (item >= NITEM)
                 continue;
-            const int ib = item / NJ, j = item % NJ;
-            const int64_t ridx = static_cast<int64_t>(ia * ND + ib) * r.nCells + e;
+            const int j = item % NJ;
             if (j < DIM)
             {
                 T* rw = row + j * kRowCap;
-                const int pos = bUU + DIM * r.rank[0][ridx];
+                const int pos = bUU + DIM * rk0[m];
 #pragma unroll
                 for (int l = 0; l < DIM; ++l)
                     rw[NG_IDX(pos + l, kRowCap, 42)] += acc[m][l];
                 if (GD)
-                    rw[NG_IDX(bUE + r.rank[1][ridx], kRowCap, 42)] += acc[m][DIM];
+                    rw[NG_IDX(bUE + rk1[m], kRowCap, 42)] += acc[m][DIM];
             }
             else
             {
                 T* rw = row + DIM * kRowCap;
-                const int pos = bEU + DIM * r.rank[2][ridx];
+                const int pos = bEU + DIM * rk0[m];
 #pragma unroll
                 for (int l = 0; l < DIM; ++l)
                     rw[NG_IDX(pos + l, kRowCap, 42)] += acc[m][l];
-                rw[NG_IDX(bEE + r.rank[3][ridx], kRowCap, 42)] += acc[m][DIM];
+                rw[NG_IDX(bEE + rk1[m], kRowCap, 42)] += acc[m][DIM];
             }
         }
         __syncwarp();

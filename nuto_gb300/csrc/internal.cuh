@@ -186,6 +186,7 @@ struct PairMap
     // J-neighbours of every I-node in CSR column order (the node-block SpMV reconstructs column indices from them)
     DBuf<int64_t> dNbrPtr; // nNodes_I + 1
     DBuf<int32_t> dNbrIdx;
+    DBuf<int32_t> dNbrCol; // combined row of component 0 of each neighbour entry
     std::vector<int64_t> hNbrPtr; // host copies (multigrid hierarchy set-up)
     std::vector<int32_t> hNbrIdx;
 };

@@ -391,6 +391,7 @@ NodeSpmv MakeNodeSpmv(const Ctx& c)
     {
         A.nbrPtr[p] = c.pairs[p].dNbrPtr.p;
         A.nbrIdx[p] = c.pairs[p].dNbrIdx.p;
+        A.nbrCol[p] = c.pairs[p].dNbrCol.p;
         A.blk[p] = c.pairs[p].dBlk.p;
         A.nbrTotal[p] = static_cast<int64_t>(c.pairs[p].dNbrIdx.n);
     }

@@ -84,6 +84,7 @@ struct NodeSpmv
     const int64_t* gdof[kMaxSlots];
     const int64_t* nbrPtr[kMaxSlots * kMaxSlots];
     const int32_t* nbrIdx[kMaxSlots * kMaxSlots];
+    const int32_t* nbrCol[kMaxSlots * kMaxSlots]; // combined row of component 0 of every neighbour entry
     const int32_t* blk[kMaxSlots * kMaxSlots];
     const int64_t* rowPtr;
     int64_t nnz, nRows, nbrTotal[kMaxSlots * kMaxSlots];
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restr
             const int nn = static_cast<int>(A.nbrPtr[p][a + 1] - q0);
             for (int kk = lane; kk < nn; kk += 32)
             {
-                const int64_t gb = A.gdof[J][A.nbrIdx[p][NG_IDX(q0 + kk, A.nbrTotal[p], 17)]];
+                const int64_t gb = A.nbrCol[p][NG_IDX(q0 + kk, A.nbrTotal[p], 17)];
                 for (int d = 0; d < ncJ; ++d)
                     xs[wid][NG_IDX(len + ncJ * kk + d, kMaxRowLen, 20)] = x[NG_IDX(gb + d, A.nRows, 18)];
             }
