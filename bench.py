@@ -113,9 +113,11 @@ def gpu_index(local_rank):
     return local_rank
 
 
-def spmv_bytes(n_dofs, nnz, value_bytes):
-    # values + column indices + row pointers + mask + x gather (compulsory once) + y write
-    return nnz * (value_bytes + 4) + (n_dofs + 1) * 8 + n_dofs * (1 + 2 * value_bytes)
+def spmv_bytes(g, value_bytes):
+    """Bytes the node-block SpMV must move once: CSR values, row pointers, the per-node neighbour lists (pointers and
+    neighbour columns, which replace the column indices), constraint mask, x read once, y written once."""
+    n, nnz = g.n_dofs, g.nnz
+    return nnz * value_bytes + (n + 1) * 8 + g.neighbour_list_bytes() + n * (1 + 2 * value_bytes)
 
 
 def tangent_bytes(setup, nnz, value_bytes):
@@ -142,15 +144,28 @@ def load_traffic():
     return {}
 
 
-def run_steps(g, opts, t_values, torch):
-    agg = {"matrix_assemblies": 0, "newton_iterations": 0, "krylov_iterations": 0, "ms_spmv": 0.0,
-           "spmv_launches": 0, "kernel_launches": 0, "ms_assemble_matrix": 0.0, "ms_assemble_vector": 0.0,
-           "ms_krylov": 0.0, "residual_evaluations": 0}
-    for t in t_values:
-        g.do_step(t, opts)
-        st = g.stats()
+AGG_KEYS = ("matrix_assemblies", "newton_iterations", "krylov_iterations", "ms_spmv", "spmv_launches",
+            "kernel_launches", "ms_assemble_matrix", "ms_assemble_vector", "ms_krylov", "residual_evaluations")
+
+
+def run_steps(g, opts, t_start, t_values):
+    """Advances the load from t_start through every t in t_values with AdaptiveSolve (time step 1/LOAD_STEPS, cut
+    back by halves on NoConvergence as the reference's AdaptiveSolve does). Returns the summed step statistics,
+    failed attempts included (their work was done), and the number of cut-backs."""
+    from nuto_gb300.adaptive import AdaptiveSolve
+
+    dt = 1.0 / LOAD_STEPS
+    ad = AdaptiveSolve(g, opts, dt=dt, dt_max=dt, dt_min=dt / 256)
+    t = t_start
+    for tv in t_values:
+        ad.solve(tv, t)
+        t = tv
+    agg = {k: 0 for k in AGG_KEYS}
+    for st in ad.stats:
         for k in agg:
             agg[k] += st[k]
+    agg["cutbacks"] = ad.cutbacks
+    agg["do_steps"] = len(ad.stats)
     return agg
 
 
@@ -239,7 +254,7 @@ def run_ours(args):
     from nuto_gb300 import configs
 
     nuto_gb300.load()
-    s = configs.hex8_gradient_damage(args.size, load_steps=LOAD_STEPS)
+    s = configs.hex8_gradient_damage(args.size, load_steps=LOAD_STEPS, imperfection=True)
     g = s.build_gpu(device=local)
     n_dofs, nnz = g.n_dofs, g.nnz
     opts32 = g.default_options(precision=nuto_gb300.FP32, newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20,
@@ -248,8 +263,8 @@ def run_ours(args):
                                max_krylov=20000)
     dt = 1.0 / LOAD_STEPS
     g.set_state(None, 0.0, True)
-    for k in range(1, args.warmup + 1):
-        g.do_step(k * dt, opts32)
+    g.history = s.history0
+    run_steps(g, opts32, 0.0, [k * dt for k in range(1, args.warmup + 1)])
     x_w, t_w = g.get_state()
     kappa_w = g.history
     t_values = [(args.warmup + k) * dt for k in range(1, args.steps + 1)]
@@ -268,7 +283,7 @@ def run_ours(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        agg = run_steps(g, opts, t_values, torch)
+        agg = run_steps(g, opts, t_w, t_values)
         e1.record()
         barrier()
         return e0.elapsed_time(e1) / 1e3, agg
@@ -313,11 +328,21 @@ def run_ours(args):
     barrier()
     h0 = time.perf_counter()
     assemblies = 0
-    for t in t_values:
-        g.do_step_host(t, xa, ka, xb, kb, opts32)
-        assemblies += g.stats()["matrix_assemblies"]
-        xa, xb = xb, xa
-        ka, kb = kb, ka
+    t, step = t_w, dt
+    for tv in t_values:
+        while t < tv - 1e-14:  # AdaptiveSolve's cut-back on the host-buffer entry point
+            tn = min(tv, t + step)
+            try:
+                g.do_step_host(tn, xa, ka, xb, kb, opts32)
+            except nuto_gb300.NoConvergence:
+                assemblies += g.stats()["matrix_assemblies"]
+                step *= 0.5
+                continue
+            assemblies += g.stats()["matrix_assemblies"]
+            xa, xb = xb, xa
+            ka, kb = kb, ka
+            t = tn
+            step = min(dt, step * 1.5) if g.stats()["newton_iterations"] < 3 else step
     barrier()
     sec_e2e = time.perf_counter() - h0
     e2e = {"value": world * n_dofs * assemblies / sec_e2e, "unit": "DOF/s",
@@ -327,15 +352,17 @@ def run_ours(args):
     peak, peak_kind = load_peaks()
     traffic = load_traffic()
     per_launch = agg32["ms_spmv"] / max(agg32["spmv_launches"], 1) / 1e3
-    sb = spmv_bytes(n_dofs, nnz, 4)
+    sb = spmv_bytes(g, 4)
     achieved = sb / per_launch / 1e9
-    roof = {"kernel": "k_spmv<float,float,32,*> (Krylov SpMV, FP32 CSR)", "bound": "hbm", "achieved": achieved,
+    roof = {"kernel": "k_spmv_node<float,float,0> (Krylov SpMV of the whole FP32 tangent, node-block CSR)",
+            "bound": "hbm", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
             "traffic": traffic.get("k_spmv_fp32_bytes_per_launch"), "algorithmic_bytes_per_launch": sb,
             "mean_launch_us": per_launch * 1e6, "launches": agg32["spmv_launches"]}
     tb = tangent_bytes(s, nnz, 4)
     asm_launch = agg32["ms_assemble_matrix"] / max(agg32["matrix_assemblies"], 1) / 1e3
-    assembly = {"kernel": "k_tangent<float> (FP32 tangent assembly incl. value reset)", "bound": "hbm",
+    assembly = {"kernel": "k_tangent<float,REC> + k_tangent_rows<float> (FP32 tangent: records + row gather)",
+                "bound": "hbm",
                 "achieved": tb / asm_launch / 1e9, "peak": peak, "unit": "GB/s",
                 "frac": tb / asm_launch / 1e9 / peak, "algorithmic_bytes_per_launch": tb,
                 "mean_launch_ms": asm_launch * 1e3, "assembled_dofs_per_s": n_dofs / asm_launch,
@@ -347,8 +374,9 @@ def run_ours(args):
            "config": {"workload": "hex8_gradient_damage_%d^3: Hex8 2x2x2 Gauss, beam 1x1x4 m, u + eeq, "
                                   "GradientDamage(c=0.01, LinearElasticDamage(30000, 0.2, FULL), "
                                   "DamageLawExponential(1e-4, 100, 0.99), ModifiedMises(k=10)), 20 load steps to "
-                                  "u_z=2e-3; timed load steps %d..%d" % (args.size, args.warmup + 1,
-                                                                        args.warmup + args.steps),
+                                  "u_z=2e-3 (AdaptiveSolve cut-back), imperfection kappa=3 kappa0 in the two middle "
+                                  "cell layers; timed load steps %d..%d" % (args.size, args.warmup + 1,
+                                                                           args.warmup + args.steps),
                       "n_dofs": n_dofs, "nnz": nnz, "precision": "FP32 tangent + FP32 GMRES(40), FP64 residual, "
                                                                 "history and Newton test",
                       "newton_tolerance": "|C^T r| <= 1e-8 |C^T (r + K db)| of the load step",
@@ -356,6 +384,7 @@ def run_ours(args):
                       "parallelism": "replicas" if world > 1 else "single GPU"},
            "newton_step_ms": 1e3 * sec32 / max(agg32["matrix_assemblies"], 1),
            "newton_iterations": agg32["newton_iterations"], "tangent_solves": agg32["matrix_assemblies"],
+           "do_steps": agg32["do_steps"], "cutbacks": agg32["cutbacks"],
            "krylov_iterations": agg32["krylov_iterations"],
            "roofline": roof, "roofline_assembly": assembly, "fp64": fp64, "e2e": e2e,
            "gpu_launches": int(agg32["kernel_launches"]), "clocks": clk}

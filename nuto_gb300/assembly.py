@@ -89,6 +89,14 @@ class GpuCellGroup:
         self.n_dofs, self.nnz = n.value, nnz.value
         return self.n_dofs, self.nnz
 
+    def neighbour_list_bytes(self):
+        """Bytes of the per-node neighbour lists (int64 pointers, int32 neighbour columns) of every slot pair, for
+        meshes whose DOF types share one node graph (every set-up here): node pairs P = nnz / (sum of components)^2."""
+        layers = [self.mesh.layers[l] for l in self.layers]
+        ncomp = sum(L.ncomp for L in layers)
+        pairs = self.nnz // (ncomp * ncomp)
+        return sum(pairs * 4 + (L.num_nodes + 1) * 8 for L in layers) * len(layers)
+
     def pattern(self):
         rp = np.empty(self.n_dofs + 1, dtype=np.int64)
         ci = np.empty(self.nnz, dtype=np.int32)

@@ -34,6 +34,8 @@ class Setup:
     constraints: list = field(default_factory=list)
     load_steps: int = 1
     t_end: float = 1.0
+    # initial history kappa [cell, ip] (None: zero), e.g. an imperfection
+    history0: object = None
 
     def dependent_counts(self):
         return [len(c[0]) for c in self.constraints]
@@ -77,7 +79,17 @@ def quad4_elastic(n=200, u_right=0.01):
     return Setup("quad4_elastic_%dx%d" % (n, n), m, [d], 2, integ, [cons], 1, 1.0)
 
 
-def hex8_gradient_damage(n=64, length=4.0, u_end=2e-3, load_steps=20):
+def gradient_damage_imperfection(n, n_ip, kappa0=1e-4):
+    """kappa = 3 kappa0 at every integration point of the two cell layers n/2 and n/2 + 1 along the beam axis: the
+    imperfection of StructuralGradientDamage.cpp:66-68 (there: two cells of a 1D bar), which makes the damage
+    localise there instead of at a round-off-dependent place."""
+    iz = np.arange(n * n * n) // (n * n)
+    k = np.zeros((n * n * n, n_ip))
+    k[(iz == n // 2) | (iz == n // 2 + 1)] = 3.0 * kappa0
+    return k
+
+
+def hex8_gradient_damage(n=64, length=4.0, u_end=2e-3, load_steps=20, imperfection=False):
     m = M.create_bricks(n, n, n).scale(1.0, 1.0, length)
     d = M.add_dof_interpolation(m, 3)
     e = M.add_dof_interpolation(m, 1)
@@ -88,7 +100,8 @@ def hex8_gradient_damage(n=64, length=4.0, u_end=2e-3, load_steps=20):
     integ = dict(kind=GRADIENT_DAMAGE, dim=3, E=30000.0, nu=0.2, plane_state=PLANE_STRAIN,
                  damage_application=DAMAGE_FULL, kappa0=1e-4, beta=100.0, alpha=0.99, k=10.0, c=0.01, disp_slot=0,
                  eeq_slot=1)
-    return Setup("hex8_gradient_damage_%d^3" % n, m, [d, e], 2, integ, [cons_d, _empty()], load_steps, 1.0)
+    h0 = gradient_damage_imperfection(n, 8, integ["kappa0"]) if imperfection else None
+    return Setup("hex8_gradient_damage_%d^3" % n, m, [d, e], 2, integ, [cons_d, _empty()], load_steps, 1.0, h0)
 
 
 def hex20_local_damage(n=80, u_end=3e-4, load_steps=5):

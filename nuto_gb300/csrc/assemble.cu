@@ -822,6 +822,13 @@ __global__ void __launch_bounds__(RowShape<T, DIM, ND, NIP, KIND>::warps * 32)
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     T* recBuf = reinterpret_cast<T*>(smRaw) + wid * Sh::perWarp;
     T* row = recBuf + 2 * Sh::recs;
+    __shared__ T sN[GD ? NIP * ND : 1]; // shape values N(q, node), gradient damage only
+    if (GD)
+    {
+        for (int i = threadIdx.x; i < NIP * ND; i += blockDim.x)
+            sN[i] = static_cast<T>(r.tabN[i]);
+        __syncthreads();
+    }
     const int64_t a = static_cast<int64_t>(blockIdx.x) * Sh::warps + wid;
     if (a >= r.nNodes)
         return; // the whole warp leaves; only warp-level synchronisation follows
@@ -895,21 +902,31 @@ __global__ void __launch_bounds__(RowShape<T, DIM, ND, NIP, KIND>::warps * 32)
         }
         AsyncWait<1>();
         __syncwarp();
-        T acc[MAXIT][DIM + 1];
+        // Every item (neighbour b, row j) uses one branch-free form; j < DIM is displacement row j, j == DIM the
+        // eeq row:  v[l] += c1 gb[l] + c2 ga[l] + c3 Qb[l],  v[DIM] += d1 Nb + d2 (ga . gb),  plus mu (ga . gb)
+        // on the diagonal of displacement rows (kept apart and added once per cell).
+        T acc[MAXIT][DIM + 1], accd[MAXIT];
 #pragma unroll
         for (int m = 0; m < MAXIT; ++m)
+        {
+            accd[m] = T(0);
 #pragma unroll
             for (int l = 0; l <= DIM; ++l)
                 acc[m][l] = T(0);
+        }
         for (int q = 0; q < NIP; ++q)
         {
             const T* Rq = rec + q * R::size;
             const T* ga = Rq + R::g + ia * DIM;
             const T lamw = Rq[R::rec + 0], muw = Rq[R::rec + 1];
-            T Pa[DIM];
-            if (LD || GD)
-                BtS<T, DIM>(ga, Rq + R::st, Pa);
-            const T Na = GD ? static_cast<T>(r.tabN[q * ND + ia]) : T(0);
+            const T Na = GD ? sN[q * ND + ia] : T(0);
+            T gs = T(0); // (c g' w' k' w grad eeq) . g_a, gradient damage only
+            if (GD)
+            {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    gs += ga[d] * Rq[R::rec + 4 + d];
+            }
 #pragma unroll
             for (int m = 0; m < MAXIT; ++m)
             {
@@ -917,58 +934,55 @@ __global__ void __launch_bounds__(RowShape<T, DIM, ND, NIP, KIND>::warps * 32)
                 if (item >= NITEM)
                     continue;
                 const int ib = item / NJ, j = item % NJ;
+                const bool urow = j < DIM;
+                const int jj = urow ? j : 0;
                 const T* gb = Rq + R::g + ib * DIM;
                 T gab = T(0);
 #pragma unroll
                 for (int d = 0; d < DIM; ++d)
                     gab += ga[d] * gb[d];
+                const T gaj = ga[jj], gbj = gb[jj];
+                T c1 = lamw * gaj, c2 = muw * gbj, c3 = T(0);
                 T Qb[DIM];
-                if (LD || (GD && j == DIM))
-                    BtS<T, DIM>(gb, Rq + R::st + VD, Qb);
-                if (j < DIM)
+                if (LD || GD)
                 {
-                    T gaj = T(0), gbj = T(0);
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d)
-                        if (d == j)
-                        {
-                            gaj = ga[d];
-                            gbj = gb[d];
-                        }
-#pragma unroll
-                    for (int l = 0; l < DIM; ++l)
-                        acc[m][l] += lamw * gaj * gb[l] + muw * ga[l] * gbj;
+                    // row jj of B_a^T s and all of B_b^T t (Voigt: 2D xx yy xy; 3D xx yy zz yz zx xy)
+                    const T* sv = Rq + R::st;
                     T paj = T(0);
 #pragma unroll
                     for (int d = 0; d < DIM; ++d)
-                        if (d == j)
-                        {
-                            acc[m][d] += muw * gab;
-                            if (LD || GD)
-                                paj = Pa[d];
-                        }
+                        paj += ga[d] * sv[d == jj ? jj : (DIM == 2 ? 2 : 6 - jj - d)];
+                    BtS<T, DIM>(gb, Rq + R::st + VD, Qb);
                     if (LD)
-                    {
-#pragma unroll
-                        for (int l = 0; l < DIM; ++l)
-                            acc[m][l] += paj * Qb[l];
-                    }
+                        c3 = paj;
                     if (GD)
-                        acc[m][DIM] += paj * static_cast<T>(r.tabN[q * ND + ib]);
+                    {
+                        const T Nb = sN[q * ND + ib];
+                        c1 = urow ? c1 : T(0);
+                        c2 = urow ? c2 : T(0);
+                        c3 = urow ? T(0) : -Na;
+                        const T d1 = urow ? paj : Rq[R::rec + 2] * Na + gs;
+                        const T d2 = urow ? T(0) : Rq[R::rec + 3];
+                        acc[m][DIM] += d1 * Nb + d2 * gab;
+                    }
                 }
-                else if (GD)
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
                 {
-                    const T Nb = static_cast<T>(r.tabN[q * ND + ib]);
-                    T gs = T(0);
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d)
-                        gs += ga[d] * Rq[R::rec + 4 + d];
-#pragma unroll
-                    for (int l = 0; l < DIM; ++l)
-                        acc[m][l] -= Na * Qb[l];
-                    acc[m][DIM] += Rq[R::rec + 2] * Na * Nb + Rq[R::rec + 3] * gab + gs * Nb;
+                    acc[m][l] += c1 * gb[l] + c2 * ga[l];
+                    if (LD || GD)
+                        acc[m][l] += c3 * Qb[l];
                 }
+                accd[m] += urow ? muw * gab : T(0);
             }
+        }
+#pragma unroll
+        for (int m = 0; m < MAXIT; ++m)
+        {
+            const int j = (lane + 32 * m) % NJ;
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                acc[m][l] += l == j ? accd[m] : T(0);
         }
         // add the items into the row buffer at the ranks of b (distinct positions: no conflicts)
 #pragma unroll
