@@ -120,8 +120,9 @@ typedef struct nuto_gpu_step_options
     double newton_atol;
     int max_newton;     /* NewtonRaphson::Solve maxIterations (the reference uses 6) */
     int line_search;    /* 1: NuTo::NewtonRaphson::LineSearch (6 halvings), 0: plain Newton */
-    double krylov_rtol; /* inner Krylov tolerance relative to |rhs| */
+    double krylov_rtol; /* inner Krylov tolerance relative to |rhs| (the lower bound with forcing = 1) */
     int max_krylov;
+    int forcing;        /* 0: every solve to krylov_rtol; 1: Eisenstat-Walker forcing terms (choice 1) */
 } nuto_gpu_step_options;
 
 /* statistics of the last nuto_gpu_do_step / nuto_gpu_solve */

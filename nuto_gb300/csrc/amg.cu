@@ -15,7 +15,7 @@
 // node SpMV serves every level; level 0 is a diagonal-block view of the tangent itself.
 //
 // Per tangent (device, FP32): Galerkin coarse values A_c = P^T A P by one pass over the finer values with
-// atomics; Jacobi diagonals and Gershgorin bounds of D^-1 A per level. Cycle: V(2,2) with Chebyshev-Jacobi
+// atomics; Jacobi diagonals and Gershgorin bounds of D^-1 A per level. Cycle: V(1,2) with Chebyshev-Jacobi
 // smoothing on [lmax / 10, lmax] and a degree-6 Chebyshev solve on the coarsest level. The sweep is a fixed
 // linear operator; GMRES uses it in flexible form (stored preconditioned basis) so FP32 rounding inside the cycle
 // does not limit the attainable residual.
@@ -30,7 +30,7 @@ namespace nuto_gpu
 
 constexpr int kCoarsest = 64; // nodes on the coarsest level
 constexpr int kMaxLevels = 12;
-constexpr int kPreDegree = 2;
+constexpr int kPreDegree = 1;
 constexpr int kPostDegree = 2;
 constexpr int kCoarseDegree = 6;
 constexpr float kSmoothRatio = 10.f; // smoothing interval [lmax / ratio, lmax]

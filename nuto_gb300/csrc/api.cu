@@ -915,6 +915,7 @@ int nuto_gpu_default_step_options(nuto_gpu_step_options* o)
     o->line_search = 1;
     o->krylov_rtol = 1e-3;
     o->max_krylov = 20000;
+    o->forcing = 1;
     return NUTO_GPU_OK;
 }
 

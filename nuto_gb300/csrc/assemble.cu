@@ -1118,7 +1118,9 @@ static void LaunchTangentRows(Ctx& c, const double* u, T* vals)
 template <typename T>
 static void LaunchTangentT(Ctx& c, const double* u, T* vals)
 {
-    if (RowsSupported(c) && !c.forceAtomicTangent)
+    // FP32: row gather (no atomics). FP64: the element kernel; on GB300's FP64 pipe the per-lane recomputation of
+    // the rank-1 factors in the row kernel costs more than the FP64 atomics it saves.
+    if (sizeof(T) == 4 && RowsSupported(c) && !c.forceAtomicTangent)
     {
         LaunchTangentRows<T>(c, u, vals);
         return;

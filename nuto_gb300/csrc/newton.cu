@@ -147,22 +147,22 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     // FP64: one Krylov solve to krylov_rtol. FP32: FP32 Krylov sweeps inside an FP64 refinement on the FP32
     // tangent (r = rhs - K32 dx accumulated in FP64) until the true relative residual reaches krylov_rtol: the
     // FP32 iteration's own residual estimate is not trusted for the Newton direction.
+    double eta = o.krylov_rtol; // forcing term of the current linear solve
     auto solve = [&](const double* rhs, double* out) {
         const auto k0 = std::chrono::steady_clock::now();
         int it = 0;
         double* relp = &lastRel;
         if (mixed)
-            KrylovSolveExport<double, float>(c, method, w.K32.p, rhs, out, false, o.krylov_rtol, o.max_krylov, &it,
-                                             relp);
+            KrylovSolveExport<double, float>(c, method, w.K32.p, rhs, out, false, eta, o.max_krylov, &it, relp);
         else if (fp32)
         {
             const double bn = MaskedNorm(c, rhs);
             NG_CUDA(cudaMemsetAsync(out, 0, n * sizeof(double), c.stream));
             NG_CUDA(cudaMemcpyAsync(w.refR.p, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
             double rel = bn > 0. ? 1. : 0.;
-            for (int sweep = 0; sweep < 4 && rel > o.krylov_rtol && it < o.max_krylov; ++sweep)
+            for (int sweep = 0; sweep < 4 && rel > eta && it < o.max_krylov; ++sweep)
             {
-                const double inner = std::min(0.5, std::max(o.krylov_rtol / rel, 1e-5));
+                const double inner = std::min(0.5, std::max(eta / rel, 1e-5));
                 int its = 0;
                 KrylovSolveExport<float, float>(c, method, w.K32.p, w.refR.p, out, true, inner, o.max_krylov - it,
                                                 &its, nullptr);
@@ -174,8 +174,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
             lastRel = rel;
         }
         else
-            KrylovSolveExport<double, double>(c, method, w.K64.p, rhs, out, false, o.krylov_rtol, o.max_krylov,
-                                              &it, relp);
+            KrylovSolveExport<double, double>(c, method, w.K64.p, rhs, out, false, eta, o.max_krylov, &it, relp);
         lastKrylov = it;
         T.Collect();
         S.ms_krylov += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - k0).count();
@@ -218,12 +217,33 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     if (verbose)
         std::fprintf(stderr, "[nuto_gpu] t = %g: trial |C^T r| = %.3e (ref %.3e, tol %.3e), krylov %d (rel %.2e)\n", tNew,
                      nr, refNorm, tol, lastKrylov, lastRel);
+    // Forcing terms (forcing = 1): Eisenstat-Walker choice 1, eta_k = | |F_k| - |F_k-1 + a J s_k-1| | / |F_k-1|,
+    // the disagreement between the residual and its linear model; with the safeguard eta_k >= eta_k-1^1.618 when
+    // that exceeds 0.1, clamped to [krylov_rtol, 0.5] and to no less than 0.5 tol / |F_k| (no over-solving of the
+    // last iteration). An inaccurate (FP32) tangent gives loose solves, an accurate one tight solves.
+    double prevNr = nr, stepAlpha = 1., stepRel = lastRel;
     while (!conv && it < o.max_newton)
     {
         assembleK(w.xs.p);
         k_masked_sum<<<gb, 256, 0, c.stream>>>(n, c.dMask.p, w.f.p, nullptr, w.rhs.p);
         S.kernel_launches += 1;
+        if (o.forcing == 1)
+        {
+            double e = 0.1;
+            if (it > 0)
+            {
+                const double model = ((1. - stepAlpha) + stepAlpha * stepRel) * prevNr;
+                e = std::fabs(nr - model) / prevNr;
+                const double sg = std::pow(eta, 1.618);
+                if (sg > 0.1)
+                    e = std::max(e, sg);
+            }
+            e = std::max(e, 0.5 * tol / nr);
+            eta = std::min(0.5, std::max(o.krylov_rtol, e));
+        }
         solve(w.rhs.p, w.dx.p);
+        stepRel = lastRel;
+        prevNr = nr;
         ++it;
         if (o.line_search)
         {
@@ -236,6 +256,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
                 S.kernel_launches += 1;
                 const double trial = residual(w.xs.p);
                 nr = trial;
+                stepAlpha = alpha;
                 if (trial < tol)
                 {
                     conv = true;
@@ -246,8 +267,8 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
                     break;
             }
             if (verbose)
-                std::fprintf(stderr, "[nuto_gpu] iteration %d: |C^T r| = %.3e, krylov %d (rel %.2e), alpha %g\n", it, nr,
-                             lastKrylov, lastRel, conv ? alpha : 2 * alpha);
+                std::fprintf(stderr, "[nuto_gpu] iteration %d: |C^T r| = %.3e, krylov %d (rel %.2e, eta %.1e), alpha %g\n",
+                             it, nr, lastKrylov, lastRel, eta, stepAlpha);
         }
         else
         {

@@ -94,7 +94,7 @@ constexpr int kMaxRowLen = 256; // longest row of a node (Hex20 displacements: 3
 constexpr int kMaxComp = 3;     // components per DOF node
 
 template <typename TV, typename TX, int NDOT>
-__global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
+__global__ void __launch_bounds__(kBS, 6) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
                                                     const uint8_t* __restrict__ mask, const TX* __restrict__ x,
                                                     TX* __restrict__ y, const TX* __restrict__ w0, double* sc, int* st,
                                                     int fin)
@@ -112,26 +112,23 @@ __global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restr
     double d0 = 0., d1 = 0.;
     if (valid)
     {
-        // x of the node's neighbours in the column order of its rows
-        int len = 0;
-        for (int J = 0; J < A.ns; ++J)
+        // independent loads first: neighbour ranges of every slot pair, the node's rows and block offset
+        int64_t q0[kMaxSlots];
+        int nn[kMaxSlots];
+#pragma unroll
+        for (int J = 0; J < kMaxSlots; ++J)
         {
-            const int p = I * A.ns + J;
-            const int ncJ = A.ncomp[J];
-            const int64_t q0 = A.nbrPtr[p][a];
-            const int nn = static_cast<int>(A.nbrPtr[p][a + 1] - q0);
-            for (int kk = lane; kk < nn; kk += 32)
+            q0[J] = 0;
+            nn[J] = 0;
+            if (J < A.ns)
             {
-                const int64_t gb = A.nbrCol[p][NG_IDX(q0 + kk, A.nbrTotal[p], 17)];
-                for (int d = 0; d < ncJ; ++d)
-                    xs[wid][NG_IDX(len + ncJ * kk + d, kMaxRowLen, 20)] = x[NG_IDX(gb + d, A.nRows, 18)];
+                const int p = I * A.ns + J;
+                q0[J] = A.nbrPtr[p][a];
+                nn[J] = static_cast<int>(A.nbrPtr[p][a + 1] - q0[J]);
             }
-            len += ncJ * nn;
         }
-        __syncwarp();
         const int64_t g0 = A.gdof[I][a];
         const int32_t seg = A.blk[I * A.ns][a]; // 0 for a whole-row operator, the block start for a block view
-        // all rows of the node stream together (ncI independent loads per step keep more bytes in flight)
         int64_t rs[kMaxComp];
         TX s[kMaxComp];
 #pragma unroll
@@ -140,6 +137,24 @@ __global__ void __launch_bounds__(kBS) k_spmv_node(NodeSpmv A, const TV* __restr
             rs[c] = c < ncI ? A.rowPtr[NG_IDX(g0 + c, A.nRows, 16)] + seg : 0;
             s[c] = TX(0);
         }
+        // x of the node's neighbours in the column order of its rows (both slot pairs in one pass)
+        const int nc0 = A.ncomp[0], nc1 = A.ns > 1 ? A.ncomp[1] : 0;
+        const int tot = nn[0] + nn[1];
+#pragma unroll 2
+        for (int t = lane; t < tot; t += 32)
+        {
+            const int J = t >= nn[0] ? 1 : 0;
+            const int kk = t - (J ? nn[0] : 0);
+            const int ncJ = J ? nc1 : nc0;
+            const int p = I * A.ns + J;
+            const int64_t qJ = J ? q0[1] : q0[0];
+            const int64_t gb = A.nbrCol[p][NG_IDX(qJ + kk, A.nbrTotal[p], 17)];
+            const int base = J ? nc0 * nn[0] + nc1 * kk : nc0 * kk;
+            for (int d = 0; d < ncJ; ++d)
+                xs[wid][NG_IDX(base + d, kMaxRowLen, 20)] = x[NG_IDX(gb + d, A.nRows, 18)];
+        }
+        const int len = nc0 * nn[0] + nc1 * nn[1];
+        __syncwarp();
 #pragma unroll 4
         for (int q = lane; q < len; q += 32)
         {

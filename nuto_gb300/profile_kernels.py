@@ -2,9 +2,10 @@
 
     python -m nuto_gb300.profile_kernels --size 64 [--gmres-iterations 20]
 
-Launch order: geometry cache, residual (x3), FP32 tangent (x3), FP64 tangent (x1), then one FP32 GMRES solve of
---gmres-iterations iterations (node-block SpMV, orthogonalisation kernels). The state is a damaged state reached
-by three elastic load steps and one damaging step, so the damage branches of the kernels are exercised.
+Launch order: geometry cache, residual (x3), FP32 tangent (x3; records + row gather), FP64 tangent (x1), then one
+Jacobi-preconditioned FP32 GMRES solve of --gmres-iterations iterations (every k_spmv_node launch is a product with
+the whole tangent), then one multigrid-preconditioned solve of the same length. With --load-steps the state is the
+one reached by that many load steps of the benchmark schedule, so the damage branches of the kernels are exercised.
 """
 
 import argparse
@@ -48,10 +49,15 @@ def main():
         g.build_matrix(u, nuto_gb300.FP32, out=k32)
     g.build_matrix(u, nuto_gb300.FP64, out=k64)
     b = torch.ones(g.n_dofs, dtype=torch.float64, device="cuda")
+    g.set_preconditioner(nuto_gb300.PRECOND_JACOBI)
     x, it, rel, ok = g.solve(k32, b, precision=nuto_gb300.FP32, method=3, rtol=1e-12,
                              max_iterations=a.gmres_iterations)
+    g.set_preconditioner(nuto_gb300.PRECOND_AMG)
+    x, it2, rel, ok = g.solve(k32, b, precision=nuto_gb300.FP32, method=3, rtol=1e-12,
+                              max_iterations=a.gmres_iterations)
     torch.cuda.synchronize()
-    print("size %d: n_dofs %d nnz %d, gmres iterations %d" % (a.size, g.n_dofs, g.nnz, it))
+    print("size %d: n_dofs %d nnz %d, gmres iterations %d (Jacobi) + %d (multigrid)" % (a.size, g.n_dofs, g.nnz, it,
+                                                                                        it2))
 
 
 if __name__ == "__main__":

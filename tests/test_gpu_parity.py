@@ -335,10 +335,11 @@ def test_multigrid_levels_solve(kind, n, steps):
 
 
 @pytest.mark.parametrize("kind,n", [("quad4", 5), ("hex8gd", 3), ("hex20", 2)])
-@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("precision", [32])
 def test_tangent_row_gather_matches_element_atomics(kind, n, precision, monkeypatch):
-    """The row-gather tangent (records + one warp per node row) and the element-wise atomic tangent give the same
-    CSR values on a damaged state (rounding-level differences only: the summation order differs)."""
+    """The FP32 row-gather tangent (records + one warp per node row) and the element-wise atomic tangent give the
+    same CSR values on a damaged state (rounding-level differences only: the summation order differs). FP64 always
+    uses the element kernel."""
     _torch()
     rng = np.random.default_rng(11)
     s, g, (om, layers, P, cons) = _build(kind, n)
