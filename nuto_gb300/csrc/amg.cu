@@ -689,7 +689,7 @@ static void Chebyshev(Ctx& c, AmgLevel& L, const float* vals, const uint8_t* mas
 }
 
 // e = V-cycle(b) on level l of hierarchy H
-static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const float* b, float* e, const int* st)
+static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const float* b, float* e, const int* st, bool sym)
 {
     Amg& M = *c.amg;
     AmgLevel& L = H[l];
@@ -702,22 +702,22 @@ static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const float* b, f
     }
     AmgLevel& C = H[l + 1];
     int* stw = const_cast<int*>(st);
-    Chebyshev(c, L, vals, mask, b, e, kPreDegree, true, kSmoothRatio, st);
+    Chebyshev(c, L, vals, mask, b, e, sym ? kPostDegree : kPreDegree, true, kSmoothRatio, st);
     SpmvNode<float, float, 0>(c.stream, L.spmv, vals, e, L.t.p, nullptr, nullptr, stw, 0, mask);
     k_sub<<<Blocks(C.nDofs), 256, 0, c.stream>>>(C.nDofs, nullptr, nullptr, C.b.p, st);
     k_restrict<<<Blocks(L.nNodes), 256, 0, c.stream>>>(L.spmv, mask, b, L.t.p, C.aggOf.p, C.spmv, C.b.p, st);
     c.stats.kernel_launches += 3;
-    VCycle(c, H, l + 1, C.b.p, C.e.p, st);
+    VCycle(c, H, l + 1, C.b.p, C.e.p, st, sym);
     k_prolong<<<Blocks(L.nNodes), 256, 0, c.stream>>>(L.spmv, mask, C.aggOf.p, C.spmv, C.e.p, e, st);
     c.stats.kernel_launches += 1;
     Chebyshev(c, L, vals, mask, b, e, kPostDegree, false, kSmoothRatio, st);
 }
 
 // block Gauss-Seidel sweep in slot order on combined FP32 vectors: z_0 = V_0(v_0), z_1 = V_1(v_1 - K_10 z_0)
-static void Sweep(Ctx& c, const float* v, float* z, const int* st)
+static void Sweep(Ctx& c, const float* v, float* z, const int* st, bool sym)
 {
     Amg& M = *c.amg;
-    VCycle(c, M.h[0], 0, v, z, st);
+    VCycle(c, M.h[0], 0, v, z, st, sym);
     for (int I = 1; I < M.ns; ++I)
     {
         AmgLevel& L = M.h[I][0];
@@ -728,29 +728,30 @@ static void Sweep(Ctx& c, const float* v, float* z, const int* st)
                                   const_cast<int*>(st), 0, c.dMask.p);
         k_sub<<<Blocks(n), 256, 0, c.stream>>>(n, v + o, M.res32.p + o, M.res32.p + o, st);
         c.stats.kernel_launches += 3;
-        VCycle(c, M.h[I], 0, M.res32.p, z, st);
+        VCycle(c, M.h[I], 0, M.res32.p, z, st, sym);
     }
 }
 
 // z = M^-1 v for the tangent of the last AmgSetup (FP32 cycle; FP64 vectors are converted). With st given,
-// every kernel returns at once when the Krylov state is not RUN.
+// every kernel returns at once when the Krylov state is not RUN. sym = true runs equal pre- and post-smoothing
+// (a symmetric cycle for PCG on a single slot); otherwise the cheaper V(1,2) for GMRES.
 template <typename T>
-void AmgApply(Ctx& c, const T* v, T* z, const int* st)
+void AmgApply(Ctx& c, const T* v, T* z, const int* st, bool sym)
 {
     Amg& M = *c.amg;
     const int64_t n = c.nDofs;
     if constexpr (sizeof(T) == 4)
-        Sweep(c, v, z, st);
+        Sweep(c, v, z, st, sym);
     else
     {
         k_convert<double, float><<<Blocks(n), 256, 0, c.stream>>>(n, v, M.in32.p, st);
-        Sweep(c, M.in32.p, M.out32.p, st);
+        Sweep(c, M.in32.p, M.out32.p, st, sym);
         k_convert<float, double><<<Blocks(n), 256, 0, c.stream>>>(n, M.out32.p, z, st);
         c.stats.kernel_launches += 2;
     }
 }
-template void AmgApply<float>(Ctx&, const float*, float*, const int*);
-template void AmgApply<double>(Ctx&, const double*, double*, const int*);
+template void AmgApply<float>(Ctx&, const float*, float*, const int*, bool);
+template void AmgApply<double>(Ctx&, const double*, double*, const int*, bool);
 
 int AmgLevels(const Ctx& c)
 {

@@ -437,9 +437,10 @@ struct IpRecord
 
 // REC = false: element-wise tangent, node-pair blocks added into the CSR values with atomics.
 // REC = true: phases 0 and A only; the integration-point records are written for k_tangent_rows.
-template <typename T, int DIM, int ND, int NIP, int KIND, bool REC>
+// T is the arithmetic of the geometry, strain and law evaluation; TO the type of the written values or records.
+template <typename T, int DIM, int ND, int NIP, int KIND, bool REC, typename TO = T>
 __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, ScatterArgs S, int pUU, int pUE, int pEU,
-                                                 int pEE, const double* __restrict__ u, T* __restrict__ vals)
+                                                 int pEE, const double* __restrict__ u, TO* __restrict__ vals)
 {
     constexpr int VD = DIM == 2 ? 3 : 6;
     constexpr bool GD = KIND == NUTO_GPU_GRADIENT_DAMAGE;
@@ -616,7 +617,7 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
         // records of the block's cells are one contiguous range: coalesced stores
         using R = IpRecord<DIM, ND, KIND>;
         const int cells = static_cast<int>(n - cell0 < CPB ? n - cell0 : CPB);
-        T* out = vals + cell0 * NIP * R::size;
+        TO* out = vals + cell0 * NIP * R::size;
         for (int it = threadIdx.x; it < cells * NIP * R::size; it += blockDim.x)
         {
             const int f = it % R::size;
@@ -629,7 +630,7 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
                 v = sRec[cl][q][f - R::rec];
             else
                 v = sST[cl][q][(f - R::st) / VD][(f - R::st) % VD];
-            out[it] = v;
+            out[it] = static_cast<TO>(v);
         }
         return;
     }
@@ -1101,8 +1102,11 @@ static void LaunchTangentRows(Ctx& c, const double* u, T* vals)
         T* recs = reinterpret_cast<T*>(c.dRecords.p);
         constexpr int CPB = TangentShape<C::nd, C::nip>::cpb;
         const int blocks = static_cast<int>((c.nCells + CPB - 1) / CPB);
-        k_tangent<T, C::dim, C::nd, C::nip, C::kind, true><<<blocks, TangentShape<C::nd, C::nip>::threads, 0,
-                                                               c.stream>>>(a, c.law, s, 0, 0, 0, 0, u, recs);
+        // the law is evaluated in FP64 and rounded into FP32 records: the loading/unloading and damage-threshold
+        // branches then agree with the FP64 residual's (an FP32 eeq or strain near kappa_h or kappa0 can take the
+        // other branch and change the coupling blocks of the tangent by far more than a rounding error)
+        k_tangent<double, C::dim, C::nd, C::nip, C::kind, true, T><<<blocks, TangentShape<C::nd, C::nip>::threads, 0,
+                                                                     c.stream>>>(a, c.law, s, 0, 0, 0, 0, u, recs);
         AfterLaunch(c, "k_tangent (records)");
         auto kern = k_tangent_rows<T, C::dim, C::nd, C::nip, C::kind>;
         if (Sh::smem > 48 * 1024)

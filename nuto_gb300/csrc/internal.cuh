@@ -310,7 +310,7 @@ void FreeAmg(Ctx& c);
 template <typename TV>
 void AmgSetup(Ctx& c, const TV* vals);
 template <typename T>
-void AmgApply(Ctx& c, const T* v, T* z, const int* st);
+void AmgApply(Ctx& c, const T* v, T* z, const int* st, bool sym);
 int AmgLevels(const Ctx& c);
 
 // ---- kernel argument blocks (by value) ----

@@ -751,7 +751,7 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
             T* vj1 = G.V.p + static_cast<int64_t>(j + 1) * n;
             T* zj = amg ? G.Z.p + static_cast<int64_t>(j) * n : G.z.p;
             if (amg)
-                AmgApply<T>(c, G.V.p + static_cast<int64_t>(j) * n, zj, st);
+                AmgApply<T>(c, G.V.p + static_cast<int64_t>(j) * n, zj, st, false);
             SpmvTimed<TV, T, 0>(c, vals, zj, G.w.p, nullptr, nullptr, st, FIN_NONE, c.dMask.p);
             c.stats.kernel_launches += 4 + (j + 1 < cols ? 1 : 0);
             k_gm_dots<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, G.w.p, gs + GL::H1, st);
@@ -855,7 +855,7 @@ static int KrylovSolve(Ctx& c, int method, const TV* vals, const double* b, doub
         // x = 0, r = b, p = 0; z = M^-1 r; rho = r.z; p = z
         k_krylov_init<T, false><<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, V.x.p, V.r.p, V.rh.p, V.p.p, V.v.p,
                                                              V.z.p, V.dinv.p, sc, st);
-        AmgApply<T>(c, V.r.p, V.z.p, st);
+        AmgApply<T>(c, V.r.p, V.z.p, st, true);
         k_pcg_rz<T><<<grid, kBS, 0, c.stream>>>(n, V.r.p, V.z.p, sc, st, 1);
         k_pcg_dir<T><<<grid, kBS, 0, c.stream>>>(n, V.p.p, V.z.p, sc, st);
         c.stats.kernel_launches += 2;
@@ -883,7 +883,7 @@ static int KrylovSolve(Ctx& c, int method, const TV* vals, const double* b, doub
                                                             amg ? nullptr : V.dinv.p, sc, st);
                 if (amg)
                 {
-                    AmgApply<T>(c, V.r.p, V.z.p, st);
+                    AmgApply<T>(c, V.r.p, V.z.p, st, true);
                     k_pcg_rz<T><<<grid, kBS, 0, c.stream>>>(n, V.r.p, V.z.p, sc, st, 0);
                     c.stats.kernel_launches += 1;
                 }

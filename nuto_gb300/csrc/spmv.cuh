@@ -92,9 +92,10 @@ struct NodeSpmv
 
 constexpr int kMaxRowLen = 256; // longest row of a node (Hex20 displacements: 3 x 81)
 constexpr int kMaxComp = 3;     // components per DOF node
+constexpr int kPre = 4;         // row chunks of 32 values prefetched into registers (rows up to 128 entries)
 
 template <typename TV, typename TX, int NDOT>
-__global__ void __launch_bounds__(kBS, 6) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
+__global__ void __launch_bounds__(kBS, 5) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
                                                     const uint8_t* __restrict__ mask, const TX* __restrict__ x,
                                                     TX* __restrict__ y, const TX* __restrict__ w0, double* sc, int* st,
                                                     int fin)
@@ -137,8 +138,20 @@ __global__ void __launch_bounds__(kBS, 6) k_spmv_node(NodeSpmv A, const TV* __re
             rs[c] = c < ncI ? A.rowPtr[NG_IDX(g0 + c, A.nRows, 16)] + seg : 0;
             s[c] = TX(0);
         }
-        // x of the node's neighbours in the column order of its rows (both slot pairs in one pass)
         const int nc0 = A.ncomp[0], nc1 = A.ns > 1 ? A.ncomp[1] : 0;
+        const int len = nc0 * nn[0] + nc1 * nn[1];
+        // the first kPre chunks of every row go to registers before the gather, so that the value stream and the
+        // gather's dependent loads are in flight together
+        TV v[kMaxComp][kPre];
+#pragma unroll
+        for (int c = 0; c < kMaxComp; ++c)
+#pragma unroll
+            for (int k = 0; k < kPre; ++k)
+            {
+                const int q = lane + 32 * k;
+                v[c][k] = (c < ncI && q < len) ? val[NG_IDX(rs[c] + q, A.nnz, 19)] : TV(0);
+            }
+        // x of the node's neighbours in the column order of its rows (both slot pairs in one pass)
         const int tot = nn[0] + nn[1];
 #pragma unroll 2
         for (int t = lane; t < tot; t += 32)
@@ -153,10 +166,20 @@ __global__ void __launch_bounds__(kBS, 6) k_spmv_node(NodeSpmv A, const TV* __re
             for (int d = 0; d < ncJ; ++d)
                 xs[wid][NG_IDX(base + d, kMaxRowLen, 20)] = x[NG_IDX(gb + d, A.nRows, 18)];
         }
-        const int len = nc0 * nn[0] + nc1 * nn[1];
         __syncwarp();
-#pragma unroll 4
-        for (int q = lane; q < len; q += 32)
+#pragma unroll
+        for (int k = 0; k < kPre; ++k)
+        {
+            const int q = lane + 32 * k;
+            if (q < len)
+            {
+                const TX xv = xs[wid][q];
+#pragma unroll
+                for (int c = 0; c < kMaxComp; ++c)
+                    s[c] += static_cast<TX>(v[c][k]) * xv;
+            }
+        }
+        for (int q = lane + 32 * kPre; q < len; q += 32) // rows longer than 32 kPre entries (Hex20)
         {
             const TX xv = xs[wid][q];
 #pragma unroll
