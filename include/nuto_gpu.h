@@ -188,6 +188,16 @@ int nuto_gpu_get_history(nuto_gpu_ctx* ctx, double* kappa);
 int nuto_gpu_build_vector(nuto_gpu_ctx* ctx, const double* d_u, double* d_f);
 /* CSR values of sum over cells of the integrand's Hessian0; d_values is nnz floats (FP32) or doubles (FP64) */
 int nuto_gpu_build_matrix(nuto_gpu_ctx* ctx, const double* d_u, int precision, void* d_values);
+/* The FP32 values of nuto_gpu_build_matrix(ctx, d_u, NUTO_GPU_FP32, d_values), computed without allocating any
+   memory: the integration-point records go to a fixed 16 MiB device array inside the library instead of a buffer
+   of the context. For callers that must not allocate device memory once set up. Limit: cells x integration points
+   x record size <= 4,194,304 floats (12,192 Hex8 gradient-damage cells, 2,099 Hex20 local-damage cells); larger
+   meshes get NUTO_GPU_EINVAL. Call nuto_gpu_build_matrix with NUTO_GPU_FP32 once first: it completes the set-up
+   that allocates (NUTO_GPU_ESTATE otherwise). The first call on each device also looks up the array's address,
+   so make it before any stream capture. The array is shared by all contexts on a device: calls that can overlap
+   (other streams, other host threads) race and must be serialised by the caller. No counterpart in the
+   reference. */
+int nuto_gpu_build_matrix_noalloc(nuto_gpu_ctx* ctx, const double* d_u, float* d_values);
 /* kappa <- max(kappa, kappa(u)) at every integration point */
 int nuto_gpu_update_history(nuto_gpu_ctx* ctx, const double* d_u);
 /* scatter of caller-given cell vectors (n_cells x n_local doubles, slot-major, node, component) */

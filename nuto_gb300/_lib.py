@@ -87,6 +87,7 @@ SIGNATURES = {
     "nuto_gpu_get_history": (_i, [_vp, _vp]),
     "nuto_gpu_build_vector": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_build_matrix": (_i, [_vp, _vp, _i, _vp]),
+    "nuto_gpu_build_matrix_noalloc": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_update_history": (_i, [_vp, _vp]),
     "nuto_gpu_assemble_cell_vectors": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_assemble_cell_matrices": (_i, [_vp, _vp, _i, _vp]),

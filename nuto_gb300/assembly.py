@@ -144,6 +144,15 @@ class GpuCellGroup:
         self._call("nuto_gpu_build_matrix", _ptr(u), precision, _ptr(v))
         return v
 
+    def build_matrix_noalloc(self, u, out=None):
+        """FP32 tangent through nuto_gpu_build_matrix_noalloc (records in the library's static device array; the
+        library allocates nothing). build_matrix(u, FP32) must have run once on this group."""
+        torch = _torch()
+        u = self._dev(u, torch.float64)
+        v = out if out is not None else torch.empty(self.nnz, dtype=torch.float32, device=u.device)
+        self._call("nuto_gpu_build_matrix_noalloc", _ptr(u), _ptr(v))
+        return v
+
     def update_history(self, u):
         torch = _torch()
         u = self._dev(u, torch.float64)

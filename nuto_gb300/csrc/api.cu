@@ -854,6 +854,16 @@ int nuto_gpu_build_matrix(nuto_gpu_ctx* ctx, const double* u, int precision, voi
     });
 }
 
+int nuto_gpu_build_matrix_noalloc(nuto_gpu_ctx* ctx, const double* u, float* values)
+{
+    return Guard(ctx, [&] {
+        NG_CHECK(ctx->havePattern, NUTO_GPU_ESTATE, "build_pattern first");
+        NG_CHECK(ctx->haveIntegrand, NUTO_GPU_ESTATE, "set_integrand first");
+        LaunchTangentNoAlloc(*ctx, u, values);
+        return NUTO_GPU_OK;
+    });
+}
+
 int nuto_gpu_update_history(nuto_gpu_ctx* ctx, const double* u)
 {
     return Guard(ctx, [&] {

@@ -10,6 +10,7 @@
 #include "internal.cuh"
 
 #include <algorithm>
+#include <mutex>
 
 namespace nuto_gpu
 {
@@ -1324,6 +1325,74 @@ void LaunchCellMatrices(Ctx& c, const double* ke, int precision, void* values)
         k_cell_matrices<double><<<blocks, 256, 0, c.stream>>>(c.nCells, v, s, ke, static_cast<double*>(values));
     }
     AfterLaunch(c, "k_cell_matrices");
+}
+
+// ---- FP32 tangent without allocation (nuto_gpu_build_matrix_noalloc) --------------------------------------------
+// The row-gather tangent with its integration-point records in a fixed device array of this file instead of the
+// context's record buffer, so that the call allocates nothing. The array is shared by every context on a device:
+// calls that may overlap (other streams, other host threads) must be serialised by the caller. Nothing in it has
+// to start at zero: every record is written before it is read, and every CSR value is written once.
+constexpr size_t kStaticRecordFloats = size_t(1) << 22; // 16 MiB
+constexpr int kMaxDevices = 64;
+static __device__ __align__(256) float g_staticRecords[kStaticRecordFloats];
+static std::mutex g_staticRecordsMutex;
+static float* g_staticRecordsPtr[kMaxDevices] = {};
+
+// Address of the record array on the current device; looked up once per device (cudaGetSymbolAddress).
+static float* StaticRecords(int device)
+{
+    std::lock_guard<std::mutex> lock(g_staticRecordsMutex);
+    NG_CHECK(device >= 0 && device < kMaxDevices, NUTO_GPU_EINVAL, "device index out of range");
+    if (!g_staticRecordsPtr[device])
+    {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_staticRecords);
+        if (e != cudaSuccess)
+            throw Error{NUTO_GPU_ECUDA, std::string("cudaGetSymbolAddress(static records): ") + cudaGetErrorString(e)};
+        g_staticRecordsPtr[device] = static_cast<float*>(p);
+    }
+    return g_staticRecordsPtr[device];
+}
+
+void LaunchTangentNoAlloc(Ctx& c, const double* u, float* vals)
+{
+    NG_CHECK(c.haveGeo && c.rowsMode >= 0, NUTO_GPU_ESTATE,
+             "nuto_gpu_build_matrix_noalloc: call nuto_gpu_build_matrix (FP32) once first; that call completes the "
+             "set-up that allocates (integration-point geometry, record layout)");
+    NG_CHECK(c.rowsMode == 1, NUTO_GPU_EINVAL,
+             "nuto_gpu_build_matrix_noalloc: the row-gather tangent does not apply to this set-up (the displacement "
+             "and eeq fields need the same interpolation)");
+    c.valsVersion++;
+    CellArgs a = MakeCellArgs(c);
+    ScatterArgs s = MakeScatterArgs(c);
+    RowArgs r = MakeRowArgs(c);
+    DispatchCfg(c, [&](auto cfg) {
+        using C = decltype(cfg);
+        using R = IpRecord<C::dim, C::nd, C::kind>;
+        using Sh = RowShape<float, C::dim, C::nd, C::nip, C::kind>;
+        const size_t need = static_cast<size_t>(c.nCells) * C::nip * R::size;
+        if (need > kStaticRecordFloats)
+            throw Error{NUTO_GPU_EINVAL,
+                        "nuto_gpu_build_matrix_noalloc: the records need " + std::to_string(need) +
+                                " floats, the static array holds " + std::to_string(kStaticRecordFloats) + " (at most " +
+                                std::to_string(kStaticRecordFloats / (C::nip * R::size)) +
+                                " cells of this kind); use nuto_gpu_build_matrix"};
+        float* recs = StaticRecords(c.device);
+        constexpr int CPB = TangentShape<C::nd, C::nip>::cpb;
+        const int blocks = static_cast<int>((c.nCells + CPB - 1) / CPB);
+        k_tangent<double, C::dim, C::nd, C::nip, C::kind, true, float><<<blocks, TangentShape<C::nd, C::nip>::threads,
+                                                                          0, c.stream>>>(a, c.law, s, 0, 0, 0, 0, u,
+                                                                                         recs);
+        AfterLaunch(c, "k_tangent (records, static)");
+        auto kern = k_tangent_rows<float, C::dim, C::nd, C::nip, C::kind>;
+        if (Sh::smem > 48 * 1024)
+            NG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(Sh::smem)));
+        const int64_t rowBlocks = (r.nNodes + Sh::warps - 1) / Sh::warps;
+        kern<<<static_cast<unsigned>(rowBlocks), Sh::warps * 32, Sh::smem, c.stream>>>(r, recs, vals);
+        AfterLaunch(c, "k_tangent_rows (static records)");
+    });
+    c.stats.kernel_launches += 2;
 }
 
 } // namespace nuto_gpu

@@ -299,6 +299,7 @@ void BuildTables(Ctx& c);
 void BuildGeometryCache(Ctx& c);
 void LaunchResidual(Ctx& c, const double* u, double* f);
 void LaunchTangent(Ctx& c, const double* u, int precision, void* values);
+void LaunchTangentNoAlloc(Ctx& c, const double* u, float* values);
 void LaunchHistory(Ctx& c, const double* u);
 void LaunchCellVectors(Ctx& c, const double* fe, double* f);
 void LaunchCellMatrices(Ctx& c, const double* ke, int precision, void* values);
