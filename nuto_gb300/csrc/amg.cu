@@ -14,11 +14,11 @@
 // DOFs take part in neither restriction nor prolongation. Coarse operators keep the node-block CSR layout, so the
 // node SpMV serves every level; level 0 is a diagonal-block view of the tangent itself.
 //
-// Per tangent (device, FP32): Galerkin coarse values A_c = P^T A P by one pass over the finer values with
-// atomics; Jacobi diagonals and Gershgorin bounds of D^-1 A per level. Cycle: V(1,2) with Chebyshev-Jacobi
+// Per tangent (device, in the arithmetic of the tangent: FP32 or FP64): Galerkin coarse values A_c = P^T A P by
+// one pass over the finer values with atomics; Jacobi diagonals and Gershgorin bounds of D^-1 A per level. Cycle: V(1,2) with Chebyshev-Jacobi
 // smoothing on [lmax / 10, lmax] and a degree-6 Chebyshev solve on the coarsest level. The sweep is a fixed
-// linear operator; GMRES uses it in flexible form (stored preconditioned basis) so FP32 rounding inside the cycle
-// does not limit the attainable residual.
+// linear operator; GMRES uses it in flexible form (stored preconditioned basis) so rounding inside the cycle does
+// not limit the attainable residual.
 #include "spmv.cuh"
 
 #include <algorithm>
@@ -35,6 +35,14 @@ constexpr int kPostDegree = 2;
 constexpr int kCoarseDegree = 6;
 constexpr float kSmoothRatio = 10.f; // smoothing interval [lmax / ratio, lmax]
 constexpr float kCoarseRatio = 30.f;
+
+// vectors and coarse values of one level in the preconditioner's arithmetic TA (FP32 for FP32 tangents, FP64 for
+// the plain FP64 path); on level 0 the vectors span the combined system and vals is unused (the tangent is used)
+template <typename TA>
+struct Num
+{
+    DBuf<TA> vals, dinv, e, b, t, d;
+};
 
 struct AmgLevel
 {
@@ -54,11 +62,25 @@ struct AmgLevel
     // transfer from the finer level
     DBuf<int32_t> aggOf;   // finer node -> node of this level
     DBuf<uint16_t> cRank;  // finer neighbour entry -> rank in this level's neighbour list
-    // numerics
-    DBuf<float> vals, dinv, e, b, t, d;
+    // numerics, per arithmetic of the preconditioner (allocated on first use of that arithmetic)
+    Num<float> n32;
+    Num<double> n64;
     float lmax = 1.f;
     NodeSpmv spmv{};
 };
+
+template <typename TA>
+static Num<TA>& N(AmgLevel& L);
+template <>
+Num<float>& N<float>(AmgLevel& L)
+{
+    return L.n32;
+}
+template <>
+Num<double>& N<double>(AmgLevel& L)
+{
+    return L.n64;
+}
 
 struct Amg
 {
@@ -66,9 +88,10 @@ struct Amg
     std::vector<AmgLevel> h[kMaxSlots];
     DBuf<float> lmaxDev; // all levels of all hierarchies
     std::vector<float> lmaxHost;
-    DBuf<float> fine32; // FP32 copy of an FP64 tangent
-    DBuf<float> in32, out32, res32; // combined-length work vectors of the sweep
-    const float* fine = nullptr;
+    DBuf<float> in32, out32, res32; // combined-length work vectors of the sweep (FP32 cycle)
+    DBuf<double> res64;              // the same for the FP64 cycle
+    int prec = 32;                   // arithmetic of the last set-up: that of the tangent values
+    const void* fine = nullptr;      // the tangent of the last set-up (level-0 operator)
     const void* setupVals = nullptr;
     uint64_t setupVersion = 0;
     bool built = false;
@@ -379,16 +402,10 @@ static void BuildSlotHierarchy(Ctx& c, int I, const double* ext, std::vector<Amg
         UploadV(C.cRank, cr);
         C.zeroMask.alloc(C.nDofs);
         NG_CUDA(cudaMemset(C.zeroMask.p, 0, C.nDofs));
-        C.vals.alloc(C.nnz);
-        for (DBuf<float>* b : {&C.dinv, &C.e, &C.b, &C.t, &C.d})
-            b->alloc(C.nDofs);
         FillSpmv(C);
         H.push_back(std::move(C));
         GrowBins(bin, c.dim);
     }
-    // level-0 work vectors span the combined system (the view writes rows of this slot only)
-    for (DBuf<float>* b : {&H[0].dinv, &H[0].t, &H[0].d})
-        b->alloc(c.nDofs);
     H[0].nnz = c.nnz;
 }
 
@@ -424,18 +441,17 @@ static void BuildHierarchy(Ctx& c)
     }
     M.lmaxDev.alloc(total);
     M.lmaxHost.assign(total, 0.f);
-    for (DBuf<float>* b : {&M.in32, &M.out32, &M.res32})
-        b->alloc(c.nDofs);
     M.setupVals = nullptr;
     M.built = true;
 }
 
 // ---- device: per-tangent set-up -----------------------------------------------------------------------------------
 // Galerkin coarse values: one warp per finer node adds its (unconstrained) rows into the aggregate's rows
+template <typename TA>
 __global__ void __launch_bounds__(kBS) k_amg_coarsen(NodeSpmv F, const uint8_t* __restrict__ fmask,
-                                                      const float* __restrict__ fv, NodeSpmv C,
+                                                      const TA* __restrict__ fv, NodeSpmv C,
                                                       const int32_t* __restrict__ agg, const uint16_t* __restrict__ cr,
-                                                      float* cv)
+                                                      TA* cv)
 {
     const int64_t a = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -466,9 +482,10 @@ __global__ void __launch_bounds__(kBS) k_amg_coarsen(NodeSpmv F, const uint8_t* 
 
 // Jacobi diagonal (0 where the DOF is constrained or the diagonal is not positive) and the Gershgorin bound
 // max_r sum_j |a_rj| / a_rr of the spectral radius of D^-1 A (positive floats order like their bit patterns)
+template <typename TA>
 __global__ void __launch_bounds__(kBS) k_amg_diag(NodeSpmv A, const uint8_t* __restrict__ mask,
-                                                   const float* __restrict__ v, const int32_t* __restrict__ diagOff,
-                                                   float* dinv, float* lmax)
+                                                   const TA* __restrict__ v, const int32_t* __restrict__ diagOff,
+                                                   TA* dinv, float* lmax)
 {
     const int64_t a = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -483,17 +500,17 @@ __global__ void __launch_bounds__(kBS) k_amg_diag(NodeSpmv A, const uint8_t* __r
         const int64_t rs = A.rowPtr[r] + A.blk[0][a];
         float s = 0.f;
         for (int q = lane; q < len; q += 32)
-            s += fabsf(v[NG_IDX(rs + q, A.nnz, 32)]);
+            s += fabsf(static_cast<float>(v[NG_IDX(rs + q, A.nnz, 32)]));
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
             s += __shfl_down_sync(0xffffffffu, s, o);
         if (lane == 0)
         {
-            const float dg = v[NG_IDX(rs + diagOff[a] + c, A.nnz, 35)];
-            const bool use = !mask[r] && dg > 0.f;
-            dinv[r] = use ? 1.f / dg : 0.f;
+            const TA dg = v[NG_IDX(rs + diagOff[a] + c, A.nnz, 35)];
+            const bool use = !mask[r] && dg > TA(0);
+            dinv[r] = use ? TA(1) / dg : TA(0);
             if (use)
-                atomicMax(reinterpret_cast<int*>(lmax), __float_as_int(s / dg));
+                atomicMax(reinterpret_cast<int*>(lmax), __float_as_int(s / static_cast<float>(dg)));
         }
     }
 }
@@ -505,44 +522,48 @@ __device__ __forceinline__ bool Idle(const int* st)
 }
 
 // first Chebyshev step from zero: d = dinv b / theta; e = d
-__global__ void k_cheb0(int64_t n, const float* __restrict__ dinv, const float* __restrict__ b, float* d, float* e,
-                        float invTheta, const int* st)
+template <typename TA>
+__global__ void k_cheb0(int64_t n, const TA* __restrict__ dinv, const TA* __restrict__ b, TA* d, TA* e, TA invTheta,
+                        const int* st)
 {
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i >= n || Idle(st))
         return;
-    const float v = dinv[i] * b[i] * invTheta;
+    const TA v = dinv[i] * b[i] * invTheta;
     d[i] = v;
     e[i] = v;
 }
 
 // first Chebyshev step from a nonzero e (t = A e): d = dinv (b - t) / theta; e += d
-__global__ void k_cheb1(int64_t n, const float* __restrict__ dinv, const float* __restrict__ b,
-                        const float* __restrict__ t, float* d, float* e, float invTheta, const int* st)
+template <typename TA>
+__global__ void k_cheb1(int64_t n, const TA* __restrict__ dinv, const TA* __restrict__ b, const TA* __restrict__ t,
+                        TA* d, TA* e, TA invTheta, const int* st)
 {
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i >= n || Idle(st))
         return;
-    const float v = dinv[i] * (b[i] - t[i]) * invTheta;
+    const TA v = dinv[i] * (b[i] - t[i]) * invTheta;
     d[i] = v;
     e[i] += v;
 }
 
 // later Chebyshev steps (t = A e): d = c1 d + c2 dinv (b - t); e += d
-__global__ void k_chebk(int64_t n, const float* __restrict__ dinv, const float* __restrict__ b,
-                        const float* __restrict__ t, float* d, float* e, float c1, float c2, const int* st)
+template <typename TA>
+__global__ void k_chebk(int64_t n, const TA* __restrict__ dinv, const TA* __restrict__ b, const TA* __restrict__ t,
+                        TA* d, TA* e, TA c1, TA c2, const int* st)
 {
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i >= n || Idle(st))
         return;
-    const float v = c1 * d[i] + c2 * dinv[i] * (b[i] - t[i]);
+    const TA v = c1 * d[i] + c2 * dinv[i] * (b[i] - t[i]);
     d[i] = v;
     e[i] += v;
 }
 
 // coarse b = P^T (b - t) with t = A e (cb zeroed before); constrained finer DOFs are skipped
-__global__ void k_restrict(NodeSpmv F, const uint8_t* __restrict__ fmask, const float* __restrict__ b,
-                           const float* __restrict__ t, const int32_t* __restrict__ agg, NodeSpmv C, float* cb,
+template <typename TA>
+__global__ void k_restrict(NodeSpmv F, const uint8_t* __restrict__ fmask, const TA* __restrict__ b,
+                           const TA* __restrict__ t, const int32_t* __restrict__ agg, NodeSpmv C, TA* cb,
                            const int* st)
 {
     const int64_t a = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -556,8 +577,9 @@ __global__ void k_restrict(NodeSpmv F, const uint8_t* __restrict__ fmask, const 
 }
 
 // e += P ce
+template <typename TA>
 __global__ void k_prolong(NodeSpmv F, const uint8_t* __restrict__ fmask, const int32_t* __restrict__ agg, NodeSpmv C,
-                          const float* __restrict__ ce, float* e, const int* st)
+                          const TA* __restrict__ ce, TA* e, const int* st)
 {
     const int64_t a = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (a >= F.totalWarps || Idle(st))
@@ -570,12 +592,13 @@ __global__ void k_prolong(NodeSpmv F, const uint8_t* __restrict__ fmask, const i
 }
 
 // y = a - b (elementwise); a == nullptr gives y = 0
-__global__ void k_sub(int64_t n, const float* a, const float* b, float* y, const int* st)
+template <typename TA>
+__global__ void k_sub(int64_t n, const TA* a, const TA* b, TA* y, const int* st)
 {
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i >= n || Idle(st))
         return;
-    y[i] = a ? a[i] - b[i] : 0.f;
+    y[i] = a ? a[i] - b[i] : TA(0);
 }
 
 template <typename TA, typename TB>
@@ -592,8 +615,28 @@ static unsigned Blocks(int64_t n, int bs = 256)
     return static_cast<unsigned>((n + bs - 1) / bs);
 }
 
+// device vectors of every level in arithmetic TA (on first use of TA)
+template <typename TA>
+static void EnsureNum(Ctx& c, Amg& M)
+{
+    for (int I = 0; I < M.ns; ++I)
+        for (size_t l = 0; l < M.h[I].size(); ++l)
+        {
+            AmgLevel& L = M.h[I][l];
+            Num<TA>& U = N<TA>(L);
+            const int64_t n = l == 0 ? c.nDofs : L.nDofs;
+            if (U.dinv.n == static_cast<size_t>(n))
+                continue;
+            if (l > 0)
+                U.vals.alloc(L.nnz);
+            for (DBuf<TA>* b : {&U.dinv, &U.e, &U.b, &U.t, &U.d})
+                b->alloc(n);
+        }
+}
+
 // Builds the hierarchy on first use and the coarse operators for the tangent `vals` unless they were built for
-// the same values already (same pointer and tangent version).
+// the same values already (same pointer and tangent version). The preconditioner works in the arithmetic of the
+// tangent values: FP32 for FP32 tangents, FP64 for FP64 tangents.
 template <typename TV>
 void AmgSetup(Ctx& c, const TV* vals)
 {
@@ -604,37 +647,29 @@ void AmgSetup(Ctx& c, const TV* vals)
         BuildHierarchy(c);
     if (M.setupVals == static_cast<const void*>(vals) && M.setupVersion == c.valsVersion)
         return;
-    const float* fine;
-    if constexpr (sizeof(TV) == 4)
-        fine = vals;
-    else
-    {
-        if (M.fine32.n != static_cast<size_t>(c.nnz))
-            M.fine32.alloc(c.nnz);
-        k_convert<double, float><<<Blocks(c.nnz), 256, 0, c.stream>>>(c.nnz, vals, M.fine32.p, nullptr);
-        c.stats.kernel_launches += 1;
-        fine = M.fine32.p;
-    }
-    M.fine = fine;
+    EnsureNum<TV>(c, M);
+    M.prec = sizeof(TV) == 4 ? 32 : 64;
+    M.fine = vals;
     NG_CUDA(cudaMemsetAsync(M.lmaxDev.p, 0, M.lmaxHost.size() * sizeof(float), c.stream));
     size_t slot = 0;
     for (int I = 0; I < M.ns; ++I)
     {
         std::vector<AmgLevel>& H = M.h[I];
         H[0].spmv = SlotView(c, I);
-        k_amg_diag<<<Blocks(H[0].nNodes * 32), kBS, 0, c.stream>>>(H[0].spmv, c.dMask.p, fine, H[0].diagOff.p,
-                                                                    H[0].dinv.p, M.lmaxDev.p + slot);
+        k_amg_diag<TV><<<Blocks(H[0].nNodes * 32), kBS, 0, c.stream>>>(H[0].spmv, c.dMask.p, vals, H[0].diagOff.p,
+                                                                        N<TV>(H[0]).dinv.p, M.lmaxDev.p + slot);
         c.stats.kernel_launches += 1;
         for (size_t l = 1; l < H.size(); ++l)
         {
             AmgLevel& Fi = H[l - 1];
             AmgLevel& C = H[l];
-            NG_CUDA(cudaMemsetAsync(C.vals.p, 0, C.nnz * sizeof(float), c.stream));
-            k_amg_coarsen<<<Blocks(Fi.nNodes * 32), kBS, 0, c.stream>>>(
-                    Fi.spmv, l == 1 ? c.dMask.p : Fi.zeroMask.p, l == 1 ? fine : Fi.vals.p, C.spmv, C.aggOf.p,
-                    C.cRank.p, C.vals.p);
-            k_amg_diag<<<Blocks(C.nNodes * 32), kBS, 0, c.stream>>>(C.spmv, C.zeroMask.p, C.vals.p, C.diagOff.p,
-                                                                     C.dinv.p, M.lmaxDev.p + slot + l);
+            Num<TV>& CU = N<TV>(C);
+            NG_CUDA(cudaMemsetAsync(CU.vals.p, 0, C.nnz * sizeof(TV), c.stream));
+            k_amg_coarsen<TV><<<Blocks(Fi.nNodes * 32), kBS, 0, c.stream>>>(
+                    Fi.spmv, l == 1 ? c.dMask.p : Fi.zeroMask.p, l == 1 ? vals : N<TV>(Fi).vals.p, C.spmv, C.aggOf.p,
+                    C.cRank.p, CU.vals.p);
+            k_amg_diag<TV><<<Blocks(C.nNodes * 32), kBS, 0, c.stream>>>(C.spmv, C.zeroMask.p, CU.vals.p, C.diagOff.p,
+                                                                         CU.dinv.p, M.lmaxDev.p + slot + l);
             c.stats.kernel_launches += 2;
         }
         slot += H.size();
@@ -658,94 +693,120 @@ template void AmgSetup<double>(Ctx&, const double*);
 
 // Chebyshev smoothing of A e = b on [lmax / ratio, lmax]. Vectors are base pointers of the level (combined
 // length on level 0); elementwise work runs over rows [off, off + n). fromZero starts at e = 0 (no product).
-static void Chebyshev(Ctx& c, AmgLevel& L, const float* vals, const uint8_t* mask, const float* b, float* e,
-                      int degree, bool fromZero, float ratio, const int* st)
+template <typename TA>
+static void Chebyshev(Ctx& c, AmgLevel& L, const TA* vals, const uint8_t* mask, const TA* b, TA* e, int degree,
+                      bool fromZero, float ratio, const int* st)
 {
+    Num<TA>& U = N<TA>(L);
     const int64_t n = L.nDofs, o = L.off;
-    const float lmax = L.lmax, lmin = L.lmax / ratio;
-    const float theta = 0.5f * (lmax + lmin), delta = 0.5f * (lmax - lmin);
-    const float sigma = theta / delta;
+    const double lmax = L.lmax, lmin = L.lmax / ratio;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+    const double sigma = theta / delta;
     int* stw = const_cast<int*>(st); // the SpMV only reads the state when it computes no dot products
-    float rho = 1.f / sigma;
+    double rho = 1. / sigma;
     if (fromZero)
-        k_cheb0<<<Blocks(n), 256, 0, c.stream>>>(n, L.dinv.p + o, b + o, L.d.p + o, e + o, 1.f / theta, st);
+        k_cheb0<TA><<<Blocks(n), 256, 0, c.stream>>>(n, U.dinv.p + o, b + o, U.d.p + o, e + o, TA(1. / theta), st);
     else
     {
-        SpmvNode<float, float, 0>(c.stream, L.spmv, vals, e, L.t.p, nullptr, nullptr, stw, 0, mask);
-        k_cheb1<<<Blocks(n), 256, 0, c.stream>>>(n, L.dinv.p + o, b + o, L.t.p + o, L.d.p + o, e + o, 1.f / theta,
-                                                 st);
+        SpmvNode<TA, TA, 0>(c.stream, L.spmv, vals, e, U.t.p, nullptr, nullptr, stw, 0, mask);
+        k_cheb1<TA><<<Blocks(n), 256, 0, c.stream>>>(n, U.dinv.p + o, b + o, U.t.p + o, U.d.p + o, e + o,
+                                                     TA(1. / theta), st);
         c.stats.kernel_launches += 1;
     }
     c.stats.kernel_launches += 1;
     for (int k = 1; k < degree; ++k)
     {
-        const float rhoNew = 1.f / (2.f * sigma - rho);
-        SpmvNode<float, float, 0>(c.stream, L.spmv, vals, e, L.t.p, nullptr, nullptr, stw, 0, mask);
-        k_chebk<<<Blocks(n), 256, 0, c.stream>>>(n, L.dinv.p + o, b + o, L.t.p + o, L.d.p + o, e + o, rhoNew * rho,
-                                                 2.f * rhoNew / delta, st);
+        const double rhoNew = 1. / (2. * sigma - rho);
+        SpmvNode<TA, TA, 0>(c.stream, L.spmv, vals, e, U.t.p, nullptr, nullptr, stw, 0, mask);
+        k_chebk<TA><<<Blocks(n), 256, 0, c.stream>>>(n, U.dinv.p + o, b + o, U.t.p + o, U.d.p + o, e + o,
+                                                     TA(rhoNew * rho), TA(2. * rhoNew / delta), st);
         c.stats.kernel_launches += 2;
         rho = rhoNew;
     }
 }
 
 // e = V-cycle(b) on level l of hierarchy H
-static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const float* b, float* e, const int* st, bool sym)
+template <typename TA>
+static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const TA* b, TA* e, const int* st, bool sym)
 {
     Amg& M = *c.amg;
     AmgLevel& L = H[l];
-    const float* vals = l == 0 ? M.fine : L.vals.p;
+    Num<TA>& U = N<TA>(L);
+    const TA* vals = l == 0 ? static_cast<const TA*>(M.fine) : U.vals.p;
     const uint8_t* mask = l == 0 ? c.dMask.p : L.zeroMask.p;
     if (l + 1 == H.size())
     {
-        Chebyshev(c, L, vals, mask, b, e, kCoarseDegree, true, kCoarseRatio, st);
+        Chebyshev<TA>(c, L, vals, mask, b, e, kCoarseDegree, true, kCoarseRatio, st);
         return;
     }
     AmgLevel& C = H[l + 1];
+    Num<TA>& CU = N<TA>(C);
     int* stw = const_cast<int*>(st);
-    Chebyshev(c, L, vals, mask, b, e, sym ? kPostDegree : kPreDegree, true, kSmoothRatio, st);
-    SpmvNode<float, float, 0>(c.stream, L.spmv, vals, e, L.t.p, nullptr, nullptr, stw, 0, mask);
-    k_sub<<<Blocks(C.nDofs), 256, 0, c.stream>>>(C.nDofs, nullptr, nullptr, C.b.p, st);
-    k_restrict<<<Blocks(L.nNodes), 256, 0, c.stream>>>(L.spmv, mask, b, L.t.p, C.aggOf.p, C.spmv, C.b.p, st);
+    Chebyshev<TA>(c, L, vals, mask, b, e, sym ? kPostDegree : kPreDegree, true, kSmoothRatio, st);
+    SpmvNode<TA, TA, 0>(c.stream, L.spmv, vals, e, U.t.p, nullptr, nullptr, stw, 0, mask);
+    k_sub<TA><<<Blocks(C.nDofs), 256, 0, c.stream>>>(C.nDofs, nullptr, nullptr, CU.b.p, st);
+    k_restrict<TA><<<Blocks(L.nNodes), 256, 0, c.stream>>>(L.spmv, mask, b, U.t.p, C.aggOf.p, C.spmv, CU.b.p, st);
     c.stats.kernel_launches += 3;
-    VCycle(c, H, l + 1, C.b.p, C.e.p, st, sym);
-    k_prolong<<<Blocks(L.nNodes), 256, 0, c.stream>>>(L.spmv, mask, C.aggOf.p, C.spmv, C.e.p, e, st);
+    VCycle<TA>(c, H, l + 1, CU.b.p, CU.e.p, st, sym);
+    k_prolong<TA><<<Blocks(L.nNodes), 256, 0, c.stream>>>(L.spmv, mask, C.aggOf.p, C.spmv, CU.e.p, e, st);
     c.stats.kernel_launches += 1;
-    Chebyshev(c, L, vals, mask, b, e, kPostDegree, false, kSmoothRatio, st);
+    Chebyshev<TA>(c, L, vals, mask, b, e, kPostDegree, false, kSmoothRatio, st);
 }
 
-// block Gauss-Seidel sweep in slot order on combined FP32 vectors: z_0 = V_0(v_0), z_1 = V_1(v_1 - K_10 z_0)
-static void Sweep(Ctx& c, const float* v, float* z, const int* st, bool sym)
+// block Gauss-Seidel sweep in slot order on combined vectors: z_0 = V_0(v_0), z_1 = V_1(v_1 - K_10 z_0)
+template <typename TA>
+static void Sweep(Ctx& c, const TA* v, TA* z, TA* res, const int* st, bool sym)
 {
     Amg& M = *c.amg;
-    VCycle(c, M.h[0], 0, v, z, st, sym);
+    VCycle<TA>(c, M.h[0], 0, v, z, st, sym);
     for (int I = 1; I < M.ns; ++I)
     {
         AmgLevel& L = M.h[I][0];
         const int64_t o = L.off, n = L.nDofs;
         // z_I = 0, res = K z on the rows of slot I, res = v_I - res
-        k_sub<<<Blocks(n), 256, 0, c.stream>>>(n, nullptr, nullptr, z + o, st);
-        SpmvNode<float, float, 0>(c.stream, RowsView(c, I), M.fine, z, M.res32.p, nullptr, nullptr,
-                                  const_cast<int*>(st), 0, c.dMask.p);
-        k_sub<<<Blocks(n), 256, 0, c.stream>>>(n, v + o, M.res32.p + o, M.res32.p + o, st);
+        k_sub<TA><<<Blocks(n), 256, 0, c.stream>>>(n, nullptr, nullptr, z + o, st);
+        SpmvNode<TA, TA, 0>(c.stream, RowsView(c, I), static_cast<const TA*>(M.fine), z, res, nullptr, nullptr,
+                            const_cast<int*>(st), 0, c.dMask.p);
+        k_sub<TA><<<Blocks(n), 256, 0, c.stream>>>(n, v + o, res + o, res + o, st);
         c.stats.kernel_launches += 3;
-        VCycle(c, M.h[I], 0, M.res32.p, z, st, sym);
+        VCycle<TA>(c, M.h[I], 0, res, z, st, sym);
     }
 }
 
-// z = M^-1 v for the tangent of the last AmgSetup (FP32 cycle; FP64 vectors are converted). With st given,
-// every kernel returns at once when the Krylov state is not RUN. sym = true runs equal pre- and post-smoothing
-// (a symmetric cycle for PCG on a single slot); otherwise the cheaper V(1,2) for GMRES.
+// z = M^-1 v for the tangent of the last AmgSetup, in that tangent's arithmetic (FP64 Krylov vectors with an
+// FP32 tangent are converted). With st given, every kernel returns at once when the Krylov state is not RUN.
+// sym = true runs equal pre- and post-smoothing (a symmetric cycle for PCG on a single slot); otherwise the
+// cheaper V(1,2) for GMRES.
 template <typename T>
 void AmgApply(Ctx& c, const T* v, T* z, const int* st, bool sym)
 {
     Amg& M = *c.amg;
     const int64_t n = c.nDofs;
+    if (M.prec == 64)
+    {
+        if constexpr (sizeof(T) == 8)
+        {
+            if (M.res64.n != static_cast<size_t>(n))
+                M.res64.alloc(n);
+            Sweep<double>(c, v, z, M.res64.p, st, sym);
+        }
+        else
+            throw Error{NUTO_GPU_EINVAL, "FP32 Krylov vectors with an FP64 multigrid set-up"};
+        return;
+    }
+    if (M.res32.n != static_cast<size_t>(n))
+        M.res32.alloc(n);
     if constexpr (sizeof(T) == 4)
-        Sweep(c, v, z, st, sym);
+        Sweep<float>(c, v, z, M.res32.p, st, sym);
     else
     {
+        if (M.in32.n != static_cast<size_t>(n))
+        {
+            M.in32.alloc(n);
+            M.out32.alloc(n);
+        }
         k_convert<double, float><<<Blocks(n), 256, 0, c.stream>>>(n, v, M.in32.p, st);
-        Sweep(c, M.in32.p, M.out32.p, st, sym);
+        Sweep<float>(c, M.in32.p, M.out32.p, M.res32.p, st, sym);
         k_convert<float, double><<<Blocks(n), 256, 0, c.stream>>>(n, M.out32.p, z, st);
         c.stats.kernel_launches += 2;
     }
