@@ -315,6 +315,20 @@ def run_ours(args):
                 / (sec32 / max(agg32["matrix_assemblies"], 1)),
                 "speedup_mixed_vs_fp64_load_step": sec64 / sec32,
                 "max_rel_displacement_error_mixed_vs_fp64": err}
+        # both results against an FP64 solution of the same steps converged to 1e-11 (untimed): the displacement
+        # uncertainty that the 1e-8 residual tolerance itself leaves is the scale for the mixed path's error
+        opts_t = g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-11, krylov_rtol=1e-6, max_newton=40,
+                                   max_krylov=20000)
+        try:
+            g.set_state(x_w, t_w, False)
+            g.history = kappa_w
+            run_steps(g, opts_t, t_w, t_values)
+            xt, _ = g.get_state()
+            sc = max(np.abs(xt).max(), 1e-300)
+            fp64["max_rel_displacement_error_vs_fp64_1e-11"] = {
+                "mixed": float(np.abs(x32 - xt).max() / sc), "fp64": float(np.abs(x64 - xt).max() / sc)}
+        except Exception as exc:  # the reference solution is a diagnostic only
+            fp64["max_rel_displacement_error_vs_fp64_1e-11"] = {"error": str(exc)}
 
     # end to end through the C ABI with pinned host buffers (state + history copied in and out every step)
     n_hist = s.mesh.num_cells * g.n_ip
