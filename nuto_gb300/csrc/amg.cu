@@ -22,6 +22,7 @@
 #include "spmv.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <numeric>
 #include <unordered_map>
 
@@ -82,6 +83,17 @@ Num<double>& N<double>(AmgLevel& L)
     return L.n64;
 }
 
+// One sweep (all launches of both V-cycles) captured as a CUDA graph on fixed input/output vectors. The graph is
+// recaptured after every set-up (the Chebyshev coefficients are kernel arguments) and the executable graph updated
+// in place (same topology), so a sweep costs one launch on the host instead of about 150.
+struct SweepGraph
+{
+    cudaGraphExec_t exec = nullptr;
+    uint64_t setup = 0;      // set-up counter the graph was captured for
+    const int* st = nullptr; // Krylov state pointer baked into the graph
+    int64_t launches = 0;    // kernels per replay
+};
+
 struct Amg
 {
     int ns = 0;
@@ -89,12 +101,22 @@ struct Amg
     DBuf<float> lmaxDev; // all levels of all hierarchies
     std::vector<float> lmaxHost;
     DBuf<float> in32, out32, res32; // combined-length work vectors of the sweep (FP32 cycle)
-    DBuf<double> res64;              // the same for the FP64 cycle
+    DBuf<double> in64, out64, res64; // the same for the FP64 cycle
     int prec = 32;                   // arithmetic of the last set-up: that of the tangent values
     const void* fine = nullptr;      // the tangent of the last set-up (level-0 operator)
     const void* setupVals = nullptr;
     uint64_t setupVersion = 0;
+    uint64_t setups = 0; // set-ups so far
     bool built = false;
+    bool graphs = true;           // NUTO_GPU_GRAPHS=0 launches the sweep kernel by kernel
+    SweepGraph graph[2][2];       // [FP64][symmetric]
+    ~Amg()
+    {
+        for (auto& row : graph)
+            for (SweepGraph& g : row)
+                if (g.exec)
+                    cudaGraphExecDestroy(g.exec);
+    }
 };
 
 void FreeAmg(Ctx& c)
@@ -641,7 +663,11 @@ template <typename TV>
 void AmgSetup(Ctx& c, const TV* vals)
 {
     if (!c.amg)
+    {
         c.amg = new Amg();
+        const char* gr = std::getenv("NUTO_GPU_GRAPHS");
+        c.amg->graphs = !(gr && gr[0] == '0');
+    }
     Amg& M = *c.amg;
     if (!M.built)
         BuildHierarchy(c);
@@ -687,6 +713,7 @@ void AmgSetup(Ctx& c, const TV* vals)
         }
     M.setupVals = vals;
     M.setupVersion = c.valsVersion;
+    M.setups++;
 }
 template void AmgSetup<float>(Ctx&, const float*);
 template void AmgSetup<double>(Ctx&, const double*);
@@ -777,36 +804,120 @@ static void Sweep(Ctx& c, const TA* v, TA* z, TA* res, const int* st, bool sym)
 // FP32 tangent are converted). With st given, every kernel returns at once when the Krylov state is not RUN.
 // sym = true runs equal pre- and post-smoothing (a symmetric cycle for PCG on a single slot); otherwise the
 // cheaper V(1,2) for GMRES.
+// Runs Sweep<TA>(in, out) through the graph of (TA, sym), capturing or updating it when the set-up changed. Returns
+// false when graphs are off or the capture failed (the caller then launches the sweep kernel by kernel).
+template <typename TA>
+static bool SweepGraphRun(Ctx& c, TA* in, TA* out, TA* res, const int* st, bool sym)
+{
+    Amg& M = *c.amg;
+    if (!M.graphs)
+        return false;
+    SweepGraph& G = M.graph[sizeof(TA) == 8 ? 1 : 0][sym ? 1 : 0];
+    if (!G.exec || G.setup != M.setups || G.st != st)
+    {
+        const int64_t before = c.stats.kernel_launches;
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        {
+            cudaGetLastError();
+            M.graphs = false;
+            return false;
+        }
+        Sweep<TA>(c, in, out, res, st, sym);
+        const cudaError_t ec = cudaStreamEndCapture(c.stream, &graph);
+        G.launches = c.stats.kernel_launches - before;
+        c.stats.kernel_launches = before;
+        bool ok = ec == cudaSuccess && graph != nullptr;
+        if (ok && G.exec)
+        {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(G.exec, graph, &info) != cudaSuccess)
+            {
+                cudaGetLastError();
+                cudaGraphExecDestroy(G.exec);
+                G.exec = nullptr;
+            }
+        }
+        if (ok && !G.exec)
+            ok = cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess;
+        if (graph)
+            cudaGraphDestroy(graph);
+        if (!ok)
+        {
+            cudaGetLastError();
+            if (G.exec)
+                cudaGraphExecDestroy(G.exec);
+            G.exec = nullptr;
+            M.graphs = false;
+            return false;
+        }
+        G.setup = M.setups;
+        G.st = st;
+    }
+    NG_CUDA(cudaGraphLaunch(G.exec, c.stream));
+    c.stats.kernel_launches += G.launches;
+    return true;
+}
+
+// z = M^-1 v for the tangent of the last AmgSetup, in that tangent's arithmetic (FP64 Krylov vectors with an
+// FP32 tangent are converted). With st given, every kernel returns at once when the Krylov state is not RUN.
+// sym = true runs equal pre- and post-smoothing (a symmetric cycle for PCG on a single slot); otherwise the
+// cheaper V(1,2) for GMRES. The sweep runs as a CUDA graph on fixed vectors (input and output copied).
 template <typename T>
 void AmgApply(Ctx& c, const T* v, T* z, const int* st, bool sym)
 {
     Amg& M = *c.amg;
     const int64_t n = c.nDofs;
+    const size_t bytesN = static_cast<size_t>(n);
     if (M.prec == 64)
     {
         if constexpr (sizeof(T) == 8)
         {
-            if (M.res64.n != static_cast<size_t>(n))
+            if (M.res64.n != bytesN)
+            {
                 M.res64.alloc(n);
+                M.in64.alloc(n);
+                M.out64.alloc(n);
+            }
+            if (M.graphs)
+            {
+                NG_CUDA(cudaMemcpyAsync(M.in64.p, v, n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+                if (SweepGraphRun<double>(c, M.in64.p, M.out64.p, M.res64.p, st, sym))
+                {
+                    NG_CUDA(cudaMemcpyAsync(z, M.out64.p, n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+                    return;
+                }
+            }
             Sweep<double>(c, v, z, M.res64.p, st, sym);
         }
         else
             throw Error{NUTO_GPU_EINVAL, "FP32 Krylov vectors with an FP64 multigrid set-up"};
         return;
     }
-    if (M.res32.n != static_cast<size_t>(n))
+    if (M.res32.n != bytesN)
+    {
         M.res32.alloc(n);
+        M.in32.alloc(n);
+        M.out32.alloc(n);
+    }
     if constexpr (sizeof(T) == 4)
+    {
+        if (M.graphs)
+        {
+            NG_CUDA(cudaMemcpyAsync(M.in32.p, v, n * sizeof(float), cudaMemcpyDeviceToDevice, c.stream));
+            if (SweepGraphRun<float>(c, M.in32.p, M.out32.p, M.res32.p, st, sym))
+            {
+                NG_CUDA(cudaMemcpyAsync(z, M.out32.p, n * sizeof(float), cudaMemcpyDeviceToDevice, c.stream));
+                return;
+            }
+        }
         Sweep<float>(c, v, z, M.res32.p, st, sym);
+    }
     else
     {
-        if (M.in32.n != static_cast<size_t>(n))
-        {
-            M.in32.alloc(n);
-            M.out32.alloc(n);
-        }
         k_convert<double, float><<<Blocks(n), 256, 0, c.stream>>>(n, v, M.in32.p, st);
-        Sweep<float>(c, M.in32.p, M.out32.p, M.res32.p, st, sym);
+        if (!SweepGraphRun<float>(c, M.in32.p, M.out32.p, M.res32.p, st, sym))
+            Sweep<float>(c, M.in32.p, M.out32.p, M.res32.p, st, sym);
         k_convert<float, double><<<Blocks(n), 256, 0, c.stream>>>(n, M.out32.p, z, st);
         c.stats.kernel_launches += 2;
     }

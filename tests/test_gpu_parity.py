@@ -354,3 +354,27 @@ def test_tangent_row_gather_matches_element_atomics(kind, n, precision, monkeypa
     atom = g2.build_matrix(u, precision).double().cpu().numpy()
     tol = 1e-13 if precision == 64 else 2e-6
     assert np.abs(rows - atom).max() <= tol * np.abs(atom).max()
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_multigrid_sweep_graph_matches_kernel_launches(precision, monkeypatch):
+    """The multigrid sweep replayed as a CUDA graph and launched kernel by kernel (NUTO_GPU_GRAPHS=0) give the same
+    GMRES solution (up to the order of the atomic restriction sums) and iteration count within one restart."""
+    _torch()
+    rng = np.random.default_rng(12)
+    b = None
+    out = {}
+    for graphs in ("1", "0"):
+        monkeypatch.setenv("NUTO_GPU_GRAPHS", graphs)
+        s, g, (om, layers, P, cons) = _build("hex8gd", 8)
+        if b is None:
+            u, kappa = _damage_state("hex8gd", P, rng)
+            b = rng.uniform(-1, 1, P.n_dofs)
+        g.history = kappa
+        vals = g.build_matrix(u, precision)
+        x, it, rel, ok = g.solve(vals, b, precision=precision, method=3, rtol=1e-8, max_iterations=5000)
+        assert ok, (graphs, it, rel)
+        out[graphs] = (x.cpu().numpy(), it)
+    (x1, it1), (x0, it0) = out["1"], out["0"]
+    assert np.abs(x1 - x0).max() <= 1e-5 * np.abs(x0).max()
+    assert abs(it1 - it0) <= 40
