@@ -28,6 +28,9 @@
  *   nuto_gpu_build_matrix       SimpleAssembler::BuildMatrix(cells, dofs, Bind(integrand, &Hessian0)) + ToEigen
  *                                                                        nuto/mechanics/cell/SimpleAssembler.cpp:100-156
  *   nuto_gpu_update_history     TimeDependentProblem::UpdateHistory      nuto/mechanics/tools/TimeDependentProblem.cpp:78-85
+ *   nuto_gpu_build_lumped_mass  SimpleAssembler::BuildDiagonallyLumpedMatrix + DynamicMomentumBalance::Hessian2
+ *                                                                        nuto/mechanics/cell/SimpleAssembler.cpp:67-98
+ *   nuto_gpu_eval_ip            Cell::Eval (post-processing of kappa, damage, strain, stress) nuto/mechanics/cell/Cell.h:80-93
  *   nuto_gpu_assemble_cell_vectors / _matrices
  *                               the scatter half of SimpleAssembler::BuildVector/BuildMatrix for caller-given cell
  *                               results (any CellInterface::VectorFunction/MatrixFunction)
@@ -200,6 +203,20 @@ int nuto_gpu_build_matrix(nuto_gpu_ctx* ctx, const double* d_u, int precision, v
 int nuto_gpu_build_matrix_noalloc(nuto_gpu_ctx* ctx, const double* d_u, float* d_values);
 /* kappa <- max(kappa, kappa(u)) at every integration point */
 int nuto_gpu_update_history(nuto_gpu_ctx* ctx, const double* d_u);
+/* Lumped mass: SimpleAssembler::BuildDiagonallyLumpedMatrix (nuto/mechanics/cell/SimpleAssembler.cpp:67-98) of
+   DynamicMomentumBalance<D>::Hessian2 (nuto/mechanics/integrands/DynamicMomentumBalance.h:22-30) with density rho:
+   per cell the diagonal of rho N^T N det J w, scaled by (sum of all entries / sum of the diagonal) / components,
+   summed into d_m (combined layout; the displacement rows, zero elsewhere). */
+int nuto_gpu_build_lumped_mass(nuto_gpu_ctx* ctx, double rho, double* d_m);
+/* Values at every integration point for post-processing: Cell::Eval (nuto/mechanics/cell/Cell.h:80-93) with
+   GradientDamage::Kappa (nuto/mechanics/integrands/GradientDamage.h:127-130), the damage law, Nabla::Strain and the
+   law's stress. d_out is n_cells x n_ip x width doubles (width: Voigt size for strain and stress, else 1). */
+#define NUTO_GPU_IP_KAPPA 0  /* max(kappa history, eeq) / max(kappa history, local equivalent strain) */
+#define NUTO_GPU_IP_DAMAGE 1 /* omega(kappa) of DamageLawExponential, 0 for linear elasticity */
+#define NUTO_GPU_IP_STRAIN 2 /* engineering strain, Voigt order */
+#define NUTO_GPU_IP_STRESS 3 /* stress of the law (LinearElastic, LinearElasticDamage with omega) */
+#define NUTO_GPU_IP_EEQ 4    /* nonlocal eeq (gradient damage), else the local modified-Mises equivalent strain */
+int nuto_gpu_eval_ip(nuto_gpu_ctx* ctx, const double* d_u, int quantity, double* d_out);
 /* scatter of caller-given cell vectors (n_cells x n_local doubles, slot-major, node, component) */
 int nuto_gpu_assemble_cell_vectors(nuto_gpu_ctx* ctx, const double* d_cell_vectors, double* d_f);
 /* scatter of caller-given cell matrices (n_cells x n_local x n_local doubles, row-major) into CSR values */

@@ -19,6 +19,7 @@ INTERACTION_CONSTANT, INTERACTION_DECREASING = 0, 1
 FP32, FP64, MIXED = 32, 64, 48
 SOLVER_AUTO, SOLVER_PCG, SOLVER_BICGSTAB, SOLVER_GMRES = 0, 1, 2, 3
 PRECOND_JACOBI, PRECOND_AMG = 1, 2
+IP_KAPPA, IP_DAMAGE, IP_STRAIN, IP_STRESS, IP_EEQ = 0, 1, 2, 3, 4
 
 _ERRNAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ENOCONV: "ENOCONV", ENAN: "ENAN", ETIMEOUT: "ETIMEOUT",
              ECUDA: "ECUDA", ESTATE: "ESTATE"}
@@ -88,6 +89,8 @@ SIGNATURES = {
     "nuto_gpu_build_vector": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_build_matrix": (_i, [_vp, _vp, _i, _vp]),
     "nuto_gpu_build_matrix_noalloc": (_i, [_vp, _vp, _vp]),
+    "nuto_gpu_build_lumped_mass": (_i, [_vp, _d, _vp]),
+    "nuto_gpu_eval_ip": (_i, [_vp, _vp, _i, _vp]),
     "nuto_gpu_update_history": (_i, [_vp, _vp]),
     "nuto_gpu_assemble_cell_vectors": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_assemble_cell_matrices": (_i, [_vp, _vp, _i, _vp]),

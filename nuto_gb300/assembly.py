@@ -153,6 +153,23 @@ class GpuCellGroup:
         self._call("nuto_gpu_build_matrix_noalloc", _ptr(u), _ptr(v))
         return v
 
+    def lumped_mass(self, rho, out=None):
+        """BuildDiagonallyLumpedMatrix of DynamicMomentumBalance::Hessian2 with density rho (combined layout)."""
+        torch = _torch()
+        dev = torch.device("cuda", self.device)
+        m = out if out is not None else torch.empty(self.n_dofs, dtype=torch.float64, device=dev)
+        self._call("nuto_gpu_build_lumped_mass", float(rho), _ptr(m))
+        return m
+
+    def eval_ip(self, u, quantity):
+        """Cell::Eval of an IP_* quantity at every integration point: (n_cells, n_ip, width) on the device."""
+        torch = _torch()
+        u = self._dev(u, torch.float64)
+        w = (3 if self.mesh.dim == 2 else 6) if quantity in (_lib.IP_STRAIN, _lib.IP_STRESS) else 1
+        out = torch.empty((self.mesh.num_cells, self.n_ip, w), dtype=torch.float64, device=u.device)
+        self._call("nuto_gpu_eval_ip", _ptr(u), int(quantity), _ptr(out))
+        return out
+
     def update_history(self, u):
         torch = _torch()
         u = self._dev(u, torch.float64)

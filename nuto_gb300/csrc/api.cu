@@ -864,6 +864,26 @@ int nuto_gpu_build_matrix_noalloc(nuto_gpu_ctx* ctx, const double* u, float* val
     });
 }
 
+int nuto_gpu_build_lumped_mass(nuto_gpu_ctx* ctx, double rho, double* m)
+{
+    return Guard(ctx, [&] {
+        RequireReady(*ctx);
+        LaunchLumpedMass(*ctx, rho, m);
+        return NUTO_GPU_OK;
+    });
+}
+
+int nuto_gpu_eval_ip(nuto_gpu_ctx* ctx, const double* u, int quantity, double* out)
+{
+    return Guard(ctx, [&] {
+        RequireReady(*ctx);
+        NG_CHECK(quantity >= NUTO_GPU_IP_KAPPA && quantity <= NUTO_GPU_IP_EEQ, NUTO_GPU_EINVAL,
+                 "unknown integration-point quantity");
+        LaunchEvalIp(*ctx, u, quantity, out);
+        return NUTO_GPU_OK;
+    });
+}
+
 int nuto_gpu_update_history(nuto_gpu_ctx* ctx, const double* u)
 {
     return Guard(ctx, [&] {

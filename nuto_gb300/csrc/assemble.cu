@@ -1218,6 +1218,158 @@ void LaunchHistory(Ctx& c, const double* u)
     c.stats.kernel_launches += 1;
 }
 
+// ---- lumped mass: SimpleAssembler::BuildDiagonallyLumpedMatrix (SimpleAssembler.cpp:67-98) of
+// DynamicMomentumBalance::Hessian2 (DynamicMomentumBalance.h:22-30) ---------------------------------------------
+// One thread per cell. The cell block is rho N^T N det J w with N the component-interleaved shape matrix, so its
+// diagonal entry of (node a, component c) is rho sum_q w det J N_a^2, its diagonal sum ncomp times the sum of those
+// and its full sum ncomp rho sum_q w det J (sum_a N_a)^2; the lumped entry is diagonal * (full / diagonal sum) /
+// ncomp, the reference's scaling (DofType::GetNum divides it by the component count).
+template <int DIM, int ND, int NIP>
+__global__ void __launch_bounds__(128) k_lumped_mass(CellArgs a, int ncomp, double rho, double* __restrict__ m)
+{
+    const int64_t n = a.nCells;
+    const int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (e >= n)
+        return;
+    double diag[ND];
+#pragma unroll
+    for (int i = 0; i < ND; ++i)
+        diag[i] = 0;
+    double full = 0;
+    for (int q = 0; q < NIP; ++q)
+    {
+        const double wdj = a.geo64[NG_IDX(static_cast<int64_t>(q) * a.geoStride * n + e, a.geoSize, 6)];
+        double sumN = 0;
+#pragma unroll
+        for (int i = 0; i < ND; ++i)
+        {
+            const double Ni = a.tabN_D[q * ND + i];
+            diag[i] += rho * Ni * Ni * wdj;
+            sumN += Ni;
+        }
+        full += rho * sumN * sumN * wdj;
+    }
+    double diagSum = 0;
+#pragma unroll
+    for (int i = 0; i < ND; ++i)
+        diagSum += diag[i];
+    const double scale = ((ncomp * full) / (ncomp * diagSum)) / ncomp;
+#pragma unroll
+    for (int i = 0; i < ND; ++i)
+    {
+        const int64_t g = a.gdofD[NG_IDX(a.connD[static_cast<int64_t>(i) * n + e], a.nNodesD, 2)];
+        for (int c = 0; c < ncomp; ++c)
+            atomicAdd(m + NG_IDX(g + c, a.nDofs, 8), diag[i] * scale);
+    }
+}
+
+void LaunchLumpedMass(Ctx& c, double rho, double* m)
+{
+    NG_CUDA(cudaMemsetAsync(m, 0, c.nDofs * sizeof(double), c.stream));
+    CellArgs a = MakeCellArgs(c);
+    const int ncomp = c.slots[c.prm.disp_slot].ncomp;
+    const int blocks = static_cast<int>((c.nCells + 127) / 128);
+    DispatchCfg(c, [&](auto cfg) {
+        using C = decltype(cfg);
+        k_lumped_mass<C::dim, C::nd, C::nip><<<blocks, 128, 0, c.stream>>>(a, ncomp, rho, m);
+    });
+    AfterLaunch(c, "k_lumped_mass");
+    c.stats.kernel_launches += 1;
+}
+
+// ---- integration-point values for post-processing: Cell::Eval (Cell.h:80-93) -----------------------------------
+// One thread per (cell, point): strain from the cached FP64 geometry, kappa = max(kappa_h, eeq or eps_eq)
+// (GradientDamage::Kappa, GradientDamage.h:127-130; EvolutionImplicit), omega(kappa), the law's stress.
+// out[(cell * NIP + q) * width + r].
+template <int DIM, int ND, int NIP, int KIND>
+__global__ void __launch_bounds__(128) k_eval_ip(CellArgs a, LawParams L, const double* __restrict__ u, int quantity,
+                                                 double* __restrict__ out)
+{
+    constexpr int VD = DIM == 2 ? 3 : 6;
+    const int64_t n = a.nCells;
+    const int64_t it = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (it >= n * NIP)
+        return;
+    const int64_t e = it / NIP;
+    const int q = static_cast<int>(it % NIP);
+    const double* G = a.geo64 + NG_IDX(static_cast<int64_t>(q) * a.geoStride * n + e, a.geoSize, 6);
+    double H[DIM][DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int j = 0; j < DIM; ++j)
+            H[i][j] = 0;
+    for (int nd = 0; nd < ND; ++nd)
+    {
+        const int64_t g = a.gdofD[NG_IDX(a.connD[static_cast<int64_t>(nd) * n + e], a.nNodesD, 2)];
+#pragma unroll
+        for (int c = 0; c < DIM; ++c)
+        {
+            const double uc = u[NG_IDX(g + c, a.nDofs, 3)];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                H[c][d] += uc * G[(1 + nd * DIM + d) * n];
+        }
+    }
+    double eps[VD];
+    StrainFromH<double, DIM>(H, eps);
+    double eqs = 0;
+    if (KIND == NUTO_GPU_GRADIENT_DAMAGE)
+    {
+        for (int nd = 0; nd < ND; ++nd)
+            eqs += a.tabN_D[q * ND + nd] *
+                   u[NG_IDX(a.gdofE[NG_IDX(a.connE[static_cast<int64_t>(nd) * n + e], a.nNodesE, 4)], a.nDofs, 5)];
+    }
+    else if (KIND == NUTO_GPU_MB_LOCAL_DAMAGE)
+        eqs = MisesValue<double, DIM>(L, eps);
+    const double kh = a.kappa[NG_IDX(e * NIP + q, n * NIP, 7)];
+    const double kap = KIND == NUTO_GPU_MB_LINEAR_ELASTIC ? 0. : fmax(kh, eqs);
+    const double omega = KIND == NUTO_GPU_MB_LINEAR_ELASTIC ? 0. : DamageOmega<double>(L, kap);
+    const int w = (quantity == NUTO_GPU_IP_STRAIN || quantity == NUTO_GPU_IP_STRESS) ? VD : 1;
+    double* o = out + it * w;
+    if (quantity == NUTO_GPU_IP_KAPPA)
+        o[0] = kap;
+    else if (quantity == NUTO_GPU_IP_DAMAGE)
+        o[0] = omega;
+    else if (quantity == NUTO_GPU_IP_EEQ)
+        o[0] = KIND == NUTO_GPU_MB_LINEAR_ELASTIC ? MisesValue<double, DIM>(L, eps) : eqs;
+    else if (quantity == NUTO_GPU_IP_STRAIN)
+    {
+#pragma unroll
+        for (int r = 0; r < VD; ++r)
+            o[r] = eps[r];
+    }
+    else
+    {
+        double sig[VD];
+        if (KIND == NUTO_GPU_MB_LINEAR_ELASTIC)
+            ElasticStress<double, DIM>(L, eps, sig);
+        else
+            LedStress<double, DIM>(L, eps, omega, sig);
+#pragma unroll
+        for (int r = 0; r < VD; ++r)
+            o[r] = sig[r];
+    }
+}
+
+int IpWidth(const Ctx& c, int quantity)
+{
+    return (quantity == NUTO_GPU_IP_STRAIN || quantity == NUTO_GPU_IP_STRESS) ? (c.dim == 2 ? 3 : 6) : 1;
+}
+
+void LaunchEvalIp(Ctx& c, const double* u, int quantity, double* out)
+{
+    CellArgs a = MakeCellArgs(c);
+    const int64_t items = c.nCells * c.ip.nIp;
+    const int blocks = static_cast<int>((items + 127) / 128);
+    DispatchCfg(c, [&](auto cfg) {
+        using C = decltype(cfg);
+        k_eval_ip<C::dim, C::nd, C::nip, C::kind><<<blocks, 128, 0, c.stream>>>(a, c.law, u, quantity, out);
+    });
+    AfterLaunch(c, "k_eval_ip");
+    c.stats.kernel_launches += 1;
+}
+
 // ---- scatter of caller-given cell results (SimpleAssembler scatter, SimpleAssembler.cpp:53-59, 118-137) -----
 struct SlotView
 {

@@ -301,6 +301,9 @@ void LaunchResidual(Ctx& c, const double* u, double* f);
 void LaunchTangent(Ctx& c, const double* u, int precision, void* values);
 void LaunchTangentNoAlloc(Ctx& c, const double* u, float* values);
 void LaunchHistory(Ctx& c, const double* u);
+void LaunchLumpedMass(Ctx& c, double rho, double* m);
+void LaunchEvalIp(Ctx& c, const double* u, int quantity, double* out);
+int IpWidth(const Ctx& c, int quantity);
 void LaunchCellVectors(Ctx& c, const double* fe, double* f);
 void LaunchCellMatrices(Ctx& c, const double* ke, int precision, void* values);
 int SolveLinear(Ctx& c, int precision, int method, const void* values, const double* b, double* x, double rtol,

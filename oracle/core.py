@@ -100,6 +100,10 @@ def lib():
                 "oracle_matrix_copy": (None, [vp, P(ll), P(i), P(d)]),
                 "oracle_matrix_release": (None, [vp]),
                 "oracle_update_history": (None, [vp, P(d)]),
+                "oracle_lumped_mass": (None, [vp, d, P(d)]),
+                "oracle_lump_hrz": (None, [P(d), i, i, P(d)]),
+                "oracle_ip_width": (i, [vp, i]),
+                "oracle_eval_ip": (None, [vp, P(d), i, P(d)]),
                 "oracle_cell_nlocal": (i, [vp]),
                 "oracle_cell_dofs": (None, [vp, i, P(ll)]),
                 "oracle_cell_integrate": (None, [vp, i, P(d), P(d), P(d)]),
@@ -280,6 +284,20 @@ class Problem:
         u = np.ascontiguousarray(u, dtype=np.float64)
         self.L.oracle_update_history(self.h, _dp(u))
 
+    def lumped_mass(self, rho):
+        """BuildDiagonallyLumpedMatrix of DynamicMomentumBalance::Hessian2 (combined layout)."""
+        m = np.empty(self.n_dofs)
+        self.L.oracle_lumped_mass(self.h, float(rho), _dp(m))
+        return m
+
+    def eval_ip(self, u, quantity):
+        """Cell::Eval of IP_KAPPA / IP_DAMAGE / IP_STRAIN / IP_STRESS / IP_EEQ: (n_el, n_ip, width)."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        w = int(self.L.oracle_ip_width(self.h, quantity))
+        out = np.empty((self.n_el, self.n_ip, w))
+        self.L.oracle_eval_ip(self.h, _dp(u), quantity, _dp(out))
+        return out
+
     def cell_dofs(self, cell):
         out = np.empty(self.n_local, dtype=np.int64)
         self.L.oracle_cell_dofs(self.h, cell, _llp(out))
@@ -354,3 +372,16 @@ def local_damage(dim, E, nu, app, plane_state, kappa0, beta, alpha, k, kappa_his
     lib().oracle_local_damage(dim, E, nu, app, plane_state, kappa0, beta, alpha, k, kappa_hist, _dp(strain), _dp(s),
                               _dp(t))
     return s, t.reshape(vd, vd)
+
+
+IP_KAPPA, IP_DAMAGE, IP_STRAIN, IP_STRESS, IP_EEQ = 0, 1, 2, 3, 4
+
+
+def lump_hrz(M, ncomp):
+    """SimpleAssembler::BuildDiagonallyLumpedMatrix of one local block (SimpleAssembler.cpp:83-87)."""
+    M = np.ascontiguousarray(M, dtype=np.float64)
+    nl = M.shape[0]
+    out = np.empty(nl)
+    lib().oracle_lump_hrz(_dp(M), nl, ncomp, _dp(out))
+    return out
+

@@ -744,6 +744,16 @@ enum IntegrandKind
     GRADIENT_DAMAGE = 2 // GradientDamage<D, Constant|Decreasing, DamageLawExponential>
 };
 
+// integration-point quantities of EvalIp (Cell::Eval post-processing)
+enum IpQuantity
+{
+    IP_KAPPA = 0,
+    IP_DAMAGE = 1,
+    IP_STRAIN = 2,
+    IP_STRESS = 3,
+    IP_EEQ = 4
+};
+
 struct IntegrandParams
 {
     int kind;
@@ -1287,7 +1297,162 @@ struct Problem
             }
         }
     }
+
+    //! DynamicMomentumBalance::Hessian2 (DynamicMomentumBalance.h:22-30) integrated over cell e: the (disp, disp)
+    //! block rho N^T N det J w summed over the integration points (Cell.h:105-119), n_en*ncomp square, row-major.
+    void MassCell(int e, double rho, std::vector<double>& M) const
+    {
+        const Mesh& m = *mesh;
+        const DofLayer& Ld = m.layers[slots[0]];
+        const int nl = Ld.nEn * Ld.ncomp;
+        M.assign(static_cast<size_t>(nl) * nl, 0.);
+        double X[60];
+        m.ElementCoords(e, X);
+        for (int ip = 0; ip < q.n; ++ip)
+        {
+            const double* xi = q.points[ip].data();
+            double Ng[20], dNg[60];
+            Shape(m.geoInterp, xi, Ng, dNg);
+            const Jacobian jac = ComputeJacobian(m.dim, m.nGeoEn, X, dNg);
+            double Nd[20], dNd[60];
+            Shape(Ld.interp, xi, Nd, dNd);
+            const Mat N = NMatrix(Nd, Ld.nEn, Ld.ncomp);
+            const Mat NtN = Mul(T(N), N);
+            const double fac = jac.det * q.weights[ip];
+            for (int i = 0; i < nl * nl; ++i)
+                M[i] += NtN.v[i] * rho * fac;
+        }
+    }
+
+    //! Values at every integration point of cell e (Cell::Eval, Cell.h:80-93), for post-processing:
+    //! IP_KAPPA GradientDamage::Kappa / EvolutionImplicit kappa, IP_DAMAGE omega(kappa), IP_STRAIN Nabla::Strain,
+    //! IP_STRESS the law's stress, IP_EEQ the nonlocal eeq (gradient damage) or the local equivalent strain.
+    //! out: q.n x IpWidth(quantity)
+    int IpWidth(int quantity) const
+    {
+        return (quantity == IP_STRAIN || quantity == IP_STRESS) ? VoigtDim(mesh->dim) : 1;
+    }
+    void EvalCell(int e, const double* u, int quantity, double* out) const
+    {
+        const Mesh& m = *mesh;
+        const int dim = m.dim;
+        const int vd = VoigtDim(dim);
+        const int w = IpWidth(quantity);
+        double X[60];
+        m.ElementCoords(e, X);
+        std::vector<int64_t> dofs;
+        CellDofs(e, dofs);
+        const DofLayer& Ld = m.layers[slots[0]];
+        const bool gd = p.kind == GRADIENT_DAMAGE;
+        for (int ip = 0; ip < q.n; ++ip)
+        {
+            const double* xi = q.points[ip].data();
+            double Ng[20], dNg[60];
+            Shape(m.geoInterp, xi, Ng, dNg);
+            const Jacobian jac = ComputeJacobian(dim, m.nGeoEn, X, dNg);
+            double Nd[20], dNd[60], g[60];
+            Shape(Ld.interp, xi, Nd, dNd);
+            GlobalDerivatives(jac, Ld.nEn, dNd, g);
+            const Mat Bd = BStrain(dim, Ld.nEn, g);
+            double strain[6] = {0, 0, 0, 0, 0, 0};
+            for (int r = 0; r < vd; ++r)
+                for (int j = 0; j < Ld.nEn * dim; ++j)
+                    strain[r] += Bd(r, j) * u[dofs[localOffset[0] + j]];
+            const double kh = kappa[static_cast<size_t>(e) * q.n + ip];
+            double eqs = 0;
+            if (gd)
+            {
+                const DofLayer& Le = m.layers[slots[1]];
+                double Ne[20], dNe[60];
+                Shape(Le.interp, xi, Ne, dNe);
+                for (int nn = 0; nn < Le.nEn; ++nn)
+                    eqs += Ne[nn] * u[dofs[localOffset[1] + nn]];
+            }
+            else if (p.kind == MB_LOCAL_DAMAGE)
+                eqs = norm.Value(strain);
+            const double kap = p.kind == MB_LINEAR_ELASTIC ? 0. : std::max(kh, eqs);
+            const double omega = p.kind == MB_LINEAR_ELASTIC ? 0. : dmg.Damage(kap);
+            double* o = out + static_cast<size_t>(ip) * w;
+            switch (quantity)
+            {
+            case IP_KAPPA:
+                o[0] = kap;
+                break;
+            case IP_DAMAGE:
+                o[0] = omega;
+                break;
+            case IP_EEQ:
+                o[0] = p.kind == MB_LINEAR_ELASTIC ? norm.Value(strain) : eqs;
+                break;
+            case IP_STRAIN:
+                for (int r = 0; r < vd; ++r)
+                    o[r] = strain[r];
+                break;
+            case IP_STRESS:
+                if (p.kind == MB_LINEAR_ELASTIC)
+                    for (int r = 0; r < vd; ++r)
+                    {
+                        o[r] = 0;
+                        for (int c = 0; c < vd; ++c)
+                            o[r] += Cel(r, c) * strain[c];
+                    }
+                else
+                    led.Stress(strain, omega, o);
+                break;
+            }
+        }
+    }
 };
+
+//! SimpleAssembler::BuildDiagonallyLumpedMatrix (SimpleAssembler.cpp:67-98) for one local block of one DOF type:
+//! the diagonal scaled by (sum of all entries / sum of the diagonal) / number of components (DofType::GetNum).
+inline void LumpHRZ(const double* M, int nl, int ncomp, double* out)
+{
+    double diagSum = 0, fullSum = 0;
+    for (int i = 0; i < nl; ++i)
+        diagSum += M[static_cast<size_t>(i) * nl + i];
+    for (int i = 0; i < nl * nl; ++i)
+        fullSum += M[i];
+    for (int i = 0; i < nl; ++i)
+        out[i] = M[static_cast<size_t>(i) * nl + i] * ((fullSum / diagSum) / ncomp);
+}
+
+//! BuildDiagonallyLumpedMatrix of DynamicMomentumBalance::Hessian2 over all cells into the combined vector
+//! (displacement rows; the other slots stay zero), per-thread partial vectors summed at the end.
+inline void BuildLumpedMass(const Problem& P, double rho, double* mvec)
+{
+    const int64_t n = P.nDofs;
+    for (int64_t i = 0; i < n; ++i)
+        mvec[i] = 0;
+    const DofLayer& Ld = P.mesh->layers[P.slots[0]];
+    const int nl = Ld.nEn * Ld.ncomp;
+#pragma omp parallel
+    {
+        std::vector<double> local(n, 0.), M, lump(nl);
+        std::vector<int64_t> dofs;
+#pragma omp for nowait
+        for (int e = 0; e < P.mesh->nEl; ++e)
+        {
+            P.MassCell(e, rho, M);
+            LumpHRZ(M.data(), nl, Ld.ncomp, lump.data());
+            P.CellDofs(e, dofs);
+            for (int i = 0; i < nl; ++i)
+                local[dofs[P.localOffset[0] + i]] += lump[i];
+        }
+#pragma omp critical
+        for (int64_t i = 0; i < n; ++i)
+            mvec[i] += local[i];
+    }
+}
+
+//! Cell::Eval of one quantity at every integration point of every cell: out is nEl x nIp x width
+inline void EvalIp(const Problem& P, const double* u, int quantity, double* out)
+{
+    const int w = P.IpWidth(quantity);
+#pragma omp parallel for
+    for (int e = 0; e < P.mesh->nEl; ++e)
+        P.EvalCell(e, u, quantity, out + static_cast<size_t>(e) * P.q.n * w);
+}
 
 // ------------------------------------------------------------------------------------------------
 // Assembly: SimpleAssembler::BuildVector (SimpleAssembler.cpp:38-65) and ::BuildMatrix (:100-156) with

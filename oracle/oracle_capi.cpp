@@ -194,6 +194,26 @@ void oracle_update_history(void* prob, const double* u)
     static_cast<ProblemBox*>(prob)->P.UpdateHistory(u);
 }
 
+void oracle_lumped_mass(void* prob, double rho, double* m)
+{
+    BuildLumpedMass(static_cast<ProblemBox*>(prob)->P, rho, m);
+}
+
+void oracle_lump_hrz(const double* M, int nl, int ncomp, double* out)
+{
+    LumpHRZ(M, nl, ncomp, out);
+}
+
+int oracle_ip_width(void* prob, int quantity)
+{
+    return static_cast<ProblemBox*>(prob)->P.IpWidth(quantity);
+}
+
+void oracle_eval_ip(void* prob, const double* u, int quantity, double* out)
+{
+    EvalIp(static_cast<ProblemBox*>(prob)->P, u, quantity, out);
+}
+
 int oracle_cell_nlocal(void* prob)
 {
     return static_cast<ProblemBox*>(prob)->P.nLocal;

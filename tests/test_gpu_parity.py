@@ -361,6 +361,8 @@ def test_multigrid_sweep_graph_matches_kernel_launches(precision, monkeypatch):
     """The multigrid sweep replayed as a CUDA graph and launched kernel by kernel (NUTO_GPU_GRAPHS=0) give the same
     GMRES solution (up to the order of the atomic restriction sums) and iteration count within one restart."""
     _torch()
+    from nuto_gb300 import configs
+
     rng = np.random.default_rng(12)
     b = None
     out = {}
@@ -368,7 +370,10 @@ def test_multigrid_sweep_graph_matches_kernel_launches(precision, monkeypatch):
         monkeypatch.setenv("NUTO_GPU_GRAPHS", graphs)
         s, g, (om, layers, P, cons) = _build("hex8gd", 8)
         if b is None:
-            u, kappa = _damage_state("hex8gd", P, rng)
+            # a well-posed damaged tangent: elastic displacements and the two pre-damaged middle layers
+            u = _state(P, rng, 1e-6)
+            u[3 * P.mesh.layer_num_nodes(0):] = 0.0
+            kappa = configs.gradient_damage_imperfection(8, g.n_ip)
             b = rng.uniform(-1, 1, P.n_dofs)
         g.history = kappa
         vals = g.build_matrix(u, precision)
@@ -378,3 +383,32 @@ def test_multigrid_sweep_graph_matches_kernel_launches(precision, monkeypatch):
     (x1, it1), (x0, it0) = out["1"], out["0"]
     assert np.abs(x1 - x0).max() <= 1e-5 * np.abs(x0).max()
     assert abs(it1 - it0) <= 40
+
+
+@pytest.mark.parametrize("kind,n", CASES)
+def test_lumped_mass(kind, n):
+    """BuildDiagonallyLumpedMatrix of DynamicMomentumBalance::Hessian2 on the GPU against the oracle (FP64)."""
+    _torch()
+    s, g, (om, layers, P, cons) = _build(kind, n)
+    ref = P.lumped_mass(2.5)
+    m = g.lumped_mass(2.5).cpu().numpy()
+    assert np.abs(m - ref).max() <= FP64_REL * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("kind,n", [("quad4", 5), ("hex8gd", 3), ("hex20", 2)])
+def test_eval_ip(kind, n):
+    """Cell::Eval post-processing values (kappa, damage, strain, stress, equivalent strain) against the oracle."""
+    _torch()
+    from oracle import core
+
+    rng = np.random.default_rng(17)
+    s, g, (om, layers, P, cons) = _build(kind, n)
+    u, kappa = _damage_state(kind, P, rng)
+    if kappa is not None:
+        P.kappa = kappa
+        g.history = kappa
+    for q in (core.IP_KAPPA, core.IP_DAMAGE, core.IP_STRAIN, core.IP_STRESS, core.IP_EEQ):
+        ref = P.eval_ip(u, q)
+        got = g.eval_ip(u, q).cpu().numpy()
+        assert got.shape == ref.shape, q
+        assert np.abs(got - ref).max() <= FP64_REL * max(np.abs(ref).max(), 1e-300), q

@@ -386,3 +386,65 @@ def test_build_vector_matches_cellwise_scatter(oracle_lib):
         idx = P.cell_dofs(c)
         Kref[np.ix_(idx, idx)] += Ke
     assert np.abs(K - Kref).max() <= 1e-13 * np.abs(Kref).max()
+
+
+def test_lumped_mass_hrz_known_answer():
+    """test/mechanics/cell/SimpleAssembler.cpp:116-150: two cells [0,1,2] and [2,3,4] with the local matrix
+    11..33 on a one-component DOF type: diagonal scaled by total / diagonal sum, summed at the shared DOF."""
+    from oracle import core
+
+    M = np.array([[11, 12, 13], [21, 22, 23], [31, 32, 33]], dtype=float)
+    lump = core.lump_hrz(M, 1)
+    total = M.sum()
+    expect = np.array([11.0, 22.0, 33.0]) * (total / (11.0 + 22.0 + 33.0))
+    assert np.allclose(lump, expect, rtol=1e-15)
+    glob = np.zeros(5)
+    glob[[0, 1, 2]] += lump
+    glob[[2, 3, 4]] += lump
+    assert np.allclose(glob, [expect[0], expect[1], expect[2] + expect[0], expect[1], expect[2]], rtol=1e-15)
+    # the DofType::GetNum division: a block with ncomp components sharing the scalar pattern
+    assert np.allclose(core.lump_hrz(np.kron(M, np.eye(3)), 3), np.repeat(expect, 3) / 3, rtol=1e-14)
+
+
+@pytest.mark.parametrize("kind,n", [("quad4", 4), ("hex8gd", 2), ("hex20", 2)])
+def test_lumped_mass_total_is_rho_volume_over_components(kind, n):
+    from oracle import setups
+
+    om, layers, P, cons = {"quad4": setups.quad4_elastic, "hex8gd": setups.hex8_gradient_damage,
+                           "hex20": setups.hex20_local_damage}[kind](n)
+    rho = 2.5
+    m = P.lumped_mass(rho)
+    volume = {"quad4": 1.0, "hex8gd": 4.0, "hex20": 1.0}[kind]
+    ncomp = 2 if kind == "quad4" else 3
+    n_disp = ncomp * om.layer_num_nodes(layers[0])
+    assert abs(m[:n_disp].sum() - rho * volume) <= 1e-12 * rho * volume
+    for c in range(ncomp):
+        assert abs(m[c:n_disp:ncomp].sum() - rho * volume / ncomp) <= 1e-12 * rho * volume
+    assert np.all(m[n_disp:] == 0.0)
+    assert np.all(m[:n_disp] > 0)  # HRZ scales the positive diagonal (unlike row-sum lumping of Hex20)
+
+
+def test_eval_ip_consistency():
+    """Cell::Eval values: kappa after UpdateHistory equals the history, elastic stress is C eps, damage is
+    omega(kappa)."""
+    from oracle import core, setups
+
+    om, layers, P, cons = setups.hex8_gradient_damage(2)
+    rng = np.random.default_rng(3)
+    u = rng.uniform(-2e-4, 2e-4, P.n_dofs)
+    nd = 3 * om.layer_num_nodes(layers[0])
+    u[nd:] = rng.uniform(0, 4e-4, P.n_dofs - nd)
+    P.kappa = rng.uniform(0, 3e-4, (P.n_el, P.n_ip))
+    kap = P.eval_ip(u, core.IP_KAPPA)[..., 0]
+    P.update_history(u)
+    assert np.array_equal(kap, P.kappa)
+    om_ = P.eval_ip(u, core.IP_DAMAGE)[..., 0]
+    k0, beta, alpha = 1e-4, 100.0, 0.99
+    ref = np.where(kap < k0, 0.0, 1 - k0 / kap * (1 - alpha + alpha * np.exp(beta * (k0 - kap))))
+    assert np.allclose(om_, ref, rtol=1e-13, atol=1e-16)
+    omq, layq, Pq, _ = setups.quad4_elastic(3)
+    uq = rng.uniform(-1e-3, 1e-3, Pq.n_dofs)
+    eps = Pq.eval_ip(uq, core.IP_STRAIN)
+    sig = Pq.eval_ip(uq, core.IP_STRESS)
+    C = core.linear_elastic_C(2, 30000.0, 0.2, core.PLANE_STRAIN)
+    assert np.allclose(sig, eps @ C.T, rtol=1e-13, atol=1e-12)
