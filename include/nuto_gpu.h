@@ -30,6 +30,9 @@
  *   nuto_gpu_update_history     TimeDependentProblem::UpdateHistory      nuto/mechanics/tools/TimeDependentProblem.cpp:78-85
  *   nuto_gpu_build_lumped_mass  SimpleAssembler::BuildDiagonallyLumpedMatrix + DynamicMomentumBalance::Hessian2
  *                                                                        nuto/mechanics/cell/SimpleAssembler.cpp:67-98
+ *   nuto_gpu_add_boundary_cells / nuto_gpu_build_external_load
+ *                               NeumannBc::ExternalLoad on boundary cells nuto/mechanics/integrands/NeumannBc.h:28-36
+ *   nuto_gpu_set_constant_gradient  a constant gradient function          nuto/mechanics/tools/TimeDependentProblem.cpp:56-66
  *   nuto_gpu_eval_ip            Cell::Eval (post-processing of kappa, damage, strain, stress) nuto/mechanics/cell/Cell.h:80-93
  *   nuto_gpu_assemble_cell_vectors / _matrices
  *                               the scatter half of SimpleAssembler::BuildVector/BuildMatrix for caller-given cell
@@ -208,6 +211,20 @@ int nuto_gpu_update_history(nuto_gpu_ctx* ctx, const double* d_u);
    per cell the diagonal of rho N^T N det J w, scaled by (sum of all entries / sum of the diagonal) / components,
    summed into d_m (combined layout; the displacement rows, zero elsewhere). */
 int nuto_gpu_build_lumped_mass(nuto_gpu_ctx* ctx, double rho, double* d_m);
+/* Boundary cells for NeumannBc<D>::ExternalLoad (nuto/mechanics/integrands/NeumannBc.h:28-36): Line2 faces in 2D
+   or Quad4 faces in 3D on the context's coordinate nodes (coord_conn, n_faces x nodes_per_face) and on the DOF
+   nodes of a displacement slot (dof_conn), integrated with the codimension-1 Jacobian of
+   nuto/mechanics/cell/Jacobian.h:51-88 and a tensor Gauss rule. *group receives the group index. */
+int nuto_gpu_add_boundary_cells(nuto_gpu_ctx* ctx, int slot, int64_t n_faces, int nodes_per_face,
+                                const int32_t* coord_conn, const int32_t* dof_conn, int gauss_points_per_direction,
+                                int* group);
+/* f = sum over the group's cells of ExternalLoad = N^T p det J w (SimpleAssembler::BuildVector over boundary cells,
+   nuto/mechanics/cell/SimpleAssembler.cpp:38-65); traction p has dim entries (host), d_f combined layout. */
+int nuto_gpu_build_external_load(nuto_gpu_ctx* ctx, int group, const double* traction, double* d_f);
+/* A constant vector added to the residual of nuto_gpu_do_step, R = f_int(u) + g, as a u-independent gradient
+   function of TimeDependentProblem::AddGradientFunction (nuto/mechanics/tools/TimeDependentProblem.cpp:56-66)
+   would add it (e.g. g = -external load for force-driven steps). d_g == NULL removes it. */
+int nuto_gpu_set_constant_gradient(nuto_gpu_ctx* ctx, const double* d_g);
 /* Values at every integration point for post-processing: Cell::Eval (nuto/mechanics/cell/Cell.h:80-93) with
    GradientDamage::Kappa (nuto/mechanics/integrands/GradientDamage.h:127-130), the damage law, Nabla::Strain and the
    law's stress. d_out is n_cells x n_ip x width doubles (width: Voigt size for strain and stress, else 1). */

@@ -91,6 +91,9 @@ SIGNATURES = {
     "nuto_gpu_build_matrix_noalloc": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_build_lumped_mass": (_i, [_vp, _d, _vp]),
     "nuto_gpu_eval_ip": (_i, [_vp, _vp, _i, _vp]),
+    "nuto_gpu_add_boundary_cells": (_i, [_vp, _i, _i64, _i, _vp, _vp, _i, _P(_i)]),
+    "nuto_gpu_build_external_load": (_i, [_vp, _i, _vp, _vp]),
+    "nuto_gpu_set_constant_gradient": (_i, [_vp, _vp]),
     "nuto_gpu_update_history": (_i, [_vp, _vp]),
     "nuto_gpu_assemble_cell_vectors": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_assemble_cell_matrices": (_i, [_vp, _vp, _i, _vp]),

@@ -161,6 +161,34 @@ class GpuCellGroup:
         self._call("nuto_gpu_build_lumped_mass", float(rho), _ptr(m))
         return m
 
+    def add_boundary_cells(self, face_coord_conn, face_dof_conn, gauss=2, slot=0):
+        """Boundary cells (Line2 in 2D, Quad4 in 3D) for NeumannBc loads; returns the group index."""
+        fc = np.ascontiguousarray(face_coord_conn, dtype=np.int32)
+        fd = np.ascontiguousarray(face_dof_conn, dtype=np.int32)
+        grp = ctypes.c_int()
+        self._call("nuto_gpu_add_boundary_cells", int(slot), fc.shape[0], fc.shape[1], _ptr(fc), _ptr(fd), int(gauss),
+                   ctypes.byref(grp))
+        return grp.value
+
+    def external_load(self, group, traction, out=None):
+        """Sum of NeumannBc::ExternalLoad over a boundary cell group (combined layout, on the device)."""
+        torch = _torch()
+        p = np.ascontiguousarray(traction, dtype=np.float64)
+        f = out if out is not None else torch.empty(self.n_dofs, dtype=torch.float64,
+                                                    device=torch.device("cuda", self.device))
+        self._call("nuto_gpu_build_external_load", int(group), _ptr(p), _ptr(f))
+        return f
+
+    def set_constant_gradient(self, g):
+        """A constant vector added to the residual of do_step (None removes it)."""
+        torch = _torch()
+        if g is None:
+            self._call("nuto_gpu_set_constant_gradient", None)
+            return
+        g = self._dev(g, torch.float64)
+        self._call("nuto_gpu_set_constant_gradient", _ptr(g))
+        torch.cuda.synchronize()
+
     def eval_ip(self, u, quantity):
         """Cell::Eval of an IP_* quantity at every integration point: (n_cells, n_ip, width) on the device."""
         torch = _torch()

@@ -873,6 +873,75 @@ int nuto_gpu_build_lumped_mass(nuto_gpu_ctx* ctx, double rho, double* m)
     });
 }
 
+int nuto_gpu_add_boundary_cells(nuto_gpu_ctx* ctx, int slot, int64_t nFaces, int nodesPerFace,
+                                const int32_t* coordConn, const int32_t* dofConn, int gauss, int* group)
+{
+    return Guard(ctx, [&] {
+        NG_CHECK(ctx->haveCells, NUTO_GPU_ESTATE, "set_cells first");
+        NG_CHECK(slot >= 0 && slot < static_cast<int>(ctx->slots.size()), NUTO_GPU_EINVAL, "unknown slot");
+        const Slot& S = ctx->slots[slot];
+        NG_CHECK(S.ncomp == ctx->dim, NUTO_GPU_EINVAL, "boundary loads act on a displacement slot (ncomp == dim)");
+        NG_CHECK((ctx->dim == 2 && nodesPerFace == 2) || (ctx->dim == 3 && nodesPerFace == 4), NUTO_GPU_EINVAL,
+                 "boundary cells are Line2 in 2D and Quad4 in 3D");
+        NG_CHECK(gauss >= 1 && gauss <= 3, NUTO_GPU_EINVAL, "1..3 Gauss points per direction supported");
+        NG_CHECK(nFaces > 0 && coordConn && dofConn, NUTO_GPU_EINVAL, "empty boundary cell group");
+        for (int64_t i = 0; i < nFaces * nodesPerFace; ++i)
+        {
+            NG_CHECK(coordConn[i] >= 0 && coordConn[i] < ctx->nCoord, NUTO_GPU_EINVAL,
+                     "boundary coordinate connectivity out of range");
+            NG_CHECK(dofConn[i] >= 0 && dofConn[i] < S.nNodes, NUTO_GPU_EINVAL, "boundary DOF connectivity out of range");
+        }
+        BoundaryGroup B;
+        B.slot = slot;
+        B.nfe = nodesPerFace;
+        B.nFaces = nFaces;
+        Upload(B.coordConnT, Planar(std::vector<int32_t>(coordConn, coordConn + nFaces * nodesPerFace), nFaces,
+                                    nodesPerFace));
+        Upload(B.dofConnT,
+               Planar(std::vector<int32_t>(dofConn, dofConn + nFaces * nodesPerFace), nFaces, nodesPerFace));
+        std::vector<double> pts, w;
+        Gauss1D(gauss, pts, w);
+        B.nq = gauss;
+        for (int i = 0; i < gauss; ++i)
+        {
+            B.gp[i] = pts[i];
+            B.gw[i] = w[i];
+        }
+        ctx->boundary.push_back(std::move(B));
+        if (group)
+            *group = static_cast<int>(ctx->boundary.size()) - 1;
+        return NUTO_GPU_OK;
+    });
+}
+
+int nuto_gpu_build_external_load(nuto_gpu_ctx* ctx, int group, const double* traction, double* f)
+{
+    return Guard(ctx, [&] {
+        NG_CHECK(group >= 0 && group < static_cast<int>(ctx->boundary.size()), NUTO_GPU_EINVAL,
+                 "unknown boundary cell group");
+        NG_CHECK(traction, NUTO_GPU_EINVAL, "traction vector missing");
+        LaunchExternalLoad(*ctx, ctx->boundary[group], traction, f);
+        return NUTO_GPU_OK;
+    });
+}
+
+int nuto_gpu_set_constant_gradient(nuto_gpu_ctx* ctx, const double* g)
+{
+    return Guard(ctx, [&] {
+        if (!g)
+        {
+            ctx->dConstGrad.free();
+            return NUTO_GPU_OK;
+        }
+        NG_CHECK(ctx->nDofs > 0, NUTO_GPU_ESTATE, "add the DOF types first");
+        if (ctx->dConstGrad.n != static_cast<size_t>(ctx->nDofs))
+            ctx->dConstGrad.alloc(ctx->nDofs);
+        NG_CUDA(cudaMemcpyAsync(ctx->dConstGrad.p, g, ctx->nDofs * sizeof(double), cudaMemcpyDeviceToDevice,
+                                ctx->stream));
+        return NUTO_GPU_OK;
+    });
+}
+
 int nuto_gpu_eval_ip(nuto_gpu_ctx* ctx, const double* u, int quantity, double* out)
 {
     return Guard(ctx, [&] {

@@ -1277,6 +1277,138 @@ void LaunchLumpedMass(Ctx& c, double rho, double* m)
     c.stats.kernel_launches += 1;
 }
 
+// ---- boundary loads: NeumannBc<D>::ExternalLoad (NeumannBc.h:28-36) summed by SimpleAssembler::BuildVector -------
+// One thread per face: f(node, c) += N_node p_c det J w with the codimension-1 Jacobian (Jacobian.h:51-88):
+// det J = |dx/dxi| for Line2 faces in 2D, |dx/dxi x dx/deta| for Quad4 faces in 3D.
+struct FaceArgs
+{
+    int64_t nFaces, nCoord, nNodes, nDofs;
+    const int32_t* coordConn; // planar [i][face]
+    const int32_t* dofConn;
+    const double* coords;
+    const int64_t* gdof;
+    int nq;
+    double gp[3], gw[3];
+    double p[3];
+};
+
+template <int DIM, int NFE>
+__global__ void __launch_bounds__(128) k_external_load(FaceArgs A, double* __restrict__ f)
+{
+    const int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (e >= A.nFaces)
+        return;
+    double X[NFE][DIM];
+#pragma unroll
+    for (int i = 0; i < NFE; ++i)
+    {
+        const int32_t cn = A.coordConn[NG_IDX(static_cast<int64_t>(i) * A.nFaces + e, NFE * A.nFaces, 11)];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            X[i][d] = A.coords[NG_IDX(static_cast<int64_t>(cn) * DIM + d, A.nCoord * DIM, 12)];
+    }
+    double fe[NFE][DIM];
+#pragma unroll
+    for (int i = 0; i < NFE; ++i)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            fe[i][d] = 0;
+    const int nq2 = DIM == 2 ? 1 : A.nq;
+    for (int qb = 0; qb < nq2; ++qb)
+        for (int qa = 0; qa < A.nq; ++qa)
+        {
+            // tensor Gauss point, first coordinate fastest (IntegrationTypeTensorProduct.cpp:28-38)
+            const double r = A.gp[qa], t = DIM == 2 ? 0. : A.gp[qb];
+            const double w = DIM == 2 ? A.gw[qa] : A.gw[qa] * A.gw[qb];
+            double N[NFE], dN[NFE][2];
+            if (NFE == 2)
+            {
+                N[0] = 0.5 * (1. - r);
+                N[1] = 0.5 * (1. + r);
+                dN[0][0] = -0.5;
+                dN[1][0] = 0.5;
+                dN[0][1] = dN[1][1] = 0;
+            }
+            else
+            {
+                const double sr[4] = {-1, 1, 1, -1}, ss[4] = {-1, -1, 1, 1};
+#pragma unroll
+                for (int i = 0; i < NFE; ++i)
+                {
+                    N[i] = 0.25 * (1. + sr[i] * r) * (1. + ss[i] * t);
+                    dN[i][0] = 0.25 * sr[i] * (1. + ss[i] * t);
+                    dN[i][1] = 0.25 * ss[i] * (1. + sr[i] * r);
+                }
+            }
+            double J[DIM][2];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+            {
+                J[d][0] = J[d][1] = 0;
+#pragma unroll
+                for (int i = 0; i < NFE; ++i)
+                {
+                    J[d][0] += X[i][d] * dN[i][0];
+                    J[d][1] += X[i][d] * dN[i][1];
+                }
+            }
+            double detJ;
+            if (DIM == 2)
+                detJ = sqrt(J[0][0] * J[0][0] + J[1][0] * J[1][0]);
+            else
+            {
+                const double c0 = J[1][0] * J[2 % DIM][1] - J[2 % DIM][0] * J[1][1];
+                const double c1 = J[2 % DIM][0] * J[0][1] - J[0][0] * J[2 % DIM][1];
+                const double c2 = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+                detJ = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+            }
+            const double fac = detJ * w;
+#pragma unroll
+            for (int i = 0; i < NFE; ++i)
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    fe[i][d] += N[i] * A.p[d] * fac;
+        }
+#pragma unroll
+    for (int i = 0; i < NFE; ++i)
+    {
+        const int32_t dn = A.dofConn[NG_IDX(static_cast<int64_t>(i) * A.nFaces + e, NFE * A.nFaces, 13)];
+        const int64_t g = A.gdof[NG_IDX(dn, A.nNodes, 14)];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            atomicAdd(f + NG_IDX(g + d, A.nDofs, 15), fe[i][d]);
+    }
+}
+
+void LaunchExternalLoad(Ctx& c, const BoundaryGroup& B, const double* p, double* f)
+{
+    NG_CUDA(cudaMemsetAsync(f, 0, c.nDofs * sizeof(double), c.stream));
+    const Slot& S = c.slots[B.slot];
+    FaceArgs A{};
+    A.nFaces = B.nFaces;
+    A.nCoord = c.nCoord;
+    A.nNodes = S.nNodes;
+    A.nDofs = c.nDofs;
+    A.coordConn = B.coordConnT.p;
+    A.dofConn = B.dofConnT.p;
+    A.coords = c.dCoords.p;
+    A.gdof = S.dGdof.p;
+    A.nq = B.nq;
+    for (int i = 0; i < 3; ++i)
+    {
+        A.gp[i] = B.gp[i];
+        A.gw[i] = B.gw[i];
+        A.p[i] = i < c.dim ? p[i] : 0.;
+    }
+    const unsigned blocks = static_cast<unsigned>((B.nFaces + 127) / 128);
+    if (c.dim == 2)
+        k_external_load<2, 2><<<blocks, 128, 0, c.stream>>>(A, f);
+    else
+        k_external_load<3, 4><<<blocks, 128, 0, c.stream>>>(A, f);
+    AfterLaunch(c, "k_external_load");
+    c.stats.kernel_launches += 1;
+}
+
 // ---- integration-point values for post-processing: Cell::Eval (Cell.h:80-93) -----------------------------------
 // One thread per (cell, point): strain from the cached FP64 geometry, kappa = max(kappa_h, eeq or eps_eq)
 // (GradientDamage::Kappa, GradientDamage.h:127-130; EvolutionImplicit), omega(kappa), the law's stress.

@@ -219,6 +219,19 @@ struct IpTables
 struct SolverWork;
 struct Amg;
 
+// Boundary cells of one DOF slot (NeumannBc loads): Line2 faces of a 2D mesh or Quad4 faces of a 3D mesh, on the
+// context's coordinate nodes and the slot's DOF nodes.
+struct BoundaryGroup
+{
+    int slot = 0;
+    int nfe = 0; // nodes per face
+    int64_t nFaces = 0;
+    DBuf<int32_t> coordConnT; // planar [i][face]
+    DBuf<int32_t> dofConnT;   // planar [i][face]
+    int nq = 0;               // Gauss points per direction
+    double gp[3] = {0, 0, 0}, gw[3] = {0, 0, 0};
+};
+
 struct Ctx
 {
     int device = 0;
@@ -287,6 +300,8 @@ struct Ctx
 
     SolverWork* work = nullptr;
     Amg* amg = nullptr;
+    std::vector<BoundaryGroup> boundary;
+    DBuf<double> dConstGrad; // added to the residual of nuto_gpu_do_step (empty: none)
     int precond = NUTO_GPU_PRECOND_AMG;
     uint64_t valsVersion = 1; // bumped by every tangent assembly and every caller-supplied solve
     bool syncCheck = false; // NUTO_GPU_SYNC_CHECK=1 or a checked build
@@ -302,6 +317,7 @@ void LaunchTangent(Ctx& c, const double* u, int precision, void* values);
 void LaunchTangentNoAlloc(Ctx& c, const double* u, float* values);
 void LaunchHistory(Ctx& c, const double* u);
 void LaunchLumpedMass(Ctx& c, double rho, double* m);
+void LaunchExternalLoad(Ctx& c, const BoundaryGroup& B, const double* p, double* f);
 void LaunchEvalIp(Ctx& c, const double* u, int quantity, double* out);
 int IpWidth(const Ctx& c, int quantity);
 void LaunchCellVectors(Ctx& c, const double* fe, double* f);

@@ -49,6 +49,15 @@ __global__ void k_update(int64_t n, const double* __restrict__ x0, const double*
     out[i] = x0[i] - alpha * dx[i] + (db ? db[i] : 0.);
 }
 
+// f += g: a constant gradient contribution (e.g. NeumannBc::ExternalLoad of boundary cells registered with
+// TimeDependentProblem::AddGradientFunction, TimeDependentProblem.cpp:56-66)
+__global__ void k_add(int64_t n, const double* __restrict__ g, double* __restrict__ f)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i < n)
+        f[i] += g[i];
+}
+
 namespace
 {
 struct Timers
@@ -136,6 +145,11 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     auto residual = [&](const double* x) {
         const int k = T.Begin();
         LaunchResidual(c, x, w.f.p);
+        if (c.dConstGrad.p)
+        {
+            k_add<<<gb, 256, 0, c.stream>>>(n, c.dConstGrad.p, w.f.p);
+            S.kernel_launches += 1;
+        }
         T.End(k, &S.ms_assemble_vector);
         S.residual_evaluations++;
         const double r = MaskedNorm(c, w.f.p);
@@ -191,6 +205,11 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     {
         const int k = T.Begin();
         LaunchResidual(c, x, w.f.p);
+        if (c.dConstGrad.p)
+        {
+            k_add<<<gb, 256, 0, c.stream>>>(n, c.dConstGrad.p, w.f.p);
+            S.kernel_launches += 1;
+        }
         T.End(k, &S.ms_assemble_vector);
         S.residual_evaluations++;
     }

@@ -137,3 +137,24 @@ def component_constraints(mesh, layer, nodes, directions, rhs_const=0.0, rhs_slo
     dofs = L.dof_numbers[np.asarray(nodes)[:, None], np.asarray(directions)[None, :]].ravel()
     n = dofs.size
     return (dofs.astype(np.int32), np.full(n, float(rhs_const)), np.full(n, float(rhs_slope)))
+
+
+# local node lists of the faces of the linear cells, each a valid Line2 / Quad4 order
+QUAD4_EDGES = np.array([[0, 1], [1, 2], [3, 2], [0, 3]], dtype=np.int64)
+HEX8_FACES = np.array([[0, 1, 2, 3], [4, 5, 6, 7], [0, 3, 7, 4], [1, 2, 6, 5], [0, 1, 5, 4], [3, 2, 6, 7]],
+                      dtype=np.int64)
+
+
+def boundary_faces(mesh, layer, direction, offset, tol=1e-10):
+    """Boundary cells on the plane x_direction = offset (edges of Quad4 meshes, faces of Hex8 meshes) in cell order:
+    (coordinate connectivity, DOF-node connectivity of the layer), both n_faces x nodes-per-face. The layer must use
+    the coordinate interpolation (the DOF nodes of a face are the face's coordinate nodes)."""
+    L = mesh.layers[layer]
+    faces = QUAD4_EDGES if mesh.geo_interp == QUAD4 else HEX8_FACES
+    geo = mesh.conn[:, faces]   # cells x faces x nodes-per-face
+    dof = L.conn[:, faces]
+    on = np.all(np.abs(mesh.coords[geo, direction] - offset) < tol, axis=2)
+    cells, which = np.nonzero(on)
+    return (np.ascontiguousarray(geo[cells, which], dtype=np.int32),
+            np.ascontiguousarray(dof[cells, which], dtype=np.int32))
+

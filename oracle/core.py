@@ -104,6 +104,8 @@ def lib():
                 "oracle_lump_hrz": (None, [P(d), i, i, P(d)]),
                 "oracle_ip_width": (i, [vp, i]),
                 "oracle_eval_ip": (None, [vp, P(d), i, P(d)]),
+                "oracle_external_load": (None, [vp, i, i, P(i), P(ll), P(d), i, P(d)]),
+                "oracle_neumann_ip": (None, [i, i, P(d), P(d), P(d)]),
                 "oracle_cell_nlocal": (i, [vp]),
                 "oracle_cell_dofs": (None, [vp, i, P(ll)]),
                 "oracle_cell_integrate": (None, [vp, i, P(d), P(d), P(d)]),
@@ -163,6 +165,16 @@ class Mesh:
     def scale(self, sx, sy, sz=1.0):
         self.L.oracle_mesh_scale(self.h, sx, sy, sz)
         return self
+
+    def external_load(self, n_dofs, face_coord_conn, face_dofs, traction, gauss=2):
+        """SimpleAssembler::BuildVector of NeumannBc::ExternalLoad over boundary cells (Line2 in 2D, Quad4 in 3D):
+        face_coord_conn (n_faces, nfe) coordinate nodes, face_dofs (n_faces, nfe, dim) combined DOF indices."""
+        fc = np.ascontiguousarray(face_coord_conn, dtype=np.int32)
+        fd = np.ascontiguousarray(face_dofs, dtype=np.int64)
+        p = np.ascontiguousarray(traction, dtype=np.float64)
+        f = np.zeros(n_dofs)
+        self.L.oracle_external_load(self.h, fc.shape[1], fc.shape[0], _ip(fc), _llp(fd), _dp(p), gauss, _dp(f))
+        return f
 
     def __del__(self):
         try:
@@ -383,5 +395,14 @@ def lump_hrz(M, ncomp):
     nl = M.shape[0]
     out = np.empty(nl)
     lib().oracle_lump_hrz(_dp(M), nl, ncomp, _dp(out))
+    return out
+
+
+def neumann_ip(nfe, dim, xi, traction):
+    """NeumannBc::ExternalLoad at one natural point of a boundary cell: N^T p, node-major."""
+    x = np.ascontiguousarray(np.atleast_1d(xi), dtype=np.float64)
+    p = np.ascontiguousarray(traction, dtype=np.float64)
+    out = np.empty(nfe * dim)
+    lib().oracle_neumann_ip(nfe, dim, _dp(x), _dp(p), _dp(out))
     return out
 

@@ -1445,6 +1445,93 @@ inline void BuildLumpedMass(const Problem& P, double rho, double* mvec)
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// Boundary cells: NeumannBc<D>::ExternalLoad (NeumannBc.h:28-36) on line cells in 2D and Quad4 cells in 3D, with
+// the codimension-1 Jacobian (Jacobian.h:51-88): det J = |dx/dxi| for lines, |dx/dxi x dx/deta| for surfaces.
+// ------------------------------------------------------------------------------------------------
+//! shape functions of the boundary cell (Line2 natural coordinate in [-1, 1]; Quad4 as the volume Quad4)
+inline void FaceShape(int nfe, const double* xi, double* N, double* dN /* nfe x 2 */)
+{
+    if (nfe == 2)
+    {
+        N[0] = 0.5 * (1. - xi[0]);
+        N[1] = 0.5 * (1. + xi[0]);
+        dN[0] = -0.5;
+        dN[2] = 0.5;
+        dN[1] = dN[3] = 0;
+        return;
+    }
+    double N4[4], dN4[12];
+    Shape(QUAD4, xi, N4, dN4);
+    for (int i = 0; i < 4; ++i)
+    {
+        N[i] = N4[i];
+        dN[i * 2 + 0] = dN4[i * 3 + 0];
+        dN[i * 2 + 1] = dN4[i * 3 + 1];
+    }
+}
+
+//! det J of a codimension-1 cell: X is nfe x dim, dN nfe x 2 (natural derivatives)
+inline double FaceDetJ(int dim, int nfe, const double* X, const double* dN)
+{
+    double J[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    const int nd = dim - 1;
+    for (int d = 0; d < dim; ++d)
+        for (int k = 0; k < nd; ++k)
+            for (int i = 0; i < nfe; ++i)
+                J[d][k] += X[i * dim + d] * dN[i * 2 + k];
+    if (dim == 2)
+    {
+        // extended [J | n] with n = (J1, -J0) / |J|; det J = -det(extended) = |J|
+        const double len = std::sqrt(J[0][0] * J[0][0] + J[1][0] * J[1][0]);
+        const double n0 = J[1][0] / len, n1 = -J[0][0] / len;
+        return -(J[0][0] * n1 - J[1][0] * n0);
+    }
+    // n = normalized(J_0 x J_1); det [J_0 J_1 n] = (J_0 x J_1) . n
+    const double c0 = J[1][0] * J[2][1] - J[2][0] * J[1][1];
+    const double c1 = J[2][0] * J[0][1] - J[0][0] * J[2][1];
+    const double c2 = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+    const double len = std::sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+    return (c0 * c0 + c1 * c1 + c2 * c2) / len;
+}
+
+//! NeumannBc::ExternalLoad at one integration point: N^T p (nfe x dim, node-major)
+inline void NeumannIp(int nfe, int dim, const double* N, const double* p, double* out)
+{
+    for (int i = 0; i < nfe; ++i)
+        for (int c = 0; c < dim; ++c)
+            out[i * dim + c] = N[i] * p[c];
+}
+
+//! SimpleAssembler::BuildVector of ExternalLoad over boundary cells into f (combined layout, added):
+//! faceCoordConn nFaces x nfe coordinate nodes, faceDofs nFaces x nfe x dim combined DOF indices
+inline void BuildExternalLoad(const Mesh& m, int nfe, int nFaces, const int* faceCoordConn, const int64_t* faceDofs,
+                              const double* p, int gauss, double* f)
+{
+    const int dim = m.dim;
+    const Quadrature q = TensorGauss(dim - 1, gauss);
+    std::vector<double> fe(static_cast<size_t>(nfe) * dim), ipv(static_cast<size_t>(nfe) * dim);
+    for (int e = 0; e < nFaces; ++e)
+    {
+        double X[12];
+        for (int i = 0; i < nfe; ++i)
+            for (int d = 0; d < dim; ++d)
+                X[i * dim + d] = m.coords[static_cast<size_t>(faceCoordConn[e * nfe + i]) * dim + d];
+        std::fill(fe.begin(), fe.end(), 0.);
+        for (int ip = 0; ip < q.n; ++ip)
+        {
+            double N[4], dN[8];
+            FaceShape(nfe, q.points[ip].data(), N, dN);
+            const double fac = FaceDetJ(dim, nfe, X, dN) * q.weights[ip];
+            NeumannIp(nfe, dim, N, p, ipv.data());
+            for (size_t i = 0; i < fe.size(); ++i)
+                fe[i] += ipv[i] * fac;
+        }
+        for (int i = 0; i < nfe * dim; ++i)
+            f[faceDofs[static_cast<size_t>(e) * nfe * dim + i]] += fe[i];
+    }
+}
+
 //! Cell::Eval of one quantity at every integration point of every cell: out is nEl x nIp x width
 inline void EvalIp(const Problem& P, const double* u, int quantity, double* out)
 {

@@ -214,6 +214,20 @@ void oracle_eval_ip(void* prob, const double* u, int quantity, double* out)
     EvalIp(static_cast<ProblemBox*>(prob)->P, u, quantity, out);
 }
 
+void oracle_external_load(void* mesh, int nfe, int nFaces, const int* faceCoordConn, const long long* faceDofs,
+                          const double* p, int gauss, double* f)
+{
+    std::vector<int64_t> dofs(faceDofs, faceDofs + static_cast<size_t>(nFaces) * nfe * static_cast<Mesh*>(mesh)->dim);
+    BuildExternalLoad(*static_cast<Mesh*>(mesh), nfe, nFaces, faceCoordConn, dofs.data(), p, gauss, f);
+}
+
+void oracle_neumann_ip(int nfe, int dim, const double* xi, const double* p, double* out)
+{
+    double N[4], dN[8];
+    FaceShape(nfe, xi, N, dN);
+    NeumannIp(nfe, dim, N, p, out);
+}
+
 int oracle_cell_nlocal(void* prob)
 {
     return static_cast<ProblemBox*>(prob)->P.nLocal;

@@ -412,3 +412,62 @@ def test_eval_ip(kind, n):
         got = g.eval_ip(u, q).cpu().numpy()
         assert got.shape == ref.shape, q
         assert np.abs(got - ref).max() <= FP64_REL * max(np.abs(ref).max(), 1e-300), q
+
+
+@pytest.mark.parametrize("kind", ["quad4", "hex8gd"])
+def test_external_load(kind):
+    """NeumannBc::ExternalLoad over boundary cells (Line2 edges / Quad4 faces) on the GPU against the oracle."""
+    _torch()
+    from nuto_gb300 import mesh as M
+    from oracle import core
+
+    s, g, (om, layers, P, cons) = _build(kind, 4 if kind == "quad4" else 3)
+    m = s.mesh
+    d = s.layers[0]
+    if kind == "quad4":
+        fc, fd = M.boundary_faces(m, d, 0, 1.0)
+        p = np.array([0.7, -0.2])
+    else:
+        fc, fd = M.boundary_faces(m, d, 2, 4.0)
+        p = np.array([0.1, 0.2, -1.3])
+    grp = g.add_boundary_cells(fc, fd, gauss=2)
+    f = g.external_load(grp, p).cpu().numpy()
+    L = m.layers[d]
+    omesh = core.Mesh.from_arrays(m.dim, m.geo_interp, m.coords, m.conn)
+    ref = omesh.external_load(g.n_dofs, fc, L.dof_numbers[fd], p, gauss=2)
+    assert np.abs(f - ref).max() <= FP64_REL * np.abs(ref).max()
+
+
+def test_force_driven_patch():
+    """Force-driven patch test (PatchTest.cpp:93-327 in spirit): a plane-strain square pulled by a uniform traction
+    p on its right edge, x fixed on the left edge and y at the origin; the bilinear cells reproduce the analytic
+    field u_x = (1 - nu^2) p x / E, u_y = -nu (1 + nu) p y / E exactly. The load enters nuto_gpu_do_step as the
+    constant gradient -f_ext."""
+    _torch()
+    import nuto_gb300
+    from nuto_gb300 import configs
+    from nuto_gb300 import mesh as M
+
+    m = M.create_quads(4, 4)
+    d = M.add_dof_interpolation(m, 2)
+    left = M.nodes_at_axis(m, d, 0, 0.0)
+    origin = [n for n in left if abs(m.layers[d].node_coords[n, 1]) < 1e-12]
+    cons = configs._merge(M.component_constraints(m, d, left, [0]), M.component_constraints(m, d, origin, [1]))
+    E, nu, p = 30000.0, 0.2, 3.0
+    integ = dict(kind=nuto_gb300.MB_LINEAR_ELASTIC, dim=2, E=E, nu=nu, plane_state=nuto_gb300._lib.PLANE_STRAIN,
+                 disp_slot=0)
+    s = configs.Setup("patch", m, [d], 2, integ, [cons])
+    g = s.build_gpu()
+    fc, fd = M.boundary_faces(m, d, 0, 1.0)
+    grp = g.add_boundary_cells(fc, fd, gauss=2)
+    fext = g.external_load(grp, [p, 0.0])
+    g.set_constant_gradient(-fext)
+    g.set_state(None, 0.0, True)
+    g.do_step(1.0, g.default_options(precision=64, newton_rtol=0.0, newton_atol=1e-12, krylov_rtol=1e-13))
+    x, _ = g.get_state()
+    X = m.layers[d].node_coords
+    ux = (1 - nu ** 2) * p * X[:, 0] / E
+    uy = -nu * (1 + nu) * p * X[:, 1] / E
+    u = x.reshape(-1, 2)
+    assert np.abs(u[:, 0] - ux).max() <= 1e-9 * np.abs(ux).max()
+    assert np.abs(u[:, 1] - uy).max() <= 1e-9 * np.abs(ux).max()

@@ -448,3 +448,41 @@ def test_eval_ip_consistency():
     sig = Pq.eval_ip(uq, core.IP_STRESS)
     C = core.linear_elastic_C(2, 30000.0, 0.2, core.PLANE_STRAIN)
     assert np.allclose(sig, eps @ C.T, rtol=1e-13, atol=1e-12)
+
+
+def test_neumann_known_answers():
+    """test/mechanics/integrands/NeumannBc.cpp:17-76: ExternalLoad = N^T p of a Line2 boundary cell in 2D at the
+    natural points -1, 0, +1 (all of p at the first node, half at each node, all at the second node)."""
+    from oracle import core
+
+    p = np.array([4.0, 42.0])
+    assert np.allclose(core.neumann_ip(2, 2, [-1.0], p), [4, 42, 0, 0], atol=1e-15)
+    assert np.allclose(core.neumann_ip(2, 2, [1.0], p), [0, 0, 4, 42], atol=1e-15)
+    assert np.allclose(core.neumann_ip(2, 2, [0.0], p), [2, 21, 2, 21], atol=1e-15)
+
+
+@pytest.mark.parametrize("kind", ["quad4", "hex8"])
+def test_external_load_total_force(kind):
+    """The boundary load of a uniform traction sums to traction x boundary measure (codimension-1 det J)."""
+    from oracle import core
+    from nuto_gb300 import mesh as M
+
+    if kind == "quad4":
+        m = M.create_quads(5, 3).scale(2.0, 1.5)
+        d = M.add_dof_interpolation(m, 2)
+        fc, fd = M.boundary_faces(m, d, 0, 2.0)
+        om = core.Mesh.from_arrays(2, core.QUAD4, m.coords, m.conn)
+        p, measure = np.array([0.3, -1.2]), 1.5
+    else:
+        m = M.create_bricks(3, 2, 4).scale(1.0, 2.0, 3.0)
+        d = M.add_dof_interpolation(m, 3)
+        fc, fd = M.boundary_faces(m, d, 2, 3.0)
+        om = core.Mesh.from_arrays(3, core.HEX8, m.coords, m.conn)
+        p, measure = np.array([0.3, -1.2, 2.0]), 2.0
+    L = m.layers[d]
+    dim = m.dim
+    dofs = L.dof_numbers[fd]  # faces x nodes x dim
+    f = om.external_load(L.num_dofs, fc, dofs, p, gauss=2)
+    for c in range(dim):
+        assert abs(f[c::dim].sum() - p[c] * measure) <= 1e-13 * abs(p[c] * measure)
+    assert np.count_nonzero(f) == dim * np.unique(fd).size
