@@ -98,8 +98,9 @@ def test_c4_hex20_80_full_size_properties():
         t[comp::3] = 1.0
         assert float((A @ t).abs().max()) <= 1e-11 * scale
         assert float(g.build_vector(t * 1e-3).abs().max()) <= 1e-11 * scale * 1e-3
-    # elastic state (below the damage threshold): f_int linear in u and equal to K u
-    u = torch.as_tensor(rng.uniform(-1e-6, 1e-6, nd), device=dev)
+    # elastic state (strains ~1e-7, far below the damage threshold kappa0 = 1e-4 on cells of edge 1/80):
+    # f_int linear in u and equal to K u
+    u = torch.as_tensor(rng.uniform(-1e-9, 1e-9, nd), device=dev)
     f1 = g.build_vector(u)
     f2 = g.build_vector(2.0 * u)
     fs = float(f1.abs().max())
