@@ -92,43 +92,20 @@ struct NodeSpmv
 
 constexpr int kMaxRowLen = 256; // longest row of a node (Hex20 displacements: 3 x 81)
 constexpr int kMaxComp = 3;     // components per DOF node
+constexpr int kPre = 4;         // row chunks of 32 values prefetched into registers (rows up to 128 entries)
 
-// asynchronous global -> shared copies of single values (cp.async, 4 or 8 bytes) in commit groups
-template <typename T>
-__device__ __forceinline__ void SpmvAsyncCopy(T* dst, const T* src)
-{
-    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(dst));
-    if constexpr (sizeof(T) == 4)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(src) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(src) : "memory");
-}
-
-// warps per block: 8 with FP32 values and vectors, 4 when either is FP64 (static shared memory stays <= 48 KB)
-template <typename TV, typename TX>
-struct SpmvShape
-{
-    static constexpr int warps = (sizeof(TV) == 8 || sizeof(TX) == 8) ? 4 : 8;
-};
-
-// One warp per DOF node. The node's row values (rows of a node are consecutive CSR rows of equal length) are
-// copied into shared memory with cp.async as soon as the row start is known, so that they stream from HBM while
-// the warp gathers the neighbours' x; no registers are tied up by the copies, which keeps the occupancy high.
 template <typename TV, typename TX, int NDOT>
-__global__ void __launch_bounds__(SpmvShape<TV, TX>::warps * 32) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
-                                                                           const uint8_t* __restrict__ mask,
-                                                                           const TX* __restrict__ x,
-                                                                           TX* __restrict__ y, const TX* __restrict__ w0,
-                                                                           double* sc, int* st, int fin)
+__global__ void __launch_bounds__(kBS, 5) k_spmv_node(NodeSpmv A, const TV* __restrict__ val,
+                                                    const uint8_t* __restrict__ mask, const TX* __restrict__ x,
+                                                    TX* __restrict__ y, const TX* __restrict__ w0, double* sc, int* st,
+                                                    int fin)
 {
-    constexpr int WPB = SpmvShape<TV, TX>::warps;
-    __shared__ double sh[WPB];
-    __shared__ TX xs[WPB][kMaxRowLen];
-    __shared__ TV vs[WPB][kMaxComp * kMaxRowLen];
+    __shared__ double sh[kBS / 32];
+    __shared__ TX xs[kBS / 32][kMaxRowLen];
     if (st && st[ST_STATE] != RUN)
         return;
+    const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int64_t warp = static_cast<int64_t>(blockIdx.x) * WPB + wid;
     const int I = (A.ns > 1 && warp >= A.firstWarp[1]) ? 1 : 0;
     const int64_t a = warp - A.firstWarp[I];
     const bool valid = warp < A.totalWarps && a < A.nNodes[I];
@@ -136,6 +113,7 @@ __global__ void __launch_bounds__(SpmvShape<TV, TX>::warps * 32) k_spmv_node(Nod
     double d0 = 0., d1 = 0.;
     if (valid)
     {
+        // independent loads first: neighbour ranges of every slot pair, the node's rows and block offset
         int64_t q0[kMaxSlots];
         int nn[kMaxSlots];
 #pragma unroll
@@ -152,19 +130,30 @@ __global__ void __launch_bounds__(SpmvShape<TV, TX>::warps * 32) k_spmv_node(Nod
         }
         const int64_t g0 = A.gdof[I][a];
         const int32_t seg = A.blk[I * A.ns][a]; // 0 for a whole-row operator, the block start for a block view
-        const int64_t r0 = A.rowPtr[NG_IDX(g0, A.nRows, 16)];
-        const int64_t stride = ncI > 1 ? A.rowPtr[g0 + 1] - r0 : 0; // full row length (rows of a node are equal)
+        int64_t rs[kMaxComp];
+        TX s[kMaxComp];
+#pragma unroll
+        for (int c = 0; c < kMaxComp; ++c)
+        {
+            rs[c] = c < ncI ? A.rowPtr[NG_IDX(g0 + c, A.nRows, 16)] + seg : 0;
+            s[c] = TX(0);
+        }
         const int nc0 = A.ncomp[0], nc1 = A.ns > 1 ? A.ncomp[1] : 0;
         const int len = nc0 * nn[0] + nc1 * nn[1];
-        for (int c = 0; c < ncI; ++c)
-        {
-            const int64_t rs = r0 + c * stride + seg;
-            for (int k = lane; k < len; k += 32)
-                SpmvAsyncCopy(&vs[wid][NG_IDX(c * len + k, kMaxComp * kMaxRowLen, 21)], val + NG_IDX(rs + k, A.nnz, 19));
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        // the first kPre chunks of every row go to registers before the gather, so that the value stream and the
+        // gather's dependent loads are in flight together
+        TV v[kMaxComp][kPre];
+#pragma unroll
+        for (int c = 0; c < kMaxComp; ++c)
+#pragma unroll
+            for (int k = 0; k < kPre; ++k)
+            {
+                const int q = lane + 32 * k;
+                v[c][k] = (c < ncI && q < len) ? val[NG_IDX(rs[c] + q, A.nnz, 19)] : TV(0);
+            }
         // x of the node's neighbours in the column order of its rows (both slot pairs in one pass)
         const int tot = nn[0] + nn[1];
+#pragma unroll 2
         for (int t = lane; t < tot; t += 32)
         {
             const int J = t >= nn[0] ? 1 : 0;
@@ -177,19 +166,26 @@ __global__ void __launch_bounds__(SpmvShape<TV, TX>::warps * 32) k_spmv_node(Nod
             for (int d = 0; d < ncJ; ++d)
                 xs[wid][NG_IDX(base + d, kMaxRowLen, 20)] = x[NG_IDX(gb + d, A.nRows, 18)];
         }
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncwarp();
-        TX s[kMaxComp];
 #pragma unroll
-        for (int c = 0; c < kMaxComp; ++c)
-            s[c] = TX(0);
-        for (int q = lane; q < len; q += 32)
+        for (int k = 0; k < kPre; ++k)
+        {
+            const int q = lane + 32 * k;
+            if (q < len)
+            {
+                const TX xv = xs[wid][q];
+#pragma unroll
+                for (int c = 0; c < kMaxComp; ++c)
+                    s[c] += static_cast<TX>(v[c][k]) * xv;
+            }
+        }
+        for (int q = lane + 32 * kPre; q < len; q += 32) // rows longer than 32 kPre entries (Hex20)
         {
             const TX xv = xs[wid][q];
 #pragma unroll
             for (int c = 0; c < kMaxComp; ++c)
                 if (c < ncI)
-                    s[c] += static_cast<TX>(vs[wid][c * len + q]) * xv;
+                    s[c] += static_cast<TX>(val[NG_IDX(rs[c] + q, A.nnz, 19)]) * xv;
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
@@ -259,9 +255,9 @@ template <typename TV, typename TX, int NDOT>
 void SpmvNode(cudaStream_t stream, const NodeSpmv& A, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc,
               int* st, int fin, const uint8_t* mask)
 {
-    constexpr int WPB = SpmvShape<TV, TX>::warps;
-    const unsigned blocks = static_cast<unsigned>((A.totalWarps + WPB - 1) / WPB);
-    k_spmv_node<TV, TX, NDOT><<<blocks, WPB * 32, 0, stream>>>(A, vals, mask, x, y, w0, sc, st, fin);
+    const int64_t threads = A.totalWarps * 32;
+    const unsigned blocks = static_cast<unsigned>((threads + kBS - 1) / kBS);
+    k_spmv_node<TV, TX, NDOT><<<blocks, kBS, 0, stream>>>(A, vals, mask, x, y, w0, sc, st, fin);
 }
 
 } // namespace nuto_gpu
