@@ -391,7 +391,7 @@ def run_ours(args):
                                   "u_z=2e-3 (AdaptiveSolve cut-back), imperfection kappa=3 kappa0 in the two middle "
                                   "cell layers; timed load steps %d..%d" % (args.size, args.warmup + 1,
                                                                            args.warmup + args.steps),
-                      "n_dofs": n_dofs, "nnz": nnz, "precision": "FP32 tangent + FP32 GMRES(40), FP64 residual, "
+                      "n_dofs": n_dofs, "nnz": nnz, "precision": "FP32 tangent + FP32 GMRES(80), FP64 residual, "
                                                                 "history and Newton test",
                       "newton_tolerance": "|C^T r| <= 1e-8 |C^T (r + K db)| of the load step",
                       "krylov_rtol": KRYLOV_RTOL, "l2": "inputs larger than L2 (FP32 tangent %.0f MB)" % (nnz * 4 / 1e6),

@@ -553,6 +553,8 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
 #endif
     const char* tk = std::getenv("NUTO_GPU_TANGENT");
     c->forceAtomicTangent = tk && std::string(tk) == "atomic";
+    const char* gr = std::getenv("NUTO_GPU_GMRES_RESTART");
+    c->gmresRestart = gr ? std::atoi(gr) : 0;
     const int rc = Guard(c, [&] {
         NG_CUDA(cudaSetDevice(device));
         NG_CUDA(cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device));

@@ -283,6 +283,7 @@ struct Ctx
     // row-gather tangent: integration-point records and the displacement-node -> eeq-node map
     int rowsMode = -1; // -1 not decided, 0 element-wise atomics, 1 row gather
     bool forceAtomicTangent = false; // NUTO_GPU_TANGENT=atomic selects the element-wise kernel
+    int gmresRestart = 0;            // NUTO_GPU_GMRES_RESTART; 0 = the default length
     DBuf<int32_t> dEOf;
     DBuf<unsigned char> dRecords;
 

@@ -475,72 +475,177 @@ void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double
 
 
 // ---- restarted GMRES(m), right Jacobi preconditioning ----------------------------------------------------------
-// Arnoldi with classical Gram-Schmidt and one re-orthogonalisation (CGS2); the FP64 Hessenberg column, its Givens
-// rotation and the residual estimate are formed by the last block of the second projection, so a whole cycle is
-// enqueued without a host round trip. The basis is stored in T (FP32 or FP64).
+// Arnoldi with classical Gram-Schmidt and one re-orthogonalisation (CGS2) in three passes over the basis
+// (projection; update fused with the second projection; second update with the norm). The FP64 Hessenberg column,
+// its Givens rotation and the residual estimate are formed by the last block of the second update, so a whole cycle
+// is enqueued without a host round trip. The basis is stored in T (FP32 or FP64).
 using GL = GmresLayout;
 
-// acc[i] += V_i . w for i < nv, eight basis vectors per pass; per-thread partial sums in T (the FP64 pipe is
-// narrow), FP64 across threads
-constexpr int kDotChunk = 8;
+// Projections on the basis in warp units: a unit is 32 x kUnitRows consecutive rows, lane l reading rows
+// base + l + 32 k, so every basis vector is streamed once per pass with coalesced loads. Per basis vector and unit
+// the lanes' products are summed by a warp butterfly in T; lane i % 32 keeps the running sum of vector i in a
+// register, and at the end of the block the warps' sums are added in T and each block adds one FP64 value per
+// vector to the accumulator. No FP64 arithmetic per row or per unit (the FP64 pipe is narrow on this part).
+constexpr int kUnitRows = 4;
+constexpr int kGmresFirstChunk = 4; // iterations enqueued before the first look at the residual estimate
+constexpr int kGmresMaxChunk = 16;
+constexpr int kProjChunks = (GL::m + 1 + 31) / 32;
 
 template <typename T>
-__global__ void __launch_bounds__(kBS) k_gm_dots(int64_t n, const T* __restrict__ V, int nv, const T* __restrict__ w,
-                                                  double* acc, const int* st)
+__device__ __forceinline__ T WarpAllSum(T v)
 {
-    __shared__ double sh[kBS / 32][kDotChunk];
-    if (st[ST_STATE] != RUN)
-        return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// adds the block's per-vector sums (lane registers acc[c] hold vector lane + 32 c of each warp) to out[0, nv)
+template <typename T>
+__device__ __forceinline__ void ProjFlush(const T (&acc)[kProjChunks], int nv, double* out)
+{
+    __shared__ T red[kBS / 32][kProjChunks * 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int i0 = 0; i0 < nv; i0 += kDotChunk)
+#pragma unroll
+    for (int c = 0; c < kProjChunks; ++c)
+        red[wid][c * 32 + lane] = acc[c];
+    __syncthreads();
+    for (int i = threadIdx.x; i < nv; i += blockDim.x)
     {
-        T s[kDotChunk];
+        T t = T(0);
 #pragma unroll
-        for (int c = 0; c < kDotChunk; ++c)
-            s[c] = T(0);
-        for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < n;
-             r += static_cast<int64_t>(gridDim.x) * blockDim.x)
-        {
-            const T wr = w[r];
-#pragma unroll
-            for (int c = 0; c < kDotChunk; ++c)
-                if (i0 + c < nv)
-                    s[c] += V[static_cast<int64_t>(i0 + c) * n + r] * wr;
-        }
-#pragma unroll
-        for (int c = 0; c < kDotChunk; ++c)
-        {
-            const double v = WarpSum(static_cast<double>(s[c]));
-            if (lane == 0)
-                sh[wid][c] = v;
-        }
-        __syncthreads();
-        if (threadIdx.x < kDotChunk && i0 + static_cast<int>(threadIdx.x) < nv)
-        {
-            double t = 0;
-            for (int q = 0; q < static_cast<int>(blockDim.x >> 5); ++q)
-                t += sh[q][threadIdx.x];
-            atomicAdd(acc + i0 + threadIdx.x, t);
-        }
-        __syncthreads();
+        for (int q = 0; q < kBS / 32; ++q)
+            t += red[q][i];
+        atomicAdd(out + i, static_cast<double>(t));
     }
 }
 
-// w -= sum_i h_i V_i. With finalize: also |w|^2, and the last block completes Arnoldi column j: H(:, j) = h1 + h2,
-// H(j+1, j) = |w|, earlier rotations applied, new rotation formed, residual estimate |g(j+1)| tested.
-template <typename T, bool FINAL>
-__global__ void __launch_bounds__(kBS) k_gm_update(int64_t n, const T* __restrict__ V, int nv, double* gs, T* w,
-                                                    int* st, int j)
+// products of the unit's rows (held in r[]) with basis vectors 0 .. nv-1, summed into acc
+template <typename T>
+__device__ __forceinline__ void ProjUnit(const T* __restrict__ V, int64_t n, int nv, int64_t base, bool full,
+                                         const T (&r)[kUnitRows], T (&acc)[kProjChunks])
 {
-    __shared__ double sh[kBS / 32];
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int c = 0; c < kProjChunks; ++c)
+    {
+        if (c * 32 >= nv)
+            break;
+        const int iend = min(32, nv - c * 32);
+#pragma unroll 4
+        for (int ii = 0; ii < iend; ++ii)
+        {
+            const T* Vi = V + static_cast<int64_t>(c * 32 + ii) * n;
+            T p = T(0);
+            if (full)
+            {
+#pragma unroll
+                for (int k = 0; k < kUnitRows; ++k)
+                    p += Vi[base + 32 * k] * r[k];
+            }
+            else
+            {
+#pragma unroll
+                for (int k = 0; k < kUnitRows; ++k)
+                    if (base + 32 * k < n)
+                        p += Vi[base + 32 * k] * r[k];
+            }
+            p = WarpAllSum(p);
+            if (lane == ii)
+                acc[c] += p;
+        }
+    }
+}
+
+// acc[i] += V_i . w for i < nv
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_gm_proj(int64_t n, const T* __restrict__ V, int nv, const T* __restrict__ w,
+                                                  double* acc, const int* st)
+{
+    if (st[ST_STATE] != RUN)
+        return;
+    const int lane = threadIdx.x & 31;
+    T sums[kProjChunks];
+#pragma unroll
+    for (int c = 0; c < kProjChunks; ++c)
+        sums[c] = T(0);
+    const int64_t units = (n + 32 * kUnitRows - 1) / (32 * kUnitRows);
+    const int64_t warps = static_cast<int64_t>(gridDim.x) * (kBS / 32);
+    for (int64_t u = blockIdx.x * static_cast<int64_t>(kBS / 32) + (threadIdx.x >> 5); u < units; u += warps)
+    {
+        const int64_t base = u * 32 * kUnitRows + lane;
+        const bool full = (u + 1) * 32 * kUnitRows <= n;
+        T r[kUnitRows];
+#pragma unroll
+        for (int k = 0; k < kUnitRows; ++k)
+            r[k] = base + 32 * k < n ? w[base + 32 * k] : T(0);
+        ProjUnit(V, n, nv, base, full, r, sums);
+    }
+    ProjFlush(sums, nv, acc);
+}
+
+// w -= sum_i h_i V_i with h the first projection (gs + H1), then acc2[i] += V_i . w: the update of classical
+// Gram-Schmidt and the re-orthogonalisation's projection in one pass (the unit's V values are re-read from cache)
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_gm_update_proj(int64_t n, const T* __restrict__ V, int nv, const double* h,
+                                                         T* __restrict__ w, double* acc2, const int* st)
+{
     __shared__ T hs[GL::m + 1];
     if (st[ST_STATE] != RUN)
         return;
-    const double* h = gs + (FINAL ? GL::H2 : GL::H1);
     for (int i = threadIdx.x; i < nv; i += blockDim.x)
         hs[i] = static_cast<T>(h[i]);
     __syncthreads();
-    double nrm = 0;
+    const int lane = threadIdx.x & 31;
+    T sums[kProjChunks];
+#pragma unroll
+    for (int c = 0; c < kProjChunks; ++c)
+        sums[c] = T(0);
+    const int64_t units = (n + 32 * kUnitRows - 1) / (32 * kUnitRows);
+    const int64_t warps = static_cast<int64_t>(gridDim.x) * (kBS / 32);
+    for (int64_t u = blockIdx.x * static_cast<int64_t>(kBS / 32) + (threadIdx.x >> 5); u < units; u += warps)
+    {
+        const int64_t base = u * 32 * kUnitRows + lane;
+        const bool full = (u + 1) * 32 * kUnitRows <= n;
+        T r[kUnitRows];
+#pragma unroll
+        for (int k = 0; k < kUnitRows; ++k)
+            r[k] = base + 32 * k < n ? w[base + 32 * k] : T(0);
+#pragma unroll 4
+        for (int i = 0; i < nv; ++i)
+        {
+            const T hi = hs[i];
+            const T* Vi = V + static_cast<int64_t>(i) * n;
+#pragma unroll
+            for (int k = 0; k < kUnitRows; ++k)
+                if (base + 32 * k < n)
+                    r[k] -= hi * Vi[base + 32 * k];
+        }
+#pragma unroll
+        for (int k = 0; k < kUnitRows; ++k)
+            if (base + 32 * k < n)
+                w[base + 32 * k] = r[k];
+        ProjUnit(V, n, nv, base, full, r, sums);
+    }
+    ProjFlush(sums, nv, acc2);
+}
+
+// w -= sum_i h_i V_i with h the second projection (gs + H2), |w|^2; the last block completes Arnoldi column j:
+// H(:, j) = h1 + h2, H(j+1, j) = |w|, earlier rotations applied, new rotation formed, residual estimate |g(j+1)|
+// tested. Row sums of |w|^2 are formed in T per thread and block, one FP64 atomic per block.
+template <typename T>
+__global__ void __launch_bounds__(kBS) k_gm_update(int64_t n, const T* __restrict__ V, int nv, double* gs, T* w,
+                                                    int* st, int j)
+{
+    __shared__ T sh[kBS / 32];
+    __shared__ T hs[GL::m + 1];
+    if (st[ST_STATE] != RUN)
+        return;
+    const double* h = gs + GL::H2;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x)
+        hs[i] = static_cast<T>(h[i]);
+    __syncthreads();
+    T nrm = T(0);
     for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < n;
          r += static_cast<int64_t>(gridDim.x) * blockDim.x)
     {
@@ -548,12 +653,19 @@ __global__ void __launch_bounds__(kBS) k_gm_update(int64_t n, const T* __restric
         for (int i = 0; i < nv; ++i)
             a -= hs[i] * V[static_cast<int64_t>(i) * n + r];
         w[r] = a;
-        if (FINAL)
-            nrm += static_cast<double>(a) * static_cast<double>(a);
+        nrm += a * a;
     }
-    if (!FINAL)
-        return;
-    BlockAccumulate(nrm, gs + GL::ACC, sh);
+    nrm = WarpAllSum(nrm);
+    if ((threadIdx.x & 31) == 0)
+        sh[threadIdx.x >> 5] = nrm;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        T t = T(0);
+        for (int q = 0; q < static_cast<int>(blockDim.x >> 5); ++q)
+            t += sh[q];
+        atomicAdd(gs + GL::ACC, static_cast<double>(t));
+    }
     if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
     {
         st[ST_COUNTER] = 0;
@@ -700,7 +812,8 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
     GVecs<T>& G = *gp;
     const int64_t n = c.nDofs;
     K.ensure(n);
-    G.ensure(n);
+    const int m = c.gmresRestart > 1 ? std::min(c.gmresRestart, static_cast<int>(GL::m)) : kGmresRestart;
+    G.ensure(n, m);
     if (w.gsc.n != static_cast<size_t>(GL::SIZE))
     {
         w.gsc.alloc(GL::SIZE);
@@ -714,6 +827,10 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
     NG_CUDA(cudaMemsetAsync(st, 0, ST_COUNT * sizeof(int), c.stream));
     NG_CUDA(cudaMemsetAsync(gs, 0, GL::SIZE * sizeof(double), c.stream));
     const int grid = GridFor(c, n);
+    // projection kernels: warp units of 32 kUnitRows rows, four blocks per SM
+    const int64_t units = (n + 32 * kUnitRows - 1) / (32 * kUnitRows);
+    const int gridP = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((units + kBS / 32 - 1) / (kBS / 32),
+                                                                             static_cast<int64_t>(c.smCount) * 4)));
     const unsigned g256 = static_cast<unsigned>((n + 255) / 256);
     const bool amg = c.precond == NUTO_GPU_PRECOND_AMG;
     if (amg)
@@ -735,7 +852,6 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
     std::vector<double> history;
     double beta0 = -1.;
     bool first = true;
-    const int m = GL::m;
     while (total < maxit)
     {
         // r = rhs - A x, v_0 = r / |r|
@@ -746,21 +862,53 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
         first = false;
         k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, G.V.p, amg ? nullptr : G.z.p, K.dinv.p, gs, st);
         const int cols = std::min(m, maxit - total);
-        for (int j = 0; j < cols; ++j)
+        // The cycle is enqueued in chunks: after each chunk the host reads the state and the residual estimate and
+        // sizes the next chunk from the observed convergence rate (the iterations still needed, 1 .. 16). Kernels
+        // of iterations enqueued after convergence return at once but still cost a launch each (about 140 per
+        // iteration with the multigrid sweep), so a cycle is never enqueued far past the expected convergence.
+        int j = 0, chunk = kGmresFirstChunk, jCheck = 0;
+        double resCheck = -1.;
+        while (j < cols)
         {
-            T* vj1 = G.V.p + static_cast<int64_t>(j + 1) * n;
-            T* zj = amg ? G.Z.p + static_cast<int64_t>(j) * n : G.z.p;
-            if (amg)
-                AmgApply<T>(c, G.V.p + static_cast<int64_t>(j) * n, zj, st, false);
-            SpmvTimed<TV, T, 0>(c, vals, zj, G.w.p, nullptr, nullptr, st, FIN_NONE, c.dMask.p);
-            c.stats.kernel_launches += 4 + (j + 1 < cols ? 1 : 0);
-            k_gm_dots<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, G.w.p, gs + GL::H1, st);
-            k_gm_update<T, false><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, gs, G.w.p, st, j);
-            k_gm_dots<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, G.w.p, gs + GL::H2, st);
-            k_gm_update<T, true><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, gs, G.w.p, st, j);
-            if (j + 1 < cols)
-                k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, vj1, amg ? nullptr : G.z.p, K.dinv.p, gs,
-                                                              st);
+            const int jEnd = std::min(cols, j + chunk);
+            for (; j < jEnd; ++j)
+            {
+                T* vj1 = G.V.p + static_cast<int64_t>(j + 1) * n;
+                T* zj = amg ? G.Z.p + static_cast<int64_t>(j) * n : G.z.p;
+                if (amg)
+                    AmgApply<T>(c, G.V.p + static_cast<int64_t>(j) * n, zj, st, false);
+                SpmvTimed<TV, T, 0>(c, vals, zj, G.w.p, nullptr, nullptr, st, FIN_NONE, c.dMask.p);
+                c.stats.kernel_launches += 3 + (j + 1 < cols ? 1 : 0);
+                k_gm_proj<T><<<gridP, kBS, 0, c.stream>>>(n, G.V.p, j + 1, G.w.p, gs + GL::H1, st);
+                k_gm_update_proj<T><<<gridP, kBS, 0, c.stream>>>(n, G.V.p, j + 1, gs + GL::H1, G.w.p, gs + GL::H2,
+                                                                  st);
+                k_gm_update<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, gs, G.w.p, st, j);
+                if (j + 1 < cols)
+                    k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, vj1, amg ? nullptr : G.z.p, K.dinv.p,
+                                                                  gs, st);
+            }
+            if (j >= cols)
+                break;
+            NG_CUDA(cudaMemcpyAsync(w.hStat, st, ST_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            NG_CUDA(cudaMemcpyAsync(w.hG + GL::G, gs + GL::G, (GL::SIZE - GL::G) * sizeof(double),
+                                    cudaMemcpyDeviceToHost, c.stream));
+            NG_CUDA(cudaStreamSynchronize(c.stream));
+            if (w.hStat[ST_STATE] != RUN)
+                break;
+            const int jd = w.hStat[ST_JDONE];
+            const double res = std::fabs(w.hG[GL::G + jd]);
+            const double tol = std::sqrt(std::max(w.hG[GL::TOL2], 0.));
+            const double ref = resCheck > 0. ? resCheck : w.hG[GL::BETA];
+            const int span = jd - (resCheck > 0. ? jCheck : 0);
+            chunk = kGmresMaxChunk;
+            if (span > 0 && ref > 0. && res > 0. && res < ref && tol > 0.)
+            {
+                const double rate = std::log(res / ref) / span; // log of the mean reduction per iteration
+                const double need = std::log(tol / res) / rate;
+                chunk = static_cast<int>(std::min<double>(kGmresMaxChunk, std::max(1., std::ceil(need))));
+            }
+            resCheck = res;
+            jCheck = jd;
         }
         AfterLaunch(c, "gmres cycle");
         NG_CUDA(cudaMemcpyAsync(w.hG, gs, GL::SIZE * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -782,8 +930,8 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
             {
                 double s = w.hG[GL::G + i];
                 for (int l = i + 1; l < k; ++l)
-                    s -= w.hG[GL::H + l * (m + 1) + i] * y[l];
-                const double d = w.hG[GL::H + i * (m + 1) + i];
+                    s -= w.hG[GL::H + l * (GL::m + 1) + i] * y[l];
+                const double d = w.hG[GL::H + i * (GL::m + 1) + i];
                 y[i] = d != 0. ? s / d : 0.;
             }
             NG_CUDA(cudaMemcpyAsync(gs + GL::Y, y, k * sizeof(double), cudaMemcpyHostToDevice, c.stream));
@@ -867,8 +1015,12 @@ static int KrylovSolve(Ctx& c, int method, const TV* vals, const double* b, doub
         k_krylov_init<T, false><<<grid, kBS, 0, c.stream>>>(n, c.dMask.p, b, V.x.p, V.r.p, V.rh.p, V.p.p, V.v.p,
                                                              V.z.p, V.dinv.p, sc, st);
     AfterLaunch(c, "krylov");
-    const int chunk = 16;
-    int done = 0;
+    // Iterations are enqueued in chunks with a look at the state in between; with the multigrid cycle (about 70
+    // launches per iteration even when they return at once after convergence) the next chunk is sized from the
+    // observed reduction of |r|^2, as in the GMRES cycle.
+    int chunk = amg ? kGmresFirstChunk : 16;
+    int done = 0, itCheck = 0;
+    double rrCheck = -1.;
     int state = RUN;
     while (done < maxit)
     {
@@ -908,6 +1060,21 @@ static int KrylovSolve(Ctx& c, int method, const TV* vals, const double* b, doub
         state = w.hStat[ST_STATE];
         if (state != RUN)
             break;
+        if (amg)
+        {
+            const int itNow = w.hStat[ST_ITERS];
+            const double rr = w.hScal[SC_RR], tol2 = w.hScal[SC_TOL2];
+            const double ref = rrCheck > 0. ? rrCheck : w.hScal[SC_BB] * w.hScal[SC_SCALE] * w.hScal[SC_SCALE];
+            const int span = itNow - itCheck;
+            chunk = kGmresMaxChunk;
+            if (span > 0 && ref > 0. && rr > 0. && rr < ref && tol2 > 0.)
+            {
+                const double need = std::log(tol2 / rr) / (std::log(rr / ref) / span);
+                chunk = static_cast<int>(std::min<double>(kGmresMaxChunk, std::max(1., std::ceil(need))));
+            }
+            rrCheck = rr;
+            itCheck = itNow;
+        }
     }
     const int it = w.hStat[ST_ITERS];
     const double bb = w.hScal[SC_BB] * w.hScal[SC_SCALE] * w.hScal[SC_SCALE];

@@ -162,6 +162,11 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     // tangent (r = rhs - K32 dx accumulated in FP64) until the true relative residual reaches krylov_rtol: the
     // FP32 iteration's own residual estimate is not trusted for the Newton direction.
     double eta = o.krylov_rtol; // forcing term of the current linear solve
+    // NUTO_GPU_VERBOSE=1: one line per Newton iteration on stderr, like QuasistaticSolver::Info (2: also the FP32
+    // refinement sweeps)
+    const char* vb = std::getenv("NUTO_GPU_VERBOSE");
+    const bool verbose = vb && (vb[0] == '1' || vb[0] == '2');
+    const bool verboseSweeps = vb && vb[0] == '2';
     auto solve = [&](const double* rhs, double* out) {
         const auto k0 = std::chrono::steady_clock::now();
         int it = 0;
@@ -184,6 +189,9 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
                 SpmvFull64(c, NUTO_GPU_FP32, w.K32.p, out, w.refKx.p);
                 Residual64(c, rhs, w.refKx.p, w.refR.p);
                 rel = bn > 0. ? MaskedNorm(c, w.refR.p) / bn : 0.;
+                if (verboseSweeps)
+                    std::fprintf(stderr, "[nuto_gpu]   sweep %d: inner %.1e, krylov %d, true rel %.2e\n", sweep, inner,
+                                 its, rel);
             }
             lastRel = rel;
         }
@@ -196,9 +204,6 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
 
     const double tOld = c.time;
     double* x = c.dX.p;
-    // NUTO_GPU_VERBOSE=1: one line per Newton iteration on stderr, like QuasistaticSolver::Info
-    const char* vb = std::getenv("NUTO_GPU_VERBOSE");
-    const bool verbose = vb && vb[0] == '1';
 
     // trial state: K(x_old), R(x_old, t_new), x_trial = x - C (C^T K C)^-1 C^T (R + K db) + db
     assembleK(x);

@@ -58,7 +58,9 @@ struct KVecs
     }
 };
 
-constexpr int kGmresRestart = 40;
+// GMRES restart length: default, and the largest the scalar block holds (NUTO_GPU_GMRES_RESTART picks another)
+constexpr int kGmresRestart = 80;
+constexpr int kGmresMax = 160;
 
 // GMRES workspace: Krylov basis V (m + 1 vectors of n), work vectors and the FP64 Arnoldi scalars.
 template <typename T>
@@ -67,27 +69,29 @@ struct GVecs
     DBuf<T> V, w, z;
     DBuf<T> Z; // preconditioned basis of the flexible form (m vectors), allocated on first use
     int64_t n = 0;
-    void ensure(int64_t count)
+    int m = 0;
+    void ensure(int64_t count, int restart)
     {
-        if (n == count)
+        if (n == count && m == restart)
             return;
-        V.alloc(static_cast<size_t>(count) * (kGmresRestart + 1));
+        V.alloc(static_cast<size_t>(count) * (restart + 1));
         w.alloc(count);
         z.alloc(count);
         Z.free();
         n = count;
+        m = restart;
     }
     void ensureZ()
     {
-        if (Z.n != static_cast<size_t>(n) * kGmresRestart)
-            Z.alloc(static_cast<size_t>(n) * kGmresRestart);
+        if (Z.n != static_cast<size_t>(n) * m)
+            Z.alloc(static_cast<size_t>(n) * m);
     }
 };
 
 // offsets into the GMRES scalar block (doubles)
 struct GmresLayout
 {
-    static constexpr int m = kGmresRestart;
+    static constexpr int m = kGmresMax;          // capacity; a cycle uses the first restart columns
     static constexpr int H = 0;                  // (m + 1) x m, column-major
     static constexpr int G = H + (m + 1) * m;    // m + 1: rotated right-hand side
     static constexpr int CS = G + m + 1;         // m: Givens cosines
