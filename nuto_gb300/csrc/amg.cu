@@ -228,6 +228,16 @@ static NodeSpmv SlotView(const Ctx& c, int I)
     A.rowPtr = c.dRowPtr.p;
     A.nnz = c.nnz;
     A.nRows = c.nDofs;
+    if (c.nb.total > 0)
+    {
+        A.nbBase[0] = c.nb.pair[I * ns + I].base.p;
+        A.nbOff[0] = c.nb.pair[I * ns + I].off;
+        A.nbSeg4 = c.nb.pair[I * ns + I].maxSeg4;
+        A.nb32 = c.nb.v32.p;
+        A.nb64 = c.nb.v64.p;
+        A.nbSrc32 = c.nb.src32;
+        A.nbSrc64 = c.nb.src64;
+    }
     return A;
 }
 

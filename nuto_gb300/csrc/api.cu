@@ -411,6 +411,41 @@ static void BuildPattern(Ctx& c)
                 col[q] = static_cast<int32_t>(SJ.offset + SJ.dof0[nbr[p].idx[q]]);
             Upload(M.dNbrCol, col);
         }
+    }
+    {
+        // padded pair layout: per pair, the I-nodes' blocks of ncomp_I segments of ncomp_J * nn values, each
+        // padded to a multiple of 4
+        NbLayout& L = c.nb;
+        L.src32 = L.src64 = nullptr;
+        L.v32.free();
+        L.v64.free();
+        L.total = 0;
+        L.maxSeg4 = 0;
+        for (int p = 0; p < ns * ns; ++p)
+        {
+            const Slot& SI = c.slots[p / ns];
+            const Slot& SJ = c.slots[p % ns];
+            const std::vector<int64_t>& ptr = nbr[p].ptr;
+            std::vector<int64_t> base(SI.nNodes);
+            int64_t pos = 0;
+            int mx = 0;
+            for (int64_t a = 0; a < SI.nNodes; ++a)
+            {
+                const int seg4 = static_cast<int>((SJ.ncomp * (ptr[a + 1] - ptr[a]) + 3) / 4 * 4);
+                base[a] = pos;
+                pos += static_cast<int64_t>(SI.ncomp) * seg4;
+                mx = std::max(mx, seg4);
+            }
+            L.pair[p].off = L.total;
+            L.pair[p].maxSeg4 = mx;
+            Upload(L.pair[p].base, base);
+            L.total += (pos + 3) / 4 * 4;
+            L.maxSeg4 = std::max(L.maxSeg4, mx);
+        }
+    }
+    for (int p = 0; p < ns * ns; ++p)
+    {
+        PairMap& M = c.pairs[p];
         M.hNbrPtr = std::move(nbr[p].ptr);
         M.hNbrIdx = std::move(nbr[p].idx);
     }

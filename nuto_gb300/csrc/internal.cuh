@@ -232,6 +232,28 @@ struct BoundaryGroup
     double gp[3] = {0, 0, 0}, gw[3] = {0, 0, 0};
 };
 
+// Solver copy of the tangent in the padded pair layout: for every slot pair (I, J) and I-node a, the node's ncomp_I
+// row segments of the J-columns (ncomp_J values per J-neighbour, CSR column order) follow each other, each padded
+// with zeros to a multiple of 4 values; every node block starts at a multiple of 4 values. The SpMV streams these
+// blocks with 16-byte loads. Filled from the CSR values once per tangent (same pointer and version: reused).
+struct NbLayout
+{
+    struct Pair
+    {
+        DBuf<int64_t> base; // per I-node: first value of the node's block, relative to off
+        int64_t off = 0;    // first value of the pair
+        int maxSeg4 = 0;    // longest padded segment
+    };
+    Pair pair[kMaxSlots * kMaxSlots];
+    int64_t total = 0;
+    int maxSeg4 = 0;
+    DBuf<float> v32;
+    DBuf<double> v64;
+    const void* src32 = nullptr;
+    const void* src64 = nullptr;
+    uint64_t ver32 = 0, ver64 = 0;
+};
+
 struct Ctx
 {
     int device = 0;
@@ -302,6 +324,7 @@ struct Ctx
     SolverWork* work = nullptr;
     Amg* amg = nullptr;
     std::vector<BoundaryGroup> boundary;
+    NbLayout nb;
     DBuf<double> dConstGrad; // added to the residual of nuto_gpu_do_step (empty: none)
     int precond = NUTO_GPU_PRECOND_AMG;
     uint64_t valsVersion = 1; // bumped by every tangent assembly and every caller-supplied solve
@@ -333,6 +356,10 @@ void AmgSetup(Ctx& c, const TV* vals);
 template <typename T>
 void AmgApply(Ctx& c, const T* v, T* z, const int* st, bool sym);
 int AmgLevels(const Ctx& c);
+// fills the padded pair layout of TV from the CSR values `vals` unless it holds them already (same pointer and
+// tangent version)
+template <typename TV>
+void EnsureNb(Ctx& c, const TV* vals);
 
 // ---- kernel argument blocks (by value) ----
 struct CellArgs

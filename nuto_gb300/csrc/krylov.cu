@@ -398,8 +398,84 @@ NodeSpmv MakeNodeSpmv(const Ctx& c)
     A.rowPtr = c.dRowPtr.p;
     A.nnz = c.nnz;
     A.nRows = c.nDofs;
+    if (c.nb.total > 0)
+    {
+        for (int p = 0; p < A.ns * A.ns; ++p)
+        {
+            A.nbBase[p] = c.nb.pair[p].base.p;
+            A.nbOff[p] = c.nb.pair[p].off;
+        }
+        A.nbSeg4 = c.nb.maxSeg4;
+        A.nb32 = c.nb.v32.p;
+        A.nb64 = c.nb.v64.p;
+        A.nbSrc32 = c.nb.src32;
+        A.nbSrc64 = c.nb.src64;
+    }
     return A;
 }
+
+// CSR values -> padded pair layout: one warp per node of the combined operator, lanes over the segment
+template <typename TV>
+__global__ void __launch_bounds__(kBS) k_nb_pack(NodeSpmv A, const TV* __restrict__ csr, TV* __restrict__ nb)
+{
+    const int64_t u = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (u >= A.totalWarps)
+        return;
+    const int I = (A.ns > 1 && u >= A.firstWarp[1]) ? 1 : 0;
+    const int64_t a = u - A.firstWarp[I];
+    if (a >= A.nNodes[I])
+        return;
+    const int ncI = A.ncomp[I];
+    const int64_t g0 = A.gdof[I][a];
+    for (int J = 0; J < A.ns; ++J)
+    {
+        const int p = I * A.ns + J;
+        const int nn = static_cast<int>(A.nbrPtr[p][a + 1] - A.nbrPtr[p][a]);
+        const int seg = A.ncomp[J] * nn, seg4 = (seg + 3) & ~3;
+        const int32_t blk = A.blk[p][a];
+        TV* dst = nb + A.nbOff[p] + A.nbBase[p][a];
+        for (int c = 0; c < ncI; ++c)
+        {
+            const TV* src = csr + A.rowPtr[NG_IDX(g0 + c, A.nRows, 65)] + blk;
+            for (int q = lane; q < seg4; q += 32)
+                dst[c * seg4 + q] = q < seg ? src[NG_IDX(q, A.nnz, 66)] : TV(0);
+        }
+    }
+}
+
+template <typename TV>
+void EnsureNb(Ctx& c, const TV* vals)
+{
+    NbLayout& L = c.nb;
+    if (L.total <= 0 || !vals)
+        return;
+    const void*& src = sizeof(TV) == 4 ? L.src32 : L.src64;
+    uint64_t& ver = sizeof(TV) == 4 ? L.ver32 : L.ver64;
+    if (src == static_cast<const void*>(vals) && ver == c.valsVersion)
+        return;
+    TV* dst;
+    if constexpr (sizeof(TV) == 4)
+    {
+        if (L.v32.n != static_cast<size_t>(L.total))
+            L.v32.alloc(L.total);
+        dst = L.v32.p;
+    }
+    else
+    {
+        if (L.v64.n != static_cast<size_t>(L.total))
+            L.v64.alloc(L.total);
+        dst = L.v64.p;
+    }
+    src = vals; // before MakeNodeSpmv: the view carries the source pointer
+    ver = c.valsVersion;
+    const NodeSpmv A = MakeNodeSpmv(c);
+    k_nb_pack<TV><<<static_cast<unsigned>((A.totalWarps * 32 + kBS - 1) / kBS), kBS, 0, c.stream>>>(A, vals, dst);
+    c.stats.kernel_launches += 1;
+    AfterLaunch(c, "padded pair layout");
+}
+template void EnsureNb<float>(Ctx&, const float*);
+template void EnsureNb<double>(Ctx&, const double*);
 
 template <typename TV, typename TX, int NDOT>
 static void SpmvLaunch(Ctx& c, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc, int* st, int fin,
@@ -464,6 +540,10 @@ void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double
         NG_CUDA(cudaMemsetAsync(w.zeroMask.p, 0, c.nDofs, c.stream));
     }
     c.stats.kernel_launches += 1;
+    if (precision == NUTO_GPU_FP32)
+        EnsureNb(c, static_cast<const float*>(vals));
+    else
+        EnsureNb(c, static_cast<const double*>(vals));
     if (precision == NUTO_GPU_FP32)
         SpmvLaunch<float, double, 0>(c, static_cast<const float*>(vals), x, y, nullptr, nullptr, nullptr, FIN_NONE,
                                      w.zeroMask.p);
@@ -833,6 +913,7 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
                                                                              static_cast<int64_t>(c.smCount) * 4)));
     const unsigned g256 = static_cast<unsigned>((n + 255) / 256);
     const bool amg = c.precond == NUTO_GPU_PRECOND_AMG;
+    EnsureNb(c, vals);
     if (amg)
     {
         AmgSetup<TV>(c, vals);
@@ -992,6 +1073,7 @@ static int KrylovSolve(Ctx& c, int method, const TV* vals, const double* b, doub
     NG_CUDA(cudaMemsetAsync(st, 0, ST_COUNT * sizeof(int), c.stream));
     const int grid = GridFor(c, n);
     const bool amg = pcg && c.precond == NUTO_GPU_PRECOND_AMG;
+    EnsureNb(c, vals);
     if (amg)
         AmgSetup<TV>(c, vals);
     else

@@ -88,7 +88,57 @@ struct NodeSpmv
     const int32_t* blk[kMaxSlots * kMaxSlots];
     const int64_t* rowPtr;
     int64_t nnz, nRows, nbrTotal[kMaxSlots * kMaxSlots];
+    // padded pair layout (nbBase[0] == nullptr: CSR only): per view pair the node blocks and the pair's offset, the
+    // longest padded segment, and the layout buffers with the CSR values each was filled from
+    const int64_t* nbBase[kMaxSlots * kMaxSlots];
+    int64_t nbOff[kMaxSlots * kMaxSlots];
+    int nbSeg4;
+    const float* nb32;
+    const double* nb64;
+    const void* nbSrc32;
+    const void* nbSrc64;
 };
+
+// block sums of the SpMV's dot products and, in the last block, the Krylov scalar they finish
+template <int NDOT>
+__device__ __forceinline__ void SpmvFinish(double d0, double d1, double* sc, int* st, int fin, double* sh)
+{
+    BlockAccumulate(d0, sc + SC_ACC0, sh);
+    if (NDOT >= 2)
+        BlockAccumulate(d1, sc + SC_ACC1, sh);
+    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
+    {
+        st[ST_COUNTER] = 0;
+        const double a0 = VRead(sc + SC_ACC0), a1 = VRead(sc + SC_ACC1);
+        sc[SC_ACC0] = 0.;
+        sc[SC_ACC1] = 0.;
+        if (fin == FIN_PCG_ALPHA)
+        {
+            if (!Finite(a0))
+                st[ST_STATE] = NONFINITE;
+            else if (!(a0 > 0.))
+                st[ST_STATE] = BREAKDOWN;
+            else
+                sc[SC_ALPHA] = sc[SC_RHO] / a0;
+        }
+        else if (fin == FIN_BICG_ALPHA)
+        {
+            if (!Finite(a0))
+                st[ST_STATE] = NONFINITE;
+            else if (a0 == 0.)
+                st[ST_STATE] = BREAKDOWN;
+            else
+                sc[SC_ALPHA] = sc[SC_RHO] / a0;
+        }
+        else if (fin == FIN_BICG_OMEGA)
+        {
+            if (!Finite(a0) || !Finite(a1))
+                st[ST_STATE] = NONFINITE;
+            else
+                sc[SC_OMEGA] = a1 > 0. ? a0 / a1 : 0.;
+        }
+    }
+}
 
 constexpr int kMaxRowLen = 256; // longest row of a node (Hex20 displacements: 3 x 81)
 constexpr int kMaxComp = 3;     // components per DOF node
@@ -211,50 +261,166 @@ __global__ void __launch_bounds__(kBS, 5) k_spmv_node(NodeSpmv A, const TV* __re
     }
     if (NDOT == 0)
         return;
-    BlockAccumulate(d0, sc + SC_ACC0, sh);
-    if (NDOT >= 2)
-        BlockAccumulate(d1, sc + SC_ACC1, sh);
-    if (LastBlock(st + ST_COUNTER) && threadIdx.x == 0)
-    {
-        st[ST_COUNTER] = 0;
-        const double a0 = VRead(sc + SC_ACC0), a1 = VRead(sc + SC_ACC1);
-        sc[SC_ACC0] = 0.;
-        sc[SC_ACC1] = 0.;
-        if (fin == FIN_PCG_ALPHA)
-        {
-            if (!Finite(a0))
-                st[ST_STATE] = NONFINITE;
-            else if (!(a0 > 0.))
-                st[ST_STATE] = BREAKDOWN;
-            else
-                sc[SC_ALPHA] = sc[SC_RHO] / a0;
-        }
-        else if (fin == FIN_BICG_ALPHA)
-        {
-            if (!Finite(a0))
-                st[ST_STATE] = NONFINITE;
-            else if (a0 == 0.)
-                st[ST_STATE] = BREAKDOWN;
-            else
-                sc[SC_ALPHA] = sc[SC_RHO] / a0;
-        }
-        else if (fin == FIN_BICG_OMEGA)
-        {
-            if (!Finite(a0) || !Finite(a1))
-                st[ST_STATE] = NONFINITE;
-            else
-                sc[SC_OMEGA] = a1 > 0. ? a0 / a1 : 0.;
-        }
-    }
+    SpmvFinish<NDOT>(d0, d1, sc, st, fin, sh);
 }
 
 // NodeSpmv of the context's fine-level pattern
 NodeSpmv MakeNodeSpmv(const Ctx& c);
 
+// ---- node SpMV on the padded pair layout -------------------------------------------------------------------------
+// kNbG lanes per node (four nodes per warp). For every column slot J of the view the group gathers the x of the
+// node's J-neighbours into its shared segment buffer (zero-padded to a multiple of 4), then streams the node's
+// padded row segments of pair (I, J) in 16-byte vectors, one lane per 4 columns, accumulating the ncomp_I row sums;
+// a 3-step butterfly inside the group finishes the rows. Per value: a quarter of a 16-byte load and one FMA.
+constexpr int kNbG = 8;
+
+template <typename T>
+__device__ __forceinline__ void Load4(const T* p, T (&o)[4])
+{
+    if constexpr (sizeof(T) == 4)
+    {
+        const float4 f = *reinterpret_cast<const float4*>(p);
+        o[0] = f.x;
+        o[1] = f.y;
+        o[2] = f.z;
+        o[3] = f.w;
+    }
+    else
+    {
+        const double2 f0 = reinterpret_cast<const double2*>(p)[0];
+        const double2 f1 = reinterpret_cast<const double2*>(p)[1];
+        o[0] = f0.x;
+        o[1] = f0.y;
+        o[2] = f1.x;
+        o[3] = f1.y;
+    }
+}
+
+template <typename TV>
+__device__ __forceinline__ const TV* NbValues(const NodeSpmv& A)
+{
+    if constexpr (sizeof(TV) == 4)
+        return A.nb32;
+    else
+        return A.nb64;
+}
+
+template <typename TV, typename TX, int NDOT>
+__global__ void __launch_bounds__(kBS) k_spmv_nb(NodeSpmv A, const uint8_t* __restrict__ mask,
+                                                  const TX* __restrict__ x, TX* __restrict__ y,
+                                                  const TX* __restrict__ w0, double* sc, int* st, int fin)
+{
+    extern __shared__ __align__(16) unsigned char nbSmem[];
+    __shared__ double sh[kBS / 32];
+    if (st && st[ST_STATE] != RUN)
+        return;
+    const TV* __restrict__ vals = NbValues<TV>(A);
+    const int gl = threadIdx.x & (kNbG - 1);
+    const int L = A.nbSeg4;
+    TX* xs = reinterpret_cast<TX*>(nbSmem) + (threadIdx.x / kNbG) * L;
+    const int64_t u = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / kNbG;
+    int I = 0;
+    int64_t a = 0;
+    bool valid = u < A.totalWarps;
+    if (valid)
+    {
+        I = (A.ns > 1 && u >= A.firstWarp[1]) ? 1 : 0;
+        a = u - A.firstWarp[I];
+        valid = a < A.nNodes[I];
+    }
+    const int ncI = valid ? A.ncomp[I] : 0;
+    TX s[kMaxComp];
+#pragma unroll
+    for (int c = 0; c < kMaxComp; ++c)
+        s[c] = TX(0);
+    for (int J = 0; J < A.ns; ++J) // the same trip count in every lane: the warp syncs below are uniform
+    {
+        const int p = I * A.ns + J;
+        const int ncJ = A.ncomp[J];
+        int64_t q0 = 0;
+        int nn = 0;
+        if (valid)
+        {
+            q0 = A.nbrPtr[p][a];
+            nn = static_cast<int>(A.nbrPtr[p][a + 1] - q0);
+        }
+        const int seg = ncJ * nn, seg4 = (seg + 3) & ~3;
+        for (int t = gl; t < nn; t += kNbG)
+        {
+            const int64_t col = A.nbrCol[p][NG_IDX(q0 + t, A.nbrTotal[p], 60)];
+            for (int d = 0; d < ncJ; ++d)
+                xs[NG_IDX(t * ncJ + d, L, 61)] = x[NG_IDX(col + d, A.nRows, 62)];
+        }
+        for (int t = seg + gl; t < seg4; t += kNbG)
+            xs[NG_IDX(t, L, 63)] = TX(0);
+        __syncwarp();
+        if (valid)
+        {
+            const TV* vp = vals + A.nbOff[p] + A.nbBase[p][a];
+            for (int f = 4 * gl; f < seg4; f += 4 * kNbG)
+            {
+                TX xv[4];
+                Load4(xs + f, xv);
+#pragma unroll
+                for (int c = 0; c < kMaxComp; ++c)
+                    if (c < ncI)
+                    {
+                        TV v[4];
+                        Load4(vp + c * seg4 + f, v);
+                        s[c] += static_cast<TX>(v[0]) * xv[0] + static_cast<TX>(v[1]) * xv[1] +
+                                static_cast<TX>(v[2]) * xv[2] + static_cast<TX>(v[3]) * xv[3];
+                    }
+            }
+        }
+        __syncwarp(); // the segment buffer is refilled for the next J
+    }
+#pragma unroll
+    for (int o = kNbG / 2; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < kMaxComp; ++c)
+            s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
+    double d0 = 0., d1 = 0.;
+    if (valid && gl == 0)
+    {
+        const int64_t g0 = A.gdof[I][a];
+#pragma unroll
+        for (int c = 0; c < kMaxComp; ++c)
+        {
+            if (c >= ncI)
+                break;
+            const int64_t r = NG_IDX(g0 + c, A.nRows, 64);
+            const TX yv = mask[r] ? x[r] : s[c];
+            y[r] = yv;
+            if (NDOT >= 1)
+                d0 += static_cast<double>(w0[r]) * static_cast<double>(yv);
+            if (NDOT >= 2)
+                d1 += static_cast<double>(yv) * static_cast<double>(yv);
+        }
+    }
+    if (NDOT == 0)
+        return;
+    SpmvFinish<NDOT>(d0, d1, sc, st, fin, sh);
+}
+
+// Launches the padded-layout kernel when the view has the layout and it holds `vals` (the CSR values the caller
+// passes), the CSR kernel otherwise.
 template <typename TV, typename TX, int NDOT>
 void SpmvNode(cudaStream_t stream, const NodeSpmv& A, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc,
               int* st, int fin, const uint8_t* mask)
 {
+    const void* src = sizeof(TV) == 4 ? A.nbSrc32 : A.nbSrc64;
+    if (A.nbBase[0] && src == static_cast<const void*>(vals) && A.nbSeg4 > 0)
+    {
+        const size_t perGroup = static_cast<size_t>(A.nbSeg4) * sizeof(TX);
+        int threads = kBS;
+        while (threads > 32 && (threads / kNbG) * perGroup > 48 * 1024)
+            threads -= 32;
+        const int64_t total = A.totalWarps * kNbG;
+        const unsigned blocks = static_cast<unsigned>((total + threads - 1) / threads);
+        k_spmv_nb<TV, TX, NDOT><<<blocks, threads, (threads / kNbG) * perGroup, stream>>>(A, mask, x, y, w0, sc, st,
+                                                                                          fin);
+        return;
+    }
     const int64_t threads = A.totalWarps * 32;
     const unsigned blocks = static_cast<unsigned>((threads + kBS - 1) / kBS);
     k_spmv_node<TV, TX, NDOT><<<blocks, kBS, 0, stream>>>(A, vals, mask, x, y, w0, sc, st, fin);
