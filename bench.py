@@ -35,6 +35,10 @@ LOAD_STEPS = 20
 # inexact Newton: each inner Krylov solve (both precisions) reduces its residual by 1e3; Newton on the FP64 residual
 # then converges linearly at about max(1e-3, rounding of the FP32 tangent) per iteration
 KRYLOV_RTOL = 1e-3
+# mixed path: the Newton iterations with |C^T r| below 100 x the tolerance assemble the FP64 tangent and refine the
+# FP32 solves against it (exact Jacobian for the last steps; the relative displacement error against FP64 then stays
+# below 1e-6, with the FP32 tangent alone it is about 1e-5 on the damaged beam)
+EXACT_BELOW = 100.0
 
 
 def parse():
@@ -258,7 +262,7 @@ def run_ours(args):
     g = s.build_gpu(device=local)
     n_dofs, nnz = g.n_dofs, g.nnz
     opts32 = g.default_options(precision=nuto_gb300.FP32, newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20,
-                               max_krylov=20000)
+                               max_krylov=20000, exact_tangent_below=EXACT_BELOW)
     opts64 = g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20,
                                max_krylov=20000)
     dt = 1.0 / LOAD_STEPS
@@ -306,6 +310,7 @@ def run_ours(args):
         sec64, agg64 = timed(opts64)
         x64, _ = g.get_state()
         err = float(np.abs(x32 - x64).max() / max(np.abs(x64).max(), 1e-300))
+        err_l2 = float(np.linalg.norm(x32 - x64) / max(np.linalg.norm(x64), 1e-300))
         fp64 = {"value": n_dofs * agg64["matrix_assemblies"] / sec64, "unit": "DOF/s",
                 "ms_per_step": 1e3 * sec64 / args.steps,
                 "newton_step_ms": 1e3 * sec64 / max(agg64["matrix_assemblies"], 1),
@@ -314,7 +319,8 @@ def run_ours(args):
                 "speedup_mixed_vs_fp64_newton_step": (sec64 / max(agg64["matrix_assemblies"], 1))
                 / (sec32 / max(agg32["matrix_assemblies"], 1)),
                 "speedup_mixed_vs_fp64_load_step": sec64 / sec32,
-                "max_rel_displacement_error_mixed_vs_fp64": err}
+                "max_rel_displacement_error_mixed_vs_fp64": err,
+                "l2_rel_displacement_error_mixed_vs_fp64": err_l2}
         # both results against an FP64 solution of the same steps converged to 1e-11 (untimed): the displacement
         # uncertainty that the 1e-8 residual tolerance itself leaves is the scale for the mixed path's error
         opts_t = g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-11, krylov_rtol=1e-6, max_newton=40,
@@ -327,6 +333,9 @@ def run_ours(args):
             sc = max(np.abs(xt).max(), 1e-300)
             fp64["max_rel_displacement_error_vs_fp64_1e-11"] = {
                 "mixed": float(np.abs(x32 - xt).max() / sc), "fp64": float(np.abs(x64 - xt).max() / sc)}
+            nt = max(np.linalg.norm(xt), 1e-300)
+            fp64["l2_rel_displacement_error_vs_fp64_1e-11"] = {
+                "mixed": float(np.linalg.norm(x32 - xt) / nt), "fp64": float(np.linalg.norm(x64 - xt) / nt)}
         except Exception as exc:  # the reference solution is a diagnostic only
             fp64["max_rel_displacement_error_vs_fp64_1e-11"] = {"error": str(exc)}
 
@@ -391,8 +400,10 @@ def run_ours(args):
                                   "u_z=2e-3 (AdaptiveSolve cut-back), imperfection kappa=3 kappa0 in the two middle "
                                   "cell layers; timed load steps %d..%d" % (args.size, args.warmup + 1,
                                                                            args.warmup + args.steps),
-                      "n_dofs": n_dofs, "nnz": nnz, "precision": "FP32 tangent + FP32 GMRES(80), FP64 residual, "
-                                                                "history and Newton test",
+                      "n_dofs": n_dofs, "nnz": nnz,
+                      "precision": "FP32 tangent + FP32 GMRES(80) and multigrid, FP64 residual, history and Newton "
+                                   "test; the iterations with |C^T r| < %g tol assemble the FP64 tangent and refine "
+                                   "the FP32 solves against it" % EXACT_BELOW,
                       "newton_tolerance": "|C^T r| <= 1e-8 |C^T (r + K db)| of the load step",
                       "krylov_rtol": KRYLOV_RTOL, "l2": "inputs larger than L2 (FP32 tangent %.0f MB)" % (nnz * 4 / 1e6),
                       "parallelism": "replicas" if world > 1 else "single GPU"},

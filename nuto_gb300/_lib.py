@@ -50,6 +50,7 @@ class StepOptions(ctypes.Structure):
         ("precision", ctypes.c_int), ("method", ctypes.c_int), ("newton_rtol", ctypes.c_double),
         ("newton_atol", ctypes.c_double), ("max_newton", ctypes.c_int), ("line_search", ctypes.c_int),
         ("krylov_rtol", ctypes.c_double), ("max_krylov", ctypes.c_int), ("forcing", ctypes.c_int),
+        ("exact_tangent_below", ctypes.c_double),
     ]
 
 

@@ -405,7 +405,15 @@ NodeSpmv MakeNodeSpmv(const Ctx& c)
             A.nbBase[p] = c.nb.pair[p].base.p;
             A.nbOff[p] = c.nb.pair[p].off;
         }
-        A.nbSeg4 = c.nb.maxSeg4;
+        // per group the padded segments of every column slot of one row slot side by side
+        A.nbSeg4 = 0;
+        for (int I = 0; I < A.ns; ++I)
+        {
+            int sum = 0;
+            for (int J = 0; J < A.ns; ++J)
+                sum += c.nb.pair[I * A.ns + J].maxSeg4;
+            A.nbSeg4 = std::max(A.nbSeg4, sum);
+        }
         A.nb32 = c.nb.v32.p;
         A.nb64 = c.nb.v64.p;
         A.nbSrc32 = c.nb.src32;

@@ -58,6 +58,14 @@ __global__ void k_add(int64_t n, const double* __restrict__ g, double* __restric
         f[i] += g[i];
 }
 
+// FP32 rounding of the FP64 tangent (the preconditioned FP32 operator of the exact final phase)
+__global__ void k_round(int64_t n, const double* __restrict__ a, float* __restrict__ b)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i < n)
+        b[i] = static_cast<float>(a[i]);
+}
+
 namespace
 {
 struct Timers
@@ -123,9 +131,13 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     const bool mixed = o.precision == NUTO_GPU_MIXED;
     const bool fp32 = o.precision == NUTO_GPU_FP32 || mixed; // FP32 tangent values
     const int valPrec = fp32 ? NUTO_GPU_FP32 : NUTO_GPU_FP64;
+    // FP32 tangent with an exact final phase: the last Newton iterations assemble the FP64 tangent, solve with
+    // FP32 Krylov sweeps on its FP32 rounding and refine against the FP64 tangent itself
+    const bool exactPhase = o.precision == NUTO_GPU_FP32 && o.exact_tangent_below > 0.;
+    bool exactNow = false;
     if (fp32 && w.K32.n != static_cast<size_t>(c.nnz))
         w.K32.alloc(c.nnz);
-    if (!fp32 && w.K64.n != static_cast<size_t>(c.nnz))
+    if ((!fp32 || exactPhase) && w.K64.n != static_cast<size_t>(c.nnz))
         w.K64.alloc(c.nnz);
     void* K = fp32 ? static_cast<void*>(w.K32.p) : static_cast<void*>(w.K64.p);
     const int method = ResolveMethod(c, o.method);
@@ -138,7 +150,15 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
 
     auto assembleK = [&](const double* x) {
         const int k = T.Begin();
-        LaunchTangent(c, x, valPrec, K);
+        if (exactNow)
+        {
+            LaunchTangent(c, x, NUTO_GPU_FP64, w.K64.p);
+            k_round<<<static_cast<unsigned>((c.nnz + 255) / 256), 256, 0, c.stream>>>(c.nnz, w.K64.p, w.K32.p);
+            c.valsVersion++;
+            S.kernel_launches += 1;
+        }
+        else
+            LaunchTangent(c, x, valPrec, K);
         T.End(k, &S.ms_assemble_matrix);
         S.matrix_assemblies++;
     };
@@ -179,14 +199,18 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
             NG_CUDA(cudaMemsetAsync(out, 0, n * sizeof(double), c.stream));
             NG_CUDA(cudaMemcpyAsync(w.refR.p, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
             double rel = bn > 0. ? 1. : 0.;
-            for (int sweep = 0; sweep < 4 && rel > eta && it < o.max_krylov; ++sweep)
+            const int sweeps = exactNow ? 8 : 4;
+            for (int sweep = 0; sweep < sweeps && rel > eta && it < o.max_krylov; ++sweep)
             {
                 const double inner = std::min(0.5, std::max(eta / rel, 1e-5));
                 int its = 0;
                 KrylovSolveExport<float, float>(c, method, w.K32.p, w.refR.p, out, true, inner, o.max_krylov - it,
                                                 &its, nullptr);
                 it += its;
-                SpmvFull64(c, NUTO_GPU_FP32, w.K32.p, out, w.refKx.p);
+                if (exactNow)
+                    SpmvFull64(c, NUTO_GPU_FP64, w.K64.p, out, w.refKx.p);
+                else
+                    SpmvFull64(c, NUTO_GPU_FP32, w.K32.p, out, w.refKx.p);
                 Residual64(c, rhs, w.refKx.p, w.refR.p);
                 rel = bn > 0. ? MaskedNorm(c, w.refR.p) / bn : 0.;
                 if (verboseSweeps)
@@ -248,6 +272,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     double prevNr = nr, stepAlpha = 1., stepRel = lastRel;
     while (!conv && it < o.max_newton)
     {
+        exactNow = exactPhase && nr < o.exact_tangent_below * tol;
         assembleK(w.xs.p);
         k_masked_sum<<<gb, 256, 0, c.stream>>>(n, c.dMask.p, w.f.p, nullptr, w.rhs.p);
         S.kernel_launches += 1;

@@ -329,50 +329,76 @@ __global__ void __launch_bounds__(kBS) k_spmv_nb(NodeSpmv A, const uint8_t* __re
         valid = a < A.nNodes[I];
     }
     const int ncI = valid ? A.ncomp[I] : 0;
+    // neighbour ranges and value blocks of every column slot first (independent loads)
+    int64_t q0[kMaxSlots], vbase[kMaxSlots];
+    int nn[kMaxSlots], seg4[kMaxSlots], xoff[kMaxSlots];
+    int tot = 0, xo = 0;
+#pragma unroll
+    for (int J = 0; J < kMaxSlots; ++J)
+    {
+        q0[J] = 0;
+        nn[J] = 0;
+        vbase[J] = 0;
+        if (valid && J < A.ns)
+        {
+            const int p = I * A.ns + J;
+            q0[J] = A.nbrPtr[p][a];
+            nn[J] = static_cast<int>(A.nbrPtr[p][a + 1] - q0[J]);
+            vbase[J] = A.nbOff[p] + A.nbBase[p][a];
+        }
+        seg4[J] = (A.ncomp[J < A.ns ? J : 0] * nn[J] + 3) & ~3;
+        xoff[J] = xo;
+        xo += seg4[J];
+        tot += nn[J];
+    }
+    // x of all neighbours of all column slots into the group's segment buffers (unrolled: several neighbour ->
+    // x chains in flight per lane)
+    const int nc0 = A.ncomp[0], nc1 = A.ns > 1 ? A.ncomp[1] : 0;
+#pragma unroll 4
+    for (int t = gl; t < tot; t += kNbG)
+    {
+        const int J = t >= nn[0] ? 1 : 0;
+        const int kk = t - (J ? nn[0] : 0);
+        const int ncJ = J ? nc1 : nc0;
+        const int p = I * A.ns + J;
+        const int64_t col = A.nbrCol[p][NG_IDX((J ? q0[1] : q0[0]) + kk, A.nbrTotal[p], 60)];
+        const int xb = (J ? xoff[1] : 0) + kk * ncJ;
+        for (int d = 0; d < ncJ; ++d)
+            xs[NG_IDX(xb + d, L, 61)] = x[NG_IDX(col + d, A.nRows, 62)];
+    }
+#pragma unroll
+    for (int J = 0; J < kMaxSlots; ++J)
+    {
+        const int seg = (J ? nc1 : nc0) * nn[J];
+        for (int t = seg + gl; t < seg4[J]; t += kNbG)
+            xs[NG_IDX(xoff[J] + t, L, 63)] = TX(0);
+    }
+    __syncwarp();
     TX s[kMaxComp];
 #pragma unroll
     for (int c = 0; c < kMaxComp; ++c)
         s[c] = TX(0);
-    for (int J = 0; J < A.ns; ++J) // the same trip count in every lane: the warp syncs below are uniform
-    {
-        const int p = I * A.ns + J;
-        const int ncJ = A.ncomp[J];
-        int64_t q0 = 0;
-        int nn = 0;
-        if (valid)
-        {
-            q0 = A.nbrPtr[p][a];
-            nn = static_cast<int>(A.nbrPtr[p][a + 1] - q0);
-        }
-        const int seg = ncJ * nn, seg4 = (seg + 3) & ~3;
-        for (int t = gl; t < nn; t += kNbG)
-        {
-            const int64_t col = A.nbrCol[p][NG_IDX(q0 + t, A.nbrTotal[p], 60)];
-            for (int d = 0; d < ncJ; ++d)
-                xs[NG_IDX(t * ncJ + d, L, 61)] = x[NG_IDX(col + d, A.nRows, 62)];
-        }
-        for (int t = seg + gl; t < seg4; t += kNbG)
-            xs[NG_IDX(t, L, 63)] = TX(0);
-        __syncwarp();
-        if (valid)
-        {
-            const TV* vp = vals + A.nbOff[p] + A.nbBase[p][a];
-            for (int f = 4 * gl; f < seg4; f += 4 * kNbG)
-            {
-                TX xv[4];
-                Load4(xs + f, xv);
 #pragma unroll
-                for (int c = 0; c < kMaxComp; ++c)
-                    if (c < ncI)
-                    {
-                        TV v[4];
-                        Load4(vp + c * seg4 + f, v);
-                        s[c] += static_cast<TX>(v[0]) * xv[0] + static_cast<TX>(v[1]) * xv[1] +
-                                static_cast<TX>(v[2]) * xv[2] + static_cast<TX>(v[3]) * xv[3];
-                    }
-            }
+    for (int J = 0; J < kMaxSlots; ++J)
+    {
+        const TV* vp = vals + vbase[J];
+        const TX* xj = xs + xoff[J];
+        const int sg = seg4[J];
+#pragma unroll 2
+        for (int f = 4 * gl; f < sg; f += 4 * kNbG)
+        {
+            TX xv[4];
+            Load4(xj + f, xv);
+#pragma unroll
+            for (int c = 0; c < kMaxComp; ++c)
+                if (c < ncI)
+                {
+                    TV v[4];
+                    Load4(vp + c * sg + f, v);
+                    s[c] += static_cast<TX>(v[0]) * xv[0] + static_cast<TX>(v[1]) * xv[1] +
+                            static_cast<TX>(v[2]) * xv[2] + static_cast<TX>(v[3]) * xv[3];
+                }
         }
-        __syncwarp(); // the segment buffer is refilled for the next J
     }
 #pragma unroll
     for (int o = kNbG / 2; o > 0; o >>= 1)

@@ -295,6 +295,29 @@ def test_quasistatic_hex8_gradient_damage(precision):
     assert res[-1][2].max() > 1e-4  # the last steps are in the damaged regime
 
 
+def test_exact_final_phase_within_1e6_of_converged_solution():
+    """FP32 tangent with the exact final phase (exact_tangent_below = 100, the default): at the benchmark's relative
+    Newton tolerance 1e-8, eight load steps into the damaged regime end within 1e-6 (relative, max norm) of the
+    oracle's direct-solve Newton converged to 1e-12, as the FP64 path does."""
+    _torch()
+    res = {}
+    for name, prec, ex in (("fp64", 64, 0.0), ("exact", 32, 100.0)):
+        s, g, (om, layers, P, cons) = _build("hex8gd", 6)
+        Q = QuasistaticOracle(P, cons[0], cons[1], cons[2], tolerance=1e-12, max_iterations=30)
+        g.set_state(None, 0.0, True)
+        opts = g.default_options(precision=prec, newton_rtol=1e-8, krylov_rtol=1e-3, max_newton=30,
+                                 max_krylov=50000, exact_tangent_below=ex)
+        for k in range(1, 9):
+            t = 0.05 * k
+            Q.do_step(t)
+            g.do_step(t, opts)
+        x, _ = g.get_state()
+        res[name] = np.abs(x - Q.x).max() / np.abs(Q.x).max()
+        assert P.kappa.max() > 1e-4  # damaged regime
+    assert res["fp64"] <= 1e-6, res
+    assert res["exact"] <= 1e-6, res
+
+
 @pytest.mark.parametrize("kind,n,steps", [("hex8gd", 8, 0), ("hex8gd", 8, 6), ("hex20", 4, 0), ("quad4", 40, 0)])
 def test_multigrid_levels_solve(kind, n, steps):
     """Multigrid-preconditioned solves on meshes large enough for several levels: GMRES (FP64 and FP32 values)
