@@ -190,6 +190,10 @@ int nuto_gpu_build_pattern(nuto_gpu_ctx* ctx, int64_t* n_dofs, int64_t* nnz);
 int nuto_gpu_copy_pattern(nuto_gpu_ctx* ctx, int64_t* row_ptr, int32_t* col_idx);
 /* Device pointers of the pattern (valid until the context is destroyed). */
 int nuto_gpu_pattern_device(nuto_gpu_ctx* ctx, const int64_t** d_row_ptr, const int32_t** d_col_idx);
+/* Sizes of the solver's copy of the tangent (no counterpart in the reference): values of the padded pair layout
+   the Krylov products stream (node row segments per slot pair padded to multiples of 4) and entries of the
+   neighbour lists that drive the gathers; for traffic accounting. */
+int nuto_gpu_solver_layout(const nuto_gpu_ctx* ctx, int64_t* padded_values, int64_t* neighbour_entries);
 
 int nuto_gpu_set_integrand(nuto_gpu_ctx* ctx, const nuto_gpu_integrand* params);
 int nuto_gpu_num_integration_points(const nuto_gpu_ctx* ctx);

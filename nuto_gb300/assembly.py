@@ -97,6 +97,13 @@ class GpuCellGroup:
         pairs = self.nnz // (ncomp * ncomp)
         return sum(pairs * 4 + (L.num_nodes + 1) * 8 for L in layers) * len(layers)
 
+    def solver_layout(self):
+        """(padded values, neighbour-list entries) of the solver's copy of the tangent"""
+        v = ctypes.c_int64()
+        e = ctypes.c_int64()
+        self._call("nuto_gpu_solver_layout", ctypes.byref(v), ctypes.byref(e))
+        return v.value, e.value
+
     def pattern(self):
         rp = np.empty(self.n_dofs + 1, dtype=np.int64)
         ci = np.empty(self.nnz, dtype=np.int32)

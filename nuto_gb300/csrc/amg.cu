@@ -641,6 +641,160 @@ __global__ void k_convert(int64_t n, const TA* __restrict__ a, TB* __restrict__ 
         b[i] = static_cast<TB>(a[i]);
 }
 
+// ---- device: the coarsest levels in one block ----------------------------------------------------------------
+// Levels with at most kTailNodes nodes (and every coarser one) do microseconds of work per launch; run as separate
+// launches they cost about 29 launches per slot and cycle. One block of kTailThreads threads runs their whole
+// V-cycle instead: the same Chebyshev recurrences (coefficients from the same double-precision formulas), the same
+// restriction and prolongation, and a warp-per-node product on the coarse node-block CSR, with block barriers
+// between the steps. The level vectors stay in global memory (L2-resident at these sizes).
+constexpr int kTailNodes = 128;
+constexpr int kTailMax = 8;
+constexpr int kTailThreads = 1024;
+
+template <typename TA>
+struct TailLevel
+{
+    const int64_t* rowPtr;
+    const int64_t* nbrPtr;
+    const int32_t* nbrCol;
+    const int32_t* agg; // this level's nodes -> nodes of the next coarser level (unused on the coarsest)
+    const TA* vals;
+    const TA* dinv;
+    TA *b, *e, *t, *d;
+    int64_t nNodes, nnz, nDofs, nbrTotal;
+    int ncomp;
+    double lmax;
+};
+
+template <typename TA>
+struct TailArgs
+{
+    int nl;
+    int pre, post, coarse;
+    double smoothRatio, coarseRatio;
+    TailLevel<TA> L[kTailMax];
+};
+
+template <typename TA>
+__device__ void TailSpmv(const TailLevel<TA>& L, const TA* __restrict__ x, TA* __restrict__ y)
+{
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int nc = L.ncomp;
+    for (int64_t a = threadIdx.x >> 5; a < L.nNodes; a += nw)
+    {
+        const int64_t q0 = L.nbrPtr[a];
+        const int len = static_cast<int>(L.nbrPtr[a + 1] - q0) * nc;
+        TA s[kMaxComp];
+#pragma unroll
+        for (int c = 0; c < kMaxComp; ++c)
+            s[c] = TA(0);
+        for (int q = lane; q < len; q += 32)
+        {
+            const int k = q / nc, d = q - k * nc;
+            const TA xv = x[NG_IDX(L.nbrCol[NG_IDX(q0 + k, L.nbrTotal, 70)] + d, L.nDofs, 71)];
+#pragma unroll
+            for (int c = 0; c < kMaxComp; ++c)
+                if (c < nc)
+                    s[c] += L.vals[NG_IDX(L.rowPtr[a * nc + c] + q, L.nnz, 72)] * xv;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < kMaxComp; ++c)
+                s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
+        if (lane == 0)
+            for (int c = 0; c < nc; ++c)
+                y[a * nc + c] = s[c];
+    }
+}
+
+// Chebyshev smoothing of A e = b on [lmax / ratio, lmax]; ends with a block barrier
+template <typename TA>
+__device__ void TailCheb(const TailLevel<TA>& L, int degree, bool fromZero, double ratio)
+{
+    const double lmax = L.lmax, lmin = L.lmax / ratio;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+    const double sigma = theta / delta;
+    double rho = 1. / sigma;
+    const TA invTheta = TA(1. / theta);
+    if (fromZero)
+    {
+        for (int64_t i = threadIdx.x; i < L.nDofs; i += blockDim.x)
+        {
+            const TA v = L.dinv[i] * L.b[i] * invTheta;
+            L.d[i] = v;
+            L.e[i] = v;
+        }
+    }
+    else
+    {
+        TailSpmv(L, L.e, L.t);
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < L.nDofs; i += blockDim.x)
+        {
+            const TA v = L.dinv[i] * (L.b[i] - L.t[i]) * invTheta;
+            L.d[i] = v;
+            L.e[i] += v;
+        }
+    }
+    __syncthreads();
+    for (int k = 1; k < degree; ++k)
+    {
+        const double rhoNew = 1. / (2. * sigma - rho);
+        const TA c1 = TA(rhoNew * rho), c2 = TA(2. * rhoNew / delta);
+        TailSpmv(L, L.e, L.t);
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < L.nDofs; i += blockDim.x)
+        {
+            const TA v = c1 * L.d[i] + c2 * L.dinv[i] * (L.b[i] - L.t[i]);
+            L.d[i] = v;
+            L.e[i] += v;
+        }
+        __syncthreads();
+        rho = rhoNew;
+    }
+}
+
+// e = V-cycle(b) on the tail levels: the first level's b is the restriction from the finer level, its e is read by
+// the finer level's prolongation
+template <typename TA>
+__global__ void __launch_bounds__(kTailThreads) k_amg_tail(TailArgs<TA> T, const int* st)
+{
+    if (Idle(st))
+        return;
+    for (int l = 0; l + 1 < T.nl; ++l)
+    {
+        const TailLevel<TA>& F = T.L[l];
+        const TailLevel<TA>& C = T.L[l + 1];
+        TailCheb(F, T.pre, true, T.smoothRatio);
+        TailSpmv(F, F.e, F.t);
+        for (int64_t i = threadIdx.x; i < C.nDofs; i += blockDim.x)
+            C.b[i] = TA(0);
+        __syncthreads();
+        for (int64_t a = threadIdx.x; a < F.nNodes; a += blockDim.x)
+        {
+            const int64_t A = F.agg[a];
+            for (int c = 0; c < F.ncomp; ++c)
+                atomicAdd(C.b + NG_IDX(A * C.ncomp + c, C.nDofs, 73), F.b[a * F.ncomp + c] - F.t[a * F.ncomp + c]);
+        }
+        __syncthreads();
+    }
+    TailCheb(T.L[T.nl - 1], T.coarse, true, T.coarseRatio);
+    for (int l = T.nl - 2; l >= 0; --l)
+    {
+        const TailLevel<TA>& F = T.L[l];
+        const TailLevel<TA>& C = T.L[l + 1];
+        for (int64_t a = threadIdx.x; a < F.nNodes; a += blockDim.x)
+        {
+            const int64_t A = F.agg[a];
+            for (int c = 0; c < F.ncomp; ++c)
+                F.e[a * F.ncomp + c] += C.e[NG_IDX(A * C.ncomp + c, C.nDofs, 74)];
+        }
+        __syncthreads();
+        TailCheb(F, T.post, false, T.smoothRatio);
+    }
+}
+
 // ---- host: set-up and application ------------------------------------------------------------------------------
 static unsigned Blocks(int64_t n, int bs = 256)
 {
@@ -762,6 +916,15 @@ static void Chebyshev(Ctx& c, AmgLevel& L, const TA* vals, const uint8_t* mask, 
     }
 }
 
+// first level (>= 1) from which every level has at most kTailNodes nodes, if they fit one tail launch; 0: none
+static size_t TailStart(const std::vector<AmgLevel>& H)
+{
+    for (size_t l = 1; l < H.size(); ++l)
+        if (H[l].nNodes <= kTailNodes)
+            return H.size() - l <= static_cast<size_t>(kTailMax) ? l : 0;
+    return 0;
+}
+
 // e = V-cycle(b) on level l of hierarchy H
 template <typename TA>
 static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const TA* b, TA* e, const int* st, bool sym)
@@ -771,6 +934,43 @@ static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const TA* b, TA* 
     Num<TA>& U = N<TA>(L);
     const TA* vals = l == 0 ? static_cast<const TA*>(M.fine) : U.vals.p;
     const uint8_t* mask = l == 0 ? c.dMask.p : L.zeroMask.p;
+    if (l > 0 && l == TailStart(H))
+    {
+        // this level and every coarser one in one block (b = U.b, e = U.e of this level)
+        TailArgs<TA> T{};
+        T.nl = static_cast<int>(H.size() - l);
+        T.pre = sym ? kPostDegree : kPreDegree;
+        T.post = kPostDegree;
+        T.coarse = kCoarseDegree;
+        T.smoothRatio = kSmoothRatio;
+        T.coarseRatio = kCoarseRatio;
+        for (int k = 0; k < T.nl; ++k)
+        {
+            AmgLevel& Lk = H[l + k];
+            Num<TA>& Uk = N<TA>(Lk);
+            TailLevel<TA>& D = T.L[k];
+            D.rowPtr = Lk.rowPtr.p;
+            D.nbrPtr = Lk.nbrPtr.p;
+            D.nbrCol = Lk.nbrCol.p;
+            D.agg = l + k + 1 < H.size() ? H[l + k + 1].aggOf.p : nullptr;
+            D.vals = Uk.vals.p;
+            D.dinv = Uk.dinv.p;
+            D.b = Uk.b.p;
+            D.e = Uk.e.p;
+            D.t = Uk.t.p;
+            D.d = Uk.d.p;
+            D.nNodes = Lk.nNodes;
+            D.nnz = Lk.nnz;
+            D.nDofs = Lk.nDofs;
+            D.nbrTotal = static_cast<int64_t>(Lk.nbrIdx.n);
+            D.ncomp = Lk.ncomp;
+            D.lmax = Lk.lmax;
+        }
+        // the level's b and e are the ones the caller passed (its own U.b, U.e)
+        k_amg_tail<TA><<<1, kTailThreads, 0, c.stream>>>(T, st);
+        c.stats.kernel_launches += 1;
+        return;
+    }
     if (l + 1 == H.size())
     {
         Chebyshev<TA>(c, L, vals, mask, b, e, kCoarseDegree, true, kCoarseRatio, st);

@@ -842,6 +842,20 @@ int nuto_gpu_num_integration_points(const nuto_gpu_ctx* ctx)
     return ctx ? ctx->ip.nIp : 0;
 }
 
+int nuto_gpu_solver_layout(const nuto_gpu_ctx* ctx, int64_t* padded_values, int64_t* neighbour_entries)
+{
+    if (!ctx || !padded_values || !neighbour_entries)
+        return NUTO_GPU_EINVAL;
+    if (!ctx->havePattern)
+        return NUTO_GPU_ESTATE;
+    int64_t e = 0;
+    for (const PairMap& M : ctx->pairs)
+        e += static_cast<int64_t>(M.hNbrIdx.size());
+    *padded_values = ctx->nb.total;
+    *neighbour_entries = e;
+    return NUTO_GPU_OK;
+}
+
 int nuto_gpu_set_history(nuto_gpu_ctx* ctx, const double* kappa)
 {
     return Guard(ctx, [&] {
