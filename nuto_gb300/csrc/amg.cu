@@ -43,6 +43,7 @@ template <typename TA>
 struct Num
 {
     DBuf<TA> vals, dinv, e, b, t, d;
+    DBuf<TA> nb; // coarse levels: the values in the padded layout of the level's SpMV
 };
 
 struct AmgLevel
@@ -59,6 +60,9 @@ struct AmgLevel
     DBuf<int64_t> gdof, rowPtr, nbrPtr;
     DBuf<int32_t> nbrIdx, nbrCol, blk;
     DBuf<int32_t> diagOff;  // per node: offset of the diagonal block in the node's row segment
+    DBuf<int64_t> nbBase;   // coarse levels: per node, first value of the node's block in the padded layout
+    int64_t nbTotal = 0;
+    int nbSeg4 = 0;
     DBuf<uint8_t> zeroMask; // coarse levels have no constrained rows
     // transfer from the finer level
     DBuf<int32_t> aggOf;   // finer node -> node of this level
@@ -430,6 +434,22 @@ static void BuildSlotHierarchy(Ctx& c, int I, const double* ext, std::vector<Amg
             UploadV(C.nbrCol, col);
         }
         UploadV(C.diagOff, DiagOffsets(C.hNbrPtr, C.hNbrIdx, C.ncomp));
+        {
+            // padded layout of the level: per node ncomp rows of ncomp * nn values, padded to multiples of 4
+            std::vector<int64_t> base(C.nNodes);
+            int64_t pos = 0;
+            int mx = 0;
+            for (int64_t A = 0; A < C.nNodes; ++A)
+            {
+                const int seg4 = static_cast<int>((C.ncomp * (C.hNbrPtr[A + 1] - C.hNbrPtr[A]) + 3) / 4 * 4);
+                base[A] = pos;
+                pos += static_cast<int64_t>(C.ncomp) * seg4;
+                mx = std::max(mx, seg4);
+            }
+            UploadV(C.nbBase, base);
+            C.nbTotal = pos;
+            C.nbSeg4 = mx;
+        }
         UploadV(C.aggOf, agg);
         UploadV(C.cRank, cr);
         C.zeroMask.alloc(C.nDofs);
@@ -814,7 +834,10 @@ static void EnsureNum(Ctx& c, Amg& M)
             if (U.dinv.n == static_cast<size_t>(n))
                 continue;
             if (l > 0)
+            {
                 U.vals.alloc(L.nnz);
+                U.nb.alloc(std::max<int64_t>(L.nbTotal, 4));
+            }
             for (DBuf<TA>* b : {&U.dinv, &U.e, &U.b, &U.t, &U.d})
                 b->alloc(n);
         }
@@ -861,6 +884,26 @@ void AmgSetup(Ctx& c, const TV* vals)
             k_amg_diag<TV><<<Blocks(C.nNodes * 32), kBS, 0, c.stream>>>(C.spmv, C.zeroMask.p, CU.vals.p, C.diagOff.p,
                                                                          CU.dinv.p, M.lmaxDev.p + slot + l);
             c.stats.kernel_launches += 2;
+            if (C.nbTotal > 0)
+            {
+                // the level's products stream the padded layout (filled from the new Galerkin values)
+                NodeSpmv& V = C.spmv;
+                V.nbBase[0] = C.nbBase.p;
+                V.nbOff[0] = 0;
+                V.nbSeg4 = C.nbSeg4;
+                if constexpr (sizeof(TV) == 4)
+                {
+                    V.nb32 = CU.nb.p;
+                    V.nbSrc32 = CU.vals.p;
+                }
+                else
+                {
+                    V.nb64 = CU.nb.p;
+                    V.nbSrc64 = CU.vals.p;
+                }
+                k_nb_pack<TV><<<Blocks(C.nNodes * 32), kBS, 0, c.stream>>>(V, CU.vals.p, CU.nb.p);
+                c.stats.kernel_launches += 1;
+            }
         }
         slot += H.size();
     }

@@ -428,6 +428,36 @@ __global__ void __launch_bounds__(kBS) k_spmv_nb(NodeSpmv A, const uint8_t* __re
     SpmvFinish<NDOT>(d0, d1, sc, st, fin, sh);
 }
 
+// CSR values -> padded pair layout: one warp per node of the view, lanes over the segment
+template <typename TV>
+__global__ void __launch_bounds__(kBS) k_nb_pack(NodeSpmv A, const TV* __restrict__ csr, TV* __restrict__ nb)
+{
+    const int64_t u = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (u >= A.totalWarps)
+        return;
+    const int I = (A.ns > 1 && u >= A.firstWarp[1]) ? 1 : 0;
+    const int64_t a = u - A.firstWarp[I];
+    if (a >= A.nNodes[I])
+        return;
+    const int ncI = A.ncomp[I];
+    const int64_t g0 = A.gdof[I][a];
+    for (int J = 0; J < A.ns; ++J)
+    {
+        const int p = I * A.ns + J;
+        const int nn = static_cast<int>(A.nbrPtr[p][a + 1] - A.nbrPtr[p][a]);
+        const int seg = A.ncomp[J] * nn, seg4 = (seg + 3) & ~3;
+        const int32_t blk = A.blk[p][a];
+        TV* dst = nb + A.nbOff[p] + A.nbBase[p][a];
+        for (int c = 0; c < ncI; ++c)
+        {
+            const TV* src = csr + A.rowPtr[NG_IDX(g0 + c, A.nRows, 65)] + blk;
+            for (int q = lane; q < seg4; q += 32)
+                dst[c * seg4 + q] = q < seg ? src[NG_IDX(q, A.nnz, 66)] : TV(0);
+        }
+    }
+}
+
 // Launches the padded-layout kernel when the view has the layout and it holds `vals` (the CSR values the caller
 // passes), the CSR kernel otherwise.
 template <typename TV, typename TX, int NDOT>
