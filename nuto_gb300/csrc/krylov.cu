@@ -509,6 +509,174 @@ double MaskedNorm(Ctx& c, const double* v)
     return std::sqrt(r);
 }
 
+// ---- FP32 values times FP64 vectors on the FP32 pipe --------------------------------------------------------------
+// y = K x with FP32 values and an FP64 x given as hi + lo floats (xs[i] = (hi, lo)): v * hi is formed exactly
+// (product and its FMA error term) and summed with TwoSum compensation, v * lo in plain FP32; each lane's row sums
+// go to FP64 only for the final 8-lane butterfly. About 48 bits of the sum survive (relative error ~1e-14 of
+// sum |v x|), enough for the residual of an FP32 iterative refinement, with no FP64 arithmetic per nonzero: the
+// FP64-vector form of this product is limited by the FP64 pipe on this part.
+__device__ __forceinline__ void TwoSumAcc(float& s, float& err, float p)
+{
+    const float t = s + p;
+    const float bp = t - s;
+    err += (s - (t - bp)) + (p - bp);
+    s = t;
+}
+
+__global__ void __launch_bounds__(kBS) k_spmv_nb_comp(NodeSpmv A, const uint8_t* __restrict__ mask,
+                                                       const float2* __restrict__ xs2, const double* __restrict__ x,
+                                                       double* __restrict__ y)
+{
+    extern __shared__ __align__(16) unsigned char nbSmem[];
+    const float* __restrict__ vals = A.nb32;
+    const int gl = threadIdx.x & (kNbG - 1);
+    const int L = A.nbSeg4;
+    float2* xs = reinterpret_cast<float2*>(nbSmem) + (threadIdx.x / kNbG) * L;
+    const int64_t u = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / kNbG;
+    int I = 0;
+    int64_t a = 0;
+    bool valid = u < A.totalWarps;
+    if (valid)
+    {
+        I = (A.ns > 1 && u >= A.firstWarp[1]) ? 1 : 0;
+        a = u - A.firstWarp[I];
+        valid = a < A.nNodes[I];
+    }
+    const int ncI = valid ? A.ncomp[I] : 0;
+    int64_t q0[kMaxSlots], vbase[kMaxSlots];
+    int nn[kMaxSlots], seg4[kMaxSlots], xoff[kMaxSlots];
+    int tot = 0, xo = 0;
+#pragma unroll
+    for (int J = 0; J < kMaxSlots; ++J)
+    {
+        q0[J] = 0;
+        nn[J] = 0;
+        vbase[J] = 0;
+        if (valid && J < A.ns)
+        {
+            const int p = I * A.ns + J;
+            q0[J] = A.nbrPtr[p][a];
+            nn[J] = static_cast<int>(A.nbrPtr[p][a + 1] - q0[J]);
+            vbase[J] = A.nbOff[p] + A.nbBase[p][a];
+        }
+        seg4[J] = (A.ncomp[J < A.ns ? J : 0] * nn[J] + 3) & ~3;
+        xoff[J] = xo;
+        xo += seg4[J];
+        tot += nn[J];
+    }
+    const int nc0 = A.ncomp[0], nc1 = A.ns > 1 ? A.ncomp[1] : 0;
+#pragma unroll 4
+    for (int t = gl; t < tot; t += kNbG)
+    {
+        const int J = t >= nn[0] ? 1 : 0;
+        const int kk = t - (J ? nn[0] : 0);
+        const int ncJ = J ? nc1 : nc0;
+        const int p = I * A.ns + J;
+        const int64_t col = A.nbrCol[p][NG_IDX((J ? q0[1] : q0[0]) + kk, A.nbrTotal[p], 60)];
+        const int xb = (J ? xoff[1] : 0) + kk * ncJ;
+        for (int d = 0; d < ncJ; ++d)
+            xs[NG_IDX(xb + d, L, 61)] = xs2[NG_IDX(col + d, A.nRows, 62)];
+    }
+#pragma unroll
+    for (int J = 0; J < kMaxSlots; ++J)
+    {
+        const int seg = (J ? nc1 : nc0) * nn[J];
+        for (int t = seg + gl; t < seg4[J]; t += kNbG)
+            xs[NG_IDX(xoff[J] + t, L, 63)] = make_float2(0.f, 0.f);
+    }
+    __syncwarp();
+    float sh[kMaxComp], se[kMaxComp], sl[kMaxComp];
+#pragma unroll
+    for (int c = 0; c < kMaxComp; ++c)
+        sh[c] = se[c] = sl[c] = 0.f;
+#pragma unroll
+    for (int J = 0; J < kMaxSlots; ++J)
+    {
+        const float* vp = vals + vbase[J];
+        const float2* xj = xs + xoff[J];
+        const int sg = seg4[J];
+        for (int f = 4 * gl; f < sg; f += 4 * kNbG)
+        {
+            const float4 x01 = *reinterpret_cast<const float4*>(xj + f);
+            const float4 x23 = *reinterpret_cast<const float4*>(xj + f + 2);
+            const float xh[4] = {x01.x, x01.z, x23.x, x23.z}, xl[4] = {x01.y, x01.w, x23.y, x23.w};
+#pragma unroll
+            for (int c = 0; c < kMaxComp; ++c)
+                if (c < ncI)
+                {
+                    const float4 v4 = *reinterpret_cast<const float4*>(vp + c * sg + f);
+                    const float v[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                    {
+                        const float p = v[k] * xh[k];
+                        se[c] += fmaf(v[k], xh[k], -p);
+                        TwoSumAcc(sh[c], se[c], p);
+                        sl[c] = fmaf(v[k], xl[k], sl[c]);
+                    }
+                }
+        }
+    }
+    double s[kMaxComp];
+#pragma unroll
+    for (int c = 0; c < kMaxComp; ++c)
+        s[c] = static_cast<double>(sh[c]) + (static_cast<double>(se[c]) + static_cast<double>(sl[c]));
+#pragma unroll
+    for (int o = kNbG / 2; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < kMaxComp; ++c)
+            s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
+    if (valid && gl == 0)
+    {
+        const int64_t g0 = A.gdof[I][a];
+        for (int c = 0; c < ncI; ++c)
+        {
+            const int64_t r = NG_IDX(g0 + c, A.nRows, 64);
+            y[r] = mask[r] ? x[r] : s[c];
+        }
+    }
+}
+
+// x (FP64) -> (hi, lo) floats for k_spmv_nb_comp
+__global__ void k_split_hilo(int64_t n, const double* __restrict__ x, float2* __restrict__ xs)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= n)
+        return;
+    const float h = static_cast<float>(x[i]);
+    xs[i] = make_float2(h, static_cast<float>(x[i] - static_cast<double>(h)));
+}
+
+void SpmvFull64Comp(Ctx& c, const float* vals, const double* x, double* y)
+{
+    SolverWork& w = Work(c);
+    const int64_t n = c.nDofs;
+    EnsureNb(c, vals);
+    const NodeSpmv A = MakeNodeSpmv(c);
+    if (!A.nbBase[0] || A.nbSrc32 != static_cast<const void*>(vals) || A.nbSeg4 <= 0)
+    {
+        SpmvFull64(c, NUTO_GPU_FP32, vals, x, y); // no padded layout: exact FP64 accumulation
+        return;
+    }
+    if (w.zeroMask.n != static_cast<size_t>(n))
+    {
+        w.zeroMask.alloc(n);
+        NG_CUDA(cudaMemsetAsync(w.zeroMask.p, 0, n, c.stream));
+    }
+    if (w.xsplit.n != static_cast<size_t>(2 * n))
+        w.xsplit.alloc(2 * n);
+    float2* xs = reinterpret_cast<float2*>(w.xsplit.p);
+    k_split_hilo<<<static_cast<unsigned>((n + 255) / 256), 256, 0, c.stream>>>(n, x, xs);
+    const size_t perGroup = static_cast<size_t>(A.nbSeg4) * sizeof(float2);
+    int threads = kBS;
+    while (threads > 32 && (threads / kNbG) * perGroup > 48 * 1024)
+        threads -= 32;
+    const unsigned blocks = static_cast<unsigned>((A.totalWarps * kNbG + threads - 1) / threads);
+    k_spmv_nb_comp<<<blocks, threads, (threads / kNbG) * perGroup, c.stream>>>(A, w.zeroMask.p, xs, x, y);
+    c.stats.kernel_launches += 2;
+    AfterLaunch(c, "krylov");
+}
+
 void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double* y)
 {
     SolverWork& w = Work(c);

@@ -210,7 +210,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
                 if (exactNow)
                     SpmvFull64(c, NUTO_GPU_FP64, w.K64.p, out, w.refKx.p);
                 else
-                    SpmvFull64(c, NUTO_GPU_FP32, w.K32.p, out, w.refKx.p);
+                    SpmvFull64Comp(c, w.K32.p, out, w.refKx.p);
                 Residual64(c, rhs, w.refKx.p, w.refR.p);
                 rel = bn > 0. ? MaskedNorm(c, w.refR.p) / bn : 0.;
                 if (verboseSweeps)

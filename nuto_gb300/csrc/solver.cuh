@@ -123,6 +123,7 @@ struct SolverWork
     DBuf<double> K64;
     DBuf<double> f, rhs, dx, db, x0, xs, tmp;
     DBuf<double> refR, refKx; // FP64 refinement of the FP32 Newton solves
+    DBuf<float> xsplit;       // 2n: x as (hi, lo) floats for the compensated FP32 product
     DBuf<uint8_t> zeroMask;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // CUDA-event pairs around the Krylov SpMV launches, folded into stats at synchronisation points
@@ -137,6 +138,9 @@ SolverWork& Work(Ctx& c);
 double MaskedNorm(Ctx& c, const double* v);
 // y = K x for CSR values of the given precision, all rows (no constraint masking), FP64 vectors
 void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double* y);
+// y = K x for FP32 values and FP64 vectors in compensated FP32 arithmetic (about 1e-14 relative to sum |K x|): the
+// residual of the FP32 Newton refinement
+void SpmvFull64Comp(Ctx& c, const float* vals, const double* x, double* y);
 // r = mask0(b - kx)
 void Residual64(Ctx& c, const double* b, const double* kx, double* r);
 // NUTO_GPU_SOLVER_AUTO resolves to PCG for the symmetric integrands and GMRES otherwise
