@@ -578,6 +578,8 @@ template <typename TA>
 __global__ void k_cheb0(int64_t n, const TA* __restrict__ dinv, const TA* __restrict__ b, TA* d, TA* e, TA invTheta,
                         const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i >= n || Idle(st))
         return;
@@ -591,6 +593,8 @@ template <typename TA>
 __global__ void k_cheb1(int64_t n, const TA* __restrict__ dinv, const TA* __restrict__ b, const TA* __restrict__ t,
                         TA* d, TA* e, TA invTheta, const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i >= n || Idle(st))
         return;
@@ -604,6 +608,8 @@ template <typename TA>
 __global__ void k_chebk(int64_t n, const TA* __restrict__ dinv, const TA* __restrict__ b, const TA* __restrict__ t,
                         TA* d, TA* e, TA c1, TA c2, const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i >= n || Idle(st))
         return;
@@ -618,6 +624,8 @@ __global__ void k_restrict(NodeSpmv F, const uint8_t* __restrict__ fmask, const 
                            const TA* __restrict__ t, const int32_t* __restrict__ agg, NodeSpmv C, TA* cb,
                            const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     const int64_t a = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (a >= F.totalWarps || Idle(st))
         return;
@@ -633,6 +641,8 @@ template <typename TA>
 __global__ void k_prolong(NodeSpmv F, const uint8_t* __restrict__ fmask, const int32_t* __restrict__ agg, NodeSpmv C,
                           const TA* __restrict__ ce, TA* e, const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     const int64_t a = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (a >= F.totalWarps || Idle(st))
         return;
@@ -647,6 +657,8 @@ __global__ void k_prolong(NodeSpmv F, const uint8_t* __restrict__ fmask, const i
 template <typename TA>
 __global__ void k_sub(int64_t n, const TA* a, const TA* b, TA* y, const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i >= n || Idle(st))
         return;
@@ -656,6 +668,8 @@ __global__ void k_sub(int64_t n, const TA* a, const TA* b, TA* y, const int* st)
 template <typename TA, typename TB>
 __global__ void k_convert(int64_t n, const TA* __restrict__ a, TB* __restrict__ b, const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i < n && !Idle(st))
         b[i] = static_cast<TB>(a[i]);
@@ -780,6 +794,8 @@ __device__ void TailCheb(const TailLevel<TA>& L, int degree, bool fromZero, doub
 template <typename TA>
 __global__ void __launch_bounds__(kTailThreads) k_amg_tail(TailArgs<TA> T, const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     if (Idle(st))
         return;
     for (int l = 0; l + 1 < T.nl; ++l)
@@ -939,12 +955,12 @@ static void Chebyshev(Ctx& c, AmgLevel& L, const TA* vals, const uint8_t* mask, 
     int* stw = const_cast<int*>(st); // the SpMV only reads the state when it computes no dot products
     double rho = 1. / sigma;
     if (fromZero)
-        k_cheb0<TA><<<Blocks(n), 256, 0, c.stream>>>(n, U.dinv.p + o, b + o, U.d.p + o, e + o, TA(1. / theta), st);
+        NG_CUDA(LaunchPdl(k_cheb0<TA>, Blocks(n), 256, 0, c.stream, n, U.dinv.p + o, b + o, U.d.p + o, e + o, TA(1. / theta), st));
     else
     {
         SpmvNode<TA, TA, 0>(c.stream, L.spmv, vals, e, U.t.p, nullptr, nullptr, stw, 0, mask);
-        k_cheb1<TA><<<Blocks(n), 256, 0, c.stream>>>(n, U.dinv.p + o, b + o, U.t.p + o, U.d.p + o, e + o,
-                                                     TA(1. / theta), st);
+        NG_CUDA(LaunchPdl(k_cheb1<TA>, Blocks(n), 256, 0, c.stream, n, U.dinv.p + o, b + o, U.t.p + o, U.d.p + o, e + o,
+                                                     TA(1. / theta), st));
         c.stats.kernel_launches += 1;
     }
     c.stats.kernel_launches += 1;
@@ -952,8 +968,8 @@ static void Chebyshev(Ctx& c, AmgLevel& L, const TA* vals, const uint8_t* mask, 
     {
         const double rhoNew = 1. / (2. * sigma - rho);
         SpmvNode<TA, TA, 0>(c.stream, L.spmv, vals, e, U.t.p, nullptr, nullptr, stw, 0, mask);
-        k_chebk<TA><<<Blocks(n), 256, 0, c.stream>>>(n, U.dinv.p + o, b + o, U.t.p + o, U.d.p + o, e + o,
-                                                     TA(rhoNew * rho), TA(2. * rhoNew / delta), st);
+        NG_CUDA(LaunchPdl(k_chebk<TA>, Blocks(n), 256, 0, c.stream, n, U.dinv.p + o, b + o, U.t.p + o, U.d.p + o, e + o,
+                                                     TA(rhoNew * rho), TA(2. * rhoNew / delta), st));
         c.stats.kernel_launches += 2;
         rho = rhoNew;
     }
@@ -1010,7 +1026,7 @@ static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const TA* b, TA* 
             D.lmax = Lk.lmax;
         }
         // the level's b and e are the ones the caller passed (its own U.b, U.e)
-        k_amg_tail<TA><<<1, kTailThreads, 0, c.stream>>>(T, st);
+        NG_CUDA(LaunchPdl(k_amg_tail<TA>, 1, kTailThreads, 0, c.stream, T, st));
         c.stats.kernel_launches += 1;
         return;
     }
@@ -1024,11 +1040,11 @@ static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const TA* b, TA* 
     int* stw = const_cast<int*>(st);
     Chebyshev<TA>(c, L, vals, mask, b, e, sym ? kPostDegree : kPreDegree, true, kSmoothRatio, st);
     SpmvNode<TA, TA, 0>(c.stream, L.spmv, vals, e, U.t.p, nullptr, nullptr, stw, 0, mask);
-    k_sub<TA><<<Blocks(C.nDofs), 256, 0, c.stream>>>(C.nDofs, nullptr, nullptr, CU.b.p, st);
-    k_restrict<TA><<<Blocks(L.nNodes), 256, 0, c.stream>>>(L.spmv, mask, b, U.t.p, C.aggOf.p, C.spmv, CU.b.p, st);
+    NG_CUDA(LaunchPdl(k_sub<TA>, Blocks(C.nDofs), 256, 0, c.stream, C.nDofs, nullptr, nullptr, CU.b.p, st));
+    NG_CUDA(LaunchPdl(k_restrict<TA>, Blocks(L.nNodes), 256, 0, c.stream, L.spmv, mask, b, U.t.p, C.aggOf.p, C.spmv, CU.b.p, st));
     c.stats.kernel_launches += 3;
     VCycle<TA>(c, H, l + 1, CU.b.p, CU.e.p, st, sym);
-    k_prolong<TA><<<Blocks(L.nNodes), 256, 0, c.stream>>>(L.spmv, mask, C.aggOf.p, C.spmv, CU.e.p, e, st);
+    NG_CUDA(LaunchPdl(k_prolong<TA>, Blocks(L.nNodes), 256, 0, c.stream, L.spmv, mask, C.aggOf.p, C.spmv, CU.e.p, e, st));
     c.stats.kernel_launches += 1;
     Chebyshev<TA>(c, L, vals, mask, b, e, kPostDegree, false, kSmoothRatio, st);
 }
@@ -1044,10 +1060,10 @@ static void Sweep(Ctx& c, const TA* v, TA* z, TA* res, const int* st, bool sym)
         AmgLevel& L = M.h[I][0];
         const int64_t o = L.off, n = L.nDofs;
         // z_I = 0, res = K z on the rows of slot I, res = v_I - res
-        k_sub<TA><<<Blocks(n), 256, 0, c.stream>>>(n, nullptr, nullptr, z + o, st);
+        NG_CUDA(LaunchPdl(k_sub<TA>, Blocks(n), 256, 0, c.stream, n, nullptr, nullptr, z + o, st));
         SpmvNode<TA, TA, 0>(c.stream, RowsView(c, I), static_cast<const TA*>(M.fine), z, res, nullptr, nullptr,
                             const_cast<int*>(st), 0, c.dMask.p);
-        k_sub<TA><<<Blocks(n), 256, 0, c.stream>>>(n, v + o, res + o, res + o, st);
+        NG_CUDA(LaunchPdl(k_sub<TA>, Blocks(n), 256, 0, c.stream, n, v + o, res + o, res + o, st));
         c.stats.kernel_launches += 3;
         VCycle<TA>(c, M.h[I], 0, res, z, st, sym);
     }
@@ -1168,10 +1184,10 @@ void AmgApply(Ctx& c, const T* v, T* z, const int* st, bool sym)
     }
     else
     {
-        k_convert<double, float><<<Blocks(n), 256, 0, c.stream>>>(n, v, M.in32.p, st);
+        NG_CUDA(LaunchPdl(k_convert<double, float>, Blocks(n), 256, 0, c.stream, n, v, M.in32.p, st));
         if (!SweepGraphRun<float>(c, M.in32.p, M.out32.p, M.res32.p, st, sym))
             Sweep<float>(c, M.in32.p, M.out32.p, M.res32.p, st, sym);
-        k_convert<float, double><<<Blocks(n), 256, 0, c.stream>>>(n, M.out32.p, z, st);
+        NG_CUDA(LaunchPdl(k_convert<float, double>, Blocks(n), 256, 0, c.stream, n, M.out32.p, z, st));
         c.stats.kernel_launches += 2;
     }
 }

@@ -69,6 +69,39 @@ __device__ __forceinline__ long long CheckedIndex(long long i, long long n, int 
 #define NG_IDX(i, n, site) (i)
 #endif
 
+// ---- programmatic dependent launch -----------------------------------------------------------------------------
+// The kernels of the Krylov iteration and the multigrid cycle are launched with programmatic stream serialisation:
+// a kernel's blocks may be scheduled while its predecessor in the stream drains, which hides most of the gap
+// between the many short launches of a cycle. Every such kernel calls PdlWait() before its first global memory
+// access (it returns once the predecessor grid has completed and its writes are visible; without the launch
+// attribute it returns at once) and PdlTrigger() right after, so that its own successor may be scheduled once all
+// of its blocks are running. NUTO_GPU_PDL=0 launches them normally.
+__device__ __forceinline__ void PdlWait()
+{
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+__device__ __forceinline__ void PdlTrigger()
+{
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+bool PdlEnabled();
+template <typename... KArgs, typename... Args>
+inline cudaError_t LaunchPdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                             Args... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = PdlEnabled() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 struct Ctx;
 bool SyncCheck(const Ctx& c);
 cudaStream_t StreamOf(const Ctx& c);

@@ -422,6 +422,15 @@ NodeSpmv MakeNodeSpmv(const Ctx& c)
     return A;
 }
 
+bool PdlEnabled()
+{
+    static const bool on = [] {
+        const char* e = std::getenv("NUTO_GPU_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 template <typename TV>
 void EnsureNb(Ctx& c, const TV* vals)
 {
@@ -788,6 +797,8 @@ template <typename T>
 __global__ void __launch_bounds__(kBS) k_gm_proj(int64_t n, const T* __restrict__ V, int nv, const T* __restrict__ w,
                                                   double* acc, const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     if (st[ST_STATE] != RUN)
         return;
     const int lane = threadIdx.x & 31;
@@ -816,6 +827,8 @@ template <typename T>
 __global__ void __launch_bounds__(kBS) k_gm_update_proj(int64_t n, const T* __restrict__ V, int nv, const double* h,
                                                          T* __restrict__ w, double* acc2, const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     __shared__ T hs[GL::m + 1];
     if (st[ST_STATE] != RUN)
         return;
@@ -863,6 +876,8 @@ template <typename T>
 __global__ void __launch_bounds__(kBS) k_gm_update(int64_t n, const T* __restrict__ V, int nv, double* gs, T* w,
                                                     int* st, int j)
 {
+    PdlWait();
+    PdlTrigger();
     __shared__ T sh[kBS / 32];
     __shared__ T hs[GL::m + 1];
     if (st[ST_STATE] != RUN)
@@ -938,6 +953,8 @@ template <typename T>
 __global__ void __launch_bounds__(kBS) k_gm_normalize(int64_t n, const T* __restrict__ w, T* vj, T* z,
                                                        const T* __restrict__ dinv, const double* gs, const int* st)
 {
+    PdlWait();
+    PdlTrigger();
     if (st[ST_STATE] != RUN)
         return;
     const T inv = static_cast<T>(1. / gs[GL::NRM]);
@@ -1087,7 +1104,7 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
         c.stats.kernel_launches += 2;
         k_gm_start<T><<<grid, kBS, 0, c.stream>>>(n, K.r.p, G.w.p, first ? 0 : 1, gs, st);
         first = false;
-        k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, G.V.p, amg ? nullptr : G.z.p, K.dinv.p, gs, st);
+        NG_CUDA(LaunchPdl(k_gm_normalize<T>, grid, kBS, 0, c.stream, n, G.w.p, G.V.p, amg ? nullptr : G.z.p, K.dinv.p, gs, st));
         const int cols = std::min(m, maxit - total);
         // The cycle is enqueued in chunks: after each chunk the host reads the state and the residual estimate and
         // sizes the next chunk from the observed convergence rate (the iterations still needed, 1 .. 16). Kernels
@@ -1106,13 +1123,13 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
                     AmgApply<T>(c, G.V.p + static_cast<int64_t>(j) * n, zj, st, false);
                 SpmvTimed<TV, T, 0>(c, vals, zj, G.w.p, nullptr, nullptr, st, FIN_NONE, c.dMask.p);
                 c.stats.kernel_launches += 3 + (j + 1 < cols ? 1 : 0);
-                k_gm_proj<T><<<gridP, kBS, 0, c.stream>>>(n, G.V.p, j + 1, G.w.p, gs + GL::H1, st);
-                k_gm_update_proj<T><<<gridP, kBS, 0, c.stream>>>(n, G.V.p, j + 1, gs + GL::H1, G.w.p, gs + GL::H2,
-                                                                  st);
-                k_gm_update<T><<<grid, kBS, 0, c.stream>>>(n, G.V.p, j + 1, gs, G.w.p, st, j);
+                NG_CUDA(LaunchPdl(k_gm_proj<T>, gridP, kBS, 0, c.stream, n, G.V.p, j + 1, G.w.p, gs + GL::H1, st));
+                NG_CUDA(LaunchPdl(k_gm_update_proj<T>, gridP, kBS, 0, c.stream, n, G.V.p, j + 1, gs + GL::H1, G.w.p, gs + GL::H2,
+                                                                  st));
+                NG_CUDA(LaunchPdl(k_gm_update<T>, grid, kBS, 0, c.stream, n, G.V.p, j + 1, gs, G.w.p, st, j));
                 if (j + 1 < cols)
-                    k_gm_normalize<T><<<grid, kBS, 0, c.stream>>>(n, G.w.p, vj1, amg ? nullptr : G.z.p, K.dinv.p,
-                                                                  gs, st);
+                    NG_CUDA(LaunchPdl(k_gm_normalize<T>, grid, kBS, 0, c.stream, n, G.w.p, vj1, amg ? nullptr : G.z.p, K.dinv.p,
+                                                                  gs, st));
             }
             if (j >= cols)
                 break;

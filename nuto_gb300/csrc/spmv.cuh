@@ -150,6 +150,8 @@ __global__ void __launch_bounds__(kBS, 5) k_spmv_node(NodeSpmv A, const TV* __re
                                                     TX* __restrict__ y, const TX* __restrict__ w0, double* sc, int* st,
                                                     int fin)
 {
+    PdlWait();
+    PdlTrigger();
     __shared__ double sh[kBS / 32];
     __shared__ TX xs[kBS / 32][kMaxRowLen];
     if (st && st[ST_STATE] != RUN)
@@ -310,6 +312,8 @@ __global__ void __launch_bounds__(kBS) k_spmv_nb(NodeSpmv A, const uint8_t* __re
                                                   const TX* __restrict__ x, TX* __restrict__ y,
                                                   const TX* __restrict__ w0, double* sc, int* st, int fin)
 {
+    PdlWait();
+    PdlTrigger();
     extern __shared__ __align__(16) unsigned char nbSmem[];
     __shared__ double sh[kBS / 32];
     if (st && st[ST_STATE] != RUN)
@@ -473,13 +477,13 @@ void SpmvNode(cudaStream_t stream, const NodeSpmv& A, const TV* vals, const TX* 
             threads -= 32;
         const int64_t total = A.totalWarps * kNbG;
         const unsigned blocks = static_cast<unsigned>((total + threads - 1) / threads);
-        k_spmv_nb<TV, TX, NDOT><<<blocks, threads, (threads / kNbG) * perGroup, stream>>>(A, mask, x, y, w0, sc, st,
-                                                                                          fin);
+        NG_CUDA(LaunchPdl(k_spmv_nb<TV, TX, NDOT>, blocks, threads, (threads / kNbG) * perGroup, stream, A, mask, x, y, w0, sc, st,
+                                                                                          fin));
         return;
     }
     const int64_t threads = A.totalWarps * 32;
     const unsigned blocks = static_cast<unsigned>((threads + kBS - 1) / kBS);
-    k_spmv_node<TV, TX, NDOT><<<blocks, kBS, 0, stream>>>(A, vals, mask, x, y, w0, sc, st, fin);
+    NG_CUDA(LaunchPdl(k_spmv_node<TV, TX, NDOT>, blocks, kBS, 0, stream, A, vals, mask, x, y, w0, sc, st, fin));
 }
 
 } // namespace nuto_gpu
