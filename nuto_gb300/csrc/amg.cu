@@ -237,6 +237,7 @@ static NodeSpmv SlotView(const Ctx& c, int I)
         A.nbBase[0] = c.nb.pair[I * ns + I].base.p;
         A.nbOff[0] = c.nb.pair[I * ns + I].off;
         A.nbSeg4 = c.nb.pair[I * ns + I].maxSeg4;
+        A.ncMaxRows = c.slots[I].ncomp;
         A.nb32 = c.nb.v32.p;
         A.nb64 = c.nb.v64.p;
         A.nbSrc32 = c.nb.src32;
@@ -907,6 +908,7 @@ void AmgSetup(Ctx& c, const TV* vals)
                 V.nbBase[0] = C.nbBase.p;
                 V.nbOff[0] = 0;
                 V.nbSeg4 = C.nbSeg4;
+                V.ncMaxRows = C.ncomp;
                 if constexpr (sizeof(TV) == 4)
                 {
                     V.nb32 = CU.nb.p;

@@ -407,6 +407,9 @@ NodeSpmv MakeNodeSpmv(const Ctx& c)
         }
         // per group the padded segments of every column slot of one row slot side by side
         A.nbSeg4 = 0;
+        A.ncMaxRows = 0;
+        for (int I = 0; I < A.ns; ++I)
+            A.ncMaxRows = std::max(A.ncMaxRows, c.slots[I].ncomp);
         for (int I = 0; I < A.ns; ++I)
         {
             int sum = 0;

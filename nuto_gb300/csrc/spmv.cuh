@@ -93,6 +93,7 @@ struct NodeSpmv
     const int64_t* nbBase[kMaxSlots * kMaxSlots];
     int64_t nbOff[kMaxSlots * kMaxSlots];
     int nbSeg4;
+    int ncMaxRows; // most components of a row node of the view
     const float* nb32;
     const double* nb64;
     const void* nbSrc32;
@@ -307,8 +308,17 @@ __device__ __forceinline__ const TV* NbValues(const NodeSpmv& A)
         return A.nb64;
 }
 
-template <typename TV, typename TX, int NDOT>
-__global__ void __launch_bounds__(kBS) k_spmv_nb(NodeSpmv A, const uint8_t* __restrict__ mask,
+// FP32 values: at most 40 registers (6 blocks of 256 threads per SM: more nodes in flight, measured 10 % faster per
+// GMRES iteration despite a few spilled bytes); FP64 values: at most 64 registers (4 blocks; without a cap the
+// compiler takes 90 and the FP64 path slowed by 25 %)
+template <typename TV>
+constexpr int NbMinBlocks()
+{
+    return sizeof(TV) == 4 ? 6 : 4;
+}
+
+template <typename TV, typename TX, int NDOT, int G>
+__global__ void __launch_bounds__(kBS, NbMinBlocks<TV>()) k_spmv_nb(NodeSpmv A, const uint8_t* __restrict__ mask,
                                                   const TX* __restrict__ x, TX* __restrict__ y,
                                                   const TX* __restrict__ w0, double* sc, int* st, int fin)
 {
@@ -319,10 +329,10 @@ __global__ void __launch_bounds__(kBS) k_spmv_nb(NodeSpmv A, const uint8_t* __re
     if (st && st[ST_STATE] != RUN)
         return;
     const TV* __restrict__ vals = NbValues<TV>(A);
-    const int gl = threadIdx.x & (kNbG - 1);
+    const int gl = threadIdx.x & (G - 1);
     const int L = A.nbSeg4;
-    TX* xs = reinterpret_cast<TX*>(nbSmem) + (threadIdx.x / kNbG) * L;
-    const int64_t u = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / kNbG;
+    TX* xs = reinterpret_cast<TX*>(nbSmem) + (threadIdx.x / G) * L;
+    const int64_t u = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / G;
     int I = 0;
     int64_t a = 0;
     bool valid = u < A.totalWarps;
@@ -359,7 +369,7 @@ __global__ void __launch_bounds__(kBS) k_spmv_nb(NodeSpmv A, const uint8_t* __re
     // x chains in flight per lane)
     const int nc0 = A.ncomp[0], nc1 = A.ns > 1 ? A.ncomp[1] : 0;
 #pragma unroll 4
-    for (int t = gl; t < tot; t += kNbG)
+    for (int t = gl; t < tot; t += G)
     {
         const int J = t >= nn[0] ? 1 : 0;
         const int kk = t - (J ? nn[0] : 0);
@@ -374,7 +384,7 @@ __global__ void __launch_bounds__(kBS) k_spmv_nb(NodeSpmv A, const uint8_t* __re
     for (int J = 0; J < kMaxSlots; ++J)
     {
         const int seg = (J ? nc1 : nc0) * nn[J];
-        for (int t = seg + gl; t < seg4[J]; t += kNbG)
+        for (int t = seg + gl; t < seg4[J]; t += G)
             xs[NG_IDX(xoff[J] + t, L, 63)] = TX(0);
     }
     __syncwarp();
@@ -389,7 +399,7 @@ __global__ void __launch_bounds__(kBS) k_spmv_nb(NodeSpmv A, const uint8_t* __re
         const TX* xj = xs + xoff[J];
         const int sg = seg4[J];
 #pragma unroll 2
-        for (int f = 4 * gl; f < sg; f += 4 * kNbG)
+        for (int f = 4 * gl; f < sg; f += 4 * G)
         {
             TX xv[4];
             Load4(xj + f, xv);
@@ -405,7 +415,7 @@ __global__ void __launch_bounds__(kBS) k_spmv_nb(NodeSpmv A, const uint8_t* __re
         }
     }
 #pragma unroll
-    for (int o = kNbG / 2; o > 0; o >>= 1)
+    for (int o = G / 2; o > 0; o >>= 1)
 #pragma unroll
         for (int c = 0; c < kMaxComp; ++c)
             s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
@@ -471,14 +481,22 @@ void SpmvNode(cudaStream_t stream, const NodeSpmv& A, const TV* vals, const TX* 
     const void* src = sizeof(TV) == 4 ? A.nbSrc32 : A.nbSrc64;
     if (A.nbBase[0] && src == static_cast<const void*>(vals) && A.nbSeg4 > 0)
     {
+        // 8 lanes per node; 4 for views of single-component rows and columns (one short segment per node)
+        const bool narrow = A.ns == 1 && A.ncMaxRows == 1;
+        const int G = narrow ? 4 : kNbG;
         const size_t perGroup = static_cast<size_t>(A.nbSeg4) * sizeof(TX);
         int threads = kBS;
-        while (threads > 32 && (threads / kNbG) * perGroup > 48 * 1024)
+        while (threads > 32 && (threads / G) * perGroup > 48 * 1024)
             threads -= 32;
-        const int64_t total = A.totalWarps * kNbG;
+        const int64_t total = A.totalWarps * G;
         const unsigned blocks = static_cast<unsigned>((total + threads - 1) / threads);
-        NG_CUDA(LaunchPdl(k_spmv_nb<TV, TX, NDOT>, blocks, threads, (threads / kNbG) * perGroup, stream, A, mask, x, y, w0, sc, st,
-                                                                                          fin));
+        const size_t smem = (threads / G) * perGroup;
+        if (narrow)
+            NG_CUDA(LaunchPdl(k_spmv_nb<TV, TX, NDOT, 4>, blocks, threads, smem, stream, A, mask, x, y, w0, sc, st,
+                              fin));
+        else
+            NG_CUDA(LaunchPdl(k_spmv_nb<TV, TX, NDOT, kNbG>, blocks, threads, smem, stream, A, mask, x, y, w0, sc, st,
+                              fin));
         return;
     }
     const int64_t threads = A.totalWarps * 32;
