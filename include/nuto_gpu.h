@@ -194,6 +194,9 @@ int nuto_gpu_pattern_device(nuto_gpu_ctx* ctx, const int64_t** d_row_ptr, const 
    the Krylov products stream (node row segments per slot pair padded to multiples of 4) and entries of the
    neighbour lists that drive the gathers; for traffic accounting. */
 int nuto_gpu_solver_layout(const nuto_gpu_ctx* ctx, int64_t* padded_values, int64_t* neighbour_entries);
+/* State of the multigrid preconditioner after the last solve (no counterpart in the reference): levels of the
+   first DOF slot's hierarchy (0: not built) and whether the sweep ran as a CUDA graph (1) or kernel by kernel (0). */
+int nuto_gpu_multigrid_info(const nuto_gpu_ctx* ctx, int* levels, int* graph_active);
 
 int nuto_gpu_set_integrand(nuto_gpu_ctx* ctx, const nuto_gpu_integrand* params);
 int nuto_gpu_num_integration_points(const nuto_gpu_ctx* ctx);

@@ -97,6 +97,13 @@ class GpuCellGroup:
         pairs = self.nnz // (ncomp * ncomp)
         return sum(pairs * 4 + (L.num_nodes + 1) * 8 for L in layers) * len(layers)
 
+    def multigrid_info(self):
+        """(levels of the first slot's hierarchy, 1 when the last sweeps ran as a CUDA graph)"""
+        lv = ctypes.c_int()
+        ga = ctypes.c_int()
+        self._call("nuto_gpu_multigrid_info", ctypes.byref(lv), ctypes.byref(ga))
+        return lv.value, ga.value
+
     def solver_layout(self):
         """(padded values, neighbour-list entries) of the solver's copy of the tangent"""
         v = ctypes.c_int64()

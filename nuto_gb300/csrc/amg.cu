@@ -120,7 +120,12 @@ struct Amg
             for (SweepGraph& g : row)
                 if (g.exec)
                     cudaGraphExecDestroy(g.exec);
+        if (capStream)
+            cudaStreamDestroy(capStream);
     }
+    bool graphLaunched = false;    // a sweep graph was launched since the hierarchy was built
+    std::string graphError; // why graphs were switched off (diagnostics)
+    cudaStream_t capStream = nullptr; // private stream for graph capture (the context's may be the legacy stream)
 };
 
 void FreeAmg(Ctx& c)
@@ -866,6 +871,7 @@ static void EnsureNum(Ctx& c, Amg& M)
 template <typename TV>
 void AmgSetup(Ctx& c, const TV* vals)
 {
+    HostClock hc(&c.hostMs[HP_AMG_SETUP]);
     if (!c.amg)
     {
         c.amg = new Amg();
@@ -1086,19 +1092,46 @@ static bool SweepGraphRun(Ctx& c, TA* in, TA* out, TA* res, const int* st, bool 
     SweepGraph& G = M.graph[sizeof(TA) == 8 ? 1 : 0][sym ? 1 : 0];
     if (!G.exec || G.setup != M.setups || G.st != st)
     {
+        HostClock hc(&c.hostMs[HP_GRAPH]);
         const int64_t before = c.stats.kernel_launches;
         cudaGraph_t graph = nullptr;
-        if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        // Capture on a private stream: capture is not permitted on the legacy default stream, which a caller may
+        // hand to nuto_gpu_create. Capturing records the launches without running them, so swapping the
+        // context's stream for the duration does not reorder any work; the graph is launched on the context's
+        // stream.
+        if (!M.capStream)
+            NG_CUDA(cudaStreamCreateWithFlags(&M.capStream, cudaStreamNonBlocking));
+        const cudaError_t eb = cudaStreamBeginCapture(M.capStream, cudaStreamCaptureModeThreadLocal);
+        if (eb != cudaSuccess)
         {
             cudaGetLastError();
             M.graphs = false;
+            M.graphError = std::string("begin capture: ") + cudaGetErrorString(eb);
             return false;
         }
-        Sweep<TA>(c, in, out, res, st, sym);
-        const cudaError_t ec = cudaStreamEndCapture(c.stream, &graph);
+        const cudaStream_t own = c.stream;
+        c.stream = M.capStream;
+        try
+        {
+            Sweep<TA>(c, in, out, res, st, sym);
+        }
+        catch (...)
+        {
+            c.stream = own;
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(M.capStream, &g);
+            if (g)
+                cudaGraphDestroy(g);
+            cudaGetLastError();
+            throw;
+        }
+        c.stream = own;
+        const cudaError_t ec = cudaStreamEndCapture(M.capStream, &graph);
         G.launches = c.stats.kernel_launches - before;
         c.stats.kernel_launches = before;
         bool ok = ec == cudaSuccess && graph != nullptr;
+        if (!ok)
+            M.graphError = std::string("end capture: ") + cudaGetErrorString(ec);
         if (ok && G.exec)
         {
             cudaGraphExecUpdateResultInfo info;
@@ -1110,7 +1143,12 @@ static bool SweepGraphRun(Ctx& c, TA* in, TA* out, TA* res, const int* st, bool 
             }
         }
         if (ok && !G.exec)
-            ok = cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess;
+        {
+            const cudaError_t ei = cudaGraphInstantiate(&G.exec, graph, 0);
+            ok = ei == cudaSuccess;
+            if (!ok)
+                M.graphError = std::string("instantiate: ") + cudaGetErrorString(ei);
+        }
         if (graph)
             cudaGraphDestroy(graph);
         if (!ok)
@@ -1126,6 +1164,7 @@ static bool SweepGraphRun(Ctx& c, TA* in, TA* out, TA* res, const int* st, bool 
         G.st = st;
     }
     NG_CUDA(cudaGraphLaunch(G.exec, c.stream));
+    M.graphLaunched = true;
     c.stats.kernel_launches += G.launches;
     return true;
 }
@@ -1195,6 +1234,20 @@ void AmgApply(Ctx& c, const T* v, T* z, const int* st, bool sym)
 }
 template void AmgApply<float>(Ctx&, const float*, float*, const int*, bool);
 template void AmgApply<double>(Ctx&, const double*, double*, const int*, bool);
+
+bool AmgGraphActive(const Ctx& c)
+{
+    return c.amg && c.amg->graphs && c.amg->graphLaunched;
+}
+
+const char* AmgGraphStatus(const Ctx& c)
+{
+    if (!c.amg)
+        return "no multigrid";
+    if (c.amg->graphs)
+        return "sweep graph on";
+    return c.amg->graphError.empty() ? "sweep graph off" : c.amg->graphError.c_str();
+}
 
 int AmgLevels(const Ctx& c)
 {

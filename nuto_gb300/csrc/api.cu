@@ -842,6 +842,15 @@ int nuto_gpu_num_integration_points(const nuto_gpu_ctx* ctx)
     return ctx ? ctx->ip.nIp : 0;
 }
 
+int nuto_gpu_multigrid_info(const nuto_gpu_ctx* ctx, int* levels, int* graph_active)
+{
+    if (!ctx || !levels || !graph_active)
+        return NUTO_GPU_EINVAL;
+    *levels = AmgLevels(*ctx);
+    *graph_active = AmgGraphActive(*ctx) ? 1 : 0;
+    return NUTO_GPU_OK;
+}
+
 int nuto_gpu_solver_layout(const nuto_gpu_ctx* ctx, int64_t* padded_values, int64_t* neighbour_entries)
 {
     if (!ctx || !padded_values || !neighbour_entries)

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -287,6 +288,31 @@ struct NbLayout
     uint64_t ver32 = 0, ver64 = 0;
 };
 
+// host wall time of the phases of a step (diagnostics, printed with NUTO_GPU_VERBOSE)
+enum HostPhase
+{
+    HP_TANGENT,
+    HP_RESIDUAL,
+    HP_SOLVE,
+    HP_AMG_SETUP,
+    HP_GRAPH,
+    HP_SYNC,
+    HP_COUNT
+};
+struct HostClock
+{
+    double* acc;
+    std::chrono::steady_clock::time_point t0;
+    explicit HostClock(double* a)
+        : acc(a), t0(std::chrono::steady_clock::now())
+    {
+    }
+    ~HostClock()
+    {
+        *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
 struct Ctx
 {
     int device = 0;
@@ -362,6 +388,7 @@ struct Ctx
     int precond = NUTO_GPU_PRECOND_AMG;
     uint64_t valsVersion = 1; // bumped by every tangent assembly and every caller-supplied solve
     bool syncCheck = false; // NUTO_GPU_SYNC_CHECK=1 or a checked build
+    double hostMs[HP_COUNT] = {};
 
     ~Ctx();
 };
@@ -389,6 +416,9 @@ void AmgSetup(Ctx& c, const TV* vals);
 template <typename T>
 void AmgApply(Ctx& c, const T* v, T* z, const int* st, bool sym);
 int AmgLevels(const Ctx& c);
+const char* AmgGraphStatus(const Ctx& c);
+// true when the last sweep ran as a CUDA graph
+bool AmgGraphActive(const Ctx& c);
 // fills the padded pair layout of TV from the CSR values `vals` unless it holds them already (same pointer and
 // tangent version)
 template <typename TV>

@@ -142,6 +142,8 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     void* K = fp32 ? static_cast<void*>(w.K32.p) : static_cast<void*>(w.K64.p);
     const int method = ResolveMethod(c, o.method);
     c.stats = nuto_gpu_stats{};
+    for (double& h : c.hostMs)
+        h = 0.;
     nuto_gpu_stats& S = c.stats;
     Timers T(c);
     int lastKrylov = 0;
@@ -149,6 +151,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     const unsigned gb = static_cast<unsigned>((n + 255) / 256);
 
     auto assembleK = [&](const double* x) {
+        HostClock hc(&c.hostMs[HP_TANGENT]);
         const int k = T.Begin();
         if (exactNow)
         {
@@ -163,6 +166,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
         S.matrix_assemblies++;
     };
     auto residual = [&](const double* x) {
+        HostClock hc(&c.hostMs[HP_RESIDUAL]);
         const int k = T.Begin();
         LaunchResidual(c, x, w.f.p);
         if (c.dConstGrad.p)
@@ -188,6 +192,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     const bool verbose = vb && (vb[0] == '1' || vb[0] == '2');
     const bool verboseSweeps = vb && vb[0] == '2';
     auto solve = [&](const double* rhs, double* out) {
+        HostClock hc(&c.hostMs[HP_SOLVE]);
         const auto k0 = std::chrono::steady_clock::now();
         int it = 0;
         double* relp = &lastRel;
@@ -334,6 +339,12 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     auto finish = [&]() {
         T.Collect();
         S.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (verbose)
+            std::fprintf(stderr,
+                         "[nuto_gpu] host ms: step %.1f, tangent %.1f, residual %.1f, solve %.1f (multigrid set-up "
+                         "%.1f, graph capture %.1f, waits %.1f); %s\n",
+                         S.ms_total, c.hostMs[HP_TANGENT], c.hostMs[HP_RESIDUAL], c.hostMs[HP_SOLVE],
+                         c.hostMs[HP_AMG_SETUP], c.hostMs[HP_GRAPH], c.hostMs[HP_SYNC], AmgGraphStatus(c));
     };
     if (!conv)
     {

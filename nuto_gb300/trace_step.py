@@ -6,7 +6,10 @@ PyTorch profiler (device start/end of every kernel, memset and copy, including t
 Runs --warmup load steps of the benchmark schedule (FP32 tangent, exact final phase), then traces load step
 warmup + 1 and prints: wall time, GPU busy time and the gaps between operations; the device time per kernel; and
 per Krylov iteration (delimited by the GMRES projection kernel) the time by class. Unlike a serialised ncu launch
-list the times are the ones of the real run (warm caches, back-to-back launches).
+list the times are the ones of the real run (warm caches, back-to-back launches). Two limits: with programmatic
+dependent launch a kernel's interval includes its wait for the predecessor (intervals overlap), and the activity
+buffers can drop records on steps with tens of thousands of launches (compare the operation count with the
+step's kernel_launches statistic); both are reported.
 """
 
 import argparse
@@ -75,8 +78,9 @@ def main():
     busy = sum(e["dur"] for e in ks)
     span = ks[-1]["ts"] + ks[-1]["dur"] - ks[0]["ts"]
     gaps = [ks[i + 1]["ts"] - ks[i]["ts"] - ks[i]["dur"] for i in range(len(ks) - 1)]
-    print("size %d, load step %d: %d Newton iterations, %d Krylov iterations, %d tangent assemblies" %
-          (a.size, a.warmup + 1, st["newton_iterations"], st["krylov_iterations"], st["matrix_assemblies"]))
+    print("size %d, load step %d: %d Newton iterations, %d Krylov iterations, %d tangent assemblies, %d kernel launches "
+          "(%d device operations recorded)" % (a.size, a.warmup + 1, st["newton_iterations"], st["krylov_iterations"],
+                                             st["matrix_assemblies"], st["kernel_launches"], len(ks)))
     print("wall %.1f ms, GPU span %.1f ms, GPU busy %.1f ms, %d operations, gaps %.1f ms (median %.2f us)" %
           (1e3 * (t1 - t0), span / 1e3, busy / 1e3, len(ks), sum(x for x in gaps if x > 0) / 1e3,
            float(np.median([x for x in gaps if x > 0]))))

@@ -382,7 +382,8 @@ def test_tangent_row_gather_matches_element_atomics(kind, n, precision, monkeypa
 @pytest.mark.parametrize("precision", [64, 32])
 def test_multigrid_sweep_graph_matches_kernel_launches(precision, monkeypatch):
     """The multigrid sweep replayed as a CUDA graph and launched kernel by kernel (NUTO_GPU_GRAPHS=0) give the same
-    GMRES solution (up to the order of the atomic restriction sums) and iteration count within one restart."""
+    GMRES solution (up to the order of the atomic restriction sums) and iteration count within one restart; the
+    context reports which form ran (the graph must run on the stream the tests use, the legacy default stream)."""
     _torch()
     from nuto_gb300 import configs
 
@@ -402,6 +403,8 @@ def test_multigrid_sweep_graph_matches_kernel_launches(precision, monkeypatch):
         vals = g.build_matrix(u, precision)
         x, it, rel, ok = g.solve(vals, b, precision=precision, method=3, rtol=1e-8, max_iterations=5000)
         assert ok, (graphs, it, rel)
+        levels, graph_active = g.multigrid_info()
+        assert levels >= 2 and graph_active == int(graphs), (levels, graph_active)
         out[graphs] = (x.cpu().numpy(), it)
     (x1, it1), (x0, it0) = out["1"], out["0"]
     assert np.abs(x1 - x0).max() <= 1e-5 * np.abs(x0).max()
