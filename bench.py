@@ -35,10 +35,10 @@ LOAD_STEPS = 20
 # inexact Newton: each inner Krylov solve (both precisions) reduces its residual by 1e3; Newton on the FP64 residual
 # then converges linearly at about max(1e-3, rounding of the FP32 tangent) per iteration
 KRYLOV_RTOL = 1e-3
-# mixed path: the Newton iterations with |C^T r| below 100 x the tolerance assemble the FP64 tangent and refine the
-# FP32 solves against it (exact Jacobian for the last steps; the relative displacement error against FP64 then stays
-# below 1e-6, with the FP32 tangent alone it is about 1e-5 on the damaged beam)
-EXACT_BELOW = 100.0
+# mixed path: the Newton iterations with |C^T r| below 1e4 x the tolerance assemble the FP64 tangent and refine the
+# FP32 solves against it (exact Jacobian for the last steps; the relative displacement error against the converged
+# FP64 solution then stays below 1e-6, with the FP32 tangent alone it is about 1e-5 on the damaged beam)
+EXACT_BELOW = 1.0e4
 
 
 def parse():
@@ -417,6 +417,18 @@ def run_ours(args):
            "krylov_iterations": agg32["krylov_iterations"],
            "roofline": roof, "roofline_assembly": assembly, "fp64": fp64, "e2e": e2e,
            "gpu_launches": int(agg32["kernel_launches"]), "clocks": clk}
+    if fp64 is not None:
+        # the two targets side by side: Newton-step speed-up over the FP64 GPU path, and the relative displacement
+        # error against the converged FP64 solution (1e-11 residual; the FP64 path at 1e-8 shown for scale) and
+        # against the FP64 path's own 1e-8 result
+        tight = fp64.get("max_rel_displacement_error_vs_fp64_1e-11", {})
+        tight_l2 = fp64.get("l2_rel_displacement_error_vs_fp64_1e-11", {})
+        out["north_star"] = {
+            "speedup_newton_step_mixed_vs_fp64": fp64["speedup_mixed_vs_fp64_newton_step"],
+            "mixed_vs_converged_fp64": {"max": tight.get("mixed"), "l2": tight_l2.get("mixed")},
+            "fp64_path_vs_converged_fp64": {"max": tight.get("fp64"), "l2": tight_l2.get("fp64")},
+            "mixed_vs_fp64_path": {"max": fp64["max_rel_displacement_error_mixed_vs_fp64"],
+                                   "l2": fp64["l2_rel_displacement_error_mixed_vs_fp64"]}}
     if rank == 0 and world == 1 and not args.skip_cpu:
         try:
             out["cpu_baseline"] = cpu_baseline()

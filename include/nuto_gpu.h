@@ -133,10 +133,10 @@ typedef struct nuto_gpu_step_options
                                    tangent of the remaining Newton iterations is assembled in FP64 and every
                                    solve refines against it (FP32 Krylov and preconditioner on its FP32
                                    rounding inside an FP64 refinement), so that the last Newton steps use the
-                                   exact Jacobian; 0: off. Default 100: with the FP32 tangent alone the
+                                   exact Jacobian; 0: off. Default 1e4: with the FP32 tangent alone the
                                    near-singular modes of a damaged zone converge only linearly, and a state
-                                   at the 1e-8 residual can lie 1e-5 from the FP64 solution; the exact last
-                                   iterations bring it to the FP64 path's distance (below 1e-6) */
+                                   at the 1e-8 residual can lie 1e-5 from the converged FP64 solution; with the
+                                   exact last iterations it lies as close as the FP64 path's (below 1e-6) */
 } nuto_gpu_step_options;
 
 /* statistics of the last nuto_gpu_do_step / nuto_gpu_solve */

@@ -33,7 +33,14 @@ constexpr int kCoarsest = 64; // nodes on the coarsest level
 constexpr int kMaxLevels = 12;
 constexpr int kPreDegree = 1;
 constexpr int kPostDegree = 2;
-constexpr int kCoarseDegree = 6;
+// Chebyshev degree on the coarsest level, per arithmetic of the cycle: measured on the damaged 64^3 tangent
+// (time to a 1e-4 / 1e-7 relative residual), degree 10 made the FP32 cycle 10 % faster than degree 6 and the FP64
+// cycle 3 % faster / 7 % slower
+template <typename TA>
+constexpr int CoarseDegree()
+{
+    return sizeof(TA) == 4 ? 10 : 6;
+}
 constexpr float kSmoothRatio = 10.f; // smoothing interval [lmax / ratio, lmax]
 constexpr float kCoarseRatio = 30.f;
 
@@ -1008,7 +1015,7 @@ static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const TA* b, TA* 
         T.nl = static_cast<int>(H.size() - l);
         T.pre = sym ? kPostDegree : kPreDegree;
         T.post = kPostDegree;
-        T.coarse = kCoarseDegree;
+        T.coarse = CoarseDegree<TA>();
         T.smoothRatio = kSmoothRatio;
         T.coarseRatio = kCoarseRatio;
         for (int k = 0; k < T.nl; ++k)
@@ -1040,7 +1047,7 @@ static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const TA* b, TA* 
     }
     if (l + 1 == H.size())
     {
-        Chebyshev<TA>(c, L, vals, mask, b, e, kCoarseDegree, true, kCoarseRatio, st);
+        Chebyshev<TA>(c, L, vals, mask, b, e, CoarseDegree<TA>(), true, kCoarseRatio, st);
         return;
     }
     AmgLevel& C = H[l + 1];

@@ -1075,7 +1075,7 @@ int nuto_gpu_default_step_options(nuto_gpu_step_options* o)
     o->krylov_rtol = 1e-3;
     o->max_krylov = 20000;
     o->forcing = 1;
-    o->exact_tangent_below = 100.0;
+    o->exact_tangent_below = 1.0e4;
     return NUTO_GPU_OK;
 }
 
