@@ -970,12 +970,13 @@ static void Chebyshev(Ctx& c, AmgLevel& L, const TA* vals, const uint8_t* mask, 
     int* stw = const_cast<int*>(st); // the SpMV only reads the state when it computes no dot products
     double rho = 1. / sigma;
     if (fromZero)
-        NG_CUDA(LaunchPdl(k_cheb0<TA>, Blocks(n), 256, 0, c.stream, n, U.dinv.p + o, b + o, U.d.p + o, e + o, TA(1. / theta), st));
+        NG_CUDA(LaunchPdl(k_cheb0<TA>, Blocks(n), 256, 0, c.stream, n, U.dinv.p + o, b + o, U.d.p + o, e + o,
+                          TA(1. / theta), st));
     else
     {
         SpmvNode<TA, TA, 0>(c.stream, L.spmv, vals, e, U.t.p, nullptr, nullptr, stw, 0, mask);
-        NG_CUDA(LaunchPdl(k_cheb1<TA>, Blocks(n), 256, 0, c.stream, n, U.dinv.p + o, b + o, U.t.p + o, U.d.p + o, e + o,
-                                                     TA(1. / theta), st));
+        NG_CUDA(LaunchPdl(k_cheb1<TA>, Blocks(n), 256, 0, c.stream, n, U.dinv.p + o, b + o, U.t.p + o, U.d.p + o,
+                          e + o, TA(1. / theta), st));
         c.stats.kernel_launches += 1;
     }
     c.stats.kernel_launches += 1;
@@ -983,8 +984,8 @@ static void Chebyshev(Ctx& c, AmgLevel& L, const TA* vals, const uint8_t* mask, 
     {
         const double rhoNew = 1. / (2. * sigma - rho);
         SpmvNode<TA, TA, 0>(c.stream, L.spmv, vals, e, U.t.p, nullptr, nullptr, stw, 0, mask);
-        NG_CUDA(LaunchPdl(k_chebk<TA>, Blocks(n), 256, 0, c.stream, n, U.dinv.p + o, b + o, U.t.p + o, U.d.p + o, e + o,
-                                                     TA(rhoNew * rho), TA(2. * rhoNew / delta), st));
+        NG_CUDA(LaunchPdl(k_chebk<TA>, Blocks(n), 256, 0, c.stream, n, U.dinv.p + o, b + o, U.t.p + o, U.d.p + o,
+                          e + o, TA(rhoNew * rho), TA(2. * rhoNew / delta), st));
         c.stats.kernel_launches += 2;
         rho = rhoNew;
     }
@@ -1056,10 +1057,12 @@ static void VCycle(Ctx& c, std::vector<AmgLevel>& H, size_t l, const TA* b, TA* 
     Chebyshev<TA>(c, L, vals, mask, b, e, sym ? kPostDegree : kPreDegree, true, kSmoothRatio, st);
     SpmvNode<TA, TA, 0>(c.stream, L.spmv, vals, e, U.t.p, nullptr, nullptr, stw, 0, mask);
     NG_CUDA(LaunchPdl(k_sub<TA>, Blocks(C.nDofs), 256, 0, c.stream, C.nDofs, nullptr, nullptr, CU.b.p, st));
-    NG_CUDA(LaunchPdl(k_restrict<TA>, Blocks(L.nNodes), 256, 0, c.stream, L.spmv, mask, b, U.t.p, C.aggOf.p, C.spmv, CU.b.p, st));
+    NG_CUDA(LaunchPdl(k_restrict<TA>, Blocks(L.nNodes), 256, 0, c.stream, L.spmv, mask, b, U.t.p, C.aggOf.p, C.spmv,
+                      CU.b.p, st));
     c.stats.kernel_launches += 3;
     VCycle<TA>(c, H, l + 1, CU.b.p, CU.e.p, st, sym);
-    NG_CUDA(LaunchPdl(k_prolong<TA>, Blocks(L.nNodes), 256, 0, c.stream, L.spmv, mask, C.aggOf.p, C.spmv, CU.e.p, e, st));
+    NG_CUDA(LaunchPdl(k_prolong<TA>, Blocks(L.nNodes), 256, 0, c.stream, L.spmv, mask, C.aggOf.p, C.spmv, CU.e.p, e,
+                      st));
     c.stats.kernel_launches += 1;
     Chebyshev<TA>(c, L, vals, mask, b, e, kPostDegree, false, kSmoothRatio, st);
 }
@@ -1084,10 +1087,6 @@ static void Sweep(Ctx& c, const TA* v, TA* z, TA* res, const int* st, bool sym)
     }
 }
 
-// z = M^-1 v for the tangent of the last AmgSetup, in that tangent's arithmetic (FP64 Krylov vectors with an
-// FP32 tangent are converted). With st given, every kernel returns at once when the Krylov state is not RUN.
-// sym = true runs equal pre- and post-smoothing (a symmetric cycle for PCG on a single slot); otherwise the
-// cheaper V(1,2) for GMRES.
 // Runs Sweep<TA>(in, out) through the graph of (TA, sym), capturing or updating it when the set-up changed. Returns
 // false when graphs are off or the capture failed (the caller then launches the sweep kernel by kernel).
 template <typename TA>

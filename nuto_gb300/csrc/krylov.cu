@@ -1110,7 +1110,8 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
         c.stats.kernel_launches += 2;
         k_gm_start<T><<<grid, kBS, 0, c.stream>>>(n, K.r.p, G.w.p, first ? 0 : 1, gs, st);
         first = false;
-        NG_CUDA(LaunchPdl(k_gm_normalize<T>, grid, kBS, 0, c.stream, n, G.w.p, G.V.p, amg ? nullptr : G.z.p, K.dinv.p, gs, st));
+        NG_CUDA(LaunchPdl(k_gm_normalize<T>, grid, kBS, 0, c.stream, n, G.w.p, G.V.p, amg ? nullptr : G.z.p, K.dinv.p,
+                          gs, st));
         const int cols = std::min(m, maxit - total);
         // The cycle is enqueued in chunks: after each chunk the host reads the state and the residual estimate and
         // sizes the next chunk from the observed convergence rate (the iterations still needed, 1 .. 16). Kernels
@@ -1130,12 +1131,12 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
                 SpmvTimed<TV, T, 0>(c, vals, zj, G.w.p, nullptr, nullptr, st, FIN_NONE, c.dMask.p);
                 c.stats.kernel_launches += 3 + (j + 1 < cols ? 1 : 0);
                 NG_CUDA(LaunchPdl(k_gm_proj<T>, gridP, kBS, 0, c.stream, n, G.V.p, j + 1, G.w.p, gs + GL::H1, st));
-                NG_CUDA(LaunchPdl(k_gm_update_proj<T>, gridP, kBS, 0, c.stream, n, G.V.p, j + 1, gs + GL::H1, G.w.p, gs + GL::H2,
-                                                                  st));
+                NG_CUDA(LaunchPdl(k_gm_update_proj<T>, gridP, kBS, 0, c.stream, n, G.V.p, j + 1, gs + GL::H1, G.w.p,
+                                  gs + GL::H2, st));
                 NG_CUDA(LaunchPdl(k_gm_update<T>, grid, kBS, 0, c.stream, n, G.V.p, j + 1, gs, G.w.p, st, j));
                 if (j + 1 < cols)
-                    NG_CUDA(LaunchPdl(k_gm_normalize<T>, grid, kBS, 0, c.stream, n, G.w.p, vj1, amg ? nullptr : G.z.p, K.dinv.p,
-                                                                  gs, st));
+                    NG_CUDA(LaunchPdl(k_gm_normalize<T>, grid, kBS, 0, c.stream, n, G.w.p, vj1, amg ? nullptr : G.z.p,
+                                      K.dinv.p, gs, st));
             }
             if (j >= cols)
                 break;
