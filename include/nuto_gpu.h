@@ -259,6 +259,12 @@ int nuto_gpu_assemble_cell_matrices(nuto_gpu_ctx* ctx, const double* d_cell_matr
    rows and columns are eliminated) and writes x = C y (zero at dependent DOFs). */
 int nuto_gpu_solve(nuto_gpu_ctx* ctx, int precision, int method, const void* d_values, const double* d_b,
                    double* d_x, double rtol, int max_iterations, int* iterations, double* relative_residual);
+/* y = K x for the CSR values d_values (FP32 or FP64) and FP64 device vectors, the product of the Krylov solvers
+   and the Newton refinement (padded pair layout, 16-byte value loads); no counterpart in the reference, where
+   Eigen's SparseMatrix * VectorXd does it. compensated = 1 (FP32 values only) forms the sums in compensated FP32
+   (about 1e-14 relative to sum |K x|) instead of FP64 arithmetic. */
+int nuto_gpu_spmv(nuto_gpu_ctx* ctx, int precision, const void* d_values, const double* d_x, double* d_y,
+                  int compensated);
 /* Preconditioner of the PCG and GMRES solves of nuto_gpu_solve and nuto_gpu_do_step (NUTO_GPU_PRECOND_*). The
    multigrid hierarchy (spatial aggregates of the DOF nodes, piecewise-constant transfer per component) is built
    on the first solve after build_pattern; its coarse operators are rebuilt once per tangent. No counterpart in

@@ -97,6 +97,14 @@ class GpuCellGroup:
         pairs = self.nnz // (ncomp * ncomp)
         return sum(pairs * 4 + (L.num_nodes + 1) * 8 for L in layers) * len(layers)
 
+    def spmv(self, values, x, precision=FP64, compensated=False, out=None):
+        """y = K x (FP64 vectors on the device) through nuto_gpu_spmv"""
+        torch = _torch()
+        x = self._dev(x, torch.float64)
+        y = out if out is not None else torch.empty(self.n_dofs, dtype=torch.float64, device=x.device)
+        self._call("nuto_gpu_spmv", precision, _ptr(values), _ptr(x), _ptr(y), int(bool(compensated)))
+        return y
+
     def multigrid_info(self):
         """(levels of the first slot's hierarchy, 1 when the last sweeps ran as a CUDA graph)"""
         lv = ctypes.c_int()

@@ -842,6 +842,26 @@ int nuto_gpu_num_integration_points(const nuto_gpu_ctx* ctx)
     return ctx ? ctx->ip.nIp : 0;
 }
 
+int nuto_gpu_spmv(nuto_gpu_ctx* ctx, int precision, const void* d_values, const double* d_x, double* d_y,
+                  int compensated)
+{
+    return Guard(ctx, [&] {
+        NG_CHECK(ctx->havePattern, NUTO_GPU_ESTATE, "build_pattern first");
+        NG_CHECK(precision == NUTO_GPU_FP32 || precision == NUTO_GPU_FP64, NUTO_GPU_EINVAL,
+                 "precision NUTO_GPU_FP32 or NUTO_GPU_FP64");
+        NG_CHECK(!compensated || precision == NUTO_GPU_FP32, NUTO_GPU_EINVAL,
+                 "the compensated product takes FP32 values");
+        NG_CHECK(d_values && d_x && d_y, NUTO_GPU_EINVAL, "null pointer");
+        ctx->valsVersion++; // caller-supplied values may have changed behind the same pointer
+        if (compensated)
+            SpmvFull64Comp(*ctx, static_cast<const float*>(d_values), d_x, d_y);
+        else
+            SpmvFull64(*ctx, precision, d_values, d_x, d_y);
+        NG_CUDA(cudaStreamSynchronize(ctx->stream));
+        return NUTO_GPU_OK;
+    });
+}
+
 int nuto_gpu_multigrid_info(const nuto_gpu_ctx* ctx, int* levels, int* graph_active)
 {
     if (!ctx || !levels || !graph_active)

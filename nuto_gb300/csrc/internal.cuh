@@ -416,6 +416,9 @@ void AmgSetup(Ctx& c, const TV* vals);
 template <typename T>
 void AmgApply(Ctx& c, const T* v, T* z, const int* st, bool sym);
 int AmgLevels(const Ctx& c);
+// y = K x for FP32 or FP64 CSR values and FP64 vectors (FP64 accumulation), and the compensated FP32 form
+void SpmvFull64(Ctx& c, int precision, const void* vals, const double* x, double* y);
+void SpmvFull64Comp(Ctx& c, const float* vals, const double* x, double* y);
 const char* AmgGraphStatus(const Ctx& c);
 // true when the last sweep ran as a CUDA graph
 bool AmgGraphActive(const Ctx& c);

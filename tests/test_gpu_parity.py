@@ -411,6 +411,27 @@ def test_multigrid_sweep_graph_matches_kernel_launches(precision, monkeypatch):
     assert abs(it1 - it0) <= 40
 
 
+@pytest.mark.parametrize("kind,n", CASES + [("hex8gd", 8)])
+def test_spmv_padded_layout(kind, n):
+    """y = K x through nuto_gpu_spmv (the padded-pair-layout product of the solvers) against the CSR product on the
+    host: FP64 values 1e-13, FP32 values with FP64 accumulation 1e-13 and with compensated FP32 sums 1e-12, relative
+    to max |K| |x|."""
+    torch = _torch()
+    s, g, (om, layers, P, cons) = _build(kind, n)
+    rng = np.random.default_rng(31)
+    u = _state(P, rng, 1e-4)
+    x = rng.uniform(-1, 1, P.n_dofs)
+    rp, ci = g.pattern()
+    for precision, comp, tol in ((64, False, 1e-13), (32, False, 1e-13), (32, True, 1e-12)):
+        vals = g.build_matrix(u, precision)
+        K = sp.csr_matrix((vals.double().cpu().numpy(), ci, rp), shape=(P.n_dofs, P.n_dofs))
+        y = g.spmv(vals, x, precision=precision, compensated=comp).cpu().numpy()
+        ref = K @ x
+        scale = (abs(K) @ np.abs(x)).max()
+        assert np.abs(y - ref).max() <= tol * scale, (precision, comp, np.abs(y - ref).max() / scale)
+    torch.cuda.synchronize()
+
+
 @pytest.mark.parametrize("kind,n", CASES)
 def test_lumped_mass(kind, n):
     """BuildDiagonallyLumpedMatrix of DynamicMomentumBalance::Hessian2 on the GPU against the oracle (FP64)."""
