@@ -85,6 +85,9 @@ extern "C" {
 #define NUTO_GPU_FP32 32
 #define NUTO_GPU_FP64 64
 #define NUTO_GPU_MIXED 48 /* nuto_gpu_do_step only: FP32 tangent and preconditioner, FP64 Krylov vectors */
+/* nuto_gpu_build_matrix only: FP64 values with the law in FP64 and the node-pair products in double-float FP32
+   arithmetic (about 1e-14 relative; Hex8 and Quad4, plain FP64 otherwise): the tangent of the exact final phase */
+#define NUTO_GPU_FP64X 65
 
 /* Krylov methods */
 #define NUTO_GPU_SOLVER_AUTO 0     /* PCG for the symmetric integrands, GMRES otherwise */

@@ -6,7 +6,7 @@ the configurations used by the tests and the benchmark.
 """
 
 from . import _lib, adaptive, mesh, configs  # noqa: F401
-from ._lib import (FP32, FP64, GRADIENT_DAMAGE, HEX8, HEX20, MB_LINEAR_ELASTIC, MB_LOCAL_DAMAGE,  # noqa: F401
+from ._lib import (FP32, FP64, FP64X, GRADIENT_DAMAGE, HEX8, HEX20, MB_LINEAR_ELASTIC, MB_LOCAL_DAMAGE,  # noqa: F401
                    MIXED, PRECOND_AMG, PRECOND_JACOBI, QUAD4, SOLVER_AUTO, SOLVER_BICGSTAB, SOLVER_GMRES, SOLVER_PCG,
                    NoConvergence, NutoGpuError, load)
 from .assembly import GpuCellGroup  # noqa: F401

@@ -16,7 +16,7 @@ MB_LINEAR_ELASTIC, MB_LOCAL_DAMAGE, GRADIENT_DAMAGE = 0, 1, 2
 PLANE_STRESS, PLANE_STRAIN = 0, 1
 DAMAGE_FULL, DAMAGE_UNILATERAL = 0, 1
 INTERACTION_CONSTANT, INTERACTION_DECREASING = 0, 1
-FP32, FP64, MIXED = 32, 64, 48
+FP32, FP64, MIXED, FP64X = 32, 64, 48, 65
 SOLVER_AUTO, SOLVER_PCG, SOLVER_BICGSTAB, SOLVER_GMRES = 0, 1, 2, 3
 PRECOND_JACOBI, PRECOND_AMG = 1, 2
 IP_KAPPA, IP_DAMAGE, IP_STRAIN, IP_STRESS, IP_EEQ = 0, 1, 2, 3, 4

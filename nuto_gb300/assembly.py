@@ -161,7 +161,7 @@ class GpuCellGroup:
     def build_matrix(self, u, precision=FP64, out=None):
         torch = _torch()
         u = self._dev(u, torch.float64)
-        dt = torch.float32 if precision == FP32 else torch.float64
+        dt = torch.float32 if precision == FP32 else torch.float64  # FP64 and FP64X: FP64 values
         v = out if out is not None else torch.empty(self.nnz, dtype=dt, device=u.device)
         self._call("nuto_gpu_build_matrix", _ptr(u), precision, _ptr(v))
         return v

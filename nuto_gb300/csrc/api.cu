@@ -928,8 +928,12 @@ int nuto_gpu_build_matrix(nuto_gpu_ctx* ctx, const double* u, int precision, voi
 {
     return Guard(ctx, [&] {
         RequireReady(*ctx);
-        NG_CHECK(precision == NUTO_GPU_FP32 || precision == NUTO_GPU_FP64, NUTO_GPU_EINVAL, "precision 32 or 64");
-        LaunchTangent(*ctx, u, precision, values);
+        NG_CHECK(precision == NUTO_GPU_FP32 || precision == NUTO_GPU_FP64 || precision == NUTO_GPU_FP64X,
+                 NUTO_GPU_EINVAL, "precision 32, 64 or 65");
+        if (precision == NUTO_GPU_FP64X)
+            LaunchTangentExact(*ctx, u, static_cast<double*>(values));
+        else
+            LaunchTangent(*ctx, u, precision, values);
         return NUTO_GPU_OK;
     });
 }

@@ -436,10 +436,54 @@ struct IpRecord
     static constexpr int size = st + (RANK1 ? 2 * VD : 0);
 };
 
+// ---- double-float arithmetic on the FP32 pipe -----------------------------------------------------------------
+// A value is an unevaluated sum hi + lo of two floats (about 48 significant bits). Products use the FMA-exact error
+// term, sums TwoSum; the _rn intrinsics keep the compiler from contracting the error-free transforms into FMAs.
+struct Df
+{
+    float hi, lo;
+};
+__device__ __forceinline__ Df DfSplit(double x)
+{
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - static_cast<double>(h))};
+}
+__device__ __forceinline__ Df DfNorm(float s, float e)
+{
+    const float h = __fadd_rn(s, e);
+    return {h, __fadd_rn(e, -__fadd_rn(h, -s))};
+}
+__device__ __forceinline__ Df DfAdd(Df x, Df y)
+{
+    const float s = __fadd_rn(x.hi, y.hi);
+    const float bb = __fadd_rn(s, -x.hi);
+    float e = __fadd_rn(__fadd_rn(x.hi, -__fadd_rn(s, -bb)), __fadd_rn(y.hi, -bb));
+    e = __fadd_rn(e, __fadd_rn(x.lo, y.lo));
+    return DfNorm(s, e);
+}
+__device__ __forceinline__ Df DfMul(Df x, Df y)
+{
+    const float p = __fmul_rn(x.hi, y.hi);
+    float e = __fmaf_rn(x.hi, y.hi, -p);
+    e = __fmaf_rn(x.hi, y.lo, e);
+    e = __fmaf_rn(x.lo, y.hi, e);
+    return DfNorm(p, e);
+}
+__device__ __forceinline__ Df DfNeg(Df x)
+{
+    return {-x.hi, -x.lo};
+}
+__device__ __forceinline__ double DfToDouble(Df x)
+{
+    return static_cast<double>(x.hi) + static_cast<double>(x.lo);
+}
+
 // REC = false: element-wise tangent, node-pair blocks added into the CSR values with atomics.
 // REC = true: phases 0 and A only; the integration-point records are written for k_tangent_rows.
 // T is the arithmetic of the geometry, strain and law evaluation; TO the type of the written values or records.
-template <typename T, int DIM, int ND, int NIP, int KIND, bool REC, typename TO = T>
+// DF = true (FP64 T, element-wise): the node-pair products of phase B in double-float FP32 arithmetic instead of
+// FP64 (the FP64 pipe is narrow on this part); the law stays FP64 and the result is added with FP64 atomics.
+template <typename T, int DIM, int ND, int NIP, int KIND, bool REC, typename TO = T, bool DF = false>
 __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, ScatterArgs S, int pUU, int pUE, int pEU,
                                                  int pEE, const double* __restrict__ u, TO* __restrict__ vals)
 {
@@ -459,6 +503,11 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
     __shared__ int64_t sBaseUE[GD ? CPB : 1][GD ? ND : 1][DIM];
     __shared__ int64_t sBaseEU[GD ? CPB : 1][GD ? ND : 1];
     __shared__ int64_t sBaseEE[GD ? CPB : 1][GD ? ND : 1];
+    constexpr bool USE_DF = DF && sizeof(T) == 8 && !REC;
+    __shared__ Df sGd[USE_DF ? CPB : 1][USE_DF ? NIP : 1][USE_DF ? ND : 1][DIM];
+    __shared__ Df sRecd[USE_DF ? CPB : 1][USE_DF ? NIP : 1][NREC];
+    __shared__ Df sPQd[USE_DF && RANK1 ? CPB : 1][USE_DF && RANK1 ? NIP : 1][USE_DF && RANK1 ? ND : 1][2][DIM];
+    __shared__ Df sNd[USE_DF && GD ? NIP : 1][USE_DF && GD ? ND : 1];
     const int64_t n = a.nCells;
     const int64_t cell0 = static_cast<int64_t>(blockIdx.x) * CPB;
 
@@ -649,6 +698,128 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
             BtS<T, DIM>(sG[cl][q][nd], sST[cl][q][1], sPQ[cl][q][nd][1]);
         }
         __syncthreads();
+    }
+
+    if constexpr (USE_DF)
+    {
+        // split the FP64 inputs of phase B once per (cell, point, node)
+        for (int it = threadIdx.x; it < CPB * NIP * ND; it += blockDim.x)
+        {
+            const int cl = it % CPB;
+            const int r = it / CPB;
+            const int nd = r % ND, q = r / ND;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+            {
+                sGd[cl][q][nd][d] = DfSplit(static_cast<double>(sG[cl][q][nd][d]));
+                if constexpr (RANK1)
+                {
+                    sPQd[cl][q][nd][0][d] = DfSplit(static_cast<double>(sPQ[cl][q][nd][0][d]));
+                    sPQd[cl][q][nd][1][d] = DfSplit(static_cast<double>(sPQ[cl][q][nd][1][d]));
+                }
+            }
+            if (nd == 0)
+                for (int k = 0; k < NREC; ++k)
+                    sRecd[cl][q][k] = DfSplit(static_cast<double>(sRec[cl][q][k]));
+            if constexpr (GD)
+                if (cl == 0)
+                    sNd[q][nd] = DfSplit(a.tabN_D[q * ND + nd]);
+        }
+        __syncthreads();
+        for (int it = threadIdx.x; it < CPB * ND * ND; it += blockDim.x)
+        {
+            const int cl = it % CPB;
+            const int pr = it / CPB;
+            const int ia = pr / ND, ib = pr % ND;
+            const int64_t e = cell0 + cl;
+            if (e >= n)
+                continue;
+            const Df z{0.f, 0.f};
+            Df kuu[DIM][DIM], kue[DIM], keu[DIM], kee = z;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k)
+            {
+                kue[k] = keu[k] = z;
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    kuu[k][l] = z;
+            }
+            for (int q = 0; q < NIP; ++q)
+            {
+                const Df* ga = sGd[cl][q][ia];
+                const Df* gb = sGd[cl][q][ib];
+                const Df lam = sRecd[cl][q][0], mu = sRecd[cl][q][1];
+                Df gab = DfMul(ga[0], gb[0]);
+#pragma unroll
+                for (int d = 1; d < DIM; ++d)
+                    gab = DfAdd(gab, DfMul(ga[d], gb[d]));
+                Df la[DIM], ma[DIM];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                {
+                    la[k] = DfMul(lam, ga[k]);
+                    ma[k] = DfMul(mu, ga[k]);
+                }
+                const Df mg = DfMul(mu, gab);
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                {
+#pragma unroll
+                    for (int l = 0; l < DIM; ++l)
+                        kuu[k][l] = DfAdd(kuu[k][l], DfAdd(DfMul(la[k], gb[l]), DfMul(ma[l], gb[k])));
+                    kuu[k][k] = DfAdd(kuu[k][k], mg);
+                }
+                if constexpr (LD)
+                {
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k)
+#pragma unroll
+                        for (int l = 0; l < DIM; ++l)
+                            kuu[k][l] = DfAdd(kuu[k][l], DfMul(sPQd[cl][q][ia][0][k], sPQd[cl][q][ib][1][l]));
+                }
+                if constexpr (GD)
+                {
+                    const Df Na = sNd[q][ia], Nb = sNd[q][ib];
+                    Df gs = DfMul(ga[0], sRecd[cl][q][4]);
+#pragma unroll
+                    for (int d = 1; d < DIM; ++d)
+                        gs = DfAdd(gs, DfMul(ga[d], sRecd[cl][q][4 + d]));
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k)
+                    {
+                        kue[k] = DfAdd(kue[k], DfMul(sPQd[cl][q][ia][0][k], Nb));
+                        keu[k] = DfAdd(keu[k], DfNeg(DfMul(Na, sPQd[cl][q][ib][1][k])));
+                    }
+                    kee = DfAdd(kee, DfAdd(DfMul(DfMul(sRecd[cl][q][2], Na), Nb),
+                                           DfAdd(DfMul(sRecd[cl][q][3], gab), DfMul(gs, Nb))));
+                }
+            }
+            const int64_t ridx = static_cast<int64_t>(ia * ND + ib) * n + e;
+            const int rUU = S.rank[pUU][ridx];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k)
+            {
+                const int64_t row = sBaseU[cl][ia][k] + DIM * rUU;
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    atomicAdd(vals + NG_IDX(row + l, S.nnz, 10), static_cast<TO>(DfToDouble(kuu[k][l])));
+            }
+            if constexpr (GD)
+            {
+                const int rUE = S.rank[pUE][ridx];
+                const int rEU = S.rank[pEU][ridx];
+                const int rEE = S.rank[pEE][ridx];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                    atomicAdd(vals + NG_IDX(sBaseUE[cl][ia][k] + rUE, S.nnz, 10), static_cast<TO>(DfToDouble(kue[k])));
+                const int64_t rowE = sBaseEU[cl][ia] + DIM * rEU;
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    atomicAdd(vals + NG_IDX(rowE + l, S.nnz, 10), static_cast<TO>(DfToDouble(keu[l])));
+                atomicAdd(vals + NG_IDX(sBaseEE[cl][ia] + rEE, S.nnz, 10), static_cast<TO>(DfToDouble(kee)));
+            }
+        }
+        return;
     }
 
     // phase B: one thread per (cell, node pair)
@@ -1144,6 +1315,31 @@ static void LaunchTangentT(Ctx& c, const double* u, T* vals)
                 a, c.law, s, dS * ns + dS, dS * ns + eS, eS * ns + dS, eS * ns + eS, u, vals);
     });
     AfterLaunch(c, "k_tangent");
+    c.stats.kernel_launches += 1;
+}
+
+// FP64-accurate tangent for the exact final phase of the FP32 path: the element kernel with FP64 law evaluation and
+// double-float node-pair products (Hex8 and Quad4; the larger Hex20 blocks do not fit the shared memory of the
+// split inputs and use the FP64 products)
+void LaunchTangentExact(Ctx& c, const double* u, double* vals)
+{
+    c.valsVersion++;
+    NG_CUDA(cudaMemsetAsync(vals, 0, c.nnz * sizeof(double), c.stream));
+    CellArgs a = MakeCellArgs(c);
+    ScatterArgs s = MakeScatterArgs(c);
+    const int ns = static_cast<int>(c.slots.size());
+    const int dS = c.prm.disp_slot;
+    const int eS = c.prm.kind == NUTO_GPU_GRADIENT_DAMAGE ? c.prm.eeq_slot : dS;
+    DispatchCfg(c, [&](auto cfg) {
+        using C = decltype(cfg);
+        constexpr int CPB = TangentShape<C::nd, C::nip>::cpb;
+        const int blocks = static_cast<int>((c.nCells + CPB - 1) / CPB);
+        constexpr bool df = C::nd <= 8;
+        k_tangent<double, C::dim, C::nd, C::nip, C::kind, false, double, df>
+                <<<blocks, TangentShape<C::nd, C::nip>::threads, 0, c.stream>>>(
+                        a, c.law, s, dS * ns + dS, dS * ns + eS, eS * ns + dS, eS * ns + eS, u, vals);
+    });
+    AfterLaunch(c, "k_tangent exact");
     c.stats.kernel_launches += 1;
 }
 

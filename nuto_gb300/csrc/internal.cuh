@@ -398,6 +398,7 @@ void BuildTables(Ctx& c);
 void BuildGeometryCache(Ctx& c);
 void LaunchResidual(Ctx& c, const double* u, double* f);
 void LaunchTangent(Ctx& c, const double* u, int precision, void* values);
+void LaunchTangentExact(Ctx& c, const double* u, double* vals);
 void LaunchTangentNoAlloc(Ctx& c, const double* u, float* values);
 void LaunchHistory(Ctx& c, const double* u);
 void LaunchLumpedMass(Ctx& c, double rho, double* m);

@@ -155,7 +155,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
         const int k = T.Begin();
         if (exactNow)
         {
-            LaunchTangent(c, x, NUTO_GPU_FP64, w.K64.p);
+            LaunchTangentExact(c, x, w.K64.p);
             k_round<<<static_cast<unsigned>((c.nnz + 255) / 256), 256, 0, c.stream>>>(c.nnz, w.K64.p, w.K32.p);
             c.valsVersion++;
             S.kernel_launches += 1;

@@ -412,6 +412,22 @@ def test_multigrid_sweep_graph_matches_kernel_launches(precision, monkeypatch):
 
 
 @pytest.mark.parametrize("kind,n", CASES + [("hex8gd", 8)])
+def test_fp64x_tangent_matches_fp64(kind, n):
+    """The exact final phase's tangent (FP64 law, node-pair products in double-float FP32 arithmetic) against the
+    plain FP64 tangent, in a damaged state: <= 1e-13 relative to max |K| (Hex20 uses the FP64 products: equal)."""
+    torch = _torch()
+    s, g, (om, layers, P, cons) = _build(kind, n)
+    rng = np.random.default_rng(41)
+    u = _state(P, rng, 2e-3)
+    if g.kind != 0:  # damage laws: a history above kappa0 so that the damage terms are active
+        g.history = np.full((g.mesh.num_cells, g.n_ip), 1.5e-4)
+    k64 = g.build_matrix(u, 64).cpu().numpy()
+    k65 = g.build_matrix(u, 65).cpu().numpy()
+    assert np.abs(k65 - k64).max() <= 1e-13 * np.abs(k64).max(), np.abs(k65 - k64).max() / np.abs(k64).max()
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("kind,n", CASES + [("hex8gd", 8)])
 def test_spmv_padded_layout(kind, n):
     """y = K x through nuto_gpu_spmv (the padded-pair-layout product of the solvers) against the CSR product on the
     host: FP64 values 1e-13, FP32 values with FP64 accumulation 1e-13 and with compensated FP32 sums 1e-12, relative
