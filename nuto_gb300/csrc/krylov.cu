@@ -366,6 +366,13 @@ __global__ void k_masked_sq(int64_t n, const uint8_t* __restrict__ mask, const d
 }
 
 // ---- host side -----------------------------------------------------------------------------------------------
+// host wait for the context's stream (its time is reported as HP_SYNC)
+static void WaitStream(Ctx& c)
+{
+    HostClock hc(&c.hostMs[HP_SYNC]);
+    NG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
 static int GridFor(const Ctx& c, int64_t n)
 {
     const int64_t want = (n + kBS - 1) / kBS;
@@ -515,10 +522,7 @@ double MaskedNorm(Ctx& c, const double* v)
     k_masked_sq<<<GridFor(c, c.nDofs), kBS, 0, c.stream>>>(c.nDofs, c.dMask.p, v, w.scal.p + SC_ACC2);
     c.stats.kernel_launches += 1;
     NG_CUDA(cudaMemcpyAsync(w.hScal + SC_ACC2, w.scal.p + SC_ACC2, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    {
-            HostClock hcw(&c.hostMs[HP_SYNC]);
-            NG_CUDA(cudaStreamSynchronize(c.stream));
-        }
+    WaitStream(c);
     const double r = w.hScal[SC_ACC2];
     NG_CUDA(cudaMemsetAsync(w.scal.p + SC_ACC2, 0, sizeof(double), c.stream));
     return std::sqrt(r);
@@ -1143,10 +1147,7 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
             NG_CUDA(cudaMemcpyAsync(w.hStat, st, ST_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
             NG_CUDA(cudaMemcpyAsync(w.hG + GL::G, gs + GL::G, (GL::SIZE - GL::G) * sizeof(double),
                                     cudaMemcpyDeviceToHost, c.stream));
-            {
-            HostClock hcw(&c.hostMs[HP_SYNC]);
-            NG_CUDA(cudaStreamSynchronize(c.stream));
-        }
+            WaitStream(c);
             if (w.hStat[ST_STATE] != RUN)
                 break;
             const int jd = w.hStat[ST_JDONE];
@@ -1167,10 +1168,7 @@ static int GmresSolve(Ctx& c, const TV* vals, const double* b, double* x64, bool
         AfterLaunch(c, "gmres cycle");
         NG_CUDA(cudaMemcpyAsync(w.hG, gs, GL::SIZE * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         NG_CUDA(cudaMemcpyAsync(w.hStat, st, ST_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-        {
-            HostClock hcw(&c.hostMs[HP_SYNC]);
-            NG_CUDA(cudaStreamSynchronize(c.stream));
-        }
+        WaitStream(c);
         SpmvCollect(c);
         state = w.hStat[ST_STATE];
         const int k = w.hStat[ST_JDONE];
@@ -1313,10 +1311,7 @@ static int KrylovSolve(Ctx& c, int method, const TV* vals, const double* b, doub
         done += nIt;
         NG_CUDA(cudaMemcpyAsync(w.hStat, st, ST_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         NG_CUDA(cudaMemcpyAsync(w.hScal, sc, SC_COUNT * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-        {
-            HostClock hcw(&c.hostMs[HP_SYNC]);
-            NG_CUDA(cudaStreamSynchronize(c.stream));
-        }
+        WaitStream(c);
         SpmvCollect(c);
         state = w.hStat[ST_STATE];
         if (state != RUN)
