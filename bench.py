@@ -156,6 +156,15 @@ AGG_KEYS = ("matrix_assemblies", "newton_iterations", "krylov_iterations", "ms_s
             "kernel_launches", "ms_assemble_matrix", "ms_assemble_vector", "ms_krylov", "residual_evaluations")
 
 
+def accumulate(t0, dt, k):
+    """t0 + dt, t0 + dt + dt, ... (k values), summed as the time stepping sums them"""
+    out, t = [], t0
+    for _ in range(k):
+        t = t + dt
+        out.append(t)
+    return out
+
+
 def run_steps(g, opts, t_start, t_values):
     """Advances the load from t_start through every t in t_values with AdaptiveSolve (time step 1/LOAD_STEPS, cut
     back by halves on NoConvergence as the reference's AdaptiveSolve does). Returns the summed step statistics,
@@ -272,10 +281,12 @@ def run_ours(args):
     dt = 1.0 / LOAD_STEPS
     g.set_state(None, 0.0, True)
     g.history = s.history0
-    run_steps(g, opts32, 0.0, [k * dt for k in range(1, args.warmup + 1)])
+    # load-step end times by accumulation, as AdaptiveSolve advances the time (t += dt), so that every step ends
+    # exactly on its end time (k * dt can differ from the accumulated sum in the last bit)
+    run_steps(g, opts32, 0.0, accumulate(0.0, dt, args.warmup))
     x_w, t_w = g.get_state()
     kappa_w = g.history
-    t_values = [(args.warmup + k) * dt for k in range(1, args.steps + 1)]
+    t_values = accumulate(t_w, dt, args.steps)
 
     def barrier():
         if world > 1:

@@ -1,5 +1,5 @@
 """Adaptive load stepping: AdaptiveSolve::Solve (nuto/mechanics/tools/AdaptiveSolve.cpp:18-67) over
-nuto_gpu_do_step.
+nuto_gpu_do_step (host logic only; tests/test_adaptive.py checks it against scripted step outcomes).
 
 A step that ends in NewtonRaphson::NoConvergence (NUTO_GPU_ENOCONV; the library leaves state and history
 unchanged) is retried with the time step times decrease_factor; after a step that converged in fewer than three
@@ -26,28 +26,36 @@ class AdaptiveSolve:
         self.stats = []
 
     def solve(self, t_end, t_start=0.0):
-        """Advances the group's state from t_start to t_end; returns the number of converged steps."""
+        """Advances the group's state from t_start to t_end; returns the number of converged steps.
+
+        Follows AdaptiveSolve::Solve step by step: the time step is state (kept across calls, clipped so that the
+        last step ends at t_end), at least one step is attempted, a NoConvergence halves it without advancing the
+        time, and after a step that converged in fewer than three Newton iterations it grows by increase_factor up
+        to dt_max."""
         t = t_start
         steps = 0
         if self.post_process:
             self.post_process(t)
-        while t < t_end - 1e-14:
-            dt = min(self.dt, t_end - t)
+        while True:
             try:
-                its = self.g.do_step(t + dt, self.options)
+                its = self.g.do_step(t + self.dt, self.options)
             except NoConvergence:
-                self.dt = dt * self.decrease_factor
+                self.dt *= self.decrease_factor
                 self.cutbacks += 1
                 self.stats.append(self.g.stats())
                 if self.dt < self.dt_min:
                     raise RuntimeError("time step smaller than the prescribed minimal time step %g" % self.dt_min)
-                continue
-            t += dt
+                continue  # without updating the global time
+            t += self.dt
             steps += 1
             self.stats.append(self.g.stats())
             if self.post_process:
                 self.post_process(t)
+            if t >= t_end:
+                break
             if its < 3 and self.dt < self.dt_max:
                 self.dt = min(self.dt * self.increase_factor, self.dt_max)
+            if t + self.dt > t_end:
+                self.dt = t_end - t
         self.steps += steps
         return steps
