@@ -13,6 +13,11 @@ hex8_gradient_damage
 hex20_local_damage 3D Hex20 displacements (3x3x3 Gauss) on an n^3 Hex8 coordinate mesh of the unit cube,
                    MomentumBalance + LocalIsotropicDamage (E = 30000, nu = 0.2, kappa0 = 1e-4, beta = 100,
                    alpha = 0.99, k = 10); z = 0 face fixed, z = 1 face u_z = RhsRamp(1, 3e-4) (5 load steps).
+notched_plate      2D plane-strain gradient-enhanced damage on the unit square, n x n Quad4 (2x2 Gauss), u (2 DOF)
+                   + eeq (1 DOF), the law of hex8_gradient_damage in 2D; a notch one cell high from the left edge
+                   at mid height (cells of row n/2 with x index below round(depth n) removed); bottom edge u_y = 0,
+                   the corner (0, 0) also u_x = 0, top edge u_y = RhsRamp(1, u_end) (10 load steps). One specimen of
+                   the batched workload (nuto_gb300.batch).
 """
 
 from dataclasses import dataclass, field
@@ -114,3 +119,43 @@ def hex20_local_damage(n=80, u_end=3e-4, load_steps=5):
     integ = dict(kind=MB_LOCAL_DAMAGE, dim=3, E=30000.0, nu=0.2, plane_state=PLANE_STRAIN,
                  damage_application=DAMAGE_FULL, kappa0=1e-4, beta=100.0, alpha=0.99, k=10.0, disp_slot=0)
     return Setup("hex20_local_damage_%d^3" % n, m, [d], 3, integ, [cons], load_steps, 1.0)
+
+
+def notched_plate_mesh(n, depth=0.3):
+    """Unit square, n x n Quad4 cells (UnitMeshFem::CreateQuads order) without the notch cells: row n // 2, x index
+    below round(depth n) (at least 1, at most n - 2). Coordinate nodes that no remaining cell uses are dropped; the
+    others keep their relative order."""
+    full = M.create_quads(n, n)
+    cut = notch_cells(n, depth)
+    conn = full.conn[~cut]
+    used = np.unique(conn)
+    remap = np.full(full.coords.shape[0], -1, dtype=np.int64)
+    remap[used] = np.arange(used.size)
+    return M.MeshFem(2, full.geo_interp, full.coords[used], remap[conn])
+
+
+def notch_cells(n, depth):
+    """Mask over the n x n cells (lattice order, x fastest) of the notch."""
+    if n < 4:
+        raise ValueError("a notched plate needs n >= 4")
+    iy, ix = np.divmod(np.arange(n * n), n)
+    d = min(max(int(round(depth * n)), 1), n - 2)
+    return (iy == n // 2) & (ix < d)
+
+
+def notched_plate(n=40, depth=0.3, u_end=2e-4, load_steps=10):
+    m = notched_plate_mesh(n, depth)
+    d = M.add_dof_interpolation(m, 2)
+    e = M.add_dof_interpolation(m, 1)
+    bottom = M.nodes_at_axis(m, d, 1, 0.0)
+    top = M.nodes_at_axis(m, d, 1, 1.0)
+    xy = m.layers[d].node_coords[bottom]
+    corner = bottom[np.abs(xy[:, 0]) < 1e-10]
+    cons_d = _merge(M.component_constraints(m, d, bottom, [1], 0.0),
+                    M.component_constraints(m, d, corner, [0], 0.0),
+                    M.component_constraints(m, d, top, [1], 0.0, u_end))
+    integ = dict(kind=GRADIENT_DAMAGE, dim=2, E=30000.0, nu=0.2, plane_state=PLANE_STRAIN,
+                 damage_application=DAMAGE_FULL, kappa0=1e-4, beta=100.0, alpha=0.99, k=10.0, c=0.01, disp_slot=0,
+                 eeq_slot=1)
+    return Setup("notched_plate_%dx%d_depth%.3f" % (n, n, depth), m, [d, e], 2, integ, [cons_d, _empty()],
+                 load_steps, 1.0)

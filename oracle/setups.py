@@ -52,3 +52,28 @@ def hex20_local_damage(n, u_end=3e-4):
     cons = _cat(_component(m, d, 3, m.nodes_at_axis(d, 2, 0.0), [0, 1, 2], 0.0, 0.0),
                 _component(m, d, 3, m.nodes_at_axis(d, 2, 1.0), [2], 0.0, u_end))
     return m, [d], P, cons
+
+
+def notched_plate(n, depth=0.3, u_end=2e-4):
+    """The batched workload's specimen: UnitMeshFem::CreateQuads(n, n) without the notch cells (row n // 2, the
+    first round(depth n) cells of it, clamped to 1 .. n - 2), unused coordinate nodes dropped in order; 2D
+    plane-strain gradient damage; bottom edge u_y = 0, corner (0, 0) u_x = 0, top edge u_y = RhsRamp(1, u_end)."""
+    full = core.Mesh.quads(n, n)
+    coords, conn = full.coords(2), full.conn(4)
+    cells = np.arange(n * n)
+    cut = (cells // n == n // 2) & (cells % n < min(max(int(round(depth * n)), 1), n - 2))
+    conn = conn[~cut]
+    used = np.unique(conn)
+    remap = np.full(coords.shape[0], -1, dtype=np.int64)
+    remap[used] = np.arange(used.size)
+    m = core.Mesh.from_arrays(2, core.QUAD4, coords[used], remap[conn].astype(np.int32))
+    d = m.add_dof(2)
+    e = m.add_dof(1)
+    integ = core.Integrand.make(core.GRADIENT_DAMAGE, 2, E=30000.0, nu=0.2, plane_state=core.PLANE_STRAIN,
+                                damage_application=core.FULL, kappa0=1e-4, beta=100.0, alpha=0.99, k=10.0, c=0.01)
+    P = core.Problem(m, 2, [d, e], integ)
+    bottom = m.nodes_at_axis(d, 1, 0.0)
+    corner = bottom[np.abs(m.layer_node_coords(d)[bottom, 0]) < 1e-10]
+    cons = _cat(_component(m, d, 2, bottom, [1], 0.0, 0.0), _component(m, d, 2, corner, [0], 0.0, 0.0),
+                _component(m, d, 2, m.nodes_at_axis(d, 1, 1.0), [1], 0.0, u_end))
+    return m, [d, e], P, cons

@@ -40,6 +40,9 @@ def _build(kind, n):
     elif kind == "hex8gd":
         s = configs.hex8_gradient_damage(n)
         o = osetups.hex8_gradient_damage(n)
+    elif kind == "quad4gd":
+        s = configs.notched_plate(n, 0.4)
+        o = osetups.notched_plate(n, 0.4)
     else:
         s = configs.hex20_local_damage(n)
         o = osetups.hex20_local_damage(n)
@@ -58,7 +61,7 @@ def _oracle_csr(P, u):
     return K
 
 
-CASES = [("quad4", 5), ("hex8gd", 3), ("hex20", 2)]
+CASES = [("quad4", 5), ("hex8gd", 3), ("hex20", 2), ("quad4gd", 8)]
 
 
 @pytest.mark.parametrize("kind,n", CASES)
@@ -73,9 +76,9 @@ def test_pattern_bit_exact(kind, n):
 
 
 def _damage_state(kind, P, rng):
-    if kind == "hex8gd":
+    if kind in ("hex8gd", "quad4gd"):
         u = _state(P, rng, 2e-4)
-        nd = 3 * P.mesh.layer_num_nodes(0)
+        nd = (3 if kind == "hex8gd" else 2) * P.mesh.layer_num_nodes(0)
         u[nd:] = rng.uniform(0.0, 4e-4, P.n_dofs - nd)  # eeq around and above kappa0
         kappa = rng.uniform(0.0, 3e-4, (P.n_el, P.n_ip))
     elif kind == "hex20":
@@ -177,7 +180,7 @@ def test_cell_scatter_known_answer():
     assert nnz == 4 * 4 * 2 - 4  # shared edge: 2 x 2 entries counted once
 
 
-@pytest.mark.parametrize("kind,n", [("hex8gd", 3), ("hex20", 2)])
+@pytest.mark.parametrize("kind,n", [("hex8gd", 3), ("hex20", 2), ("quad4gd", 8)])
 def test_update_history(kind, n):
     _torch()
     s, g, (om, layers, P, cons) = _build(kind, n)
@@ -295,6 +298,49 @@ def test_quasistatic_hex8_gradient_damage(precision):
     assert res[-1][2].max() > 1e-4  # the last steps are in the damaged regime
 
 
+@pytest.mark.parametrize("precision", [64, 32])
+def test_quasistatic_notched_plate(precision):
+    """Eight load steps of one notched plate (2D plane-strain gradient damage, damage from step 4): displacement,
+    eeq and kappa follow the oracle's direct-solve Newton."""
+    _torch()
+    res = _run_steps("quad4gd", 8, precision, 8, 0.8, tol=1e-12)
+    for k, (xo, xg, ko, kg, st) in enumerate(res):
+        rel = np.abs(xg - xo).max() / np.abs(xo).max()
+        assert rel <= (1e-7 if precision == 64 else 1e-6), (k, rel, st)
+        assert np.abs(kg - ko).max() <= (1e-7 if precision == 64 else 1e-6) * max(np.abs(ko).max(), 1e-4)
+    assert res[-1][2].max() > 1e-4
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_batched_plates_match_separate_oracle_solves(precision):
+    """Three notched plates of different sizes solved as one batch on the GPU (one cell group, block-diagonal
+    system, absolute Newton tolerance on the combined |C^T r|) against the oracle solving each plate alone: every
+    plate's displacement, eeq and kappa within 1e-7 (FP64) / 1e-6 (FP32 tangent) after six load steps."""
+    _torch()
+    from nuto_gb300 import batch, configs
+
+    specs = [(6, 0.25), (10, 0.5), (8, 0.4)]
+    b = batch.concatenate([configs.notched_plate(n, d) for n, d in specs])
+    g = b.build_gpu()
+    g.set_state(None, 0.0, True)
+    opts = g.default_options(precision=precision, newton_rtol=0.0, newton_atol=1e-12,
+                             krylov_rtol=1e-12 if precision == 64 else 1e-5, max_newton=30, max_krylov=50000)
+    alone = []
+    for n, d in specs:
+        _, _, Pi, ci = osetups.notched_plate(n, d)
+        alone.append((Pi, QuasistaticOracle(Pi, ci[0], ci[1], ci[2], tolerance=1e-12, max_iterations=20)))
+    for k in range(1, 7):
+        g.do_step(0.1 * k, opts)
+        for Pi, Qi in alone:
+            Qi.do_step(0.1 * k)
+    x, _ = g.get_state()
+    tol = 1e-7 if precision == 64 else 1e-6
+    for (Pi, Qi), xs, ks in zip(alone, b.split_state(x), b.split_history(g.history)):
+        assert np.abs(xs - Qi.x).max() <= tol * np.abs(Qi.x).max()
+        assert np.abs(ks - Pi.kappa).max() <= tol * np.abs(Pi.kappa).max()
+        assert Pi.kappa.max() > 1e-4
+
+
 def test_exact_final_phase_within_1e6_of_converged_solution():
     """FP32 tangent with the exact final phase (exact_tangent_below = 1e4, the default): at the benchmark's relative
     Newton tolerance 1e-8, eight load steps into the damaged regime end within 1e-6 (relative, max norm) of the
@@ -357,7 +403,7 @@ def test_multigrid_levels_solve(kind, n, steps):
         assert its[2] < its[1], its
 
 
-@pytest.mark.parametrize("kind,n", [("quad4", 5), ("hex8gd", 3), ("hex20", 2)])
+@pytest.mark.parametrize("kind,n", [("quad4", 5), ("hex8gd", 3), ("hex20", 2), ("quad4gd", 8)])
 @pytest.mark.parametrize("precision", [32])
 def test_tangent_row_gather_matches_element_atomics(kind, n, precision, monkeypatch):
     """The FP32 row-gather tangent (records + one warp per node row) and the element-wise atomic tangent give the
@@ -458,7 +504,7 @@ def test_lumped_mass(kind, n):
     assert np.abs(m - ref).max() <= FP64_REL * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("kind,n", [("quad4", 5), ("hex8gd", 3), ("hex20", 2)])
+@pytest.mark.parametrize("kind,n", [("quad4", 5), ("hex8gd", 3), ("hex20", 2), ("quad4gd", 8)])
 def test_eval_ip(kind, n):
     """Cell::Eval post-processing values (kappa, damage, strain, stress, equivalent strain) against the oracle."""
     _torch()
