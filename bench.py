@@ -14,6 +14,10 @@ roofline   the Krylov SpMV (dominant kernel): algorithmic bytes per launch / mea
 cpu_baseline / --impl reference
            the oracle (CPU restatement of NuTo's assembly, OpenMP) plus scipy SuperLU as the stand-in for
            Eigen::SparseLU, timed on a bounded sample of the same problem on the host cores.
+
+--workload plates  (not the headline) the batched workload instead: --specimens seeded notched plates (2D
+           gradient damage, side 20..120 cells) solved as one system through their 10 load steps; value = DOFs x
+           load steps / s, next to the FP64 path and the oracle solving plates of the same batch one by one.
 """
 
 import argparse
@@ -50,6 +54,8 @@ def parse():
     p.add_argument("--size", type=int, default=64)
     p.add_argument("--skip-fp64", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
+    p.add_argument("--workload", default="beam", choices=["beam", "plates"])
+    p.add_argument("--specimens", type=int, default=128)
     return p.parse_args()
 
 
@@ -236,6 +242,9 @@ def run_reference(args):
     import oracle
 
     oracle.build()
+    if args.workload == "plates":
+        run_reference_plates(args)
+        return
     for _ in range(args.warmup):
         cpu_sample(16, oracle.lib().oracle_max_threads())
     times = []
@@ -467,10 +476,179 @@ def run_ours(args):
         tdist.destroy_process_group()
 
 
+PLATES_METRIC = "batched notched plates: DOF load steps/s (DOFs of every plate x load steps at 1e-8 residual / s)"
+PLATE_STEPS = 10
+
+
+def plates_cpu_sample(ns, depths, threads, budget_s=15.0):
+    """The oracle (OpenMP assembly, SuperLU) solving plates of the batch one by one through the 10 load steps,
+    nearest to the batch's median size first, until budget_s seconds have been spent (at least one plate); Newton to
+    |C^T r| < 1e-10 (absolute; the forces are of order 1). Returns (seconds, DOF load steps, plates, iterations)."""
+    from oracle import setups
+    from oracle.core import lib
+    from oracle.quasistatic import QuasistaticOracle
+
+    lib().oracle_set_threads(threads)
+    order = np.argsort(np.abs(ns - np.median(ns)), kind="stable")
+    spent, work, count, its = 0.0, 0, 0, 0
+    for i in order:
+        om, layers, P, cons = setups.notched_plate(int(ns[i]), float(depths[i]))
+        Q = QuasistaticOracle(P, cons[0], cons[1], cons[2], tolerance=1e-10, max_iterations=20)
+        t0 = time.perf_counter()
+        for t in accumulate(0.0, 1.0 / PLATE_STEPS, PLATE_STEPS):
+            its += Q.do_step(t)
+        spent += time.perf_counter() - t0
+        work += P.n_dofs * PLATE_STEPS
+        count += 1
+        if spent >= budget_s:
+            break
+    return spent, work, count, its
+
+
+def run_reference_plates(args):
+    """The reference arm of the batched workload: the oracle solving plates of the same seeded batch one by one
+    (each step a bounded sample, plates nearest the median size first)."""
+    from nuto_gb300 import batch
+    from oracle.core import lib
+
+    _, ns, depths = batch.notched_plate_batch(args.specimens, seed=0, load_steps=PLATE_STEPS)
+    threads = lib().oracle_max_threads()
+    i = int(np.argmin(ns))
+    for _ in range(args.warmup):  # the smallest plate
+        plates_cpu_sample(ns[i:i + 1], depths[i:i + 1], threads, budget_s=0.0)
+    sec, work, count, its = 0.0, 0, 0, 0
+    for _ in range(args.steps):
+        s_, w_, c_, i_ = plates_cpu_sample(ns, depths, threads, budget_s=5.0)
+        sec, work, count, its = sec + s_, work + w_, count + c_, its + i_
+    value = work / sec
+    out = {"metric": PLATES_METRIC, "value": value, "unit": "DOF load steps/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "impl": "reference",
+           "config": {"workload": "%d notched plates (seed 0), solved one by one" % args.specimens,
+                      "parallelism": "host OpenMP"},
+           "cpu_baseline": {"value": value, "unit": "DOF load steps/s", "cores": threads, "kind": "port",
+                            "sample": "%d plate solves (10 load steps each; oracle assembly + SuperLU), %d Newton "
+                                      "iterations; the reference itself cannot be built (Eigen/Boost absent)"
+                                      % (count, its)},
+           "e2e": {"value": value, "unit": "DOF load steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_plates(args):
+    """The batched workload on one GPU (replicas under torchrun: rank r solves the batch of seed r)."""
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import nuto_gb300
+    from nuto_gb300 import batch
+    from nuto_gb300.adaptive import AdaptiveSolve
+
+    nuto_gb300.load()
+    b, ns, depths = batch.notched_plate_batch(args.specimens, seed=rank, load_steps=PLATE_STEPS)
+    g = b.build_gpu(device=local)
+    n_dofs, nnz = g.n_dofs, g.nnz
+    dt = 1.0 / PLATE_STEPS
+    t_values = accumulate(0.0, dt, PLATE_STEPS)
+    opts = {32: g.default_options(precision=nuto_gb300.FP32, newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL,
+                                  max_newton=20, max_krylov=20000, exact_tangent_below=EXACT_BELOW),
+            64: g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL,
+                                  max_newton=20, max_krylov=20000)}
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as tdist
+
+            tdist.barrier()
+        torch.cuda.synchronize()
+
+    def solve(o, t_end):
+        g.set_state(None, 0.0, True)
+        ad = AdaptiveSolve(g, o, dt=dt, dt_max=dt, dt_min=dt / 256)
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ad.solve(t_end)
+        e1.record()
+        barrier()
+        agg = {k: sum(st[k] for st in ad.stats) for k in AGG_KEYS}
+        agg["cutbacks"] = ad.cutbacks
+        return e0.elapsed_time(e1) / 1e3, agg
+
+    solve(opts[32], t_values[min(args.warmup, PLATE_STEPS) - 1] if args.warmup > 0 else 0.0)  # warm-up steps
+    clocks = ClockSampler(gpu_index(local))
+    clocks.start()
+    sec32, agg32 = solve(opts[32], t_values[-1])
+    clk = clocks.stop()
+    x32, _ = g.get_state()
+    if world > 1:
+        import torch.distributed as tdist
+
+        tt = torch.tensor([sec32], device="cuda")
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        sec32 = float(tt.item())
+    out = {"metric": PLATES_METRIC, "value": world * n_dofs * PLATE_STEPS / sec32, "unit": "DOF load steps/s",
+           "n_gpus": world, "steps": PLATE_STEPS, "warmup": args.warmup, "ms_per_step": 1e3 * sec32 / PLATE_STEPS,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+           "data": "synthetic",
+           "config": {"workload": "%d notched plates (seed %d): Quad4 2x2 Gauss on the unit square, side n ~ "
+                                  "U{20..120} cells, notch one cell high from the left edge at mid height, depth ~ "
+                                  "U[0.2, 0.5] of the width; plane-strain GradientDamage(c=0.01, "
+                                  "LinearElasticDamage(30000, 0.2, FULL), DamageLawExponential(1e-4, 100, 0.99), "
+                                  "ModifiedMises(k=10)); bottom u_y = 0, top u_y = 2e-4 t, 10 load steps, all plates "
+                                  "in one cell group" % (args.specimens, rank),
+                      "specimens": args.specimens, "cells": int(b.mesh.num_cells), "n_dofs": n_dofs, "nnz": nnz,
+                      "side_cells_min_max": [int(ns.min()), int(ns.max())],
+                      "newton_tolerance": "|C^T r| <= 1e-8 |C^T (r + K db)| of the load step (whole batch)",
+                      "l2": "inputs larger than L2 (FP32 tangent %.0f MB)" % (nnz * 4 / 1e6),
+                      "parallelism": "replicas" if world > 1 else "single GPU"},
+           "newton_iterations": agg32["newton_iterations"], "tangent_solves": agg32["matrix_assemblies"],
+           "krylov_iterations": agg32["krylov_iterations"], "cutbacks": agg32["cutbacks"],
+           "assembled_dofs_per_s": world * n_dofs * agg32["matrix_assemblies"] / sec32,
+           "specimen_load_steps_per_s": world * args.specimens * PLATE_STEPS / sec32,
+           "gpu_launches": int(agg32["kernel_launches"]), "clocks": clk}
+    if not args.skip_fp64:
+        sec64, agg64 = solve(opts[64], t_values[-1])
+        x64, _ = g.get_state()
+        out["fp64"] = {"value": n_dofs * PLATE_STEPS / sec64, "unit": "DOF load steps/s",
+                       "ms_per_step": 1e3 * sec64 / PLATE_STEPS, "newton_iterations": agg64["newton_iterations"],
+                       "krylov_iterations": agg64["krylov_iterations"], "cutbacks": agg64["cutbacks"],
+                       "speedup_mixed_vs_fp64": sec64 / sec32,
+                       "max_rel_displacement_difference_mixed_vs_fp64": float(
+                           np.abs(x32 - x64).max() / max(np.abs(x64).max(), 1e-300))}
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        try:
+            from oracle.core import lib
+
+            threads = lib().oracle_max_threads()
+            sec, work, count, its = plates_cpu_sample(ns, depths, threads)
+            out["cpu_baseline"] = {"value": work / sec, "unit": "DOF load steps/s", "cores": threads, "kind": "port",
+                                   "sample": "%d plate(s) of the same batch nearest its median size, each solved "
+                                             "alone through the 10 load steps by the oracle (OpenMP assembly, "
+                                             "SuperLU, Newton to 1e-10 absolute): %.1f s, %d Newton iterations"
+                                             % (count, sec, its)}
+        except Exception as exc:  # the CPU leg must not hide the GPU result
+            out["cpu_baseline"] = {"value": None, "error": str(exc)}
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.destroy_process_group()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "plates":
+        run_plates(args)
     else:
         run_ours(args)
 

@@ -104,3 +104,13 @@ def test_batched_newton_reproduces_separate_solves():
         assert np.abs(x - Qi.x).max() <= 1e-9 * np.abs(Qi.x).max()
         assert np.abs(kap - Pi.kappa).max() <= 1e-9 * np.abs(Pi.kappa).max()
         assert Pi.kappa.max() > 1e-4  # damaged
+
+
+def test_plates_cpu_sample_counts_work():
+    """The CPU baseline of the batched workload (bench.py): plates nearest the median size first, at least one."""
+    import bench
+
+    ns, depths = np.array([4, 6, 5]), np.array([0.3, 0.4, 0.25])
+    sec, work, count, its = bench.plates_cpu_sample(ns, depths, 1, budget_s=0.0)
+    _, _, P, _ = osetups.notched_plate(5, 0.25)
+    assert count == 1 and work == P.n_dofs * bench.PLATE_STEPS and sec > 0 and its > 0
