@@ -63,6 +63,21 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def aggregate_ranks(values, seconds, device):
+    """Whole-job figures over replica ranks: each entry of `values` summed over the ranks (all_reduce SUM), and the
+    slowest rank's time (all_reduce MAX). A single process, or no process group, returns its own figures."""
+    import torch
+    import torch.distributed as tdist
+
+    if not (tdist.is_available() and tdist.is_initialized()) or tdist.get_world_size() == 1:
+        return [float(v) for v in values], float(seconds)
+    w = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    tdist.all_reduce(w, op=tdist.ReduceOp.SUM)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return [float(v) for v in w.tolist()], float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
 
@@ -321,13 +336,9 @@ def run_ours(args):
     sec32, agg32 = timed(opts32)
     clk = clocks.stop()
     x32, _ = g.get_state()
-    if world > 1:
-        import torch.distributed as tdist
-
-        tt = torch.tensor([sec32], device="cuda")
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        sec32 = float(tt.item())
-    value = world * n_dofs * agg32["matrix_assemblies"] / sec32
+    sec32_rank = sec32  # this rank's own time, for the ratios to this rank's FP64 run
+    (work,), sec32 = aggregate_ranks([n_dofs * agg32["matrix_assemblies"]], sec32, "cuda")
+    value = work / sec32
 
     fp64 = None
     if not args.skip_fp64:
@@ -341,8 +352,8 @@ def run_ours(args):
                 "newton_iterations": agg64["newton_iterations"], "krylov_iterations": agg64["krylov_iterations"],
                 "ms_assemble_matrix_per_launch": agg64["ms_assemble_matrix"] / max(agg64["matrix_assemblies"], 1),
                 "speedup_mixed_vs_fp64_newton_step": (sec64 / max(agg64["matrix_assemblies"], 1))
-                / (sec32 / max(agg32["matrix_assemblies"], 1)),
-                "speedup_mixed_vs_fp64_load_step": sec64 / sec32,
+                / (sec32_rank / max(agg32["matrix_assemblies"], 1)),
+                "speedup_mixed_vs_fp64_load_step": sec64 / sec32_rank,
                 "max_rel_displacement_error_mixed_vs_fp64": err,
                 "l2_rel_displacement_error_mixed_vs_fp64": err_l2}
         # both results against an FP64 solution of the same steps converged to 1e-11 (untimed): the displacement
@@ -392,7 +403,8 @@ def run_ours(args):
             step = min(dt, step * 1.5) if g.stats()["newton_iterations"] < 3 else step
     barrier()
     sec_e2e = time.perf_counter() - h0
-    e2e = {"value": world * n_dofs * assemblies / sec_e2e, "unit": "DOF/s",
+    (work_e2e,), sec_e2e = aggregate_ranks([n_dofs * assemblies], sec_e2e, "cuda")
+    e2e = {"value": work_e2e / sec_e2e, "unit": "DOF/s",
            "h2d_bytes_per_step": int((n_dofs + n_hist) * 8), "d2h_bytes_per_step": int((n_dofs + n_hist) * 8),
            "ms_per_step": 1e3 * sec_e2e / args.steps}
 
@@ -581,19 +593,18 @@ def run_plates(args):
         agg["cutbacks"] = ad.cutbacks
         return e0.elapsed_time(e1) / 1e3, agg
 
-    solve(opts[32], t_values[min(args.warmup, PLATE_STEPS) - 1] if args.warmup > 0 else 0.0)  # warm-up steps
+    if args.warmup > 0:  # warm-up load steps from rest
+        solve(opts[32], t_values[min(args.warmup, PLATE_STEPS) - 1])
     clocks = ClockSampler(gpu_index(local))
     clocks.start()
     sec32, agg32 = solve(opts[32], t_values[-1])
     clk = clocks.stop()
     x32, _ = g.get_state()
-    if world > 1:
-        import torch.distributed as tdist
-
-        tt = torch.tensor([sec32], device="cuda")
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        sec32 = float(tt.item())
-    out = {"metric": PLATES_METRIC, "value": world * n_dofs * PLATE_STEPS / sec32, "unit": "DOF load steps/s",
+    # replicas: every rank solved its own batch (seed = rank); whole-job work over the slowest rank's time
+    sec32_rank = sec32
+    (work, assembled, plates), sec32 = aggregate_ranks(
+        [n_dofs * PLATE_STEPS, n_dofs * agg32["matrix_assemblies"], args.specimens * PLATE_STEPS], sec32, "cuda")
+    out = {"metric": PLATES_METRIC, "value": work / sec32, "unit": "DOF load steps/s",
            "n_gpus": world, "steps": PLATE_STEPS, "warmup": args.warmup, "ms_per_step": 1e3 * sec32 / PLATE_STEPS,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
            "data": "synthetic",
@@ -610,8 +621,8 @@ def run_plates(args):
                       "parallelism": "replicas" if world > 1 else "single GPU"},
            "newton_iterations": agg32["newton_iterations"], "tangent_solves": agg32["matrix_assemblies"],
            "krylov_iterations": agg32["krylov_iterations"], "cutbacks": agg32["cutbacks"],
-           "assembled_dofs_per_s": world * n_dofs * agg32["matrix_assemblies"] / sec32,
-           "specimen_load_steps_per_s": world * args.specimens * PLATE_STEPS / sec32,
+           "assembled_dofs_per_s": assembled / sec32,
+           "specimen_load_steps_per_s": plates / sec32,
            "gpu_launches": int(agg32["kernel_launches"]), "clocks": clk}
     if not args.skip_fp64:
         sec64, agg64 = solve(opts[64], t_values[-1])
@@ -619,7 +630,7 @@ def run_plates(args):
         out["fp64"] = {"value": n_dofs * PLATE_STEPS / sec64, "unit": "DOF load steps/s",
                        "ms_per_step": 1e3 * sec64 / PLATE_STEPS, "newton_iterations": agg64["newton_iterations"],
                        "krylov_iterations": agg64["krylov_iterations"], "cutbacks": agg64["cutbacks"],
-                       "speedup_mixed_vs_fp64": sec64 / sec32,
+                       "speedup_mixed_vs_fp64": sec64 / sec32_rank,
                        "max_rel_displacement_difference_mixed_vs_fp64": float(
                            np.abs(x32 - x64).max() / max(np.abs(x64).max(), 1e-300))}
     if rank == 0 and world == 1 and not args.skip_cpu:
