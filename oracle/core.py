@@ -110,6 +110,8 @@ def lib():
                 "oracle_cell_dofs": (None, [vp, i, P(ll)]),
                 "oracle_cell_integrate": (None, [vp, i, P(d), P(d), P(d)]),
                 "oracle_cell_volume": (d, [vp, i]),
+                "oracle_problem_set_e_scale": (None, [vp, P(d)]),
+                "oracle_cell_adjoint": (i, [vp, i, P(d), P(d), P(d), P(d)]),
                 "oracle_quadrature": (None, [i, i, P(d), P(d)]),
                 "oracle_shape": (None, [i, P(d), P(d), P(d)]),
                 "oracle_set_threads": (None, [i]),
@@ -214,6 +216,9 @@ class Mesh:
         self.L.oracle_layer_conn(self.h, layer, _ip(out))
         return out.reshape(-1, nen)
 
+    def layer_nen(self, layer):
+        return self.L.oracle_layer_nen(self.h, layer)
+
     def layer_node_coords(self, layer):
         n = self.layer_num_nodes(layer)
         out = np.empty(n * 3)
@@ -239,6 +244,7 @@ class Problem:
     def __init__(self, mesh, ips_per_dir, slots, integrand):
         self.mesh = mesh  # keep alive
         self.L = lib()
+        self.slots = [int(x) for x in slots]
         slots = np.ascontiguousarray(slots, dtype=np.int32)
         self.integrand = integrand
         self.h = self.L.oracle_problem_create(mesh.h, ips_per_dir, len(slots), _ip(slots), ctypes.byref(integrand))
@@ -321,6 +327,27 @@ class Problem:
         Ke = np.empty(self.n_local * self.n_local)
         self.L.oracle_cell_integrate(self.h, cell, _dp(u), _dp(fe), _dp(Ke))
         return fe, Ke.reshape(self.n_local, self.n_local)
+
+    def set_e_scale(self, scale):
+        """Per-cell Young's modulus as multiples of the integrand's E (None: 1 everywhere)."""
+        if scale is None:
+            self.L.oracle_problem_set_e_scale(self.h, None)
+            return
+        self._e_scale = np.ascontiguousarray(scale, dtype=np.float64).reshape(self.n_el)
+        self.L.oracle_problem_set_e_scale(self.h, _dp(self._e_scale))
+
+    def cell_adjoint(self, cell, u):
+        """Gradient damage: (D [n_local, n_ip] = d f_cell / d omega_ip, ipd [n_ip, 5] = kappa_trial, loading flag,
+        d omega/d kappa, d omega/d kappa0, d omega/d beta; N [n_ip, n_eeq_nodes] eeq shape values)."""
+        if self.integrand.kind != GRADIENT_DAMAGE:
+            raise ValueError("adjoint data exist for gradient damage only")
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        ne = self.mesh.layer_nen(self.slots[1])
+        D = np.empty(self.n_local * self.n_ip)
+        ipd = np.empty(self.n_ip * 5)
+        N = np.empty(self.n_ip * ne)
+        self.L.oracle_cell_adjoint(self.h, cell, _dp(u), _dp(D), _dp(ipd), _dp(N))
+        return D.reshape(self.n_local, self.n_ip), ipd.reshape(self.n_ip, 5), N.reshape(self.n_ip, ne)
 
     def cell_volume(self, cell):
         return self.L.oracle_cell_volume(self.h, cell)

@@ -713,6 +713,21 @@ struct DamageExponential
             return 0.;
         return kappa0 / kappa * ((1 / kappa + beta) * alpha * std::exp(beta * (kappa0 - kappa)) + (1 - alpha) / kappa);
     }
+    // partial derivatives of Damage in the law's parameters (kappa held), from the closed form above; zero below
+    // kappa0 where the damage is identically zero (adjoint of the damage parameters only)
+    double DKappa0(double kappa) const
+    {
+        if (kappa < kappa0)
+            return 0.;
+        const double x = std::exp(beta * (kappa0 - kappa));
+        return -(1 - alpha + alpha * x) / kappa - kappa0 / kappa * alpha * beta * x;
+    }
+    double DBeta(double kappa) const
+    {
+        if (kappa < kappa0)
+            return 0.;
+        return -kappa0 / kappa * alpha * (kappa0 - kappa) * std::exp(beta * (kappa0 - kappa));
+    }
 };
 
 // NonlocalInteraction::Constant / Decreasing: nuto/mechanics/integrands/GradientDamage.h:153-184
@@ -1008,6 +1023,13 @@ struct Problem
     std::vector<int> slots; // layers in the order of the `dofs` vector, e.g. {disp, eeq}
     IntegrandParams p{};
     std::vector<double> kappa; // nEl x nIp, the public mKappas member of the integrand / evolution
+    // per-cell Young's modulus as a multiple of p.E (empty: 1 everywhere). The laws are linear in E, so the stress
+    // and its derivatives scale with it; the equivalent strain and the eeq equation do not depend on E.
+    std::vector<double> eScale;
+    double EScale(int e) const
+    {
+        return eScale.empty() ? 1. : eScale[static_cast<size_t>(e)];
+    }
     std::vector<int64_t> slotOffset; // combined global offset per slot (DofVectorConvertEigen.h:21-53)
     int64_t nDofs = 0;
     std::vector<int> localOffset; // local offset per slot inside a cell vector
@@ -1142,6 +1164,9 @@ struct Problem
                                 Ct(r, c) = dsde[r * vd + c] + dsdw[r] * dOdK * dK[c];
                     }
                 }
+                const double se = EScale(e);
+                for (int r = 0; r < vd; ++r)
+                    sigma[r] *= se;
                 if (wantF)
                     for (int j = 0; j < ndd; ++j)
                     {
@@ -1152,6 +1177,8 @@ struct Problem
                     }
                 if (wantK)
                 {
+                    for (double& v : Ct.v)
+                        v *= se;
                     const Mat K = Mul(T(Bd), Mul(Ct, Bd));
                     for (int i = 0; i < ndd; ++i)
                         for (int j = 0; j < ndd; ++j)
@@ -1175,10 +1202,13 @@ struct Problem
             const double kap = std::max(kh, eeq);
             const double omega = dmg.Damage(kap);
             const double g = inter.Factor(omega);
+            const double se = EScale(e);
             if (wantF)
             {
                 double sigma[6];
                 led.Stress(strain, omega, sigma);
+                for (int r = 0; r < vd; ++r)
+                    sigma[r] *= se;
                 for (int j = 0; j < ndd; ++j)
                 {
                     double s = 0;
@@ -1203,6 +1233,12 @@ struct Problem
                 double dsde[36], dsdw[6], dnorm[6];
                 led.DstressDstrain(strain, omega, dsde);
                 led.DstressDomega(strain, omega, dsdw);
+                for (int r = 0; r < vd; ++r)
+                {
+                    dsdw[r] *= se;
+                    for (int c = 0; c < vd; ++c)
+                        dsde[r * vd + c] *= se;
+                }
                 norm.Derivative(strain, dnorm);
                 Mat Cw(vd, vd);
                 for (int r = 0; r < vd; ++r)
@@ -1295,6 +1331,85 @@ struct Problem
                     kh = std::max(norm.Value(strain), kh);
                 }
             }
+        }
+    }
+
+    //! Adjoint ingredients of cell e at the state u (gradient damage only), with the history kappa_h of the step:
+    //! D (nLocal x nIp, row-major): column ip is d f_e / d omega_ip, the derivative of the cell vector with respect
+    //!   to the damage at integration point ip with everything else held (displacement rows B^T dsigma/domega w detJ,
+    //!   eeq rows Be^T c g'(omega) grad eeq w detJ);
+    //! ipd (nIp x 5): kappa_trial = max(kappa_h, eeq), loading flag [eeq >= kappa_h], d omega/d kappa,
+    //!   d omega/d kappa0, d omega/d beta at kappa_trial;
+    //! N (nIp x ne): the eeq shape values (d eeq_ip / d eeq nodal values).
+    void AdjointCell(int e, const double* u, double* D, double* ipd, double* Nout) const
+    {
+        const Mesh& m = *mesh;
+        const int dim = m.dim;
+        const int vd = VoigtDim(dim);
+        double X[60];
+        m.ElementCoords(e, X);
+        std::vector<int64_t> dofs;
+        CellDofs(e, dofs);
+        const DofLayer& Ld = m.layers[slots[0]];
+        const DofLayer& Le = m.layers[slots[1]];
+        const int nd = Ld.nEn, ne = Le.nEn, ndd = nd * dim;
+        const int od = localOffset[0], oe = localOffset[1];
+        const double se = EScale(e);
+        for (int i = 0; i < nLocal * q.n; ++i)
+            D[i] = 0;
+        for (int ip = 0; ip < q.n; ++ip)
+        {
+            const double* xi = q.points[ip].data();
+            double Ng[20], dNg[60];
+            Shape(m.geoInterp, xi, Ng, dNg);
+            const Jacobian jac = ComputeJacobian(dim, m.nGeoEn, X, dNg);
+            const double fac = jac.det * q.weights[ip];
+            double Nd[20], dNd[60], gd_[60];
+            Shape(Ld.interp, xi, Nd, dNd);
+            GlobalDerivatives(jac, nd, dNd, gd_);
+            const Mat Bd = BStrain(dim, nd, gd_);
+            double strain[6] = {0, 0, 0, 0, 0, 0};
+            for (int r = 0; r < vd; ++r)
+                for (int j = 0; j < ndd; ++j)
+                    strain[r] += Bd(r, j) * u[dofs[od + j]];
+            double Ne[20], dNe[60], ge[60];
+            Shape(Le.interp, xi, Ne, dNe);
+            GlobalDerivatives(jac, ne, dNe, ge);
+            const Mat Be = BGradient(dim, ne, ge);
+            double eeq = 0, geq[3] = {0, 0, 0};
+            for (int n = 0; n < ne; ++n)
+            {
+                eeq += Ne[n] * u[dofs[oe + n]];
+                for (int k = 0; k < dim; ++k)
+                    geq[k] += Be(k, n) * u[dofs[oe + n]];
+            }
+            const double kh = kappa[static_cast<size_t>(e) * q.n + ip];
+            const double kap = std::max(kh, eeq);
+            const double omega = dmg.Damage(kap);
+            double dsdw[6];
+            led.DstressDomega(strain, omega, dsdw);
+            for (int j = 0; j < ndd; ++j)
+            {
+                double v = 0;
+                for (int r = 0; r < vd; ++r)
+                    v += Bd(r, j) * dsdw[r];
+                D[static_cast<size_t>(od + j) * q.n + ip] = v * se * fac;
+            }
+            const double dg = inter.Derivative(omega);
+            for (int n = 0; n < ne; ++n)
+            {
+                double v = 0;
+                for (int k = 0; k < dim; ++k)
+                    v += Be(k, n) * geq[k];
+                D[static_cast<size_t>(oe + n) * q.n + ip] = p.c * dg * v * fac;
+                Nout[ip * ne + n] = Ne[n];
+            }
+            double* o = ipd + ip * 5;
+            o[0] = kap;
+            o[1] = eeq >= kh ? 1. : 0.;
+            o[2] = dmg.Derivative(kap);
+            o[3] = dmg.DKappa0(kap);
+            o[4] = dmg.DBeta(kap);
         }
     }
 
@@ -1398,6 +1513,8 @@ struct Problem
                     }
                 else
                     led.Stress(strain, omega, o);
+                for (int r = 0; r < vd; ++r)
+                    o[r] *= EScale(e);
                 break;
             }
         }

@@ -251,6 +251,26 @@ void oracle_cell_integrate(void* prob, int cell, const double* u, double* fe, do
         std::memcpy(Ke, res.K.data(), res.K.size() * sizeof(double));
 }
 
+//! per-cell Young's modulus as multiples of the integrand's E (null: 1 everywhere)
+void oracle_problem_set_e_scale(void* prob, const double* scale)
+{
+    auto& P = static_cast<ProblemBox*>(prob)->P;
+    if (scale)
+        P.eScale.assign(scale, scale + P.mesh->nEl);
+    else
+        P.eScale.clear();
+}
+
+//! adjoint ingredients of one gradient-damage cell (Problem::AdjointCell); returns -1 for other integrands
+int oracle_cell_adjoint(void* prob, int cell, const double* u, double* D, double* ipd, double* N)
+{
+    const auto& P = static_cast<ProblemBox*>(prob)->P;
+    if (P.p.kind != GRADIENT_DAMAGE)
+        return -1;
+    P.AdjointCell(cell, u, D, ipd, N);
+    return 0;
+}
+
 //! Cell::Integrate(ScalarFunction) with f == 1: the cell volume (test/mechanics/cell/Cell.cpp:100)
 double oracle_cell_volume(void* prob, int cell)
 {

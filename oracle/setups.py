@@ -31,12 +31,14 @@ def quad4_elastic(n, u_right=0.01):
     return m, [d], P, cons
 
 
-def hex8_gradient_damage(n, length=4.0, u_end=2e-3):
+def hex8_gradient_damage(n, length=4.0, u_end=2e-3, law=None):
     m = core.Mesh.bricks(n, n, n).scale(1.0, 1.0, length)
     d = m.add_dof(3)
     e = m.add_dof(1)
-    integ = core.Integrand.make(core.GRADIENT_DAMAGE, 3, E=30000.0, nu=0.2, damage_application=core.FULL,
-                                kappa0=1e-4, beta=100.0, alpha=0.99, k=10.0, c=0.01)
+    params = dict(E=30000.0, nu=0.2, damage_application=core.FULL, kappa0=1e-4, beta=100.0, alpha=0.99, k=10.0,
+                  c=0.01)
+    params.update(law or {})
+    integ = core.Integrand.make(core.GRADIENT_DAMAGE, 3, **params)
     P = core.Problem(m, 2, [d, e], integ)
     cons = _cat(_component(m, d, 3, m.nodes_at_axis(d, 2, 0.0), [0, 1, 2], 0.0, 0.0),
                 _component(m, d, 3, m.nodes_at_axis(d, 2, length), [2], 0.0, u_end))
@@ -54,7 +56,7 @@ def hex20_local_damage(n, u_end=3e-4):
     return m, [d], P, cons
 
 
-def notched_plate(n, depth=0.3, u_end=2e-4):
+def notched_plate(n, depth=0.3, u_end=2e-4, law=None):
     """The batched workload's specimen: UnitMeshFem::CreateQuads(n, n) without the notch cells (row n // 2, the
     first round(depth n) cells of it, clamped to 1 .. n - 2), unused coordinate nodes dropped in order; 2D
     plane-strain gradient damage; bottom edge u_y = 0, corner (0, 0) u_x = 0, top edge u_y = RhsRamp(1, u_end)."""
@@ -69,8 +71,10 @@ def notched_plate(n, depth=0.3, u_end=2e-4):
     m = core.Mesh.from_arrays(2, core.QUAD4, coords[used], remap[conn].astype(np.int32))
     d = m.add_dof(2)
     e = m.add_dof(1)
-    integ = core.Integrand.make(core.GRADIENT_DAMAGE, 2, E=30000.0, nu=0.2, plane_state=core.PLANE_STRAIN,
-                                damage_application=core.FULL, kappa0=1e-4, beta=100.0, alpha=0.99, k=10.0, c=0.01)
+    params = dict(E=30000.0, nu=0.2, plane_state=core.PLANE_STRAIN, damage_application=core.FULL, kappa0=1e-4,
+                  beta=100.0, alpha=0.99, k=10.0, c=0.01)
+    params.update(law or {})
+    integ = core.Integrand.make(core.GRADIENT_DAMAGE, 2, **params)
     P = core.Problem(m, 2, [d, e], integ)
     bottom = m.nodes_at_axis(d, 1, 0.0)
     corner = bottom[np.abs(m.layer_node_coords(d)[bottom, 0]) < 1e-10]
