@@ -469,7 +469,7 @@ def run_ours(args):
         # against the FP64 path's own 1e-8 result
         tight = fp64.get("max_rel_displacement_error_vs_fp64_1e-11", {})
         tight_l2 = fp64.get("l2_rel_displacement_error_vs_fp64_1e-11", {})
-        out["north_star"] = {
+        out["targets"] = {
             "speedup_newton_step_mixed_vs_fp64": fp64["speedup_mixed_vs_fp64_newton_step"],
             "mixed_vs_converged_fp64": {"max": tight.get("mixed"), "l2": tight_l2.get("mixed")},
             "fp64_path_vs_converged_fp64": {"max": tight.get("fp64"), "l2": tight_l2.get("fp64")},

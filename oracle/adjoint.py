@@ -1,6 +1,6 @@
 """TEST INFRASTRUCTURE ONLY — discrete adjoint of the quasistatic gradient-damage load path on the oracle.
 
-The reference has no adjoint (no counterpart in NuTo: parity unpinned); this is the checker for one, verified by
+The reference has no adjoint (no counterpart in NuTo: parity unpinned); this is the oracle for one, verified by
 central finite differences of complete oracle forward solves (tests/test_oracle_adjoint.py).
 
 Forward (QuasistaticSolver::DoStep per load step, nuto/mechanics/tools/QuasistaticSolver.cpp:116-147): step n

@@ -2,7 +2,7 @@
 //
 // CPU restatement of NuTo's element-assembly path (cell integration, integrands, constitutive laws,
 // structured meshes, first-touch DOF numbering, SimpleAssembler::BuildVector/BuildMatrix with the
-// reference's triplet + setFromTriplets assembly). It is the checker for the CUDA path and the CPU
+// reference's triplet + setFromTriplets assembly). It is the oracle for the CUDA path and the CPU
 // baseline of the benchmark; it is never linked into the product library.
 //
 // Every function cites the reference file:line it restates (paths relative to the NuTo project root).

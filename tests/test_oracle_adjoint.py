@@ -1,7 +1,7 @@
 """The oracle's discrete adjoint of the gradient-damage load path (oracle/adjoint.py) against central finite
 differences of complete forward solves: dL/dE_e (per-cell Young's modulus), dL/dkappa0 and dL/dbeta of a
 displacement misfit after load steps into the damaged regime, on a notched plate (Quad4) and a beam (Hex8). The
-reference has no adjoint; this pins the checker that a GPU adjoint is compared with."""
+reference has no adjoint; this pins the oracle that a GPU adjoint is compared with."""
 
 import numpy as np
 import pytest
