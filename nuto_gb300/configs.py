@@ -13,6 +13,11 @@ hex8_gradient_damage
 hex20_local_damage 3D Hex20 displacements (3x3x3 Gauss) on an n^3 Hex8 coordinate mesh of the unit cube,
                    MomentumBalance + LocalIsotropicDamage (E = 30000, nu = 0.2, kappa0 = 1e-4, beta = 100,
                    alpha = 0.99, k = 10); z = 0 face fixed, z = 1 face u_z = RhsRamp(1, 3e-4) (5 load steps).
+hex8_adjoint       the adjoint workload: hex8_gradient_damage on the unit cube (n^3 cells, z = 1 face u_z =
+                   RhsRamp(1, 5e-4), the beam's mean strain, 10 load steps), a per-cell lognormal Young's modulus
+                   (mean 30000, CoV 0.3, Gaussian correlation exp(-r^2 / (2 l^2)) with l = 0.1 between cell
+                   centroids, seeded), a second field of the next seed as the synthetic truth, and 256 seeded
+                   observed surface nodes (all three displacement components; the fixed z = 0 face excluded).
 notched_plate      2D plane-strain gradient-enhanced damage on the unit square, n x n Quad4 (2x2 Gauss), u (2 DOF)
                    + eeq (1 DOF), the law of hex8_gradient_damage in 2D; a notch one cell high from the left edge
                    at mid height (cells of row n/2 with x index below round(depth n) removed); bottom edge u_y = 0,
@@ -159,3 +164,52 @@ def notched_plate(n=40, depth=0.3, u_end=2e-4, load_steps=10):
                  eeq_slot=1)
     return Setup("notched_plate_%dx%d_depth%.3f" % (n, n, depth), m, [d, e], 2, integ, [cons_d, _empty()],
                  load_steps, 1.0)
+
+
+def lognormal_cell_field(n, rng, mean=30000.0, cov=0.3, corr_length=0.1):
+    """Per-cell values exp(mu + sigma g) on the n^3 cells of the unit cube (lattice order, x fastest), g a standard
+    Gaussian random field at the cell centroids with correlation exp(-|x - y|^2 / (2 l^2)); sigma^2 = ln(1 + cov^2)
+    and mu = ln(mean) - sigma^2 / 2 give the field the prescribed mean and coefficient of variation. The Gaussian
+    correlation factorises over the axes, so g = (L_z x L_y x L_x) w with L L^T the 1D correlation matrix of the
+    centroid coordinates (symmetric square root through its eigen-decomposition: the matrix is numerically
+    singular for l >> 1/n) and w white noise."""
+    g = gaussian_cell_field(n, rng, corr_length)
+    s2 = np.log1p(cov * cov)
+    return np.exp(np.log(mean) - 0.5 * s2 + np.sqrt(s2) * g).reshape(-1)
+
+
+def gaussian_cell_field(n, rng, corr_length=0.1):
+    """The standard Gaussian random field g of lognormal_cell_field, shape [z][y][x]."""
+    x = (np.arange(n) + 0.5) / n
+    C = np.exp(-((x[:, None] - x[None, :]) ** 2) / (2.0 * corr_length ** 2))
+    lam, V = np.linalg.eigh(C)
+    L = (V * np.sqrt(np.clip(lam, 0.0, None))) @ V.T
+    w = rng.standard_normal((n, n, n))  # [z][y][x]
+    return np.einsum("ck,bj,ai,kji->cba", L, L, L, w, optimize=True)
+
+
+@dataclass
+class AdjointCase:
+    setup: Setup
+    scale: np.ndarray       # per-cell E / 30000 of the field the gradient is taken at
+    true_scale: np.ndarray  # per-cell E / 30000 of the synthetic truth (the target is its response)
+    obs_nodes: np.ndarray   # observed displacement DOF nodes
+    obs_dofs: np.ndarray    # their combined DOF indices, three per node
+
+
+def hex8_adjoint(n=32, seed=0, n_obs=256, load_steps=10, u_end=5e-4):
+    s = hex8_gradient_damage(n, length=1.0, u_end=u_end, load_steps=load_steps)
+    s.name = "hex8_adjoint_%d^3_seed%d" % (n, seed)
+    rng = np.random.default_rng(seed)
+    E0 = s.integrand["E"]
+    scale = lognormal_cell_field(n, rng) / E0
+    true_scale = lognormal_cell_field(n, np.random.default_rng(seed + 1)) / E0
+    L = s.mesh.layers[s.layers[0]]
+    xyz = L.node_coords
+    on_surface = np.any((np.abs(xyz) < 1e-10) | (np.abs(xyz - 1.0) < 1e-10), axis=1)
+    candidates = np.flatnonzero(on_surface & (np.abs(xyz[:, 2]) >= 1e-10))
+    if n_obs > candidates.size:
+        raise ValueError("only %d observable surface nodes" % candidates.size)
+    nodes = np.sort(rng.choice(candidates, size=n_obs, replace=False))
+    dofs = L.dof_numbers[nodes].reshape(-1).astype(np.int64)
+    return AdjointCase(s, scale, true_scale, nodes, dofs)

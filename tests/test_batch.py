@@ -114,3 +114,4 @@ def test_plates_cpu_sample_counts_work():
     sec, work, count, its = bench.plates_cpu_sample(ns, depths, 1, budget_s=0.0)
     _, _, P, _ = osetups.notched_plate(5, 0.25)
     assert count == 1 and work == P.n_dofs * bench.PLATE_STEPS and sec > 0 and its > 0
+

@@ -31,6 +31,55 @@ def _loss(build, t_values, law, scale, obs, target, adjoint=False):
     return L, A.gradient(r, E0 * scale), P
 
 
+def test_adjoint_workload_small_case_matches_central_differences():
+    """The adjoint workload's set-up (hex8_adjoint: unit cube, lognormal modulus field, truth field of the next
+    seed, observed surface nodes, 10 load steps) at 2^3 cells: the oracle's adjoint against central differences in
+    kappa0, beta and the modulus of two cells, for the summed squared misfit against the truth's response."""
+    from nuto_gb300 import configs
+
+    case = configs.hex8_adjoint(2, seed=5, n_obs=6)
+    t_values = []
+    t = 0.0
+    for _ in range(case.setup.load_steps):
+        t += 1.0 / case.setup.load_steps
+        t_values.append(t)
+
+    def build(law):
+        return osetups.hex8_gradient_damage(2, length=1.0, u_end=5e-4, law=law)
+
+    obs = case.obs_dofs
+    _, _, Pt, ct = build(None)
+    Pt.set_e_scale(case.true_scale)
+    target = AdjointOracle(Pt, ct[0], ct[1], ct[2]).forward(t_values)[obs]
+
+    def loss(law, scale, adjoint=False):
+        _, _, P, cons = build(law)
+        P.set_e_scale(scale)
+        A = AdjointOracle(P, cons[0], cons[1], cons[2])
+        u = A.forward(t_values)
+        r = np.zeros_like(u)
+        r[obs] = u[obs] - target
+        L = float(r[obs] @ r[obs])  # sum of squared misfits
+        return (L, A.gradient(2.0 * r, E0 * scale), P) if adjoint else L
+
+    base = {"kappa0": 1e-4, "beta": 100.0}
+    L, g, P = loss(base, case.scale, adjoint=True)
+    assert P.kappa.max() > 2e-4 and L > 0
+    for name in ("kappa0", "beta"):
+        h = 1e-4 * base[name]
+        up, dn = dict(base), dict(base)
+        up[name] += h
+        dn[name] -= h
+        ref = (loss(up, case.scale) - loss(dn, case.scale)) / (2 * h)
+        assert abs(g[name] - ref) <= 1e-5 * abs(ref), (name, g[name], ref)
+    for c in (0, 5):
+        sp, sm = case.scale.copy(), case.scale.copy()
+        sp[c] += 1e-6
+        sm[c] -= 1e-6
+        ref = (loss(base, sp) - loss(base, sm)) / 2e-6 / E0
+        assert abs(g["E"][c] - ref) <= 1e-5 * abs(ref), (c, g["E"][c], ref)
+
+
 @pytest.mark.parametrize("kind", ["plate", "beam"])
 def test_adjoint_matches_central_differences(kind):
     build, t_values = _case(kind)
