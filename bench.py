@@ -455,7 +455,8 @@ def run_ours(args):
                                    "test; the iterations with |C^T r| < %g tol assemble the FP64 tangent and refine "
                                    "the FP32 solves against it" % EXACT_BELOW,
                       "newton_tolerance": "|C^T r| <= 1e-8 |C^T (r + K db)| of the load step",
-                      "krylov_rtol": KRYLOV_RTOL, "l2": "inputs larger than L2 (FP32 tangent %.0f MB)" % (nnz * 4 / 1e6),
+                      "krylov_rtol": KRYLOV_RTOL,
+                      "l2": "inputs larger than L2 (FP32 tangent %.0f MB)" % (nnz * 4 / 1e6),
                       "parallelism": "replicas" if world > 1 else "single GPU"},
            "newton_step_ms": 1e3 * sec32 / max(agg32["matrix_assemblies"], 1),
            "newton_iterations": agg32["newton_iterations"], "tangent_solves": agg32["matrix_assemblies"],

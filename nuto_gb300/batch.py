@@ -1,12 +1,13 @@
 """Batched independent specimens: many small problems of uneven size assembled and solved as one system.
 
-A batch concatenates the specimens' meshes (cells of specimen 0 first, then specimen 1, ...; coordinate nodes
-offset likewise; each specimen translated to its own place on a grid so that no two specimens touch, because
-NuTo's AddDofInterpolation merges DOF nodes at equal coordinates) into one cell group, so every kernel of the path -- residual, tangent, history, the Krylov
-solver and its multigrid -- runs once over all cells and DOFs of the batch per launch. The work unit of every
-launch is the cell (or the node row), not the specimen, so specimens of uneven size need no load balancing: a
-plate of 120 x 120 cells and one of 20 x 20 are the same stream of cells. The matrix is block diagonal with one
-block per specimen; the multigrid's aggregates never cross a specimen because no matrix entry does.
+A batch concatenates the specimens' meshes into one cell group: cells of specimen 0 first, then specimen 1, ...;
+coordinate nodes offset likewise, and each specimen translated to its own place on a grid so that no two specimens
+touch (NuTo's AddDofInterpolation merges DOF nodes at equal coordinates). Every kernel of the path -- residual,
+tangent, history, the Krylov solver and its multigrid -- then runs once over all cells and DOFs of the batch per
+launch. The work unit of every launch is the cell (or the node row), not the specimen, so specimens of uneven size
+need no load balancing: a plate of 120 x 120 cells and one of 20 x 20 are the same stream of cells. The matrix is
+block diagonal with one block per specimen; the multigrid's aggregates never cross a specimen because no matrix
+entry does.
 
 Equivalence to solving each specimen alone (what NuTo's QuasistaticSolver does per problem,
 nuto/mechanics/tools/QuasistaticSolver.cpp:51-147):

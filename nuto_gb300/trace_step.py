@@ -78,9 +78,10 @@ def main():
     busy = sum(e["dur"] for e in ks)
     span = ks[-1]["ts"] + ks[-1]["dur"] - ks[0]["ts"]
     gaps = [ks[i + 1]["ts"] - ks[i]["ts"] - ks[i]["dur"] for i in range(len(ks) - 1)]
-    print("size %d, load step %d: %d Newton iterations, %d Krylov iterations, %d tangent assemblies, %d kernel launches "
-          "(%d device operations recorded)" % (a.size, a.warmup + 1, st["newton_iterations"], st["krylov_iterations"],
-                                             st["matrix_assemblies"], st["kernel_launches"], len(ks)))
+    print("size %d, load step %d: %d Newton iterations, %d Krylov iterations, %d tangent assemblies, "
+          "%d kernel launches (%d device operations recorded)"
+          % (a.size, a.warmup + 1, st["newton_iterations"], st["krylov_iterations"], st["matrix_assemblies"],
+             st["kernel_launches"], len(ks)))
     print("wall %.1f ms, GPU span %.1f ms, GPU busy %.1f ms, %d operations, gaps %.1f ms (median %.2f us)" %
           (1e3 * (t1 - t0), span / 1e3, busy / 1e3, len(ks), sum(x for x in gaps if x > 0) / 1e3,
            float(np.median([x for x in gaps if x > 0]))))
