@@ -1,19 +1,22 @@
-"""Benchmark: quasistatic load steps of the 3D implicit gradient-damage beam (Hex8, 64^3 cells, 1.1 M DOFs) on GB300.
+"""Benchmark: element assembly and quasistatic Newton solve of the 3D implicit gradient-damage beam (Hex8, 64^3 cells,
+1.1 M DOFs) on GB300.
 
-A step is one load step of the 20-step schedule to u_z = 2e-3 m (QuasistaticSolver::DoStep: trial state, Newton
-with line search to |C^T r| <= 1e-8 |C^T (r + K db)|, history update), run through the C ABI with the state and
-history resident in HBM. W warm-up load steps from rest come first, then exactly K timed load steps.
-
-value      DOFs x tangent solves / s of the mixed-precision path (FP32 tangent + FP32 GMRES, FP64 residual): the
-           assembled-and-solved DOFs per second; ms_per_step is the time of one load step and newton_step_ms the
-           time of one tangent assembly + Krylov solve + residual update.
-fp64       the same K load steps on the plain FP64 GPU path, from the same warm state, and the speed-up.
-e2e        the same metric through nuto_gpu_do_step_host with the state vector and history in pinned host memory
-           (copied in and out every step).
-roofline   the Krylov SpMV (dominant kernel): algorithmic bytes per launch / mean CUDA-event duration.
+Headline (value, --steps / --warmup): a step is one assembly pass of the beam's Newton iteration, the FP32 tangent
+(SimpleAssembler::BuildMatrix of GradientDamage::Hessian0) and the FP64 internal-force residual (BuildVector of
+GradientDamage::Gradient), at a seeded damaged state (loading, unloading, damaged and undamaged integration points
+mixed); state, history and the CSR values resident in HBM. value = DOFs x assembly passes / s ("assembled DOFs/s").
+e2e        the same passes through the C ABI with host buffers: the state copied in from pinned host memory, the
+           tangent's CSR values and the residual copied back to pinned host memory, every step.
+roofline   the FP32 tangent kernel(s) of the pass: algorithmic bytes per assembly / mean CUDA-event duration.
 cpu_baseline / --impl reference
-           the oracle (CPU restatement of NuTo's assembly, OpenMP) plus scipy SuperLU as the stand-in for
-           Eigen::SparseLU, timed on a bounded sample of the same problem on the host cores.
+           the oracle (the CPU restatement of NuTo's OpenMP SimpleAssembler with the same integrand and laws) doing
+           the same passes on the same 64^3 beam at the same state, on the host cores.
+newton     the benchmark spec's targets on the full load schedule: the 20 load steps to u_z = 2e-3 m from rest
+           (QuasistaticSolver::DoStep each: trial state, Newton with line search to |C^T r| <= 1e-8 |C^T (r + K db)|,
+           history update) once on the mixed-precision path (FP32 tangent, FP32 GMRES + multigrid, FP64 residual and
+           history) and once on the plain FP64 GPU path, Newton-step times, the phase split, and both final states
+           against an FP64 solution of the same schedule converged to 1e-11; plus the mixed schedule end to end
+           through nuto_gpu_do_step_host.
 
 --workload plates  (not the headline) the batched workload instead: --specimens seeded notched plates (2D
            gradient damage, side 20..120 cells) solved as one system through their 10 load steps; value = DOFs x
@@ -43,6 +46,10 @@ KRYLOV_RTOL = 1e-3
 # FP32 solves against it (exact Jacobian for the last steps; the relative displacement error against the converged
 # FP64 solution then stays below 1e-6, with the FP32 tangent alone it is about 1e-5 on the damaged beam)
 EXACT_BELOW = 1.0e4
+# forcing-term floor of both paths' Newton loops: the last linear solve of a load step leaves a linear residual of
+# about FORCING_FLOOR x the Newton tolerance, so the converged state sits that far below the 1e-8 test
+FORCING_FLOOR = 0.05
+TANGENT_KERNEL = "k_tangent_fused<3,8,8,GD> (FP32 tangent: geometry and law per node warp, rows written once)"
 
 
 def parse():
@@ -54,6 +61,7 @@ def parse():
     p.add_argument("--size", type=int, default=64)
     p.add_argument("--skip-fp64", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
+    p.add_argument("--skip-newton", action="store_true")
     p.add_argument("--workload", default="beam", choices=["beam", "plates"])
     p.add_argument("--specimens", type=int, default=128)
     return p.parse_args()
@@ -158,6 +166,15 @@ def tangent_bytes(setup, nnz, value_bytes):
     return nnz * value_bytes + conn + m.coords.size * 8 + setup.n_dofs * 8 + m.num_cells * n_ip * 8
 
 
+def residual_bytes(setup):
+    """Compulsory traffic of one FP64 residual: the vector written once, connectivity, coordinates, DOF values and
+    history read once."""
+    m = setup.mesh
+    conn = sum(m.layers[l].conn.size for l in setup.layers) * 4 + m.conn.size * 4
+    n_ip = setup.gauss ** m.dim
+    return setup.n_dofs * 8 + conn + m.coords.size * 8 + setup.n_dofs * 8 + m.num_cells * n_ip * 8
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -189,14 +206,17 @@ def accumulate(t0, dt, k):
 def run_steps(g, opts, t_start, t_values):
     """Advances the load from t_start through every t in t_values with AdaptiveSolve (time step 1/LOAD_STEPS, cut
     back by halves on NoConvergence as the reference's AdaptiveSolve does). Returns the summed step statistics,
-    failed attempts included (their work was done), and the number of cut-backs."""
+    failed attempts included (their work was done), the number of cut-backs and the per-load-step Newton counts."""
     from nuto_gb300.adaptive import AdaptiveSolve
 
     dt = 1.0 / LOAD_STEPS
     ad = AdaptiveSolve(g, opts, dt=dt, dt_max=dt, dt_min=dt / 256)
     t = t_start
+    per_step = []
     for tv in t_values:
+        n0 = len(ad.stats)
         ad.solve(tv, t)
+        per_step.append(sum(st["newton_iterations"] for st in ad.stats[n0:]))
         t = tv
     agg = {k: 0 for k in AGG_KEYS}
     for st in ad.stats:
@@ -204,50 +224,78 @@ def run_steps(g, opts, t_start, t_values):
             agg[k] += st[k]
     agg["cutbacks"] = ad.cutbacks
     agg["do_steps"] = len(ad.stats)
+    agg["newton_per_load_step"] = per_step
     return agg
 
 
-def cpu_sample(n_s, threads):
-    """One Newton iteration of the oracle (BuildMatrix + BuildVector + SuperLU solve of C^T K C) on an n_s^3 beam of
-    the same problem, after two elastic load steps. Returns (seconds, n_dofs)."""
-    import scipy.sparse.linalg as spla
+# the seeded state of the assembly passes: the beam's uniaxial field at load factor 0.5 (u_z = eps z, lateral
+# contraction -nu eps (x - 1/2), eps = 0.5 * 2e-3 / 4) with every displacement perturbed by up to +-20 % of eps times
+# the cell size, nodal eeq ~ U(0, 4e-4) and history kappa ~ U(0, 4e-4) per integration point: loading and unloading
+# points, damaged (kappa >= kappa0 = 1e-4) and undamaged ones, all mixed
+STATE_SEED = 0
+STATE_EPS = 0.5 * 2e-3 / 4.0
 
+
+def beam_state(u_coords, u_dofs, e_dofs, n_dofs, n_cells, n_ip, n, seed=STATE_SEED):
+    """(state vector, kappa[cell, ip]) of the assembly passes from plain arrays: displacement node coordinates and DOF
+    numbers (n_nodes x 3), eeq DOF numbers (n_nodes), the problem's size. Both arms call it with the arrays of their
+    own set-up (the DOF numbering is the same, bit for bit)."""
+    rng = np.random.default_rng(seed)
+    x = np.zeros(n_dofs)
+    h = 1.0 / n
+    eps = STATE_EPS
+    field = np.stack([-0.2 * eps * (u_coords[:, 0] - 0.5), -0.2 * eps * (u_coords[:, 1] - 0.5),
+                      eps * u_coords[:, 2]], axis=1)
+    field += rng.uniform(-0.2, 0.2, field.shape) * eps * h
+    x[np.asarray(u_dofs).reshape(-1)] = field.reshape(-1)
+    x[np.asarray(e_dofs).reshape(-1)] = rng.uniform(0.0, 4e-4, np.asarray(e_dofs).size)
+    kappa = rng.uniform(0.0, 4e-4, (n_cells, n_ip))
+    return x, kappa
+
+
+def oracle_beam(n):
+    """The oracle's 64^3 beam (or n^3) and its assembly-pass state."""
     from oracle import setups
-    from oracle.core import lib
-    from oracle.quasistatic import QuasistaticOracle
 
-    lib().oracle_set_threads(threads)
-    om, layers, P, cons = setups.hex8_gradient_damage(n_s)
-    Q = QuasistaticOracle(P, cons[0], cons[1], cons[2], tolerance=1e-10, max_iterations=20)
-    x = np.zeros(P.n_dofs)
+    om, layers, P, cons = setups.hex8_gradient_damage(n)
+    d, e = layers
+    x, kappa = beam_state(om.layer_node_coords(d), om.layer_dof_numbers(d, 3), om.layer_dof_numbers(e, 1), P.n_dofs,
+                          P.n_el, P.n_ip, n)
+    P.kappa = kappa
+    return P, x
+
+
+def oracle_pass(P, x):
+    """One assembly pass of the oracle: BuildMatrix (triplets per thread, sorted and summed into the combined CSC
+    matrix, released) and BuildVector. Returns (seconds of the matrix, seconds of the vector); oracle_pass.nnz holds
+    the matrix's nonzeros."""
+    from oracle.core import _dp
+
+    xa = np.ascontiguousarray(x)
     t0 = time.perf_counter()
-    K = Q.derivative(x)
-    r = Q.residual(x)
+    nnz = P.L.oracle_build_matrix(P.h, _dp(xa))
+    P.L.oracle_matrix_release(P.h)
     t1 = time.perf_counter()
-    db = Q.global_rhs(1.0 / LOAD_STEPS) - Q.global_rhs(0.0)
-    rhs = r + K @ db
-    Kr = K[Q.indep][:, Q.indep].tocsc()
-    spla.spsolve(Kr, rhs[Q.indep])
+    P.build_vector(xa)
     t2 = time.perf_counter()
-    cpu_sample.last = (t1 - t0, t2 - t1)
-    return t2 - t0, P.n_dofs
+    oracle_pass.nnz = int(nnz)
+    return t1 - t0, t2 - t1
 
 
-def cpu_baseline(steps=1, n_s=16):
+def cpu_baseline(n):
+    """One oracle assembly pass of the same n^3 beam at the same state on all host threads (the bounded CPU sample
+    of the headline workload)."""
     from oracle.core import lib
 
     threads = lib().oracle_max_threads()
-    times = []
-    for _ in range(steps):
-        dt, n = cpu_sample(n_s, threads)
-        times.append(dt)
-    t = float(np.median(times))
-    return {"value": n / t, "unit": "DOF/s", "cores": threads, "kind": "port",
-            "sample": "one Newton iteration (oracle BuildMatrix + BuildVector with OpenMP, SuperLU solve of C^T K C) "
-                      "of the same gradient-damage beam at %d^3 cells (%d DOFs); %.2f s, of which assembly %.2f s "
-                      "and SuperLU %.2f s" % (n_s, n, t, cpu_sample.last[0], cpu_sample.last[1]),
-            "assembly_dofs_per_s": n / cpu_sample.last[0],
-            "ms_per_newton_step": 1e3 * t}
+    lib().oracle_set_threads(threads)
+    P, x = oracle_beam(n)
+    tm, tv = oracle_pass(P, x)
+    t = tm + tv
+    return {"value": P.n_dofs / t, "unit": "DOF/s", "cores": threads, "kind": "port",
+            "sample": "one assembly pass (oracle BuildMatrix with OpenMP + sorted triplets into CSC, BuildVector) "
+                      "of the same %d^3 beam at the same state: %.2f s (matrix %.2f s, vector %.2f s)"
+                      % (n, t, tm, tv)}
 
 
 def run_reference(args):
@@ -260,26 +308,155 @@ def run_reference(args):
     if args.workload == "plates":
         run_reference_plates(args)
         return
-    for _ in range(args.warmup):
-        cpu_sample(16, oracle.lib().oracle_max_threads())
-    times = []
-    n = None
+    threads = oracle.lib().oracle_max_threads()
+    oracle.lib().oracle_set_threads(threads)
+    P, x = oracle_beam(args.size)
+    # a CPU pass has nothing to warm up but page faults: one warm-up pass whatever --warmup asks for
+    for _ in range(min(args.warmup, 1)):
+        oracle_pass(P, x)
+    tm = tv = 0.0
     for _ in range(args.steps):
-        dt, n = cpu_sample(16, oracle.lib().oracle_max_threads())
-        times.append(dt)
-    total = float(sum(times))
-    value = n * args.steps / total
-    cores = oracle.lib().oracle_max_threads()
+        a, b = oracle_pass(P, x)
+        tm, tv = tm + a, tv + b
+    total = tm + tv
+    value = P.n_dofs * args.steps / total
     out = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-           "config": {"workload": "hex8_gradient_damage beam 1x1x4, 16^3 cells sample of the 64^3 workload",
-                      "n_dofs": n, "parallelism": "host OpenMP"},
-           "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": cores, "kind": "port",
-                            "sample": "one Newton iteration per step (oracle assembly + SuperLU) on a 16^3 cell "
-                                      "sample; the reference itself cannot be built (Eigen/Boost absent)"},
+           "config": beam_config(args.size, P.n_dofs, oracle_pass.nnz),
+           "precision": "FP64 tangent and residual",
+           "ms_matrix_per_step": 1e3 * tm / args.steps, "ms_vector_per_step": 1e3 * tv / args.steps,
+           "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": threads, "kind": "port",
+                            "sample": "%d assembly passes of the %d^3 beam (oracle BuildMatrix + BuildVector, OpenMP "
+                                      "over %d threads); the reference itself cannot be built here (Eigen/Boost "
+                                      "absent)" % (args.steps, args.size, threads)},
            "e2e": {"value": value, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
+
+
+def beam_config(n, n_dofs, nnz, world=1):
+    """The headline workload, the same dictionary in both arms."""
+    return {"workload": "hex8_gradient_damage_%d^3 assembly pass: Hex8 2x2x2 Gauss, beam 1x1x4 m, u + eeq, "
+                        "GradientDamage(c=0.01, LinearElasticDamage(30000, 0.2, FULL), DamageLawExponential(1e-4, 100, "
+                        "0.99), ModifiedMises(k=10)); one step = BuildMatrix (tangent, Hessian0) + BuildVector "
+                        "(residual, Gradient) at the seeded state (uniaxial field at t = 0.5 perturbed +-20 %%, eeq "
+                        "and kappa ~ U(0, 4e-4), seed %d)" % (n, STATE_SEED),
+            "n_dofs": int(n_dofs), "nnz": int(nnz),
+            "l2": "inputs larger than L2 (the tangent's %.0f MB of FP32 values are written every step)" % (nnz * 4 / 1e6),
+            "parallelism": "replicas" if world > 1 else "none"}
+
+
+def run_newton(args, s, g, barrier):
+    """The benchmark spec's targets on the beam's full load schedule: the LOAD_STEPS load steps from rest to t = 1
+    (u_z = 2e-3 m) on the mixed-precision path and on the plain FP64 path, each timed with CUDA events; both final
+    states against an FP64 solution of the same schedule converged to 1e-11 (untimed); and the mixed schedule end
+    to end through nuto_gpu_do_step_host with the state and history in pinned host memory."""
+    import torch
+
+    import nuto_gb300
+
+    n_dofs = g.n_dofs
+    t_values = accumulate(0.0, 1.0 / LOAD_STEPS, LOAD_STEPS)
+    common = dict(newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20, max_krylov=20000,
+                  forcing_floor=FORCING_FLOOR)
+    opts32 = g.default_options(precision=nuto_gb300.FP32, exact_tangent_below=EXACT_BELOW, **common)
+    opts64 = g.default_options(precision=nuto_gb300.FP64, **common)
+
+    def schedule(opts):
+        g.set_state(None, 0.0, True)
+        g.history = s.history0
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        agg = run_steps(g, opts, 0.0, t_values)
+        e1.record()
+        barrier()
+        x, _ = g.get_state()
+        return e0.elapsed_time(e1) / 1e3, agg, x
+
+    def summary(sec, agg):
+        na = max(agg["matrix_assemblies"], 1)
+        return {"seconds": sec, "newton_step_ms": 1e3 * sec / na, "load_step_ms": 1e3 * sec / LOAD_STEPS,
+                "tangent_solves": agg["matrix_assemblies"], "newton_iterations": agg["newton_iterations"],
+                "newton_per_load_step": agg["newton_per_load_step"], "krylov_iterations": agg["krylov_iterations"],
+                "cutbacks": agg["cutbacks"], "residual_evaluations": agg["residual_evaluations"],
+                "kernel_launches": agg["kernel_launches"],
+                "launches_per_krylov_iteration": agg["kernel_launches"] / max(agg["krylov_iterations"], 1),
+                # where a Newton step's time goes (CUDA events around the phases, summed over the schedule)
+                "ms_per_newton_step": {"tangent": agg["ms_assemble_matrix"] / na,
+                                       "residual": agg["ms_assemble_vector"] / na,
+                                       "krylov": agg["ms_krylov"] / na,
+                                       "krylov_spmv": agg["ms_spmv"] / na},
+                "spmv_launches": agg["spmv_launches"],
+                "spmv_mean_us": 1e3 * agg["ms_spmv"] / max(agg["spmv_launches"], 1)}
+
+    sec32, agg32, x32 = schedule(opts32)
+    out = {"schedule": "%d load steps from rest to t = 1 (u_z = 2e-3 m), AdaptiveSolve cut-back, Newton |C^T r| <= "
+                       "1e-8 |C^T (r + K db)| per load step, Eisenstat-Walker forcing with floor %g"
+                       % (LOAD_STEPS, FORCING_FLOOR),
+           "mixed": summary(sec32, agg32)}
+    out["mixed"]["path"] = ("FP32 tangent (k_tangent_fused), FP32 GMRES(80) with the FP32 "
+                            "multigrid, FP64 residual, history, Newton test and refinement residual; iterations "
+                            "with |C^T r| < %g tol use the FP64-accurate tangent (k_tangent, FP64 law, double-float "
+                            "products) for the refinement" % EXACT_BELOW)
+    if not args.skip_fp64:
+        sec64, agg64, x64 = schedule(opts64)
+        out["fp64"] = summary(sec64, agg64)
+        out["fp64"]["path"] = ("FP64 tangent (k_tangent element kernel with FP64 atomics), FP64 GMRES(80) with the "
+                               "FP64 multigrid, FP64 residual and history")
+        opts_t = g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-11, krylov_rtol=1e-6, max_newton=40,
+                                   max_krylov=20000)
+        try:
+            _, _, xt = schedule(opts_t)
+        except Exception as exc:  # the converged solution is a diagnostic only
+            xt = None
+            out["converged_fp64_error"] = str(exc)
+
+        def rel(a, b):
+            return {"max": float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)),
+                    "l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))}
+
+        t = {"speedup_newton_step_mixed_vs_fp64": out["fp64"]["newton_step_ms"] / out["mixed"]["newton_step_ms"],
+             "speedup_schedule_mixed_vs_fp64": sec64 / sec32,
+             "mixed_vs_fp64_path": rel(x32, x64)}
+        if xt is not None:
+            t["mixed_vs_converged_fp64"] = rel(x32, xt)
+            t["fp64_path_vs_converged_fp64"] = rel(x64, xt)
+        out["targets"] = t
+
+    # the mixed schedule end to end: state and history uploaded from pinned host memory and downloaded every step
+    n_hist = s.mesh.num_cells * g.n_ip
+    xa = torch.zeros(n_dofs, dtype=torch.float64, pin_memory=True)
+    xb = torch.empty(n_dofs, dtype=torch.float64, pin_memory=True)
+    ka = torch.empty(n_hist, dtype=torch.float64, pin_memory=True)
+    kb = torch.empty(n_hist, dtype=torch.float64, pin_memory=True)
+    ka.numpy()[:] = s.history0.ravel()
+    g.set_state(None, 0.0, False)
+    barrier()
+    h0 = time.perf_counter()
+    assemblies, t, dt = 0, 0.0, 1.0 / LOAD_STEPS
+    step = dt
+    for tv in t_values:
+        while t < tv - 1e-14:  # AdaptiveSolve's cut-back on the host-buffer entry point
+            tn = min(tv, t + step)
+            try:
+                g.do_step_host(tn, xa, ka, xb, kb, opts32)
+            except nuto_gb300.NoConvergence:
+                assemblies += g.stats()["matrix_assemblies"]
+                step *= 0.5
+                continue
+            assemblies += g.stats()["matrix_assemblies"]
+            xa, xb = xb, xa
+            ka, kb = kb, ka
+            t = tn
+            step = min(dt, step * 1.5) if g.stats()["newton_iterations"] < 3 else step
+    barrier()
+    sec_e2e = time.perf_counter() - h0
+    out["mixed_e2e"] = {"seconds": sec_e2e, "newton_step_ms": 1e3 * sec_e2e / max(assemblies, 1),
+                        "h2d_bytes_per_load_step": int((n_dofs + n_hist) * 8),
+                        "d2h_bytes_per_load_step": int((n_dofs + n_hist) * 8)}
+    return out
 
 
 def run_ours(args):
@@ -298,19 +475,7 @@ def run_ours(args):
     s = configs.hex8_gradient_damage(args.size, load_steps=LOAD_STEPS, imperfection=True)
     g = s.build_gpu(device=local)
     n_dofs, nnz = g.n_dofs, g.nnz
-    opts32 = g.default_options(precision=nuto_gb300.FP32, newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20,
-                               max_krylov=20000, exact_tangent_below=EXACT_BELOW)
-    opts64 = g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20,
-                               max_krylov=20000)
-    dt = 1.0 / LOAD_STEPS
-    g.set_state(None, 0.0, True)
-    g.history = s.history0
-    # load-step end times by accumulation, as AdaptiveSolve advances the time (t += dt), so that every step ends
-    # exactly on its end time (k * dt can differ from the accumulated sum in the last bit)
-    run_steps(g, opts32, 0.0, accumulate(0.0, dt, args.warmup))
-    x_w, t_w = g.get_state()
-    kappa_w = g.history
-    t_values = accumulate(t_w, dt, args.steps)
+    Ld, Le = s.mesh.layers[s.layers[0]], s.mesh.layers[s.layers[1]]
 
     def barrier():
         if world > 1:
@@ -319,166 +484,92 @@ def run_ours(args):
             tdist.barrier()
         torch.cuda.synchronize()
 
-    def timed(opts):
-        g.set_state(x_w, t_w, False)
-        g.history = kappa_w
-        barrier()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        agg = run_steps(g, opts, t_w, t_values)
-        e1.record()
-        barrier()
-        return e0.elapsed_time(e1) / 1e3, agg
-
+    # ---- headline: assembly passes at the seeded state, everything resident in HBM ----------------------------
+    x_h, kappa_h = beam_state(Ld.node_coords, Ld.dof_numbers, Le.dof_numbers, n_dofs, s.mesh.num_cells, g.n_ip,
+                              args.size)
+    g.history = kappa_h
+    u = torch.as_tensor(x_h, device="cuda")
+    k32 = torch.empty(nnz, dtype=torch.float32, device="cuda")
+    f = torch.empty(n_dofs, dtype=torch.float64, device="cuda")
+    for _ in range(args.warmup):
+        g.build_matrix(u, nuto_gb300.FP32, out=k32)
+        g.build_vector(u, out=f)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = g.stats()["kernel_launches"]
     clocks = ClockSampler(gpu_index(local))
     clocks.start()
-    sec32, agg32 = timed(opts32)
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for a, b, c in ev:  # the library runs on torch's current stream: the events bracket its kernels
+        a.record()
+        g.build_matrix(u, nuto_gb300.FP32, out=k32)
+        b.record()
+        g.build_vector(u, out=f)
+        c.record()
+    e1.record()
+    barrier()
     clk = clocks.stop()
-    x32, _ = g.get_state()
-    sec32_rank = sec32  # this rank's own time, for the ratios to this rank's FP64 run
-    (work,), sec32 = aggregate_ranks([n_dofs * agg32["matrix_assemblies"]], sec32, "cuda")
-    value = work / sec32
+    launches = g.stats()["kernel_launches"] - launches0
+    sec = e0.elapsed_time(e1) / 1e3
+    ms_matrix = [a.elapsed_time(b) for a, b, _ in ev]
+    ms_vector = [b.elapsed_time(c) for _, b, c in ev]
+    (work,), sec = aggregate_ranks([n_dofs * args.steps], sec, "cuda")
+    value = work / sec
+    fp32_check = float(k32.abs().max().item())  # touches the result (non-finite values would show here)
 
-    fp64 = None
-    if not args.skip_fp64:
-        sec64, agg64 = timed(opts64)
-        x64, _ = g.get_state()
-        err = float(np.abs(x32 - x64).max() / max(np.abs(x64).max(), 1e-300))
-        err_l2 = float(np.linalg.norm(x32 - x64) / max(np.linalg.norm(x64), 1e-300))
-        fp64 = {"value": n_dofs * agg64["matrix_assemblies"] / sec64, "unit": "DOF/s",
-                "ms_per_step": 1e3 * sec64 / args.steps,
-                "newton_step_ms": 1e3 * sec64 / max(agg64["matrix_assemblies"], 1),
-                "newton_iterations": agg64["newton_iterations"], "krylov_iterations": agg64["krylov_iterations"],
-                "ms_assemble_matrix_per_launch": agg64["ms_assemble_matrix"] / max(agg64["matrix_assemblies"], 1),
-                "speedup_mixed_vs_fp64_newton_step": (sec64 / max(agg64["matrix_assemblies"], 1))
-                / (sec32_rank / max(agg32["matrix_assemblies"], 1)),
-                "speedup_mixed_vs_fp64_load_step": sec64 / sec32_rank,
-                "max_rel_displacement_error_mixed_vs_fp64": err,
-                "l2_rel_displacement_error_mixed_vs_fp64": err_l2}
-        # both results against an FP64 solution of the same steps converged to 1e-11 (untimed): the displacement
-        # uncertainty that the 1e-8 residual tolerance itself leaves is the scale for the mixed path's error
-        opts_t = g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-11, krylov_rtol=1e-6, max_newton=40,
-                                   max_krylov=20000)
-        try:
-            g.set_state(x_w, t_w, False)
-            g.history = kappa_w
-            run_steps(g, opts_t, t_w, t_values)
-            xt, _ = g.get_state()
-            sc = max(np.abs(xt).max(), 1e-300)
-            fp64["max_rel_displacement_error_vs_fp64_1e-11"] = {
-                "mixed": float(np.abs(x32 - xt).max() / sc), "fp64": float(np.abs(x64 - xt).max() / sc)}
-            nt = max(np.linalg.norm(xt), 1e-300)
-            fp64["l2_rel_displacement_error_vs_fp64_1e-11"] = {
-                "mixed": float(np.linalg.norm(x32 - xt) / nt), "fp64": float(np.linalg.norm(x64 - xt) / nt)}
-        except Exception as exc:  # the reference solution is a diagnostic only
-            fp64["max_rel_displacement_error_vs_fp64_1e-11"] = {"error": str(exc)}
-
-    # end to end through the C ABI with pinned host buffers (state + history copied in and out every step)
-    n_hist = s.mesh.num_cells * g.n_ip
-    xa = torch.empty(n_dofs, dtype=torch.float64, pin_memory=True)
-    xb = torch.empty(n_dofs, dtype=torch.float64, pin_memory=True)
-    ka = torch.empty(n_hist, dtype=torch.float64, pin_memory=True)
-    kb = torch.empty(n_hist, dtype=torch.float64, pin_memory=True)
-    xa.numpy()[:] = x_w
-    ka.numpy()[:] = kappa_w.ravel()
-    g.set_state(x_w, t_w, False)
+    # the same passes end to end through the C ABI with host buffers: state in from pinned memory, CSR values and
+    # residual out to pinned memory, every step
+    xp = torch.empty(n_dofs, dtype=torch.float64, pin_memory=True)
+    xp.numpy()[:] = x_h
+    kp = torch.empty(nnz, dtype=torch.float32, pin_memory=True)
+    fp = torch.empty(n_dofs, dtype=torch.float64, pin_memory=True)
+    ud = torch.empty(n_dofs, dtype=torch.float64, device="cuda")
     barrier()
     h0 = time.perf_counter()
-    assemblies = 0
-    t, step = t_w, dt
-    for tv in t_values:
-        while t < tv - 1e-14:  # AdaptiveSolve's cut-back on the host-buffer entry point
-            tn = min(tv, t + step)
-            try:
-                g.do_step_host(tn, xa, ka, xb, kb, opts32)
-            except nuto_gb300.NoConvergence:
-                assemblies += g.stats()["matrix_assemblies"]
-                step *= 0.5
-                continue
-            assemblies += g.stats()["matrix_assemblies"]
-            xa, xb = xb, xa
-            ka, kb = kb, ka
-            t = tn
-            step = min(dt, step * 1.5) if g.stats()["newton_iterations"] < 3 else step
+    for _ in range(args.steps):
+        ud.copy_(xp, non_blocking=True)
+        g.build_matrix(ud, nuto_gb300.FP32, out=k32)
+        g.build_vector(ud, out=f)
+        kp.copy_(k32, non_blocking=True)
+        fp.copy_(f, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
     barrier()
     sec_e2e = time.perf_counter() - h0
-    (work_e2e,), sec_e2e = aggregate_ranks([n_dofs * assemblies], sec_e2e, "cuda")
-    e2e = {"value": work_e2e / sec_e2e, "unit": "DOF/s",
-           "h2d_bytes_per_step": int((n_dofs + n_hist) * 8), "d2h_bytes_per_step": int((n_dofs + n_hist) * 8),
-           "ms_per_step": 1e3 * sec_e2e / args.steps}
+    (work_e2e,), sec_e2e = aggregate_ranks([n_dofs * args.steps], sec_e2e, "cuda")
+    e2e = {"value": work_e2e / sec_e2e, "unit": "DOF/s", "h2d_bytes_per_step": int(n_dofs * 8),
+           "d2h_bytes_per_step": int(nnz * 4 + n_dofs * 8), "ms_per_step": 1e3 * sec_e2e / args.steps}
 
     peak, peak_kind = load_peaks()
     traffic = load_traffic()
-    per_launch = agg32["ms_spmv"] / max(agg32["spmv_launches"], 1) / 1e3
-    sb = spmv_bytes(g, 4)
-    achieved = sb / per_launch / 1e9
-    roof = {"kernel": "k_spmv_nb<float,float,0> (Krylov SpMV of the whole FP32 tangent, padded pair layout)",
-            "bound": "hbm", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-            "traffic": traffic.get("k_spmv_fp32_bytes_per_launch"), "algorithmic_bytes_per_launch": sb,
-            "mean_launch_us": per_launch * 1e6, "launches": agg32["spmv_launches"]}
     tb = tangent_bytes(s, nnz, 4)
-    # FP32 tangent assemblies timed alone (the step statistics also count the exact final phase's FP64
-    # assemblies): five assemblies at the warm state, CUDA events on the library's stream (the current stream)
-    u_dev = torch.as_tensor(x_w, device="cuda")
-    k32 = torch.empty(nnz, dtype=torch.float32, device="cuda")
-    g.build_matrix(u_dev, nuto_gb300.FP32, out=k32)
-    torch.cuda.synchronize()
-    a0 = torch.cuda.Event(enable_timing=True)
-    a1 = torch.cuda.Event(enable_timing=True)
-    a0.record()
-    for _ in range(5):
-        g.build_matrix(u_dev, nuto_gb300.FP32, out=k32)
-    a1.record()
-    torch.cuda.synchronize()
-    asm_launch = a0.elapsed_time(a1) / 5 / 1e3
-    del k32
-    assembly = {"kernel": "k_tangent<float,REC> + k_tangent_rows<float> (FP32 tangent: records + row gather)",
-                "bound": "hbm",
-                "achieved": tb / asm_launch / 1e9, "peak": peak, "unit": "GB/s",
-                "frac": tb / asm_launch / 1e9 / peak, "algorithmic_bytes_per_launch": tb,
-                "mean_launch_ms": asm_launch * 1e3, "assembled_dofs_per_s": n_dofs / asm_launch,
-                "traffic": traffic.get("k_tangent_fp32_bytes_per_launch")}
+    asm_s = float(np.mean(ms_matrix)) / 1e3
+    roof = {"kernel": TANGENT_KERNEL, "bound": "hbm", "achieved": tb / asm_s / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": tb / asm_s / 1e9 / peak, "peak_kind": peak_kind, "traffic": traffic.get("k_tangent_fused_bytes_per_launch"),
+            "algorithmic_bytes_per_launch": tb, "mean_launch_ms": asm_s * 1e3,
+            "assembled_dofs_per_s": n_dofs / asm_s}
+    rb = residual_bytes(s)
+    res_s = float(np.mean(ms_vector)) / 1e3
 
     out = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1e3 * sec32 / args.steps, "higher_is_better": True,
+           "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-           "config": {"workload": "hex8_gradient_damage_%d^3: Hex8 2x2x2 Gauss, beam 1x1x4 m, u + eeq, "
-                                  "GradientDamage(c=0.01, LinearElasticDamage(30000, 0.2, FULL), "
-                                  "DamageLawExponential(1e-4, 100, 0.99), ModifiedMises(k=10)), 20 load steps to "
-                                  "u_z=2e-3 (AdaptiveSolve cut-back), imperfection kappa=3 kappa0 in the two middle "
-                                  "cell layers; timed load steps %d..%d" % (args.size, args.warmup + 1,
-                                                                           args.warmup + args.steps),
-                      "n_dofs": n_dofs, "nnz": nnz,
-                      "precision": "FP32 tangent + FP32 GMRES(80) and multigrid, FP64 residual, history and Newton "
-                                   "test; the iterations with |C^T r| < %g tol assemble the FP64 tangent and refine "
-                                   "the FP32 solves against it" % EXACT_BELOW,
-                      "newton_tolerance": "|C^T r| <= 1e-8 |C^T (r + K db)| of the load step",
-                      "krylov_rtol": KRYLOV_RTOL,
-                      "l2": "inputs larger than L2 (FP32 tangent %.0f MB)" % (nnz * 4 / 1e6),
-                      "parallelism": "replicas" if world > 1 else "single GPU"},
-           "newton_step_ms": 1e3 * sec32 / max(agg32["matrix_assemblies"], 1),
-           "newton_iterations": agg32["newton_iterations"], "tangent_solves": agg32["matrix_assemblies"],
-           "do_steps": agg32["do_steps"], "cutbacks": agg32["cutbacks"],
-           "krylov_iterations": agg32["krylov_iterations"],
-           "roofline": roof, "roofline_assembly": assembly, "fp64": fp64, "e2e": e2e,
-           "gpu_launches": int(agg32["kernel_launches"]), "clocks": clk}
-    if fp64 is not None:
-        # the two targets side by side: Newton-step speed-up over the FP64 GPU path, and the relative displacement
-        # error against the converged FP64 solution (1e-11 residual; the FP64 path at 1e-8 shown for scale) and
-        # against the FP64 path's own 1e-8 result
-        tight = fp64.get("max_rel_displacement_error_vs_fp64_1e-11", {})
-        tight_l2 = fp64.get("l2_rel_displacement_error_vs_fp64_1e-11", {})
-        out["targets"] = {
-            "speedup_newton_step_mixed_vs_fp64": fp64["speedup_mixed_vs_fp64_newton_step"],
-            "mixed_vs_converged_fp64": {"max": tight.get("mixed"), "l2": tight_l2.get("mixed")},
-            "fp64_path_vs_converged_fp64": {"max": tight.get("fp64"), "l2": tight_l2.get("fp64")},
-            "mixed_vs_fp64_path": {"max": fp64["max_rel_displacement_error_mixed_vs_fp64"],
-                                   "l2": fp64["l2_rel_displacement_error_mixed_vs_fp64"]}}
+           "config": beam_config(args.size, n_dofs, nnz, world),
+           "precision": "FP32 tangent (law branch decisions in FP64), FP64 residual",
+           "ms_matrix_per_step": float(np.mean(ms_matrix)), "ms_vector_per_step": float(np.mean(ms_vector)),
+           "max_abs_tangent_value": fp32_check,
+           "roofline": roof,
+           "roofline_residual": {"kernel": "k_residual (FP64 internal-force vector)", "bound": "fp64",
+                                 "algorithmic_bytes_per_launch": rb, "mean_launch_ms": res_s * 1e3,
+                                 "achieved_gbs": rb / res_s / 1e9},
+           "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+    if not args.skip_newton:
+        out["newton"] = run_newton(args, s, g, barrier)
     if rank == 0 and world == 1 and not args.skip_cpu:
         try:
-            out["cpu_baseline"] = cpu_baseline()
+            out["cpu_baseline"] = cpu_baseline(args.size)
         except Exception as exc:  # the CPU leg must not hide the GPU result
             out["cpu_baseline"] = {"value": None, "error": str(exc)}
     if rank == 0:

@@ -93,7 +93,7 @@ extern "C" {
 #define NUTO_GPU_SOLVER_AUTO 0     /* PCG for the symmetric integrands, GMRES otherwise */
 #define NUTO_GPU_SOLVER_PCG 1      /* preconditioned CG */
 #define NUTO_GPU_SOLVER_BICGSTAB 2 /* Jacobi-preconditioned BiCGStab (always Jacobi) */
-#define NUTO_GPU_SOLVER_GMRES 3    /* restarted GMRES(40), right-preconditioned (flexible form) */
+#define NUTO_GPU_SOLVER_GMRES 3    /* restarted GMRES(80), right-preconditioned (flexible form) */
 
 /* preconditioners of PCG and GMRES (nuto_gpu_set_preconditioner) */
 #define NUTO_GPU_PRECOND_JACOBI 1 /* diagonal */
@@ -140,6 +140,12 @@ typedef struct nuto_gpu_step_options
                                    near-singular modes of a damaged zone converge only linearly, and a state
                                    at the 1e-8 residual can lie 1e-5 from the converged FP64 solution; with the
                                    exact last iterations it lies as close as the FP64 path's (below 1e-6) */
+    double forcing_floor; /* forcing = 1 only: the forcing term is never below forcing_floor * tolerance / |C^T r|,
+                             so the solve of the last Newton iteration leaves a linear residual of about
+                             forcing_floor times the Newton tolerance. Default 0.5. Smaller values solve the last
+                             system more tightly: the converged state then sits further below the tolerance, and
+                             its distance to the exactly converged solution shrinks in proportion (the residual
+                             test weighs the near-singular modes of a damaged zone only weakly) */
 } nuto_gpu_step_options;
 
 /* statistics of the last nuto_gpu_do_step / nuto_gpu_solve */
@@ -206,6 +212,12 @@ int nuto_gpu_num_integration_points(const nuto_gpu_ctx* ctx);
 /* history kappa: n_cells x n_ip doubles (host pointers) */
 int nuto_gpu_set_history(nuto_gpu_ctx* ctx, const double* kappa);
 int nuto_gpu_get_history(nuto_gpu_ctx* ctx, double* kappa);
+/* Per-cell factor of the integrand's Young's modulus (host pointer, n_cells values > 0; NULL: 1 everywhere): cell e
+   integrates with E_e = scale[e] * E, which scales its stress, material tangent and dsigma/domega, i.e. the
+   displacement rows of its cell vector and matrix (the eeq rows do not depend on E). A heterogeneous modulus field,
+   the parameter of the adjoint workload; NuTo gives each cell group one law, so the reference counterpart is one
+   integrand per cell (nuto/mechanics/integrands/GradientDamage.h:25-60 with its own LinearElasticDamage). */
+int nuto_gpu_set_cell_scale(nuto_gpu_ctx* ctx, const double* scale);
 
 /* ---- hot path: device pointers, stream-ordered ---------------------------------------------------------- */
 /* f = sum over cells of the integrand's Gradient (combined layout, all DOFs incl. dependent ones) */
@@ -273,6 +285,28 @@ int nuto_gpu_spmv(nuto_gpu_ctx* ctx, int precision, const void* d_values, const 
    on the first solve after build_pattern; its coarse operators are rebuilt once per tangent. No counterpart in
    the reference, which factorises the matrix (EigenSparseSolve.cpp:22-73). */
 int nuto_gpu_set_preconditioner(nuto_gpu_ctx* ctx, int preconditioner);
+
+/* ---- discrete adjoint of the load path (no counterpart in the reference) -------------------------------- */
+/* The reverse sweep of the gradient-damage load path, one load step at a time, for a loss L(u_N) after N load steps
+   and the parameters p = (per-cell Young's modulus E_e = scale[e] * E, kappa0, beta). For load step n, with the
+   context's history set to kappa_{n-1} (nuto_gpu_history_device) and the step's converged state u_n:
+     1. nuto_gpu_adjoint_history_load(u_n, kbar, ubar): ubar += sum over the loading points (eeq >= kappa_{n-1}) of
+        kbar N on the eeq rows (kbar: n_cells x n_ip, the history adjoint carried from step n + 1; zero at n = N,
+        where ubar = dL/du_N);
+     2. assemble K(u_n) (nuto_gpu_build_matrix, FP64), transpose it (nuto_gpu_transpose_values) and solve
+        K^T lambda = ubar on the independent DOFs (nuto_gpu_solve);
+     3. nuto_gpu_adjoint_step(u_n, lambda, kbar, kbar_prev, grad_e, grad_params): grad_e[e] += dL/dE_e,
+        grad_params[0..1] += dL/dkappa0, dL/dbeta of the step, and kbar_prev = the history adjoint for step n - 1.
+   The forward it differentiates: QuasistaticSolver::DoStep (nuto/mechanics/tools/QuasistaticSolver.cpp:116-147)
+   with GradientDamage::Gradient/Hessian0/Update (nuto/mechanics/integrands/GradientDamage.h:70-125). Gradient
+   damage on Quad4 / Hex8 cells. All sums run in a fixed order (bitwise reproducible). */
+/* K^T on the same (structurally symmetric) pattern: d_transposed[p] = d_values[position of the transposed entry]. */
+int nuto_gpu_transpose_values(nuto_gpu_ctx* ctx, int precision, const void* d_values, void* d_transposed);
+/* Device pointer of the context's history kappa (n_cells x n_ip doubles), e.g. to restore a checkpoint. */
+int nuto_gpu_history_device(nuto_gpu_ctx* ctx, double** d_kappa);
+int nuto_gpu_adjoint_history_load(nuto_gpu_ctx* ctx, const double* d_u, const double* d_kbar, double* d_ubar);
+int nuto_gpu_adjoint_step(nuto_gpu_ctx* ctx, const double* d_u, const double* d_lambda, const double* d_kbar,
+                          double* d_kbar_prev, double* d_grad_e, double* d_grad_params);
 
 /* ---- quasistatic driver ------------------------------------------------------------------------------ */
 int nuto_gpu_default_step_options(nuto_gpu_step_options* opts);

@@ -50,7 +50,7 @@ class StepOptions(ctypes.Structure):
         ("precision", ctypes.c_int), ("method", ctypes.c_int), ("newton_rtol", ctypes.c_double),
         ("newton_atol", ctypes.c_double), ("max_newton", ctypes.c_int), ("line_search", ctypes.c_int),
         ("krylov_rtol", ctypes.c_double), ("max_krylov", ctypes.c_int), ("forcing", ctypes.c_int),
-        ("exact_tangent_below", ctypes.c_double),
+        ("exact_tangent_below", ctypes.c_double), ("forcing_floor", ctypes.c_double),
     ]
 
 
@@ -90,6 +90,11 @@ SIGNATURES = {
     "nuto_gpu_spmv": (_i, [_vp, _i, _vp, _vp, _vp, _i]),
     "nuto_gpu_set_history": (_i, [_vp, _vp]),
     "nuto_gpu_get_history": (_i, [_vp, _vp]),
+    "nuto_gpu_set_cell_scale": (_i, [_vp, _vp]),
+    "nuto_gpu_history_device": (_i, [_vp, _P(_vp)]),
+    "nuto_gpu_transpose_values": (_i, [_vp, _i, _vp, _vp]),
+    "nuto_gpu_adjoint_history_load": (_i, [_vp, _vp, _vp, _vp]),
+    "nuto_gpu_adjoint_step": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nuto_gpu_build_vector": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_build_matrix": (_i, [_vp, _vp, _i, _vp]),
     "nuto_gpu_build_matrix_noalloc": (_i, [_vp, _vp, _vp]),

@@ -145,6 +145,16 @@ class GpuCellGroup:
         k = np.ascontiguousarray(np.broadcast_to(kappa, (self.mesh.num_cells, self.n_ip)), dtype=np.float64)
         self._call("nuto_gpu_set_history", _ptr(k))
 
+    def set_cell_scale(self, scale):
+        """Per-cell factor of the integrand's Young's modulus (None: 1 everywhere)."""
+        if scale is None:
+            self._call("nuto_gpu_set_cell_scale", None)
+            return
+        sc = np.ascontiguousarray(scale, dtype=np.float64)
+        if sc.shape != (self.mesh.num_cells,):
+            raise ValueError("one factor per cell")
+        self._call("nuto_gpu_set_cell_scale", _ptr(sc))
+
     # ---- hot path (device tensors) ---------------------------------------------------------------------------
     def _dev(self, x, dtype):
         torch = _torch()

@@ -268,6 +268,7 @@ static void BuildPattern(Ctx& c)
         Upload(c.slots[I].dCellLoc, loc);
     }
     c.rowsMode = -1;
+    c.fusedMode = -1;
 
     // neighbour lists per (I, J): J-nodes of all cells around an I-node, sorted by DOF number
     std::vector<NodeLists> nbr(ns * ns);
@@ -588,6 +589,7 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
 #endif
     const char* tk = std::getenv("NUTO_GPU_TANGENT");
     c->forceAtomicTangent = tk && std::string(tk) == "atomic";
+    c->forceRecordTangent = tk && std::string(tk) == "records";
     const char* gr = std::getenv("NUTO_GPU_GMRES_RESTART");
     c->gmresRestart = gr ? std::atoi(gr) : 0;
     const int rc = Guard(c, [&] {
@@ -832,6 +834,7 @@ int nuto_gpu_set_integrand(nuto_gpu_ctx* ctx, const nuto_gpu_integrand* p)
         NG_CUDA(cudaMemsetAsync(ctx->dKappa.p, 0, ctx->dKappa.n * sizeof(double), ctx->stream));
         ctx->haveIntegrand = true;
         ctx->rowsMode = -1;
+        ctx->fusedMode = -1;
         ctx->haveGeo = false;
         return NUTO_GPU_OK;
     });
@@ -896,6 +899,26 @@ int nuto_gpu_set_history(nuto_gpu_ctx* ctx, const double* kappa)
     });
 }
 
+int nuto_gpu_set_cell_scale(nuto_gpu_ctx* ctx, const double* scale)
+{
+    return Guard(ctx, [&] {
+        NG_CHECK(ctx->haveCells, NUTO_GPU_ESTATE, "set_cells first");
+        if (!scale)
+        {
+            ctx->dEScale.free();
+            return NUTO_GPU_OK;
+        }
+        for (int64_t e = 0; e < ctx->nCells; ++e)
+            NG_CHECK(std::isfinite(scale[e]) && scale[e] > 0., NUTO_GPU_EINVAL, "cell scale factors must be > 0");
+        if (ctx->dEScale.n != static_cast<size_t>(ctx->nCells))
+            ctx->dEScale.alloc(ctx->nCells);
+        NG_CUDA(cudaMemcpyAsync(ctx->dEScale.p, scale, ctx->nCells * sizeof(double), cudaMemcpyHostToDevice,
+                                ctx->stream));
+        NG_CUDA(cudaStreamSynchronize(ctx->stream));
+        return NUTO_GPU_OK;
+    });
+}
+
 int nuto_gpu_get_history(nuto_gpu_ctx* ctx, double* kappa)
 {
     return Guard(ctx, [&] {
@@ -914,6 +937,48 @@ static void RequireReady(Ctx& c)
     if (!c.haveGeo)
         BuildGeometryCache(c);
 }
+
+int nuto_gpu_history_device(nuto_gpu_ctx* ctx, double** d_kappa)
+{
+    return Guard(ctx, [&] {
+        NG_CHECK(ctx->haveIntegrand, NUTO_GPU_ESTATE, "set_integrand first");
+        NG_CHECK(d_kappa, NUTO_GPU_EINVAL, "d_kappa");
+        *d_kappa = ctx->dKappa.p;
+        return NUTO_GPU_OK;
+    });
+}
+
+int nuto_gpu_transpose_values(nuto_gpu_ctx* ctx, int precision, const void* values, void* transposed)
+{
+    return Guard(ctx, [&] {
+        NG_CHECK(ctx->havePattern, NUTO_GPU_ESTATE, "build_pattern first");
+        NG_CHECK(precision == NUTO_GPU_FP32 || precision == NUTO_GPU_FP64, NUTO_GPU_EINVAL, "precision 32 or 64");
+        NG_CHECK(values != transposed, NUTO_GPU_EINVAL, "the transposed values need their own buffer");
+        LaunchTransposeValues(*ctx, precision, values, transposed);
+        return NUTO_GPU_OK;
+    });
+}
+
+int nuto_gpu_adjoint_history_load(nuto_gpu_ctx* ctx, const double* u, const double* kbar, double* ubar)
+{
+    return Guard(ctx, [&] {
+        RequireReady(*ctx);
+        LaunchAdjointHistoryLoad(*ctx, u, kbar, ubar);
+        return NUTO_GPU_OK;
+    });
+}
+
+int nuto_gpu_adjoint_step(nuto_gpu_ctx* ctx, const double* u, const double* lambda, const double* kbarIn,
+                          double* kbarOut, double* gradE, double* gradParams)
+{
+    return Guard(ctx, [&] {
+        RequireReady(*ctx);
+        NG_CHECK(kbarIn != kbarOut, NUTO_GPU_EINVAL, "kbar_in and kbar_out must differ");
+        LaunchAdjointStep(*ctx, u, lambda, kbarIn, kbarOut, gradE, gradParams);
+        return NUTO_GPU_OK;
+    });
+}
+
 
 int nuto_gpu_build_vector(nuto_gpu_ctx* ctx, const double* u, double* f)
 {
@@ -1100,6 +1165,7 @@ int nuto_gpu_default_step_options(nuto_gpu_step_options* o)
     o->max_krylov = 20000;
     o->forcing = 1;
     o->exact_tangent_below = 1.0e4;
+    o->forcing_floor = 0.5;
     return NUTO_GPU_OK;
 }
 

@@ -217,6 +217,15 @@ void BuildGeometryCache(Ctx& c)
     c.haveGeo = true;
 }
 
+static CellArgs MakeCellArgs(Ctx& c);
+
+CellArgs CellArgsOf(Ctx& c)
+{
+    if (!c.haveGeo)
+        BuildGeometryCache(c);
+    return MakeCellArgs(c);
+}
+
 static CellArgs MakeCellArgs(Ctx& c)
 {
     CellArgs a{};
@@ -240,6 +249,7 @@ static CellArgs MakeCellArgs(Ctx& c)
     a.geo32 = c.dGeo32.p;
     a.geoStride = c.geoStride;
     a.kappa = c.dKappa.p;
+    a.escale = c.dEScale.n ? c.dEScale.p : nullptr;
     return a;
 }
 
@@ -247,9 +257,12 @@ static CellArgs MakeCellArgs(Ctx& c)
 // MomentumBalance::Gradient (MomentumBalance.h:26-35) and GradientDamage::Gradient (GradientDamage.h:70-90)
 // integrated as in Cell::IntegrateGeneric (Cell.h:105-119) and scattered like SimpleAssembler::BuildVector
 // (SimpleAssembler.cpp:38-65); FP64 atomics replace the thread-local vectors.
+// The cell vectors are written planar ([local entry][cell]: the displacement entries node-major, then the eeq
+// entries) and k_gather_cell_vectors sums them per DOF in ascending cell order: the residual is bitwise the same on
+// every run (SimpleAssembler::BuildVector sums thread-local vectors and merges them in a critical section).
 template <int DIM, int ND, int NIP, int KIND>
 __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const double* __restrict__ u,
-                                                  double* __restrict__ f)
+                                                  double* __restrict__ fcell)
 {
     constexpr int VD = DIM == 2 ? 3 : 6;
     constexpr bool GD = KIND == NUTO_GPU_GRADIENT_DAMAGE;
@@ -285,6 +298,8 @@ __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const
         const int64_t G0 = static_cast<int64_t>(q) * a.geoStride * n + e;
         const double* G = a.geo64 + NG_IDX(G0, a.geoSize, 6);
         const double wdj = G[0];
+        // per-cell Young's modulus factor: scales the stress, i.e. the displacement rows
+        const double wdjE = a.escale ? wdj * a.escale[e] : wdj;
         double H[DIM][DIM];
 #pragma unroll
         for (int i = 0; i < DIM; ++i)
@@ -340,7 +355,7 @@ __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const
         }
 #pragma unroll
         for (int v = 0; v < VD; ++v)
-            sIp[cl][q][v] = sig[v] * wdj;
+            sIp[cl][q][v] = sig[v] * wdjE;
     }
     __syncthreads();
 
@@ -375,27 +390,71 @@ __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const
                 fe += s;
             }
         }
-        const int64_t g = a.gdofD[NG_IDX(a.connD[static_cast<int64_t>(nd) * n + e], a.nNodesD, 2)];
+        const int64_t nLocal = static_cast<int64_t>(ND) * (DIM + (GD ? 1 : 0));
+        (void)nLocal; // buffer extent for checked builds
 #pragma unroll
         for (int c = 0; c < DIM; ++c)
-            atomicAdd(f + NG_IDX(g + c, a.nDofs, 8), fu[c]);
+            fcell[NG_IDX((static_cast<int64_t>(nd) * DIM + c) * n + e, nLocal * n, 8)] = fu[c];
         if (GD)
-            atomicAdd(f + NG_IDX(a.gdofE[NG_IDX(a.connE[static_cast<int64_t>(nd) * n + e], a.nNodesE, 4)], a.nDofs, 8), fe);
+            fcell[NG_IDX((static_cast<int64_t>(ND) * DIM + nd) * n + e, nLocal * n, 8)] = fe;
     }
+}
+
+// f[dof] (+)= sum of the cell vectors' entries of that DOF over the node's cells in ascending cell order: one thread
+// per (node, component) of a slot; entry (off + loc * ncomp + comp) of the planar cell vectors
+__global__ void k_gather_cell_vectors(int64_t nNodes, int ncomp, int off, int64_t nCells, int64_t nLocal,
+                                      const int64_t* __restrict__ cellPtr, const int32_t* __restrict__ cellIdx,
+                                      const uint8_t* __restrict__ cellLoc, const int64_t* __restrict__ gdof,
+                                      const double* __restrict__ fcell, int64_t nDofs, double* __restrict__ f,
+                                      int add)
+{
+    const int64_t it = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (it >= nNodes * ncomp)
+        return;
+    const int64_t i = it / ncomp;
+    const int comp = static_cast<int>(it % ncomp);
+    double s = 0.;
+    for (int64_t k = cellPtr[i]; k < cellPtr[i + 1]; ++k)
+    {
+        const int64_t e = cellIdx[k];
+        const int64_t entry = off + static_cast<int64_t>(cellLoc[k]) * ncomp + comp;
+        s += fcell[NG_IDX(entry * nCells + e, nLocal * nCells, 9)];
+    }
+    double* o = f + NG_IDX(gdof[i] + comp, nDofs, 9);
+    *o = add ? *o + s : s;
+}
+
+void GatherCellVectors(Ctx& c, const Slot& S, int ncomp, int off, int64_t nLocal, double* f, bool add)
+{
+    const int64_t items = S.nNodes * ncomp;
+    k_gather_cell_vectors<<<static_cast<unsigned>((items + 255) / 256), 256, 0, c.stream>>>(
+            S.nNodes, ncomp, off, c.nCells, nLocal, S.dCellPtr.p, S.dCellIdx.p, S.dCellLoc.p, S.dGdof.p, c.dCellVec.p,
+            c.nDofs, f, add ? 1 : 0);
+    AfterLaunch(c, "k_gather_cell_vectors");
 }
 
 void LaunchResidual(Ctx& c, const double* u, double* f)
 {
-    NG_CUDA(cudaMemsetAsync(f, 0, c.nDofs * sizeof(double), c.stream));
+    const Slot& D = c.slots[c.prm.disp_slot];
+    const bool gd = c.prm.kind == NUTO_GPU_GRADIENT_DAMAGE;
+    const int64_t nLocal = static_cast<int64_t>(D.nen) * (c.dim + (gd ? 1 : 0));
+    if (c.dCellVec.n != static_cast<size_t>(nLocal * c.nCells))
+        c.dCellVec.alloc(static_cast<size_t>(nLocal * c.nCells));
+    // DOFs of slots that the integrand does not touch stay zero
+    if (c.slots.size() > static_cast<size_t>(gd ? 2 : 1))
+        NG_CUDA(cudaMemsetAsync(f, 0, c.nDofs * sizeof(double), c.stream));
     CellArgs a = MakeCellArgs(c);
     DispatchCfg(c, [&](auto cfg) {
         using C = decltype(cfg);
         constexpr int CPB = MaxI<1, 128 / MaxI<C::nip, C::nd>::v>::v;
         const int blocks = static_cast<int>((c.nCells + CPB - 1) / CPB);
-        k_residual<C::dim, C::nd, C::nip, C::kind><<<blocks, 128, 0, c.stream>>>(a, c.law, u, f);
+        k_residual<C::dim, C::nd, C::nip, C::kind><<<blocks, 128, 0, c.stream>>>(a, c.law, u, c.dCellVec.p);
     });
     AfterLaunch(c, "k_residual");
-    c.stats.kernel_launches += 1;
+    GatherCellVectors(c, D, c.dim, 0, nLocal, f, false);
+    if (gd)
+        GatherCellVectors(c, c.slots[c.prm.eeq_slot], 1, D.nen * c.dim, nLocal, f, false);
+    c.stats.kernel_launches += gd ? 3 : 2;
 }
 
 // ---- tangent: FP32 or FP64 values scattered into CSR ---------------------------------------------------------
@@ -573,6 +632,8 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
             continue;
         const int64_t widx = NG_IDX(static_cast<int64_t>(q) * a.geoStride * n + e, a.geoSize, 6);
         const T wdj = sizeof(T) == 4 ? static_cast<T>(a.geo32[widx]) : static_cast<T>(a.geo64[widx]);
+        // per-cell Young's modulus factor: scales the material tangent and dsigma/domega (displacement rows)
+        const T wdjE = a.escale ? wdj * static_cast<T>(a.escale[e]) : wdj;
         T H[DIM][DIM];
 #pragma unroll
         for (int i = 0; i < DIM; ++i)
@@ -628,7 +689,7 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
 #pragma unroll
             for (int v = 0; v < VD; ++v)
             {
-                sST[cl][q][0][v] = dsdw[v] * dOdK * wdj;
+                sST[cl][q][0][v] = dsdw[v] * dOdK * wdjE;
                 sST[cl][q][1][v] = dk[v];
             }
         }
@@ -647,7 +708,7 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
 #pragma unroll
             for (int v = 0; v < VD; ++v)
             {
-                sST[cl][q][0][v] = dsdw[v] * dOdK * dKdE * wdj; // (disp, eeq): B^T (dsigma/domega w' k') N
+                sST[cl][q][0][v] = dsdw[v] * dOdK * dKdE * wdjE; // (disp, eeq): B^T (dsigma/domega w' k') N
                 sST[cl][q][1][v] = dn[v] * wdj;                 // (eeq, disp): -N^T (deps_eq/deps)^T B
             }
             sRec[cl][q][2] = wdj;
@@ -657,8 +718,8 @@ __global__ void __launch_bounds__(256) k_tangent(CellArgs a, LawParams L, Scatte
             for (int d = 0; d < DIM; ++d)
                 sRec[cl][q][4 + d] = sc * ge[d];
         }
-        sRec[cl][q][0] = lam * wdj;
-        sRec[cl][q][1] = mu * wdj;
+        sRec[cl][q][0] = lam * wdjE;
+        sRec[cl][q][1] = mu * wdjE;
     }
     __syncthreads();
 
@@ -1298,7 +1359,11 @@ static void LaunchTangentT(Ctx& c, const double* u, T* vals)
     // the rank-1 factors in the row kernel costs more than the FP64 atomics it saves.
     if (sizeof(T) == 4 && RowsSupported(c) && !c.forceAtomicTangent)
     {
-        LaunchTangentRows<T>(c, u, vals);
+        // linear cells: geometry and law recomputed per node in FP32, no records; otherwise records + row gather
+        if (!c.forceRecordTangent && FusedTangentSupported(c))
+            LaunchTangentFused(c, u, reinterpret_cast<float*>(vals));
+        else
+            LaunchTangentRows<T>(c, u, vals);
         return;
     }
     NG_CUDA(cudaMemsetAsync(vals, 0, c.nnz * sizeof(T), c.stream));
@@ -1674,9 +1739,10 @@ __global__ void __launch_bounds__(128) k_eval_ip(CellArgs a, LawParams L, const 
             ElasticStress<double, DIM>(L, eps, sig);
         else
             LedStress<double, DIM>(L, eps, omega, sig);
+        const double se = a.escale ? a.escale[e] : 1.;
 #pragma unroll
         for (int r = 0; r < VD; ++r)
-            o[r] = sig[r];
+            o[r] = sig[r] * se;
     }
 }
 

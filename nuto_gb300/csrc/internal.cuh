@@ -364,15 +364,26 @@ struct Ctx
     // row-gather tangent: integration-point records and the displacement-node -> eeq-node map
     int rowsMode = -1; // -1 not decided, 0 element-wise atomics, 1 row gather
     bool forceAtomicTangent = false; // NUTO_GPU_TANGENT=atomic selects the element-wise kernel
+    bool forceRecordTangent = false; // NUTO_GPU_TANGENT=records selects records + row gather for linear cells
     int gmresRestart = 0;            // NUTO_GPU_GMRES_RESTART; 0 = the default length
     DBuf<int32_t> dEOf;
     DBuf<unsigned char> dRecords;
+    // fused FP32 tangent: -1 not decided, 0 not applicable, 1 used; FP32 node coordinates relative to each cell's
+    // first node (planar [(n * dim + d)][cell])
+    int fusedMode = -1;
+    DBuf<float> dRelX;
+    // residual: the cell vectors of the last residual (planar [local entry][cell]) gathered per DOF
+    DBuf<double> dCellVec;
+    // adjoint: positions of the transposed entries, per-point partial derivatives
+    DBuf<int64_t> dTransPerm;
+    DBuf<double> dAdjPart;
 
     // integrand
     bool haveIntegrand = false;
     nuto_gpu_integrand prm{};
     LawParams law{};
     DBuf<double> dKappa; // nCells x nIp
+    DBuf<double> dEScale; // per-cell factor of the integrand's Young's modulus (empty: 1 everywhere)
 
     // quasistatic state
     bool haveState = false;
@@ -400,6 +411,8 @@ void LaunchResidual(Ctx& c, const double* u, double* f);
 void LaunchTangent(Ctx& c, const double* u, int precision, void* values);
 void LaunchTangentExact(Ctx& c, const double* u, double* vals);
 void LaunchTangentNoAlloc(Ctx& c, const double* u, float* values);
+bool FusedTangentSupported(Ctx& c);
+void LaunchTangentFused(Ctx& c, const double* u, float* vals);
 void LaunchHistory(Ctx& c, const double* u);
 void LaunchLumpedMass(Ctx& c, double rho, double* m);
 void LaunchExternalLoad(Ctx& c, const BoundaryGroup& B, const double* p, double* f);
@@ -443,6 +456,7 @@ struct CellArgs
     const float* geo32;
     int geoStride;
     double* kappa;
+    const double* escale; // per-cell Young's modulus factor (nullptr: 1)
 };
 
 struct ScatterArgs
@@ -452,6 +466,13 @@ struct ScatterArgs
     const uint8_t* rank[kMaxSlots * kMaxSlots];
     const int32_t* blk[kMaxSlots * kMaxSlots];
 };
+
+CellArgs CellArgsOf(Ctx& c); // the geometry cache is built on first use
+void GatherCellVectors(Ctx& c, const Slot& S, int ncomp, int off, int64_t nLocal, double* f, bool add);
+void LaunchTransposeValues(Ctx& c, int precision, const void* in, void* out);
+void LaunchAdjointHistoryLoad(Ctx& c, const double* u, const double* kbar, double* ubar);
+void LaunchAdjointStep(Ctx& c, const double* u, const double* lam, const double* kbarIn, double* kbarOut,
+                       double* gradE, double* gradParams);
 
 // ------------------------------------------------------------------------------------------------------------
 // Constitutive laws, device side, templated on the arithmetic type. Each cites the reference it restates.

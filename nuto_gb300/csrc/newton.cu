@@ -123,6 +123,8 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     const auto t0 = std::chrono::steady_clock::now();
     NG_CHECK(o.precision == NUTO_GPU_FP32 || o.precision == NUTO_GPU_FP64 || o.precision == NUTO_GPU_MIXED,
              NUTO_GPU_EINVAL, "precision NUTO_GPU_FP32, NUTO_GPU_FP64 or NUTO_GPU_MIXED");
+    NG_CHECK(o.forcing != 1 || (o.forcing_floor > 0. && o.forcing_floor <= 1.), NUTO_GPU_EINVAL,
+             "forcing_floor in (0, 1]");
     SolverWork& w = Work(c);
     const int64_t n = c.nDofs;
     for (DBuf<double>* b : {&w.f, &w.rhs, &w.dx, &w.db, &w.x0, &w.xs, &w.tmp, &w.refR, &w.refKx})
@@ -272,8 +274,8 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
                      nr, refNorm, tol, lastKrylov, lastRel);
     // Forcing terms (forcing = 1): Eisenstat-Walker choice 1, eta_k = | |F_k| - |F_k-1 + a J s_k-1| | / |F_k-1|,
     // the disagreement between the residual and its linear model; with the safeguard eta_k >= eta_k-1^1.618 when
-    // that exceeds 0.1, clamped to [krylov_rtol, 0.5] and to no less than 0.5 tol / |F_k| (no over-solving of the
-    // last iteration). An inaccurate (FP32) tangent gives loose solves, an accurate one tight solves.
+    // that exceeds 0.1, clamped to [krylov_rtol, 0.5] and to no less than forcing_floor tol / |F_k| (no
+    // over-solving of the last iteration beyond what the caller asks for). An inaccurate (FP32) tangent gives loose solves, an accurate one tight solves.
     double prevNr = nr, stepAlpha = 1., stepRel = lastRel;
     while (!conv && it < o.max_newton)
     {
@@ -292,7 +294,7 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
                 if (sg > 0.1)
                     e = std::max(e, sg);
             }
-            e = std::max(e, 0.5 * tol / nr);
+            e = std::max(e, o.forcing_floor * tol / nr);
             eta = std::min(0.5, std::max(o.krylov_rtol, e));
         }
         solve(w.rhs.p, w.dx.p);

@@ -26,3 +26,21 @@ def test_accumulated_end_times():
         acc += 0.05
         assert t[k] == acc
     assert len(bench.accumulate(0.3, 0.1, 0)) == 0
+
+
+def test_both_arms_assemble_the_same_state():
+    """The headline's seeded state built from the product's set-up and from the oracle's set-up (the reference arm)
+    is the same vector and history, bit for bit."""
+    import numpy as np
+
+    from nuto_gb300 import configs
+
+    n = 4
+    s = configs.hex8_gradient_damage(n)
+    Ld, Le = s.mesh.layers[s.layers[0]], s.mesh.layers[s.layers[1]]
+    x, kappa = bench.beam_state(Ld.node_coords, Ld.dof_numbers, Le.dof_numbers, s.n_dofs, s.mesh.num_cells, 8, n)
+    P, xo = bench.oracle_beam(n)
+    assert np.array_equal(x, xo)
+    assert np.array_equal(kappa, P.kappa)
+    # a mix of branches: loading and unloading points, damaged and undamaged ones
+    assert 0.2 < np.mean(kappa > 1e-4) < 0.9

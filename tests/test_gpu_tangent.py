@@ -1,0 +1,219 @@
+"""GPU parity of the tangent kernels beyond the basic cases, through the C ABI.
+
+- The fused FP32 tangent (geometry and law recomputed per node in FP32, no integration-point records) against the
+  records + row-gather tangent and against the FP64 tangent, including states whose integration points sit on the
+  law's branch thresholds (eeq = kappa_h, eeq = kappa0): the loading/unloading and damage branches of the FP32
+  kernel must be the FP64 kernels' at every point, otherwise whole coupling blocks differ.
+- GradientDamage with NonlocalInteraction::Decreasing and with UNILATERAL damage application
+  (nuto/mechanics/integrands/GradientDamage.h:153-184, nuto/mechanics/constitutive/LinearElasticDamage.h:58-100)
+  against the oracle: FP64 residual and tangent <= 1e-12, FP32 tangent <= 2e-6 relative to the largest entry, and
+  load steps into the damaged range.
+- The benchmark beam (64^3 Hex8 gradient damage) at its full size: DOF numbering and CSR pattern bit-exact and the
+  FP64 residual <= 1e-12 against the oracle at the benchmark's seeded state; tangent values at 32^3.
+"""
+
+import numpy as np
+import pytest
+
+import bench
+from oracle import setups as osetups
+from oracle.quasistatic import QuasistaticOracle
+
+pytestmark = pytest.mark.gpu
+
+FP64_REL = 1e-12
+FP32_REL = 2e-6
+
+
+def _torch():
+    import torch
+
+    assert torch.cuda.is_available(), "these tests need a CUDA GPU"
+    return torch
+
+
+def _setup(kind, n, law=None):
+    from nuto_gb300 import configs
+
+    if kind == "hex8gd":
+        s = configs.hex8_gradient_damage(n)
+        o = osetups.hex8_gradient_damage(n, law=law)
+    elif kind == "quad4gd":
+        s = configs.notched_plate(n, 0.4)
+        o = osetups.notched_plate(n, 0.4, law=law)
+    else:
+        s = configs.quad4_elastic(n)
+        o = osetups.quad4_elastic(n)
+    if law:
+        s.integrand.update(law)
+    return s, o
+
+
+def _damage_state(kind, s, P, rng):
+    u = rng.uniform(-2e-4, 2e-4, P.n_dofs)
+    if kind == "quad4":
+        return u * 5.0, None
+    nd = s.mesh.layers[s.layers[0]].num_dofs
+    u[nd:] = rng.uniform(0.0, 4e-4, P.n_dofs - nd)
+    kappa = rng.uniform(0.0, 3e-4, (P.n_el, P.n_ip))
+    return u, kappa
+
+
+def _csr(P, u):
+    K = P.build_matrix_scipy(u).tocsr()
+    K.sort_indices()
+    return K
+
+
+@pytest.mark.parametrize("kind,n", [("hex8gd", 4), ("quad4gd", 8), ("quad4", 5)])
+def test_fused_tangent_matches_records_and_oracle(kind, n, monkeypatch):
+    _torch()
+    import nuto_gb300
+
+    rng = np.random.default_rng(21)
+    s, (om, layers, P, cons) = _setup(kind, n)
+    u, kappa = _damage_state(kind, s, P, rng)
+    g = s.build_gpu()
+    if kappa is not None:
+        g.history = kappa
+        P.kappa = kappa
+    fused = g.build_matrix(u, nuto_gb300.FP32).double().cpu().numpy()
+    monkeypatch.setenv("NUTO_GPU_TANGENT", "records")
+    g2 = s.build_gpu()
+    if kappa is not None:
+        g2.history = kappa
+    rec = g2.build_matrix(u, nuto_gb300.FP32).double().cpu().numpy()
+    K = _csr(P, u)
+    scale = np.abs(K.data).max()
+    assert np.abs(fused - K.data).max() <= FP32_REL * scale
+    assert np.abs(fused - rec).max() <= FP32_REL * scale
+
+
+def test_fused_tangent_branches_follow_fp64_at_the_thresholds():
+    """Integration points placed exactly on the thresholds: history kappa equal to the point's eeq (as after a
+    history update at a loading point), slightly above and below it, and nodal eeq equal to kappa0. The FP32 tangent
+    stays within FP32 rounding of the FP64 tangent, which decides these branches in FP64."""
+    _torch()
+    import nuto_gb300
+    from nuto_gb300._lib import IP_EEQ
+
+    n = 4
+    s, (om, layers, P, cons) = _setup("hex8gd", n)
+    g = s.build_gpu()
+    rng = np.random.default_rng(5)
+    nd = s.mesh.layers[s.layers[0]].num_dofs
+    u = rng.uniform(-1e-4, 1e-4, P.n_dofs)
+    u[nd:] = rng.uniform(0.5e-4, 2e-4, P.n_dofs - nd)
+    # a third of the eeq nodes exactly at kappa0
+    e_idx = np.arange(nd, P.n_dofs)
+    u[e_idx[::3]] = 1e-4
+    g.history = 0.0
+    eeq = g.eval_ip(u, IP_EEQ).cpu().numpy()[..., 0]  # FP64 eeq at every point
+    choice = rng.integers(0, 4, eeq.shape)
+    kappa = np.where(choice == 0, eeq, np.where(choice == 1, np.nextafter(eeq, np.inf),
+                                                np.where(choice == 2, np.nextafter(eeq, -np.inf), 1e-4)))
+    g.history = kappa
+    k32 = g.build_matrix(u, nuto_gb300.FP32).double().cpu().numpy()
+    k64 = g.build_matrix(u, nuto_gb300.FP64).cpu().numpy()
+    assert np.abs(k32 - k64).max() <= FP32_REL * np.abs(k64).max()
+
+
+VARIANTS = {"decreasing": dict(interaction=1, R=0.005, eta=5.0),
+            "unilateral": dict(damage_application=1),
+            "decreasing_unilateral": dict(interaction=1, R=0.05, eta=3.0, damage_application=1)}
+
+
+@pytest.mark.parametrize("variant", sorted(VARIANTS))
+@pytest.mark.parametrize("kind,n", [("hex8gd", 3), ("quad4gd", 8)])
+def test_gradient_damage_variants_against_oracle(kind, n, variant):
+    _torch()
+    import nuto_gb300
+
+    law = VARIANTS[variant]
+    s, (om, layers, P, cons) = _setup(kind, n, law)
+    g = s.build_gpu()
+    rng = np.random.default_rng(31)
+    u, kappa = _damage_state(kind, s, P, rng)
+    g.history = kappa
+    P.kappa = kappa
+    f_ref = P.build_vector(u)
+    f = g.build_vector(u).cpu().numpy()
+    assert np.abs(f - f_ref).max() <= FP64_REL * np.abs(f_ref).max()
+    K = _csr(P, u)
+    scale = np.abs(K.data).max()
+    k64 = g.build_matrix(u, nuto_gb300.FP64).cpu().numpy()
+    assert np.abs(k64 - K.data).max() <= FP64_REL * scale
+    k32 = g.build_matrix(u, nuto_gb300.FP32).double().cpu().numpy()
+    assert np.abs(k32 - K.data).max() <= FP32_REL * scale
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("variant", ["decreasing", "unilateral"])
+def test_gradient_damage_variant_load_steps(variant, precision):
+    """Eight load steps of the notched plate into the damaged range with the variant's law; displacements, eeq and
+    kappa against the oracle's direct-solve Newton (FP64 path <= 1e-7, FP32 tangent <= 1e-6 relative; the Newton
+    tolerance 1e-12 on |C^T r| bounds the eeq unknowns only to about 1e-10 absolute)."""
+    _torch()
+    law = VARIANTS[variant]
+    s, (om, layers, P, cons) = _setup("quad4gd", 8, law)
+    g = s.build_gpu()
+    tol = 1e-12
+    Q = QuasistaticOracle(P, cons[0], cons[1], cons[2], tolerance=tol, max_iterations=30)
+    g.set_state(None, 0.0, True)
+    opts = g.default_options(precision=precision, newton_rtol=0.0, newton_atol=tol,
+                             krylov_rtol=1e-12 if precision == 64 else 1e-5, max_newton=30, max_krylov=50000)
+    rel = 1e-7 if precision == 64 else 1e-6
+    steps = 8
+    for k in range(1, steps + 1):
+        t = 0.8 * k / steps  # the schedule of the plain notched-plate test: damage from step 4 on
+        Q.do_step(t)
+        g.do_step(t, opts)
+        x, _ = g.get_state()
+        assert np.abs(x - Q.x).max() <= rel * np.abs(Q.x).max(), k
+        kap = g.history
+        assert np.abs(kap - Q.P.kappa).max() <= rel * max(np.abs(Q.P.kappa).max(), 1e-4), k
+    assert Q.P.kappa.max() > 1e-4  # the steps reached the damaged range
+
+
+def test_benchmark_beam_full_size_pattern_and_residual():
+    """The 64^3 beam of the benchmark (1,098,500 DOFs): numbering and CSR pattern bit for bit, FP64 residual at the
+    benchmark's seeded state within 1e-12 of the oracle's."""
+    _torch()
+    from nuto_gb300 import configs
+
+    n = 64
+    s = configs.hex8_gradient_damage(n)
+    g = s.build_gpu()
+    Ld, Le = s.mesh.layers[s.layers[0]], s.mesh.layers[s.layers[1]]
+    x, kappa = bench.beam_state(Ld.node_coords, Ld.dof_numbers, Le.dof_numbers, g.n_dofs, s.mesh.num_cells, g.n_ip,
+                                n)
+    P, xo = bench.oracle_beam(n)
+    assert np.array_equal(x, xo) and g.n_dofs == P.n_dofs == 1098500
+    rp, ci = g.pattern()
+    cp, ri, _ = P.build_matrix_csc(np.zeros(P.n_dofs))
+    assert np.array_equal(rp, cp) and np.array_equal(ci, ri)
+    del cp, ri
+    g.history = kappa
+    f = g.build_vector(x).cpu().numpy()
+    f_ref = P.build_vector(x)
+    assert np.abs(f - f_ref).max() <= FP64_REL * np.abs(f_ref).max()
+
+
+def test_beam_32_tangent_against_oracle():
+    """The beam at 32^3 (143,748 DOFs, 13.6 M nonzeros) at the benchmark's kind of seeded state: FP64 tangent <= 1e-12
+    and the FP32 (fused) tangent <= 2e-6 relative to the largest entry."""
+    _torch()
+    import nuto_gb300
+    from nuto_gb300 import configs
+
+    n = 32
+    s = configs.hex8_gradient_damage(n)
+    g = s.build_gpu()
+    P, x = bench.oracle_beam(n)
+    g.history = P.kappa
+    K = _csr(P, x)
+    scale = np.abs(K.data).max()
+    k64 = g.build_matrix(x, nuto_gb300.FP64).cpu().numpy()
+    assert np.abs(k64 - K.data).max() <= FP64_REL * scale
+    k32 = g.build_matrix(x, nuto_gb300.FP32).double().cpu().numpy()
+    assert np.abs(k32 - K.data).max() <= FP32_REL * scale
