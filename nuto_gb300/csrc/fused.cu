@@ -59,16 +59,19 @@ struct FusedShape
     static constexpr int cpp = 32 / NIP;             // cells per pass
     static constexpr int nr = DIM + (GD ? 1 : 0);     // rows per node
     // per warp, in floats: node data (2 float4 per (cell, node)), eeq values in FP64 (2 floats each), per point
-    // the node gradients with N (float4 per node), the products B_n^T t (float4 per node, gradient damage), two
-    // float4 of scalars; the row buffer
+    // the node gradients with N (float4 per node) and four float4 of scalars (lambda w, mu w, w, c g w | P_a, the
+    // eeq-gradient coupling | the Voigt vector t of the (eeq, disp) block); the row buffer
+    // rows of float4 indexed by the integration point are padded to ND + 1 (and the scalars to 5) float4 entries:
+    // the 8 lanes of a cell, one per point, then touch 8 distinct bank groups instead of one (a stride of 128 bytes
+    // would serialise them 8-fold)
     static constexpr int nodeF = cpp * ND * 8;
     static constexpr int eF = GD ? cpp * ND * 2 : 0;
-    static constexpr int gF = cpp * NIP * ND * 4;
-    static constexpr int qF = GD ? cpp * NIP * ND * 4 : 0;
-    static constexpr int sF = cpp * NIP * 8;
+    static constexpr int gF = cpp * NIP * (ND + 1) * 4;
+    static constexpr int qF = 0;
+    static constexpr int sF = cpp * NIP * 20; // 5 float4 per point: 4 used (scalars, P_a, t), 1 of padding
     static constexpr int rowF = nr * kFusedRowCap;
     static constexpr int perWarp = nodeF + eF + gF + qF + sF + rowF;
-    static constexpr int tabF = NIP * ND * 4 + NIP;  // (dN/dxi, N) per point and node, weights
+    static constexpr int tabF = NIP * (ND + 1) * 4 + NIP; // (dN/dxi, N) per point and node, weights
     static constexpr int tabOff = (tabF + 3) / 4 * 4; // per-warp regions start 16-byte aligned
     static constexpr size_t smem = (static_cast<size_t>(kFusedWarps) * perWarp + tabOff) * sizeof(float);
     static_assert(cpp * NIP == 32 && cpp * ND == 32, "one lane per (cell, point) and per (cell, node)");
@@ -98,21 +101,21 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
     constexpr int CPP = Sh::cpp, NR = Sh::nr, VD = DIM == 2 ? 3 : 6;
     extern __shared__ __align__(16) float smF[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float4* sTab = reinterpret_cast<float4*>(smF); // [NIP][ND]: dN/dxi, N
-    float* sW = smF + NIP * ND * 4;                // [NIP]
+    constexpr int NDP = ND + 1;                     // padded row length (float4)
+    float4* sTab = reinterpret_cast<float4*>(smF); // [NIP][NDP]: dN/dxi, N
+    float* sW = smF + NIP * NDP * 4;               // [NIP]
     float* base = smF + Sh::tabOff + wid * Sh::perWarp;
     float4* sNodeX = reinterpret_cast<float4*>(base);                   // [CPP][ND]: X - X0, eeq
     float4* sNodeU = sNodeX + CPP * ND;                                 // [CPP][ND]: u
     double* sE64 = reinterpret_cast<double*>(base + Sh::nodeF);         // [CPP][ND]: eeq (gradient damage)
-    float4* sG = reinterpret_cast<float4*>(base + Sh::nodeF + Sh::eF);  // [CPP][NIP][ND]: dN/dX, N
-    float4* sQ = sG + CPP * NIP * ND;                                   // [CPP][NIP][ND]: B^T t (gradient damage)
-    float4* sS = reinterpret_cast<float4*>(base + Sh::nodeF + Sh::eF + Sh::gF + Sh::qF); // [CPP][NIP][2]
+    float4* sG = reinterpret_cast<float4*>(base + Sh::nodeF + Sh::eF);  // [CPP][NIP][NDP]: dN/dX, N
+    float4* sS = reinterpret_cast<float4*>(base + Sh::nodeF + Sh::eF + Sh::gF + Sh::qF); // [CPP][NIP][5]
     float* sRow = base + Sh::nodeF + Sh::eF + Sh::gF + Sh::qF + Sh::sF; // [NR][kFusedRowCap]
     for (int i = threadIdx.x; i < NIP * ND; i += blockDim.x)
     {
         const int q = i / ND, nd = i % ND;
         const double* d = A.tabDN + (q * ND + nd) * 3;
-        sTab[i] = F4(static_cast<float>(d[0]), static_cast<float>(d[1]), DIM == 3 ? static_cast<float>(d[2]) : 0.f,
+        sTab[q * NDP + nd] = F4(static_cast<float>(d[0]), static_cast<float>(d[1]), DIM == 3 ? static_cast<float>(d[2]) : 0.f,
                      static_cast<float>(A.tabN[q * ND + nd]));
     }
     for (int i = threadIdx.x; i < NIP; i += blockDim.x)
@@ -192,7 +195,7 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
             {
                 const int64_t e = A.cellIdx[kc];
                 const int ia = A.cellLoc[kc];
-                const float4* T = sTab + q * ND;
+                const float4* T = sTab + q * NDP;
                 const float4* X = sNodeX + cs * ND;
                 const float4* U = sNodeU + cs * ND;
                 float J[DIM][DIM];
@@ -253,7 +256,7 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
                     for (int j = 0; j < DIM; ++j)
                         H[i][j] = 0.f;
                 }
-                float4* G = sG + (cs * NIP + q) * ND;
+                float4* G = sG + (cs * NIP + q) * NDP;
 #pragma unroll
                 for (int nd = 0; nd < ND; ++nd)
                 {
@@ -311,7 +314,7 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
                     for (int nd = 1; nd < ND; ++nd)
                         gA[d] = nd == ia ? g[nd][d] : gA[d];
                 }
-                float4* S = sS + (cs * NIP + q) * 2;
+                float4* S = sS + (cs * NIP + q) * 5;
                 if (!GD)
                 {
                     // LinearElastic: C11 = lambda + 2 mu, C12 = lambda, C33 = mu
@@ -388,41 +391,48 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
                     const float3 pa = BtV<DIM>(gA[0], gA[1], DIM == 3 ? gA[DIM - 1] : 0.f, sv);
                     S[0] = F4(lam * wdjE, mu * wdjE, wdj, c * gI * wdj);
                     S[1] = F4(pa.x, pa.y, pa.z, sc * gs);
-                    float4* Q = sQ + (cs * NIP + q) * ND;
-#pragma unroll
-                    for (int nd = 0; nd < ND; ++nd)
-                    {
-                        const float3 qb = BtV<DIM>(g[nd][0], g[nd][1], DIM == 3 ? g[nd][DIM - 1] : 0.f, tvv);
-                        Q[nd] = F4(qb.x, qb.y, qb.z, 0.f);
-                    }
+                    S[2] = F4(tvv[0], tvv[1], tvv[2], 0.f);
+                    S[3] = F4(VD > 3 ? tvv[VD > 3 ? 3 : 0] : 0.f, VD > 4 ? tvv[VD > 4 ? 4 : 0] : 0.f,
+                              VD > 5 ? tvv[VD > 5 ? 5 : 0] : 0.f, 0.f);
                 }
             }
         }
         __syncwarp();
         // (B) lane (cell slot, neighbour b): the node-pair block (a, b) integrated over the points, added into a's
-        // rows at the ranks of b (shared-memory atomics: cells of one pass can share b)
+        // rows at the ranks of b
         {
             const int cs = lane / ND, b = lane % ND;
             const int64_t kc = kp + cs;
+            float uu[DIM][DIM], ue[DIM], eu[DIM], ee = 0.f, dg = 0.f;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k)
+            {
+                ue[k] = eu[k] = 0.f;
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    uu[k][l] = 0.f;
+            }
+            int r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+            bool active = false;
             if (kc < k1)
             {
                 const int64_t e = A.cellIdx[kc];
                 const int ia = A.cellLoc[kc];
-                float uu[DIM][DIM], ue[DIM], eu[DIM], ee = 0.f, dg = 0.f;
-#pragma unroll
-                for (int k = 0; k < DIM; ++k)
+                // ranks of b in a's neighbour lists (loaded first: their latency overlaps the integration)
+                const int64_t ridx = static_cast<int64_t>(ia * ND + b) * n + e;
+                r0 = A.rank[0][ridx];
+                if (GD)
                 {
-                    ue[k] = eu[k] = 0.f;
-#pragma unroll
-                    for (int l = 0; l < DIM; ++l)
-                        uu[k][l] = 0.f;
+                    r1 = A.rank[1][ridx];
+                    r2 = A.rank[2][ridx];
+                    r3 = A.rank[3][ridx];
                 }
 #pragma unroll 2
                 for (int q = 0; q < NIP; ++q)
                 {
-                    const float4* G = sG + (cs * NIP + q) * ND;
+                    const float4* G = sG + (cs * NIP + q) * NDP;
                     const float4 ga = G[ia], gb = G[b];
-                    const float4 s0 = sS[(cs * NIP + q) * 2];
+                    const float4 s0 = sS[(cs * NIP + q) * 5];
                     const float av[3] = {ga.x, ga.y, ga.z}, bv[3] = {gb.x, gb.y, gb.z};
                     float gab = 0.f;
 #pragma unroll
@@ -440,8 +450,10 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
                     dg += s0.y * gab;
                     if (GD)
                     {
-                        const float4 s1 = sS[(cs * NIP + q) * 2 + 1];
-                        const float4 qb = sQ[(cs * NIP + q) * ND + b];
+                        const float4 s1 = sS[(cs * NIP + q) * 5 + 1];
+                        const float4 t0 = sS[(cs * NIP + q) * 5 + 2], t1 = sS[(cs * NIP + q) * 5 + 3];
+                        const float tv[6] = {t0.x, t0.y, t0.z, t1.x, t1.y, t1.z};
+                        const float3 qb = BtV<DIM>(gb.x, gb.y, gb.z, tv); // B_b^T t
                         const float pv[3] = {s1.x, s1.y, s1.z}, qv[3] = {qb.x, qb.y, qb.z};
 #pragma unroll
                         for (int k = 0; k < DIM; ++k)
@@ -452,28 +464,35 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
                         ee += (s0.z * ga.w + s1.w) * gb.w + s0.w * gab;
                     }
                 }
-                const int64_t ridx = static_cast<int64_t>(ia * ND + b) * n + e;
-                const int r0 = A.rank[0][ridx];
+                active = true;
+            }
+            // the cells of a pass can share b: their blocks are added one cell slot after the other (the b of one
+            // cell are distinct nodes, so the 8 lanes of a slot write distinct positions); fixed order, no atomics
 #pragma unroll
-                for (int k = 0; k < DIM; ++k)
+            for (int r = 0; r < CPP; ++r)
+            {
+                if (active && cs == r)
                 {
-                    float* row = sRow + k * kFusedRowCap;
-#pragma unroll
-                    for (int l = 0; l < DIM; ++l)
-                        atomicAdd(&row[NG_IDX(bUU + DIM * r0 + l, kFusedRowCap, 56)], uu[k][l] + (k == l ? dg : 0.f));
-                }
-                if (GD)
-                {
-                    const int r1 = A.rank[1][ridx], r2 = A.rank[2][ridx], r3 = A.rank[3][ridx];
 #pragma unroll
                     for (int k = 0; k < DIM; ++k)
-                        atomicAdd(&sRow[k * kFusedRowCap + NG_IDX(bUE + r1, kFusedRowCap, 56)], ue[k]);
-                    float* row = sRow + DIM * kFusedRowCap;
+                    {
+                        float* row = sRow + k * kFusedRowCap;
 #pragma unroll
-                    for (int l = 0; l < DIM; ++l)
-                        atomicAdd(&row[NG_IDX(bEU + DIM * r2 + l, kFusedRowCap, 56)], eu[l]);
-                    atomicAdd(&row[NG_IDX(bEE + r3, kFusedRowCap, 56)], ee);
+                        for (int l = 0; l < DIM; ++l)
+                            row[NG_IDX(bUU + DIM * r0 + l, kFusedRowCap, 56)] += uu[k][l] + (k == l ? dg : 0.f);
+                        if (GD)
+                            row[NG_IDX(bUE + r1, kFusedRowCap, 56)] += ue[k];
+                    }
+                    if (GD)
+                    {
+                        float* row = sRow + DIM * kFusedRowCap;
+#pragma unroll
+                        for (int l = 0; l < DIM; ++l)
+                            row[NG_IDX(bEU + DIM * r2 + l, kFusedRowCap, 56)] += eu[l];
+                        row[NG_IDX(bEE + r3, kFusedRowCap, 56)] += ee;
+                    }
                 }
+                __syncwarp();
             }
         }
     }

@@ -28,7 +28,24 @@ def _state(s, g, seed):
     return u, kappa
 
 
+def _unchanged_memory(fn):
+    """Runs fn() and checks that the device memory in use did not change: torch's allocator holds the same
+    bytes and cudaMemGetInfo reports the same free memory (nothing was allocated on the device)."""
+    import torch
+
+    torch.cuda.synchronize()
+    held = torch.cuda.memory_allocated()
+    free0, _ = torch.cuda.mem_get_info()
+    fn()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert torch.cuda.memory_allocated() == held
+    assert free1 == free0
+
+
 def test_noalloc_tangent_matches_build_matrix_twice():
+    import torch
+
     import nuto_gb300
 
     s, g = _group(4)
@@ -36,8 +53,11 @@ def test_noalloc_tangent_matches_build_matrix_twice():
     g.history = kappa
     ref = g.build_matrix(u, nuto_gb300.FP32).double().cpu().numpy()
     scale = np.abs(ref).max()
+    ud = torch.as_tensor(u, device="cuda")
+    out = torch.empty(g.nnz, dtype=torch.float32, device="cuda")
     for _ in range(2):  # two calls in a row reuse the static records
-        v = g.build_matrix_noalloc(u).double().cpu().numpy()
+        _unchanged_memory(lambda: g.build_matrix_noalloc(ud, out=out))
+        v = out.double().cpu().numpy()
         assert np.abs(v - ref).max() <= 1e-6 * scale
     # a second state after the first: nothing of the previous call leaks into the next one
     u2, kappa2 = _state(s, g, 8)
@@ -45,6 +65,27 @@ def test_noalloc_tangent_matches_build_matrix_twice():
     ref2 = g.build_matrix(u2, nuto_gb300.FP32).double().cpu().numpy()
     v2 = g.build_matrix_noalloc(u2).double().cpu().numpy()
     assert np.abs(v2 - ref2).max() <= 1e-6 * np.abs(ref2).max()
+
+
+def test_noalloc_tangent_hex20_local_damage():
+    """The other record layout: Hex20 displacements with the local damage law (3x3x3 points, 2,099 cells at most),
+    two calls in a row against nuto_gpu_build_matrix."""
+    import torch
+
+    import nuto_gb300
+    from nuto_gb300 import configs
+
+    s = configs.hex20_local_damage(3)
+    g = s.build_gpu()
+    rng = np.random.default_rng(12)
+    u = rng.uniform(-3e-4, 3e-4, g.n_dofs)
+    g.history = rng.uniform(0.0, 3e-4, (s.mesh.num_cells, g.n_ip))
+    ref = g.build_matrix(u, nuto_gb300.FP32).double().cpu().numpy()
+    ud = torch.as_tensor(u, device="cuda")
+    out = torch.empty(g.nnz, dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        _unchanged_memory(lambda: g.build_matrix_noalloc(ud, out=out))
+        assert np.abs(out.double().cpu().numpy() - ref).max() <= 1e-6 * np.abs(ref).max()
 
 
 def test_noalloc_tangent_needs_setup_and_rejects_large_meshes():
