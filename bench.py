@@ -58,12 +58,12 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--size", type=int, default=64)
+    p.add_argument("--size", type=int, default=None, help="cells per side (beam: 64, hex20: 80)")
     p.add_argument("--skip-fp64", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--skip-newton", action="store_true")
     p.add_argument("--skip-adjoint", action="store_true")
-    p.add_argument("--workload", default="beam", choices=["beam", "plates"])
+    p.add_argument("--workload", default="beam", choices=["beam", "plates", "hex20"])
     p.add_argument("--specimens", type=int, default=128)
     return p.parse_args()
 
@@ -204,13 +204,13 @@ def accumulate(t0, dt, k):
     return out
 
 
-def run_steps(g, opts, t_start, t_values):
+def run_steps(g, opts, t_start, t_values, dt=None):
     """Advances the load from t_start through every t in t_values with AdaptiveSolve (time step 1/LOAD_STEPS, cut
     back by halves on NoConvergence as the reference's AdaptiveSolve does). Returns the summed step statistics,
     failed attempts included (their work was done), the number of cut-backs and the per-load-step Newton counts."""
     from nuto_gb300.adaptive import AdaptiveSolve
 
-    dt = 1.0 / LOAD_STEPS
+    dt = dt or 1.0 / LOAD_STEPS
     ad = AdaptiveSolve(g, opts, dt=dt, dt_max=dt, dt_min=dt / 256)
     t = t_start
     per_step = []
@@ -311,6 +311,7 @@ def run_reference(args):
         return
     threads = oracle.lib().oracle_max_threads()
     oracle.lib().oracle_set_threads(threads)
+    args.size = args.size or 64
     P, x = oracle_beam(args.size)
     # a CPU pass has nothing to warm up but page faults: one warm-up pass whatever --warmup asks for
     for _ in range(min(args.warmup, 1)):
@@ -509,6 +510,7 @@ def run_ours(args):
     from nuto_gb300 import configs
 
     nuto_gb300.load()
+    args.size = args.size or 64
     s = configs.hex8_gradient_damage(args.size, load_steps=LOAD_STEPS, imperfection=True)
     g = s.build_gpu(device=local)
     n_dofs, nnz = g.n_dofs, g.nnz
@@ -604,6 +606,16 @@ def run_ours(args):
            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
     if not args.skip_newton:
         out["newton"] = run_newton(args, s, g, barrier)
+    # launch shapes the autotuner chose (first tangent, first Krylov products) with the times it measured, and the
+    # gain over the default shapes (4 warps per block, 8 lanes per node)
+    tune = g.autotune_info()
+    tms = tune["tangent_ms"]
+    if tune["tangent_warps"] and min(tms) > 0:
+        tune["tangent_gain_over_default"] = tms[1] / tms[[2, 4, 8].index(tune["tangent_warps"])]
+    for k, ms in tune["spmv_ms"].items():
+        if tune["spmv_lanes"][k] and min(ms) > 0:
+            tune.setdefault("spmv_gain_over_default", {})[k] = ms[1] / ms[[4, 8, 16].index(tune["spmv_lanes"][k])]
+    out["autotune"] = tune
     if not args.skip_adjoint and world == 1:
         try:
             out["adjoint"] = run_adjoint()
@@ -788,12 +800,75 @@ def run_plates(args):
         tdist.destroy_process_group()
 
 
+HEX20_METRIC = "Hex20 local damage: Newton-step time & assembled DOFs/s, FP32 tangent vs FP64 GPU"
+HEX20_STEPS = 5
+
+
+def run_hex20(args):
+    """The large configuration: Hex20 displacements (3x3x3 Gauss) with the local exponential damage law on an n^3
+    cube (80^3: 6.3 M DOFs, 1.09 G nonzeros), its 5 load steps to u_z = 3e-4 from rest on the mixed path (FP32
+    tangent and Krylov, FP64 residual and history) and on the FP64 path, each timed with CUDA events; the two final
+    states compared. Not the headline."""
+    import torch
+
+    import nuto_gb300
+    from nuto_gb300 import configs
+
+    torch.cuda.set_device(0)
+    nuto_gb300.load()
+    n = args.size or 80
+    s = configs.hex20_local_damage(n, load_steps=HEX20_STEPS)
+    g = s.build_gpu(device=0)
+    t_values = accumulate(0.0, 1.0 / HEX20_STEPS, HEX20_STEPS)
+    common = dict(newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20, max_krylov=50000,
+                  forcing_floor=FORCING_FLOOR)
+    runs = {"mixed": g.default_options(precision=nuto_gb300.FP32, exact_tangent_below=EXACT_BELOW, **common),
+            "fp64": g.default_options(precision=nuto_gb300.FP64, **common)}
+    out, states = {}, {}
+    for name, o in runs.items():
+        if name == "fp64" and args.skip_fp64:
+            continue
+        g.set_state(None, 0.0, True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        agg = run_steps(g, o, 0.0, t_values, dt=1.0 / HEX20_STEPS)
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        states[name], _ = g.get_state()
+        na = max(agg["matrix_assemblies"], 1)
+        out[name] = {"seconds": sec, "newton_step_ms": 1e3 * sec / na, "tangent_solves": agg["matrix_assemblies"],
+                     "newton_per_load_step": agg["newton_per_load_step"], "krylov_iterations": agg["krylov_iterations"],
+                     "cutbacks": agg["cutbacks"],
+                     "ms_per_newton_step": {"tangent": agg["ms_assemble_matrix"] / na,
+                                            "residual": agg["ms_assemble_vector"] / na,
+                                            "krylov": agg["ms_krylov"] / na}}
+    res = {"metric": HEX20_METRIC, "value": g.n_dofs * out["mixed"]["tangent_solves"] / out["mixed"]["seconds"],
+           "unit": "DOF/s", "n_gpus": 1, "steps": HEX20_STEPS, "warmup": 0,
+           "ms_per_step": 1e3 * out["mixed"]["seconds"] / HEX20_STEPS, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+           "config": {"workload": "hex20_local_damage_%d^3: Hex20 3x3x3 Gauss on the unit cube, MomentumBalance + "
+                                  "LocalIsotropicDamage(30000, 0.2, kappa0 1e-4, beta 100, alpha 0.99, k 10), z = 0 "
+                                  "fixed, z = 1 u_z = 3e-4 t, %d load steps from rest" % (n, HEX20_STEPS),
+                      "n_dofs": int(g.n_dofs), "nnz": int(g.nnz)},
+           "runs": out}
+    if "fp64" in states:
+        a, b = states["mixed"], states["fp64"]
+        res["mixed_vs_fp64_path"] = {"max": float(np.abs(a - b).max() / np.abs(b).max()),
+                                     "l2": float(np.linalg.norm(a - b) / np.linalg.norm(b))}
+        res["speedup_newton_step_mixed_vs_fp64"] = out["fp64"]["newton_step_ms"] / out["mixed"]["newton_step_ms"]
+    print(json.dumps(res))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "plates":
         run_plates(args)
+    elif args.workload == "hex20":
+        run_hex20(args)
     else:
         run_ours(args)
 

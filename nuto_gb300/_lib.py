@@ -87,6 +87,7 @@ SIGNATURES = {
     "nuto_gpu_num_integration_points": (_i, [_vp]),
     "nuto_gpu_solver_layout": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_multigrid_info": (_i, [_vp, _vp, _vp]),
+    "nuto_gpu_autotune_info": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_spmv": (_i, [_vp, _i, _vp, _vp, _vp, _i]),
     "nuto_gpu_set_history": (_i, [_vp, _vp]),
     "nuto_gpu_get_history": (_i, [_vp, _vp]),

@@ -590,6 +590,9 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
     const char* tk = std::getenv("NUTO_GPU_TANGENT");
     c->forceAtomicTangent = tk && std::string(tk) == "atomic";
     c->forceRecordTangent = tk && std::string(tk) == "records";
+    c->tangentStaged = !(tk && std::string(tk) == "fused");
+    const char* at = std::getenv("NUTO_GPU_AUTOTUNE");
+    c->tuning.enabled = !(at && at[0] == '0');
     const char* gr = std::getenv("NUTO_GPU_GMRES_RESTART");
     c->gmresRestart = gr ? std::atoi(gr) : 0;
     const int rc = Guard(c, [&] {
@@ -863,6 +866,28 @@ int nuto_gpu_spmv(nuto_gpu_ctx* ctx, int precision, const void* d_values, const 
         NG_CUDA(cudaStreamSynchronize(ctx->stream));
         return NUTO_GPU_OK;
     });
+}
+
+int nuto_gpu_autotune_info(const nuto_gpu_ctx* ctx, int* choices, float* times_ms)
+{
+    if (!ctx)
+        return NUTO_GPU_EINVAL;
+    const Tuning& T = ctx->tuning;
+    if (choices)
+    {
+        choices[0] = T.tangentWarps;
+        for (int k = 0; k < 4; ++k)
+            choices[1 + k] = T.spmvGroup[k];
+    }
+    if (times_ms)
+    {
+        for (int k = 0; k < 3; ++k)
+            times_ms[k] = T.tangentMs[k];
+        for (int p = 0; p < 4; ++p)
+            for (int k = 0; k < 3; ++k)
+                times_ms[3 + 3 * p + k] = T.spmvMs[p][k];
+    }
+    return NUTO_GPU_OK;
 }
 
 int nuto_gpu_multigrid_info(const nuto_gpu_ctx* ctx, int* levels, int* graph_active)

@@ -1,25 +1,28 @@
-// Fused FP32 tangent: SimpleAssembler::BuildMatrix (nuto/mechanics/cell/SimpleAssembler.cpp:100-156) of
+// FP32 tangent of linear cells: SimpleAssembler::BuildMatrix (nuto/mechanics/cell/SimpleAssembler.cpp:100-156) of
 // MomentumBalance::Hessian0 (nuto/mechanics/integrands/MomentumBalance.h:36-46) and GradientDamage::Hessian0
-// (nuto/mechanics/integrands/GradientDamage.h:92-120) for linear cells (Quad4, Hex8), written straight into the CSR
-// values without integration-point records in HBM and without atomics in global memory.
+// (nuto/mechanics/integrands/GradientDamage.h:92-120) for Quad4 and Hex8 cells, written straight into the CSR values
+// without atomics in global memory.
 //
 // One warp per displacement node a assembles the complete CSR rows of a (and of its eeq node). The cells around a
-// are taken a pass of CPP = 32 / NIP at a time:
-//   (0) lane (cell, node) loads that node's data of the cell: FP32 coordinates relative to the cell's first node,
-//       displacements, eeq value;
-//   (A) lane (cell, integration point) computes J, J^-1, dN/dX, the strain, the law in FP32 and the products
-//       B_n^T t of every node of the cell, into the warp's shared memory;
-//   (B) lane (cell, neighbour b) integrates the node-pair block (a, b) over the points in registers and adds it into
-//       the warp's shared copy of a's rows at the rank of b.
-// At the end the rows are stored once, coalesced. Geometry and law are recomputed by each of the (up to) 8 warps
-// that share a cell instead of being streamed from HBM: the kernel reads the connectivity, the relative
-// coordinates, the state and the history and writes the values.
+// are taken a pass of CPP = 32 / NIP at a time; per pass the warp needs, for every point of the pass's cells, the
+// node gradients dN/dX and the law's scalars and vectors (PointData):
+//   staged (default): k_point_records evaluates PointData once per (cell, point) into per-cell contiguous records
+//       (13 float4 per point for Hex8 gradient damage); the node warp copies a pass's records into shared memory
+//       with 16-byte asynchronous copies;
+//   fused (NUTO_GPU_TANGENT=fused): (0) lane (cell, node) loads the node's coordinates relative to the cell's first
+//       node, displacements and eeq; (A) lane (cell, point) evaluates PointData in the warp (each cell's points are
+//       then evaluated by every warp whose node the cell holds, up to 8 times).
+// Then (B) lane (cell, neighbour b) integrates the node-pair block (a, b) over the points in registers and adds it
+// into the warp's shared copy of a's rows at the rank of b, one cell slot after the other (fixed order: the values
+// are bitwise reproducible). At the end the rows are stored once, coalesced.
 //
 // Branch decisions of the law are the FP64 kernels' (k_residual, k_tangent<double>): the nonlocal equivalent
 // strain at a point is formed in FP32 with an error bound, and where the bound does not separate it from the
 // history kappa or from kappa0 it is recomputed in FP64 exactly as the FP64 kernels form it. The loading/unloading
 // and damage-threshold branches therefore agree with the FP64 residual at every point; everything else is FP32.
 #include "internal.cuh"
+
+#include <type_traits>
 
 namespace nuto_gpu
 {
@@ -28,7 +31,6 @@ namespace
 {
 
 constexpr int kFusedRowCap = 128; // values per row buffer: 32 neighbour nodes of [u | eeq] in 3D
-constexpr int kFusedWarps = 4;
 
 struct FusedArgs
 {
@@ -53,9 +55,18 @@ struct FusedArgs
 };
 
 template <int DIM, int ND, int NIP, int KIND>
+struct FCfg
+{
+    static constexpr int dim = DIM, nd = ND, nip = NIP, kind = KIND;
+};
+
+// STAGED: the per-point data come from the records of k_point_records instead of being computed in the warp;
+// W: warps (displacement nodes) per block, chosen by the autotuner among 2, 4 and 8
+template <int DIM, int ND, int NIP, int KIND, bool STAGED = false, int W = 4>
 struct FusedShape
 {
     static constexpr bool GD = KIND == NUTO_GPU_GRADIENT_DAMAGE;
+    static constexpr int recF4 = ND + (GD ? 5 : 1); // float4 per record: ND gradients, the scalars
     static constexpr int cpp = 32 / NIP;             // cells per pass
     static constexpr int nr = DIM + (GD ? 1 : 0);     // rows per node
     // per warp, in floats: node data (2 float4 per (cell, node)), eeq values in FP64 (2 floats each), per point
@@ -64,16 +75,18 @@ struct FusedShape
     // rows of float4 indexed by the integration point are padded to ND + 1 (and the scalars to 5) float4 entries:
     // the 8 lanes of a cell, one per point, then touch 8 distinct bank groups instead of one (a stride of 128 bytes
     // would serialise them 8-fold)
-    static constexpr int nodeF = cpp * ND * 8;
-    static constexpr int eF = GD ? cpp * ND * 2 : 0;
-    static constexpr int gF = cpp * NIP * (ND + 1) * 4;
+    // staged: the records of a pass in their global layout, [cell][point][recF4] float4 (an odd row length of
+    // ND + 5 = 13 float4 keeps the 8 lanes of a cell on distinct bank groups); fused: gradients and scalars apart
+    static constexpr int nodeF = STAGED ? 0 : cpp * ND * 8;
+    static constexpr int eF = GD && !STAGED ? cpp * ND * 2 : 0;
+    static constexpr int gF = STAGED ? cpp * NIP * recF4 * 4 : cpp * NIP * (ND + 1) * 4;
     static constexpr int qF = 0;
-    static constexpr int sF = cpp * NIP * 20; // 5 float4 per point: 4 used (scalars, P_a, t), 1 of padding
+    static constexpr int sF = STAGED ? 0 : cpp * NIP * 20; // 5 float4 per point: 4 used (scalars, P_a, t), 1 pad
     static constexpr int rowF = nr * kFusedRowCap;
     static constexpr int perWarp = nodeF + eF + gF + qF + sF + rowF;
     static constexpr int tabF = NIP * (ND + 1) * 4 + NIP; // (dN/dxi, N) per point and node, weights
     static constexpr int tabOff = (tabF + 3) / 4 * 4; // per-warp regions start 16-byte aligned
-    static constexpr size_t smem = (static_cast<size_t>(kFusedWarps) * perWarp + tabOff) * sizeof(float);
+    static constexpr size_t smem = (static_cast<size_t>(W) * perWarp + tabOff) * sizeof(float);
     static_assert(cpp * NIP == 32 && cpp * ND == 32, "one lane per (cell, point) and per (cell, node)");
 };
 
@@ -92,13 +105,217 @@ __device__ __forceinline__ float3 BtV(float gx, float gy, float gz, const float*
                        gz * v[2] + gy * v[3] + gx * v[4]);
 }
 
-template <int DIM, int ND, int NIP, int KIND>
-__global__ void __launch_bounds__(kFusedWarps * 32)
-        k_tangent_fused(FusedArgs A, LawParams L, const double* __restrict__ u, float* __restrict__ vals)
+// Everything the node-pair blocks of one integration point need, in FP32: the node gradients dN/dX, the scalars
+// (lambda w, mu w, w, c g w for gradient damage; lambda w, mu w for LinearElastic, both with the cell's modulus
+// factor), and for gradient damage the Voigt vectors sv (disp, eeq block: dsigma/domega omega' kappa' w) and tv
+// (eeq, disp block: deps_eq/deps w) and the eeq-gradient coupling vector c g' omega' kappa' w grad eeq.
+template <int DIM, int ND>
+struct PointOut
 {
-    using Sh = FusedShape<DIM, ND, NIP, KIND>;
+    float g[ND][DIM];
+    float s0[4];
+    float sv[6], tv[6], scge[DIM];
+};
+
+// Geometry, strain and law at integration point q of cell e from the cell's node data: X (coordinates relative to
+// the first node, eeq value in .w), U (displacements), E64 (eeq values in FP64, for the branch decisions); T the
+// (dN/dxi, N) table row of q and w its weight. The loading/unloading and damage branches are the FP64 kernels'
+// (decided in FP32 where the error bound of eeq separates the operands, else in FP64 as k_tangent<double> forms
+// eeq: same order, FP64 shape values tabN).
+template <int DIM, int ND, int NIP, int KIND>
+__device__ __forceinline__ void PointData(const FusedArgs& A, const LawParams& L, const float4* T, float w,
+                                          const float4* X, const float4* U, const double* E64, int q, int64_t e,
+                                          PointOut<DIM, ND>& o)
+{
+    constexpr bool GD = KIND == NUTO_GPU_GRADIENT_DAMAGE;
+    constexpr int VD = DIM == 2 ? 3 : 6;
+    const int64_t n = A.nCells;
+    float J[DIM][DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int j = 0; j < DIM; ++j)
+            J[i][j] = 0.f;
+#pragma unroll
+    for (int nd = 0; nd < ND; ++nd)
+    {
+        const float4 x = X[nd], t = T[nd];
+        const float xv[3] = {x.x, x.y, x.z}, tv[3] = {t.x, t.y, t.z};
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = 0; j < DIM; ++j)
+                J[i][j] += xv[i] * tv[j];
+    }
+    float det, inv[DIM][DIM];
+    if (DIM == 2)
+    {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const float id = 1.f / det;
+        inv[0][0] = J[1][1] * id;
+        inv[0][1] = -J[0][1] * id;
+        inv[1][0] = -J[1][0] * id;
+        inv[1][1] = J[0][0] * id;
+    }
+    else
+    {
+        const float c00 = J[1][1] * J[2 % DIM][2 % DIM] - J[1][2 % DIM] * J[2 % DIM][1];
+        const float c10 = J[1][2 % DIM] * J[2 % DIM][0] - J[1][0] * J[2 % DIM][2 % DIM];
+        const float c20 = J[1][0] * J[2 % DIM][1] - J[1][1] * J[2 % DIM][0];
+        det = J[0][0] * c00 + J[0][1] * c10 + J[0][2 % DIM] * c20;
+        const float id = 1.f / det;
+        inv[0][0] = c00 * id;
+        inv[1][0] = c10 * id;
+        inv[2 % DIM][0] = c20 * id;
+        inv[0][1] = (J[0][2 % DIM] * J[2 % DIM][1] - J[0][1] * J[2 % DIM][2 % DIM]) * id;
+        inv[1][1] = (J[0][0] * J[2 % DIM][2 % DIM] - J[0][2 % DIM] * J[2 % DIM][0]) * id;
+        inv[2 % DIM][1] = (J[0][1] * J[2 % DIM][0] - J[0][0] * J[2 % DIM][1]) * id;
+        inv[0][2 % DIM] = (J[0][1] * J[1][2 % DIM] - J[0][2 % DIM] * J[1][1]) * id;
+        inv[1][2 % DIM] = (J[0][2 % DIM] * J[1][0] - J[0][0] * J[1][2 % DIM]) * id;
+        inv[2 % DIM][2 % DIM] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+    }
+    const float wdj = w * det;
+    // per-cell Young's modulus factor: scales the material tangent and dsigma/domega
+    const float wdjE = A.escale ? wdj * static_cast<float>(A.escale[e]) : wdj;
+    float H[DIM][DIM], ge[DIM];
+    float eeq = 0.f, eabs = 0.f;
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+    {
+        ge[i] = 0.f;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j)
+            H[i][j] = 0.f;
+    }
+#pragma unroll
+    for (int nd = 0; nd < ND; ++nd)
+    {
+        const float4 t = T[nd];
+        const float tv[3] = {t.x, t.y, t.z};
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            float s = 0.f;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j)
+                s += tv[j] * inv[j][k];
+            o.g[nd][k] = s;
+        }
+        const float4 uv = U[nd];
+        const float uc[3] = {uv.x, uv.y, uv.z};
+#pragma unroll
+        for (int c = 0; c < DIM; ++c)
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                H[c][d] += uc[c] * o.g[nd][d];
+        if (GD)
+        {
+            const float ev = X[nd].w;
+            eeq += t.w * ev;
+            eabs += fabsf(t.w * ev);
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                ge[d] += ev * o.g[nd][d];
+        }
+    }
+    float eps[VD];
+    if (DIM == 2)
+    {
+        eps[0] = H[0][0];
+        eps[1] = H[1][1];
+        eps[2 % VD] = H[0][1] + H[1][0];
+    }
+    else
+    {
+        eps[0] = H[0][0];
+        eps[1] = H[1][1];
+        eps[2] = H[DIM - 1][DIM - 1];
+        eps[3 % VD] = H[1][DIM - 1] + H[DIM - 1][1];
+        eps[4 % VD] = H[0][DIM - 1] + H[DIM - 1][0];
+        eps[5 % VD] = H[0][1] + H[1][0];
+    }
+    if (!GD)
+    {
+        // LinearElastic: C11 = lambda + 2 mu, C12 = lambda, C33 = mu
+        o.s0[0] = static_cast<float>(L.C12) * wdjE;
+        o.s0[1] = static_cast<float>(L.C33) * wdjE;
+        o.s0[2] = o.s0[3] = 0.f;
+        return;
+    }
+    const double kh64 = A.kappa[NG_IDX(e * NIP + q, n * NIP, 55)];
+    const float kh = static_cast<float>(kh64);
+    const float bound = 1.0e-6f * eabs + 1.0e-30f;
+    double e64 = 0.;
+    bool have64 = false;
+    auto eeq64 = [&]() {
+        if (!have64)
+        {
+            double s = 0.;
+            for (int nd = 0; nd < ND; ++nd)
+                s += A.tabN[q * ND + nd] * E64[nd];
+            e64 = s;
+            have64 = true;
+        }
+        return e64;
+    };
+    bool loading;
+    if (fabsf(eeq - kh) > bound + 1.0e-7f * fabsf(kh))
+        loading = eeq >= kh;
+    else
+        loading = eeq64() >= kh64;
+    bool damaged;
+    const float k0f = static_cast<float>(L.kappa0);
+    if (!loading)
+        damaged = kh64 >= L.kappa0;
+    else if (fabsf(eeq - k0f) > bound + 1.0e-7f * k0f)
+        damaged = eeq >= k0f;
+    else
+        damaged = eeq64() >= L.kappa0;
+    const float kap = loading ? (have64 ? static_cast<float>(e64) : eeq) : kh;
+    float omega = 0.f, dOdK = 0.f;
+    if (damaged)
+    {
+        // DamageLawExponential (DamageLawExponential.h:40-52) above kappa0
+        const float al = static_cast<float>(L.alpha), be = static_cast<float>(L.beta);
+        const float ex = expf(be * (k0f - kap));
+        const float r = k0f / kap;
+        omega = 1.f - r * (1.f - al + al * ex);
+        dOdK = r * ((1.f / kap + be) * al * ex + (1.f - al) / kap);
+    }
+    const float dKdE = loading ? 1.f : 0.f;
+    const float gI = InteractionFactor<float>(L, omega);
+    const float dgdw = InteractionDerivative<float>(L, omega);
+    float lam, mu;
+    LedTangentLameParams<float, DIM>(L, eps, omega, lam, mu);
+    float dsdw[VD], dn[VD];
+    LedDstressDomega<float, DIM>(L, eps, dsdw);
+    MisesDerivative<float, DIM>(L, eps, dn);
+    const float f1 = dOdK * dKdE * wdj, f1E = dOdK * dKdE * wdjE;
+#pragma unroll
+    for (int v = 0; v < 6; ++v)
+    {
+        o.sv[v] = v < VD ? dsdw[v < VD ? v : 0] * f1E : 0.f; // (disp, eeq): B^T (dsigma/domega w' k') N
+        o.tv[v] = v < VD ? dn[v < VD ? v : 0] * wdj : 0.f;   // (eeq, disp): -N^T (deps_eq/deps)^T B
+    }
+    const float c = static_cast<float>(L.c);
+    const float sc = c * dgdw * f1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+        o.scge[d] = sc * ge[d];
+    o.s0[0] = lam * wdjE;
+    o.s0[1] = mu * wdjE;
+    o.s0[2] = wdj;
+    o.s0[3] = c * gI * wdj;
+}
+
+template <int DIM, int ND, int NIP, int KIND, bool STAGED, int W>
+__global__ void __launch_bounds__(W * 32, 20 / W)
+        k_tangent_fused(FusedArgs A, LawParams L, const double* __restrict__ u, const float4* __restrict__ recs,
+                        float* __restrict__ vals)
+{
+    using Sh = FusedShape<DIM, ND, NIP, KIND, STAGED, W>;
     constexpr bool GD = Sh::GD;
-    constexpr int CPP = Sh::cpp, NR = Sh::nr, VD = DIM == 2 ? 3 : 6;
+    constexpr int CPP = Sh::cpp, NR = Sh::nr;
     extern __shared__ __align__(16) float smF[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int NDP = ND + 1;                     // padded row length (float4)
@@ -122,7 +339,7 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
         sW[i] = static_cast<float>(A.tabW[i]);
     __syncthreads();
 
-    const int64_t a = static_cast<int64_t>(blockIdx.x) * kFusedWarps + wid;
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * W + wid;
     if (a >= A.nNodes)
         return; // the whole warp leaves; only warp-level synchronisation follows
     int64_t rs[NR];
@@ -156,6 +373,52 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
     for (int64_t kp = k0; kp < k1; kp += CPP)
     {
         __syncwarp();
+        if constexpr (STAGED)
+        {
+            // records of the pass's cells into shared memory (16-byte asynchronous copies, one contiguous block per
+            // cell), then per point the node-a quantities P_a = B_a^T sv and (c g' omega' kappa' w grad eeq) . g_a
+            // in place of the record's coupling vector, so that (B) reads what the fused variant computes
+            constexpr int R4 = Sh::recF4;
+            constexpr int PER_CELL = NIP * R4; // float4 of one cell's records, contiguous in both places
+#pragma unroll
+            for (int cs = 0; cs < CPP; ++cs)
+            {
+                const int64_t kc = kp + cs;
+                if (kc >= k1)
+                    break;
+                const int64_t e = A.cellIdx[kc];
+                const float4* src = recs + NG_IDX(e, n, 58) * PER_CELL;
+                float4* dst = sG + cs * PER_CELL;
+                for (int i = lane; i < PER_CELL; i += 32)
+                {
+                    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(dst + i));
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + i) : "memory");
+                }
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            __syncwarp();
+            if (GD)
+            {
+                const int cs = lane / NIP, q = lane % NIP;
+                const int64_t kc = kp + cs;
+                if (kc < k1)
+                {
+                    const int ia = A.cellLoc[kc];
+                    const float4* row = sG + (cs * NIP + q) * R4;
+                    const float4 ga = row[ia];
+                    float4* S = sG + (cs * NIP + q) * R4 + ND;
+                    const float4 s1 = S[1], s2 = S[2], s4 = S[4];
+                    const float sv[6] = {s4.x, s4.y, s4.z, s4.w, s1.w, s2.w};
+                    const float3 pa = BtV<DIM>(ga.x, ga.y, ga.z, sv);
+                    const float gs = ga.x * s1.x + ga.y * s1.y + (DIM == 3 ? ga.z * s1.z : 0.f);
+                    S[1] = F4(pa.x, pa.y, pa.z, gs);
+                }
+            }
+            __syncwarp();
+        }
+        else
+        {
         // (0) lane (cell slot, node): the node's data of the cell
         {
             const int cs = lane / ND, nd = lane % ND;
@@ -195,209 +458,40 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
             {
                 const int64_t e = A.cellIdx[kc];
                 const int ia = A.cellLoc[kc];
-                const float4* T = sTab + q * NDP;
-                const float4* X = sNodeX + cs * ND;
-                const float4* U = sNodeU + cs * ND;
-                float J[DIM][DIM];
-#pragma unroll
-                for (int i = 0; i < DIM; ++i)
-#pragma unroll
-                    for (int j = 0; j < DIM; ++j)
-                        J[i][j] = 0.f;
-#pragma unroll
-                for (int nd = 0; nd < ND; ++nd)
-                {
-                    const float4 x = X[nd], t = T[nd];
-                    const float xv[3] = {x.x, x.y, x.z}, tv[3] = {t.x, t.y, t.z};
-#pragma unroll
-                    for (int i = 0; i < DIM; ++i)
-#pragma unroll
-                        for (int j = 0; j < DIM; ++j)
-                            J[i][j] += xv[i] * tv[j];
-                }
-                float det, inv[DIM][DIM];
-                if (DIM == 2)
-                {
-                    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-                    const float id = 1.f / det;
-                    inv[0][0] = J[1][1] * id;
-                    inv[0][1] = -J[0][1] * id;
-                    inv[1][0] = -J[1][0] * id;
-                    inv[1][1] = J[0][0] * id;
-                }
-                else
-                {
-                    const float c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-                    const float c10 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-                    const float c20 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-                    det = J[0][0] * c00 + J[0][1] * c10 + J[0][2] * c20;
-                    const float id = 1.f / det;
-                    inv[0][0] = c00 * id;
-                    inv[1][0] = c10 * id;
-                    inv[2][0] = c20 * id;
-                    inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-                    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-                    inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-                    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-                    inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-                    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-                }
-                const float wdj = sW[q] * det;
-                // per-cell Young's modulus factor: scales the material tangent and dsigma/domega
-                const float wdjE = A.escale ? wdj * static_cast<float>(A.escale[e]) : wdj;
-                // node gradients dN/dX = J^-T dN/dxi, displacement gradient, eeq and its gradient
-                float g[ND][DIM], H[DIM][DIM], ge[DIM];
-                float eeq = 0.f, eabs = 0.f;
-#pragma unroll
-                for (int i = 0; i < DIM; ++i)
-                {
-                    ge[i] = 0.f;
-#pragma unroll
-                    for (int j = 0; j < DIM; ++j)
-                        H[i][j] = 0.f;
-                }
+                PointOut<DIM, ND> o;
+                PointData<DIM, ND, NIP, KIND>(A, L, sTab + q * NDP, sW[q], sNodeX + cs * ND, sNodeU + cs * ND,
+                                              sE64 + cs * ND, q, e, o);
                 float4* G = sG + (cs * NIP + q) * NDP;
+                const float4* T = sTab + q * NDP;
 #pragma unroll
                 for (int nd = 0; nd < ND; ++nd)
-                {
-                    const float4 t = T[nd];
-                    const float tv[3] = {t.x, t.y, t.z};
-#pragma unroll
-                    for (int k = 0; k < DIM; ++k)
-                    {
-                        float s = 0.f;
-#pragma unroll
-                        for (int j = 0; j < DIM; ++j)
-                            s += tv[j] * inv[j][k];
-                        g[nd][k] = s;
-                    }
-                    G[nd] = F4(g[nd][0], g[nd][1], DIM == 3 ? g[nd][DIM - 1] : 0.f, t.w);
-                    const float4 uv = U[nd];
-                    const float uc[3] = {uv.x, uv.y, uv.z};
-#pragma unroll
-                    for (int c = 0; c < DIM; ++c)
-#pragma unroll
-                        for (int d = 0; d < DIM; ++d)
-                            H[c][d] += uc[c] * g[nd][d];
-                    if (GD)
-                    {
-                        const float ev = X[nd].w;
-                        eeq += t.w * ev;
-                        eabs += fabsf(t.w * ev);
-#pragma unroll
-                        for (int d = 0; d < DIM; ++d)
-                            ge[d] += ev * g[nd][d];
-                    }
-                }
-                float eps[VD];
-                if (DIM == 2)
-                {
-                    eps[0] = H[0][0];
-                    eps[1] = H[1][1];
-                    eps[2] = H[0][1] + H[1][0];
-                }
-                else
-                {
-                    eps[0] = H[0][0];
-                    eps[1] = H[1][1];
-                    eps[2] = H[DIM - 1][DIM - 1];
-                    eps[3] = H[1][DIM - 1] + H[DIM - 1][1];
-                    eps[4] = H[0][DIM - 1] + H[DIM - 1][0];
-                    eps[5] = H[0][1] + H[1][0];
-                }
-                float gA[DIM]; // node a's gradient (local index ia)
-#pragma unroll
-                for (int d = 0; d < DIM; ++d)
-                {
-                    gA[d] = g[0][d];
-#pragma unroll
-                    for (int nd = 1; nd < ND; ++nd)
-                        gA[d] = nd == ia ? g[nd][d] : gA[d];
-                }
+                    G[nd] = F4(o.g[nd][0], o.g[nd][1], DIM == 3 ? o.g[nd][DIM - 1] : 0.f, T[nd].w);
                 float4* S = sS + (cs * NIP + q) * 5;
-                if (!GD)
+                S[0] = F4(o.s0[0], o.s0[1], o.s0[2], o.s0[3]);
+                if (GD)
                 {
-                    // LinearElastic: C11 = lambda + 2 mu, C12 = lambda, C33 = mu
-                    S[0] = F4(static_cast<float>(L.C12) * wdjE, static_cast<float>(L.C33) * wdjE, 0.f, 0.f);
-                    S[1] = F4(0.f, 0.f, 0.f, 0.f);
-                }
-                else
-                {
-                    // branch decisions of the FP64 kernels: loading (eeq >= kappa_h) and damage (kappa >= kappa0),
-                    // decided in FP32 where the error bound of eeq separates the operands, else in FP64 formed
-                    // as k_tangent<double> forms eeq (same order, FP64 shape values)
-                    const double kh64 = A.kappa[NG_IDX(e * NIP + q, n * NIP, 55)];
-                    const float kh = static_cast<float>(kh64);
-                    const float bound = 1.0e-6f * eabs + 1.0e-30f;
-                    double e64 = 0.;
-                    bool have64 = false;
-                    auto eeq64 = [&]() {
-                        if (!have64)
-                        {
-                            double s = 0.;
-                            for (int nd = 0; nd < ND; ++nd)
-                                s += A.tabN[q * ND + nd] * sE64[cs * ND + nd];
-                            e64 = s;
-                            have64 = true;
-                        }
-                        return e64;
-                    };
-                    bool loading;
-                    if (fabsf(eeq - kh) > bound + 1.0e-7f * fabsf(kh))
-                        loading = eeq >= kh;
-                    else
-                        loading = eeq64() >= kh64;
-                    bool damaged;
-                    const float k0f = static_cast<float>(L.kappa0);
-                    if (!loading)
-                        damaged = kh64 >= L.kappa0;
-                    else if (fabsf(eeq - k0f) > bound + 1.0e-7f * k0f)
-                        damaged = eeq >= k0f;
-                    else
-                        damaged = eeq64() >= L.kappa0;
-                    const float kap = loading ? (have64 ? static_cast<float>(e64) : eeq) : kh;
-                    float omega = 0.f, dOdK = 0.f;
-                    if (damaged)
-                    {
-                        // DamageLawExponential (DamageLawExponential.h:40-52) above kappa0
-                        const float al = static_cast<float>(L.alpha), be = static_cast<float>(L.beta);
-                        const float ex = expf(be * (k0f - kap));
-                        const float r = k0f / kap;
-                        omega = 1.f - r * (1.f - al + al * ex);
-                        dOdK = r * ((1.f / kap + be) * al * ex + (1.f - al) / kap);
-                    }
-                    const float dKdE = loading ? 1.f : 0.f;
-                    const float gI = InteractionFactor<float>(L, omega);
-                    const float dgdw = InteractionDerivative<float>(L, omega);
-                    float lam, mu;
-                    LedTangentLameParams<float, DIM>(L, eps, omega, lam, mu);
-                    float dsdw[VD], dn[VD], sv[VD], tvv[VD];
-                    LedDstressDomega<float, DIM>(L, eps, dsdw);
-                    MisesDerivative<float, DIM>(L, eps, dn);
-                    const float f1 = dOdK * dKdE * wdj;
-                    const float f1E = dOdK * dKdE * wdjE;
+                    float gA[DIM]; // node a's gradient (local index ia)
 #pragma unroll
-                    for (int v = 0; v < VD; ++v)
+                    for (int d = 0; d < DIM; ++d)
                     {
-                        sv[v] = dsdw[v] * f1E; // (disp, eeq): B^T (dsigma/domega w' k') N
-                        tvv[v] = dn[v] * wdj; // (eeq, disp): -N^T (deps_eq/deps)^T B
+                        gA[d] = o.g[0][d];
+#pragma unroll
+                        for (int nd = 1; nd < ND; ++nd)
+                            gA[d] = nd == ia ? o.g[nd][d] : gA[d];
                     }
-                    const float c = static_cast<float>(L.c);
-                    const float sc = c * dgdw * f1;
                     float gs = 0.f;
 #pragma unroll
                     for (int d = 0; d < DIM; ++d)
-                        gs += gA[d] * ge[d];
-                    const float3 pa = BtV<DIM>(gA[0], gA[1], DIM == 3 ? gA[DIM - 1] : 0.f, sv);
-                    S[0] = F4(lam * wdjE, mu * wdjE, wdj, c * gI * wdj);
-                    S[1] = F4(pa.x, pa.y, pa.z, sc * gs);
-                    S[2] = F4(tvv[0], tvv[1], tvv[2], 0.f);
-                    S[3] = F4(VD > 3 ? tvv[VD > 3 ? 3 : 0] : 0.f, VD > 4 ? tvv[VD > 4 ? 4 : 0] : 0.f,
-                              VD > 5 ? tvv[VD > 5 ? 5 : 0] : 0.f, 0.f);
+                        gs += gA[d] * o.scge[d];
+                    const float3 pa = BtV<DIM>(gA[0], gA[1], DIM == 3 ? gA[DIM - 1] : 0.f, o.sv);
+                    S[1] = F4(pa.x, pa.y, pa.z, gs);
+                    S[2] = F4(o.tv[0], o.tv[1], o.tv[2], 0.f);
+                    S[3] = F4(o.tv[3], o.tv[4], o.tv[5], 0.f);
                 }
             }
         }
         __syncwarp();
+        }
         // (B) lane (cell slot, neighbour b): the node-pair block (a, b) integrated over the points, added into a's
         // rows at the ranks of b
         {
@@ -430,9 +524,11 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
 #pragma unroll 2
                 for (int q = 0; q < NIP; ++q)
                 {
-                    const float4* G = sG + (cs * NIP + q) * NDP;
+                    // gradients and scalars of point q: one record row (staged) or the padded arrays (fused)
+                    const float4* G = STAGED ? sG + (cs * NIP + q) * Sh::recF4 : sG + (cs * NIP + q) * NDP;
+                    const float4* SR = STAGED ? G + ND : sS + (cs * NIP + q) * 5;
                     const float4 ga = G[ia], gb = G[b];
-                    const float4 s0 = sS[(cs * NIP + q) * 5];
+                    const float4 s0 = SR[0];
                     const float av[3] = {ga.x, ga.y, ga.z}, bv[3] = {gb.x, gb.y, gb.z};
                     float gab = 0.f;
 #pragma unroll
@@ -450,8 +546,8 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
                     dg += s0.y * gab;
                     if (GD)
                     {
-                        const float4 s1 = sS[(cs * NIP + q) * 5 + 1];
-                        const float4 t0 = sS[(cs * NIP + q) * 5 + 2], t1 = sS[(cs * NIP + q) * 5 + 3];
+                        const float4 s1 = SR[1];
+                        const float4 t0 = SR[2], t1 = SR[3];
                         const float tv[6] = {t0.x, t0.y, t0.z, t1.x, t1.y, t1.z};
                         const float3 qb = BtV<DIM>(gb.x, gb.y, gb.z, tv); // B_b^T t
                         const float pv[3] = {s1.x, s1.y, s1.z}, qv[3] = {qb.x, qb.y, qb.z};
@@ -501,6 +597,82 @@ __global__ void __launch_bounds__(kFusedWarps * 32)
     for (int k = 0; k < NR; ++k)
         for (int i = lane; i < len[k]; i += 32)
             vals[NG_IDX(rs[k] + i, A.nnz, 57)] = sRow[k * kFusedRowCap + i];
+}
+
+// Per-point records of the staged tangent: one thread per (cell, integration point) evaluates PointData once and
+// writes ND float4 (dN/dX, N) and the scalars (gradient damage: lambda w, mu w, w, c g w | c g' w' k' w grad eeq,
+// sv4 | tv0..2, sv5 | tv3..5 | sv0..3) contiguously per cell. The node data of a block's cells are loaded once into
+// shared memory by one thread per (cell, node).
+template <int DIM, int ND, int NIP, int KIND>
+__global__ void __launch_bounds__(128) k_point_records(FusedArgs A, LawParams L, const double* __restrict__ u,
+                                                      float4* __restrict__ recs)
+{
+    constexpr bool GD = KIND == NUTO_GPU_GRADIENT_DAMAGE;
+    constexpr int CPB = 128 / NIP; // cells per block
+    constexpr int R4 = FusedShape<DIM, ND, NIP, KIND, true>::recF4;
+    static_assert(CPB * ND <= 128, "one thread per (cell, node)");
+    __shared__ float4 sX[CPB][ND], sU[CPB][ND];
+    __shared__ double sE[GD ? CPB : 1][ND];
+    __shared__ float4 sT[NIP][ND];
+    __shared__ float sWq[NIP];
+    const int64_t n = A.nCells;
+    const int64_t cell0 = static_cast<int64_t>(blockIdx.x) * CPB;
+    for (int i = threadIdx.x; i < NIP * ND; i += blockDim.x)
+    {
+        const int q = i / ND, nd = i % ND;
+        const double* d = A.tabDN + (q * ND + nd) * 3;
+        sT[q][nd] = F4(static_cast<float>(d[0]), static_cast<float>(d[1]), DIM == 3 ? static_cast<float>(d[2]) : 0.f,
+                       static_cast<float>(A.tabN[q * ND + nd]));
+    }
+    for (int i = threadIdx.x; i < NIP; i += blockDim.x)
+        sWq[i] = static_cast<float>(A.tabW[i]);
+    if (threadIdx.x < CPB * ND)
+    {
+        const int cl = threadIdx.x / ND, nd = threadIdx.x % ND;
+        const int64_t e = cell0 + cl;
+        if (e < n)
+        {
+            const int32_t nD = static_cast<int32_t>(NG_IDX(A.connD[static_cast<int64_t>(nd) * n + e], A.nNodesD, 51));
+            const int64_t gd = A.gdofD[nD];
+            float x[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+            {
+                x[d] = A.relX[(static_cast<int64_t>(nd) * DIM + d) * n + e];
+                v[d] = static_cast<float>(u[NG_IDX(gd + d, A.nDofs, 52)]);
+            }
+            float ev = 0.f;
+            if (GD)
+            {
+                const int32_t nE =
+                        static_cast<int32_t>(NG_IDX(A.connE[static_cast<int64_t>(nd) * n + e], A.nNodesE, 53));
+                const double e64 = u[NG_IDX(A.gdofE[nE], A.nDofs, 54)];
+                sE[cl][nd] = e64;
+                ev = static_cast<float>(e64);
+            }
+            sX[cl][nd] = F4(x[0], x[1], x[2], ev);
+            sU[cl][nd] = F4(v[0], v[1], v[2], 0.f);
+        }
+    }
+    __syncthreads();
+    const int cl = threadIdx.x / NIP, q = threadIdx.x % NIP;
+    const int64_t e = cell0 + cl;
+    if (cl >= CPB || e >= n)
+        return;
+    PointOut<DIM, ND> o;
+    PointData<DIM, ND, NIP, KIND>(A, L, sT[q], sWq[q], sX[cl], sU[cl], GD ? sE[cl] : nullptr, q, e, o);
+    float4* r = recs + (e * NIP + q) * R4;
+#pragma unroll
+    for (int nd = 0; nd < ND; ++nd)
+        r[nd] = F4(o.g[nd][0], o.g[nd][1], DIM == 3 ? o.g[nd][DIM - 1] : 0.f, sT[q][nd].w);
+    r[ND] = F4(o.s0[0], o.s0[1], o.s0[2], o.s0[3]);
+    if (GD)
+    {
+        r[ND + 1] = F4(o.scge[0], o.scge[1], DIM == 3 ? o.scge[DIM - 1] : 0.f, o.sv[4]);
+        r[ND + 2] = F4(o.tv[0], o.tv[1], o.tv[2], o.sv[5]);
+        r[ND + 3] = F4(o.tv[3], o.tv[4], o.tv[5], 0.f);
+        r[ND + 4] = F4(o.sv[0], o.sv[1], o.sv[2], o.sv[3]);
+    }
 }
 
 } // namespace
@@ -595,22 +767,99 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
         A.rank[k] = c.pairs[pr[k]].rank;
         A.blk[k] = c.pairs[pr[k]].dBlk.p;
     }
-    const unsigned blocks = static_cast<unsigned>((A.nNodes + kFusedWarps - 1) / kFusedWarps);
-    auto launch = [&](auto kern, size_t smem) {
-        if (smem > 48 * 1024)
-            NG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-        kern<<<blocks, kFusedWarps * 32, smem, c.stream>>>(A, c.law, u, vals);
+    const bool staged = c.tangentStaged;
+    // one assembly with W warps per block of the node-row kernel
+    auto assemble = [&](int W) {
+        auto run = [&](auto cfg) {
+            using C = decltype(cfg);
+            constexpr int DIM = C::dim, ND = C::nd, NIP = C::nip, KIND = C::kind;
+            float4* recs = nullptr;
+            if (staged)
+            {
+                const size_t bytes =
+                        static_cast<size_t>(c.nCells) * NIP * FusedShape<DIM, ND, NIP, KIND, true>::recF4 * 16;
+                if (c.dRecords.n < bytes)
+                    c.dRecords.alloc(bytes);
+                recs = reinterpret_cast<float4*>(c.dRecords.p);
+                k_point_records<DIM, ND, NIP, KIND>
+                        <<<static_cast<unsigned>((c.nCells + 128 / NIP - 1) / (128 / NIP)), 128, 0, c.stream>>>(
+                                A, c.law, u, recs);
+                AfterLaunch(c, "k_point_records");
+                c.stats.kernel_launches += 1;
+            }
+            auto rows = [&](auto w) {
+                constexpr int WW = decltype(w)::value;
+                const unsigned blocks = static_cast<unsigned>((A.nNodes + WW - 1) / WW);
+                auto launch = [&](auto kern, size_t smem) {
+                    if (smem > 48 * 1024)
+                        NG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     static_cast<int>(smem)));
+                    kern<<<blocks, WW * 32, smem, c.stream>>>(A, c.law, u, recs, vals);
+                };
+                if (staged)
+                    launch(k_tangent_fused<DIM, ND, NIP, KIND, true, WW>,
+                           FusedShape<DIM, ND, NIP, KIND, true, WW>::smem);
+                else
+                    launch(k_tangent_fused<DIM, ND, NIP, KIND, false, WW>,
+                           FusedShape<DIM, ND, NIP, KIND, false, WW>::smem);
+                AfterLaunch(c, "k_tangent_fused");
+                c.stats.kernel_launches += 1;
+            };
+            if (W == 2)
+                rows(std::integral_constant<int, 2>{});
+            else if (W == 8)
+                rows(std::integral_constant<int, 8>{});
+            else
+                rows(std::integral_constant<int, 4>{});
+        };
+        if (c.dim == 3 && gd)
+            run(FCfg<3, 8, 8, NUTO_GPU_GRADIENT_DAMAGE>{});
+        else if (c.dim == 3)
+            run(FCfg<3, 8, 8, NUTO_GPU_MB_LINEAR_ELASTIC>{});
+        else if (gd)
+            run(FCfg<2, 4, 4, NUTO_GPU_GRADIENT_DAMAGE>{});
+        else
+            run(FCfg<2, 4, 4, NUTO_GPU_MB_LINEAR_ELASTIC>{});
     };
-    if (c.dim == 3 && gd)
-        launch(k_tangent_fused<3, 8, 8, NUTO_GPU_GRADIENT_DAMAGE>, FusedShape<3, 8, 8, NUTO_GPU_GRADIENT_DAMAGE>::smem);
-    else if (c.dim == 3)
-        launch(k_tangent_fused<3, 8, 8, NUTO_GPU_MB_LINEAR_ELASTIC>, FusedShape<3, 8, 8, NUTO_GPU_MB_LINEAR_ELASTIC>::smem);
-    else if (gd)
-        launch(k_tangent_fused<2, 4, 4, NUTO_GPU_GRADIENT_DAMAGE>, FusedShape<2, 4, 4, NUTO_GPU_GRADIENT_DAMAGE>::smem);
-    else
-        launch(k_tangent_fused<2, 4, 4, NUTO_GPU_MB_LINEAR_ELASTIC>, FusedShape<2, 4, 4, NUTO_GPU_MB_LINEAR_ELASTIC>::smem);
-    AfterLaunch(c, "k_tangent_fused");
-    c.stats.kernel_launches += 1;
+    // autotuner: the first FP32 tangent of a context (outside any stream capture) assembles once with 2, 4 and 8
+    // warps per block (a warm-up and a timed assembly each; every one writes the same values) and keeps the fastest
+    Tuning& T = c.tuning;
+    if (T.tangentWarps == 0)
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        NG_CUDA(cudaStreamIsCapturing(c.stream, &cs));
+        if (!T.enabled)
+            T.tangentWarps = 4;
+        else if (cs == cudaStreamCaptureStatusNone)
+        {
+            const int cand[3] = {2, 4, 8};
+            cudaEvent_t e0, e1;
+            NG_CUDA(cudaEventCreate(&e0));
+            NG_CUDA(cudaEventCreate(&e1));
+            float best = 0.f;
+            int pick = 4;
+            for (int k = 0; k < 3; ++k)
+            {
+                assemble(cand[k]);
+                NG_CUDA(cudaEventRecord(e0, c.stream));
+                assemble(cand[k]);
+                NG_CUDA(cudaEventRecord(e1, c.stream));
+                NG_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                NG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                T.tangentMs[k] = ms;
+                if (k == 0 || ms < best)
+                {
+                    best = ms;
+                    pick = cand[k];
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            T.tangentWarps = pick;
+        }
+    }
+    assemble(T.tangentWarps ? T.tangentWarps : 4);
 }
 
 } // namespace nuto_gpu

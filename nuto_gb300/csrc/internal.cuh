@@ -313,6 +313,16 @@ struct HostClock
     }
 };
 
+// Launch shapes chosen by the autotuner (first use per context, timed with CUDA events; 0 = not tuned yet)
+struct Tuning
+{
+    bool enabled = true;             // NUTO_GPU_AUTOTUNE=0 keeps the defaults
+    int tangentWarps = 0;            // warps per block of the FP32 tangent's node-row kernel (2, 4, 8)
+    float tangentMs[3] = {0, 0, 0};  // one assembly with 2, 4, 8 warps per block
+    int spmvGroup[4] = {0, 0, 0, 0}; // lanes per node of the fine-level product, per (value, vector) type pair
+    float spmvMs[4][3] = {};         // one product with 4, 8, 16 lanes per node
+};
+
 struct Ctx
 {
     int device = 0;
@@ -370,7 +380,9 @@ struct Ctx
     DBuf<unsigned char> dRecords;
     // fused FP32 tangent: -1 not decided, 0 not applicable, 1 used; FP32 node coordinates relative to each cell's
     // first node (planar [(n * dim + d)][cell])
+    Tuning tuning;
     int fusedMode = -1;
+    bool tangentStaged = true; // per-point records computed once (NUTO_GPU_TANGENT=fused: recomputed per node warp)
     DBuf<float> dRelX;
     // residual: the cell vectors of the last residual (planar [local entry][cell]) gathered per DOF
     DBuf<double> dCellVec;

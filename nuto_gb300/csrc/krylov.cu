@@ -474,11 +474,59 @@ void EnsureNb(Ctx& c, const TV* vals)
 template void EnsureNb<float>(Ctx&, const float*);
 template void EnsureNb<double>(Ctx&, const double*);
 
+// Autotuner of the fine-level product: the first product of a context with a given value and vector type (outside
+// any stream capture) times the padded-layout kernel with 4, 8 and 16 lanes per node (one warm-up and one timed
+// launch each, y = K x without dot products, so the tuning launches only write the y the real call writes again)
+// and keeps the fastest; NUTO_GPU_AUTOTUNE=0 keeps the default.
+template <typename TV, typename TX>
+static int SpmvGroup(Ctx& c, const NodeSpmv& A, const TV* vals, const TX* x, TX* y, const uint8_t* mask)
+{
+    const int key = (sizeof(TV) == 4 ? 0 : 2) + (sizeof(TX) == 4 ? 0 : 1);
+    Tuning& T = c.tuning;
+    if (T.spmvGroup[key] > 0)
+        return T.spmvGroup[key];
+    if (!T.enabled || !SpmvPadded(A, vals))
+        return 0;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    NG_CUDA(cudaStreamIsCapturing(c.stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+        return 0;
+    const int cand[3] = {4, 8, 16};
+    cudaEvent_t e0, e1;
+    NG_CUDA(cudaEventCreate(&e0));
+    NG_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    int pick = kNbG;
+    for (int k = 0; k < 3; ++k)
+    {
+        SpmvNode<TV, TX, 0>(c.stream, A, vals, x, y, nullptr, nullptr, nullptr, FIN_NONE, mask, cand[k]);
+        NG_CUDA(cudaEventRecord(e0, c.stream));
+        SpmvNode<TV, TX, 0>(c.stream, A, vals, x, y, nullptr, nullptr, nullptr, FIN_NONE, mask, cand[k]);
+        NG_CUDA(cudaEventRecord(e1, c.stream));
+        NG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        NG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        T.spmvMs[key][k] = ms;
+        if (k == 0 || ms < best)
+        {
+            best = ms;
+            pick = cand[k];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c.stats.kernel_launches += 6;
+    T.spmvGroup[key] = pick;
+    return pick;
+}
+
 template <typename TV, typename TX, int NDOT>
 static void SpmvLaunch(Ctx& c, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc, int* st, int fin,
                        const uint8_t* mask)
 {
-    SpmvNode<TV, TX, NDOT>(c.stream, MakeNodeSpmv(c), vals, x, y, w0, sc, st, fin, mask);
+    const NodeSpmv A = MakeNodeSpmv(c);
+    const int g = SpmvGroup<TV, TX>(c, A, vals, x, y, mask);
+    SpmvNode<TV, TX, NDOT>(c.stream, A, vals, x, y, w0, sc, st, fin, mask, g);
 }
 
 // Krylov SpMV with a CUDA-event pair around it (device time of the dominant kernel, collected by SpmvCollect)

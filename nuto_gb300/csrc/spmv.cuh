@@ -474,16 +474,25 @@ __global__ void __launch_bounds__(kBS) k_nb_pack(NodeSpmv A, const TV* __restric
 
 // Launches the padded-layout kernel when the view has the layout and it holds `vals` (the CSR values the caller
 // passes), the CSR kernel otherwise.
-template <typename TV, typename TX, int NDOT>
-void SpmvNode(cudaStream_t stream, const NodeSpmv& A, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc,
-              int* st, int fin, const uint8_t* mask)
+// true when the view has the padded layout and it holds `vals` (the lanes-per-node choice applies)
+template <typename TV>
+inline bool SpmvPadded(const NodeSpmv& A, const TV* vals)
 {
     const void* src = sizeof(TV) == 4 ? A.nbSrc32 : A.nbSrc64;
-    if (A.nbBase[0] && src == static_cast<const void*>(vals) && A.nbSeg4 > 0)
+    return A.nbBase[0] && src == static_cast<const void*>(vals) && A.nbSeg4 > 0;
+}
+
+// group: lanes per node of the padded-layout kernel (4, 8 or 16; 0 = the default: 8, or 4 for views of
+// single-component rows and columns)
+template <typename TV, typename TX, int NDOT>
+void SpmvNode(cudaStream_t stream, const NodeSpmv& A, const TV* vals, const TX* x, TX* y, const TX* w0, double* sc,
+              int* st, int fin, const uint8_t* mask, int group = 0)
+{
+    if (SpmvPadded(A, vals))
     {
         // 8 lanes per node; 4 for views of single-component rows and columns (one short segment per node)
         const bool narrow = A.ns == 1 && A.ncMaxRows == 1;
-        const int G = narrow ? 4 : kNbG;
+        const int G = group ? group : (narrow ? 4 : kNbG);
         const size_t perGroup = static_cast<size_t>(A.nbSeg4) * sizeof(TX);
         int threads = kBS;
         while (threads > 32 && (threads / G) * perGroup > 48 * 1024)
@@ -491,8 +500,11 @@ void SpmvNode(cudaStream_t stream, const NodeSpmv& A, const TV* vals, const TX* 
         const int64_t total = A.totalWarps * G;
         const unsigned blocks = static_cast<unsigned>((total + threads - 1) / threads);
         const size_t smem = (threads / G) * perGroup;
-        if (narrow)
+        if (G == 4)
             NG_CUDA(LaunchPdl(k_spmv_nb<TV, TX, NDOT, 4>, blocks, threads, smem, stream, A, mask, x, y, w0, sc, st,
+                              fin));
+        else if (G == 16)
+            NG_CUDA(LaunchPdl(k_spmv_nb<TV, TX, NDOT, 16>, blocks, threads, smem, stream, A, mask, x, y, w0, sc, st,
                               fin));
         else
             NG_CUDA(LaunchPdl(k_spmv_nb<TV, TX, NDOT, kNbG>, blocks, threads, smem, stream, A, mask, x, y, w0, sc, st,
