@@ -113,15 +113,17 @@ class GpuCellGroup:
         return lv.value, ga.value
 
     def autotune_info(self):
-        """Launch shapes the autotuner chose and the times it measured: {"tangent_warps": W, "tangent_ms": [2, 4, 8
-        warps], "spmv_lanes": {"f32/f32": G, ...}, "spmv_ms": {"f32/f32": [4, 8, 16 lanes], ...}} (0: not tuned)."""
-        ch = np.zeros(5, dtype=np.int32)
-        ms = np.zeros(15, dtype=np.float32)
+        """Launch shapes the autotuner chose and the times it measured: {"tangent_warps": W, "tangent_pipelined": bool,
+        "tangent_ms": [2, 4, 8 warps], "tangent_pipelined_ms": [2, 4 warps], "spmv_lanes": {"f32/f32": G, ...},
+        "spmv_ms": {"f32/f32": [4, 8, 16 lanes], ...}} (0: not tuned)."""
+        ch = np.zeros(6, dtype=np.int32)
+        ms = np.zeros(17, dtype=np.float32)
         self._call("nuto_gpu_autotune_info", _ptr(ch), _ptr(ms))
         names = ["f32/f32", "f32/f64", "f64/f32", "f64/f64"]
-        return {"tangent_warps": int(ch[0]), "tangent_ms": [float(v) for v in ms[:3]],
-                "spmv_lanes": {k: int(ch[1 + i]) for i, k in enumerate(names)},
-                "spmv_ms": {k: [float(v) for v in ms[3 + 3 * i:6 + 3 * i]] for i, k in enumerate(names)}}
+        return {"tangent_warps": int(ch[0]), "tangent_pipelined": bool(ch[1]),
+                "tangent_ms": [float(v) for v in ms[:3]], "tangent_pipelined_ms": [float(v) for v in ms[3:5]],
+                "spmv_lanes": {k: int(ch[2 + i]) for i, k in enumerate(names)},
+                "spmv_ms": {k: [float(v) for v in ms[5 + 3 * i:8 + 3 * i]] for i, k in enumerate(names)}}
 
     def solver_layout(self):
         """(padded values, neighbour-list entries) of the solver's copy of the tangent"""

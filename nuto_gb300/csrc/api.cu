@@ -591,6 +591,11 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
     c->forceAtomicTangent = tk && std::string(tk) == "atomic";
     c->forceRecordTangent = tk && std::string(tk) == "records";
     c->tangentStaged = !(tk && std::string(tk) == "fused");
+    if (tk && std::string(tk) == "pipelined")
+    {
+        c->tuning.tangentWarps = 4; // the double-buffered node-row kernel, not tuned
+        c->tuning.tangentPipe = true;
+    }
     const char* at = std::getenv("NUTO_GPU_AUTOTUNE");
     c->tuning.enabled = !(at && at[0] == '0');
     const char* gr = std::getenv("NUTO_GPU_GMRES_RESTART");
@@ -876,16 +881,17 @@ int nuto_gpu_autotune_info(const nuto_gpu_ctx* ctx, int* choices, float* times_m
     if (choices)
     {
         choices[0] = T.tangentWarps;
+        choices[1] = T.tangentPipe ? 1 : 0;
         for (int k = 0; k < 4; ++k)
-            choices[1 + k] = T.spmvGroup[k];
+            choices[2 + k] = T.spmvGroup[k];
     }
     if (times_ms)
     {
-        for (int k = 0; k < 3; ++k)
+        for (int k = 0; k < 5; ++k)
             times_ms[k] = T.tangentMs[k];
         for (int p = 0; p < 4; ++p)
             for (int k = 0; k < 3; ++k)
-                times_ms[3 + 3 * p + k] = T.spmvMs[p][k];
+                times_ms[5 + 3 * p + k] = T.spmvMs[p][k];
     }
     return NUTO_GPU_OK;
 }

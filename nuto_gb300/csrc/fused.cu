@@ -22,6 +22,7 @@
 // and damage-threshold branches therefore agree with the FP64 residual at every point; everything else is FP32.
 #include "internal.cuh"
 
+#include <algorithm>
 #include <type_traits>
 
 namespace nuto_gpu
@@ -308,6 +309,176 @@ __device__ __forceinline__ void PointData(const FusedArgs& A, const LawParams& L
     o.s0[3] = c * gI * wdj;
 }
 
+// Copies the records of the pass's cells (cells kp .. min(kp + CPP, k1) of the node's list) into the warp's buffer
+// with 16-byte asynchronous copies, one contiguous block per cell, and commits them as one group.
+template <int DIM, int ND, int NIP, int KIND>
+__device__ __forceinline__ void StageRecords(const FusedArgs& A, const float4* __restrict__ recs, float4* sBuf,
+                                             int64_t kp, int64_t k1, int lane)
+{
+    using Sh = FusedShape<DIM, ND, NIP, KIND, true>;
+    constexpr int CPP = Sh::cpp;
+    const int64_t n = A.nCells; // the records' extent in checked builds
+    (void)n;
+    float4* sG = sBuf;
+    constexpr int R4 = Sh::recF4;
+    constexpr int PER_CELL = NIP * R4; // float4 of one cell's records, contiguous in both places
+#pragma unroll
+    for (int cs = 0; cs < CPP; ++cs)
+    {
+        const int64_t kc = kp + cs;
+        if (kc >= k1)
+            break;
+        const int64_t e = A.cellIdx[kc];
+        const float4* src = recs + NG_IDX(e, n, 58) * PER_CELL;
+        float4* dst = sG + cs * PER_CELL;
+        for (int i = lane; i < PER_CELL; i += 32)
+        {
+            const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(dst + i));
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + i) : "memory");
+        }
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// Per point of the staged pass, the node-a quantities P_a = B_a^T sv and (c g' omega' kappa' w grad eeq) . g_a in
+// place of the record's coupling vector, so that PassBlocks reads what the fused variant computes.
+template <int DIM, int ND, int NIP, int KIND>
+__device__ __forceinline__ void PrepRecords(const FusedArgs& A, float4* sG, int64_t kp, int64_t k1, int lane)
+{
+    constexpr bool GD = KIND == NUTO_GPU_GRADIENT_DAMAGE;
+    constexpr int R4 = FusedShape<DIM, ND, NIP, KIND, true>::recF4;
+    if (GD)
+    {
+        const int cs = lane / NIP, q = lane % NIP;
+        const int64_t kc = kp + cs;
+        if (kc < k1)
+        {
+            const int ia = A.cellLoc[kc];
+            const float4* row = sG + (cs * NIP + q) * R4;
+            const float4 ga = row[ia];
+            float4* S = sG + (cs * NIP + q) * R4 + ND;
+            const float4 s1 = S[1], s2 = S[2], s4 = S[4];
+            const float sv[6] = {s4.x, s4.y, s4.z, s4.w, s1.w, s2.w};
+            const float3 pa = BtV<DIM>(ga.x, ga.y, ga.z, sv);
+            const float gs = ga.x * s1.x + ga.y * s1.y + (DIM == 3 ? ga.z * s1.z : 0.f);
+            S[1] = F4(pa.x, pa.y, pa.z, gs);
+        }
+    }
+}
+
+// (B) of one pass: lane (cell slot, neighbour b) integrates the node-pair block (a, b) over the points and adds it
+// into a's rows (sRow) at the ranks of b, one cell slot after the other. sG / sS: the pass's per-point data in the
+// staged (record rows) or fused (padded arrays) layout.
+template <int DIM, int ND, int NIP, int KIND, bool STAGED>
+__device__ __forceinline__ void PassBlocks(const FusedArgs& A, const float4* sG, const float4* sS, float* sRow,
+                                           int64_t kp, int64_t k1, int lane, int32_t bUU, int32_t bUE, int32_t bEU,
+                                           int32_t bEE)
+{
+    using Sh = FusedShape<DIM, ND, NIP, KIND, STAGED>;
+    constexpr bool GD = Sh::GD;
+    constexpr int CPP = Sh::cpp, NDP = ND + 1;
+    const int64_t n = A.nCells;
+    // (B) lane (cell slot, neighbour b): the node-pair block (a, b) integrated over the points, added into a's
+    // rows at the ranks of b
+    {
+        const int cs = lane / ND, b = lane % ND;
+        const int64_t kc = kp + cs;
+        float uu[DIM][DIM], ue[DIM], eu[DIM], ee = 0.f, dg = 0.f;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            ue[k] = eu[k] = 0.f;
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                uu[k][l] = 0.f;
+        }
+        int r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+        bool active = false;
+        if (kc < k1)
+        {
+            const int64_t e = A.cellIdx[kc];
+            const int ia = A.cellLoc[kc];
+            // ranks of b in a's neighbour lists (loaded first: their latency overlaps the integration)
+            const int64_t ridx = static_cast<int64_t>(ia * ND + b) * n + e;
+            r0 = A.rank[0][ridx];
+            if (GD)
+            {
+                r1 = A.rank[1][ridx];
+                r2 = A.rank[2][ridx];
+                r3 = A.rank[3][ridx];
+            }
+#pragma unroll 2
+            for (int q = 0; q < NIP; ++q)
+            {
+                // gradients and scalars of point q: one record row (staged) or the padded arrays (fused)
+                const float4* G = STAGED ? sG + (cs * NIP + q) * Sh::recF4 : sG + (cs * NIP + q) * NDP;
+                const float4* SR = STAGED ? G + ND : sS + (cs * NIP + q) * 5;
+                const float4 ga = G[ia], gb = G[b];
+                const float4 s0 = SR[0];
+                const float av[3] = {ga.x, ga.y, ga.z}, bv[3] = {gb.x, gb.y, gb.z};
+                float gab = 0.f;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    gab += av[d] * bv[d];
+                // lambda w g_a g_b^T + mu w (g_b g_a^T + (g_a . g_b) I)
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                {
+                    const float lk = s0.x * av[k], mk = s0.y * bv[k];
+#pragma unroll
+                    for (int l = 0; l < DIM; ++l)
+                        uu[k][l] += lk * bv[l] + mk * av[l];
+                }
+                dg += s0.y * gab;
+                if (GD)
+                {
+                    const float4 s1 = SR[1];
+                    const float4 t0 = SR[2], t1 = SR[3];
+                    const float tv[6] = {t0.x, t0.y, t0.z, t1.x, t1.y, t1.z};
+                    const float3 qb = BtV<DIM>(gb.x, gb.y, gb.z, tv); // B_b^T t
+                    const float pv[3] = {s1.x, s1.y, s1.z}, qv[3] = {qb.x, qb.y, qb.z};
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k)
+                    {
+                        ue[k] += pv[k] * gb.w;
+                        eu[k] -= ga.w * qv[k];
+                    }
+                    ee += (s0.z * ga.w + s1.w) * gb.w + s0.w * gab;
+                }
+            }
+            active = true;
+        }
+        // the cells of a pass can share b: their blocks are added one cell slot after the other (the b of one
+        // cell are distinct nodes, so the 8 lanes of a slot write distinct positions); fixed order, no atomics
+#pragma unroll
+        for (int r = 0; r < CPP; ++r)
+        {
+            if (active && cs == r)
+            {
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                {
+                    float* row = sRow + k * kFusedRowCap;
+#pragma unroll
+                    for (int l = 0; l < DIM; ++l)
+                        row[NG_IDX(bUU + DIM * r0 + l, kFusedRowCap, 56)] += uu[k][l] + (k == l ? dg : 0.f);
+                    if (GD)
+                        row[NG_IDX(bUE + r1, kFusedRowCap, 56)] += ue[k];
+                }
+                if (GD)
+                {
+                    float* row = sRow + DIM * kFusedRowCap;
+#pragma unroll
+                    for (int l = 0; l < DIM; ++l)
+                        row[NG_IDX(bEU + DIM * r2 + l, kFusedRowCap, 56)] += eu[l];
+                    row[NG_IDX(bEE + r3, kFusedRowCap, 56)] += ee;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
 template <int DIM, int ND, int NIP, int KIND, bool STAGED, int W>
 __global__ void __launch_bounds__(W * 32, 20 / W)
         k_tangent_fused(FusedArgs A, LawParams L, const double* __restrict__ u, const float4* __restrict__ recs,
@@ -375,46 +546,10 @@ __global__ void __launch_bounds__(W * 32, 20 / W)
         __syncwarp();
         if constexpr (STAGED)
         {
-            // records of the pass's cells into shared memory (16-byte asynchronous copies, one contiguous block per
-            // cell), then per point the node-a quantities P_a = B_a^T sv and (c g' omega' kappa' w grad eeq) . g_a
-            // in place of the record's coupling vector, so that (B) reads what the fused variant computes
-            constexpr int R4 = Sh::recF4;
-            constexpr int PER_CELL = NIP * R4; // float4 of one cell's records, contiguous in both places
-#pragma unroll
-            for (int cs = 0; cs < CPP; ++cs)
-            {
-                const int64_t kc = kp + cs;
-                if (kc >= k1)
-                    break;
-                const int64_t e = A.cellIdx[kc];
-                const float4* src = recs + NG_IDX(e, n, 58) * PER_CELL;
-                float4* dst = sG + cs * PER_CELL;
-                for (int i = lane; i < PER_CELL; i += 32)
-                {
-                    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(dst + i));
-                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + i) : "memory");
-                }
-            }
-            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            StageRecords<DIM, ND, NIP, KIND>(A, recs, sG, kp, k1, lane);
             asm volatile("cp.async.wait_group 0;\n" ::: "memory");
             __syncwarp();
-            if (GD)
-            {
-                const int cs = lane / NIP, q = lane % NIP;
-                const int64_t kc = kp + cs;
-                if (kc < k1)
-                {
-                    const int ia = A.cellLoc[kc];
-                    const float4* row = sG + (cs * NIP + q) * R4;
-                    const float4 ga = row[ia];
-                    float4* S = sG + (cs * NIP + q) * R4 + ND;
-                    const float4 s1 = S[1], s2 = S[2], s4 = S[4];
-                    const float sv[6] = {s4.x, s4.y, s4.z, s4.w, s1.w, s2.w};
-                    const float3 pa = BtV<DIM>(ga.x, ga.y, ga.z, sv);
-                    const float gs = ga.x * s1.x + ga.y * s1.y + (DIM == 3 ? ga.z * s1.z : 0.f);
-                    S[1] = F4(pa.x, pa.y, pa.z, gs);
-                }
-            }
+            PrepRecords<DIM, ND, NIP, KIND>(A, sG, kp, k1, lane);
             __syncwarp();
         }
         else
@@ -492,111 +627,116 @@ __global__ void __launch_bounds__(W * 32, 20 / W)
         }
         __syncwarp();
         }
-        // (B) lane (cell slot, neighbour b): the node-pair block (a, b) integrated over the points, added into a's
-        // rows at the ranks of b
-        {
-            const int cs = lane / ND, b = lane % ND;
-            const int64_t kc = kp + cs;
-            float uu[DIM][DIM], ue[DIM], eu[DIM], ee = 0.f, dg = 0.f;
-#pragma unroll
-            for (int k = 0; k < DIM; ++k)
-            {
-                ue[k] = eu[k] = 0.f;
-#pragma unroll
-                for (int l = 0; l < DIM; ++l)
-                    uu[k][l] = 0.f;
-            }
-            int r0 = 0, r1 = 0, r2 = 0, r3 = 0;
-            bool active = false;
-            if (kc < k1)
-            {
-                const int64_t e = A.cellIdx[kc];
-                const int ia = A.cellLoc[kc];
-                // ranks of b in a's neighbour lists (loaded first: their latency overlaps the integration)
-                const int64_t ridx = static_cast<int64_t>(ia * ND + b) * n + e;
-                r0 = A.rank[0][ridx];
-                if (GD)
-                {
-                    r1 = A.rank[1][ridx];
-                    r2 = A.rank[2][ridx];
-                    r3 = A.rank[3][ridx];
-                }
-#pragma unroll 2
-                for (int q = 0; q < NIP; ++q)
-                {
-                    // gradients and scalars of point q: one record row (staged) or the padded arrays (fused)
-                    const float4* G = STAGED ? sG + (cs * NIP + q) * Sh::recF4 : sG + (cs * NIP + q) * NDP;
-                    const float4* SR = STAGED ? G + ND : sS + (cs * NIP + q) * 5;
-                    const float4 ga = G[ia], gb = G[b];
-                    const float4 s0 = SR[0];
-                    const float av[3] = {ga.x, ga.y, ga.z}, bv[3] = {gb.x, gb.y, gb.z};
-                    float gab = 0.f;
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d)
-                        gab += av[d] * bv[d];
-                    // lambda w g_a g_b^T + mu w (g_b g_a^T + (g_a . g_b) I)
-#pragma unroll
-                    for (int k = 0; k < DIM; ++k)
-                    {
-                        const float lk = s0.x * av[k], mk = s0.y * bv[k];
-#pragma unroll
-                        for (int l = 0; l < DIM; ++l)
-                            uu[k][l] += lk * bv[l] + mk * av[l];
-                    }
-                    dg += s0.y * gab;
-                    if (GD)
-                    {
-                        const float4 s1 = SR[1];
-                        const float4 t0 = SR[2], t1 = SR[3];
-                        const float tv[6] = {t0.x, t0.y, t0.z, t1.x, t1.y, t1.z};
-                        const float3 qb = BtV<DIM>(gb.x, gb.y, gb.z, tv); // B_b^T t
-                        const float pv[3] = {s1.x, s1.y, s1.z}, qv[3] = {qb.x, qb.y, qb.z};
-#pragma unroll
-                        for (int k = 0; k < DIM; ++k)
-                        {
-                            ue[k] += pv[k] * gb.w;
-                            eu[k] -= ga.w * qv[k];
-                        }
-                        ee += (s0.z * ga.w + s1.w) * gb.w + s0.w * gab;
-                    }
-                }
-                active = true;
-            }
-            // the cells of a pass can share b: their blocks are added one cell slot after the other (the b of one
-            // cell are distinct nodes, so the 8 lanes of a slot write distinct positions); fixed order, no atomics
-#pragma unroll
-            for (int r = 0; r < CPP; ++r)
-            {
-                if (active && cs == r)
-                {
-#pragma unroll
-                    for (int k = 0; k < DIM; ++k)
-                    {
-                        float* row = sRow + k * kFusedRowCap;
-#pragma unroll
-                        for (int l = 0; l < DIM; ++l)
-                            row[NG_IDX(bUU + DIM * r0 + l, kFusedRowCap, 56)] += uu[k][l] + (k == l ? dg : 0.f);
-                        if (GD)
-                            row[NG_IDX(bUE + r1, kFusedRowCap, 56)] += ue[k];
-                    }
-                    if (GD)
-                    {
-                        float* row = sRow + DIM * kFusedRowCap;
-#pragma unroll
-                        for (int l = 0; l < DIM; ++l)
-                            row[NG_IDX(bEU + DIM * r2 + l, kFusedRowCap, 56)] += eu[l];
-                        row[NG_IDX(bEE + r3, kFusedRowCap, 56)] += ee;
-                    }
-                }
-                __syncwarp();
-            }
-        }
+        PassBlocks<DIM, ND, NIP, KIND, STAGED>(A, sG, sS, sRow, kp, k1, lane, bUU, bUE, bEU, bEE);
     }
     __syncwarp();
 #pragma unroll
     for (int k = 0; k < NR; ++k)
         for (int i = lane; i < len[k]; i += 32)
             vals[NG_IDX(rs[k] + i, A.nnz, 57)] = sRow[k * kFusedRowCap + i];
+}
+
+// The staged node rows with the record copies double-buffered: a grid of resident blocks walks the displacement
+// nodes (warp w takes nodes w, w + number of warps, ...), and while a warp integrates one pass of cells the copies
+// of its next pass (of the same node, or the first pass of its next node) are already in flight into the other
+// buffer. Same arithmetic and order per node as k_tangent_fused<STAGED>, so the values are bitwise the same.
+template <int DIM, int ND, int NIP, int KIND, int W>
+__global__ void __launch_bounds__(W * 32) k_tangent_rows_pipe(FusedArgs A, const float4* __restrict__ recs,
+                                                            float* __restrict__ vals)
+{
+    using Sh = FusedShape<DIM, ND, NIP, KIND, true, W>;
+    constexpr bool GD = Sh::GD;
+    constexpr int CPP = Sh::cpp, NR = Sh::nr;
+    constexpr int BUF = CPP * NIP * Sh::recF4; // float4 of one pass's records
+    extern __shared__ __align__(16) float smF[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* buf0 = reinterpret_cast<float4*>(smF) + static_cast<size_t>(wid) * (2 * BUF + NR * kFusedRowCap / 4);
+    float4* buf1 = buf0 + BUF;
+    float* sRow = reinterpret_cast<float*>(buf1 + BUF);
+    const int64_t nw = static_cast<int64_t>(gridDim.x) * W;
+    int64_t a = static_cast<int64_t>(blockIdx.x) * W + wid;
+    if (a >= A.nNodes)
+        return; // the whole warp leaves; only warp-level synchronisation follows
+    // per-node set-up: row starts and lengths, block offsets, cleared rows
+    int64_t rs[NR];
+    int len[NR];
+    int32_t bUU = 0, bUE = 0, bEU = 0, bEE = 0;
+    int64_t k0 = 0, k1 = 0;
+    auto enterNode = [&](int64_t node) {
+        const int64_t g0 = A.gdofD[node];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            rs[k] = A.rowPtr[NG_IDX(g0 + k, A.nRows, 50)];
+            len[k] = static_cast<int>(A.rowPtr[g0 + k + 1] - rs[k]);
+        }
+        int32_t ae = 0;
+        if (GD)
+        {
+            ae = A.eOf[node];
+            const int64_t ge = A.gdofE[ae];
+            rs[DIM] = A.rowPtr[NG_IDX(ge, A.nRows, 50)];
+            len[DIM] = static_cast<int>(A.rowPtr[ge + 1] - rs[DIM]);
+        }
+        bUU = A.blk[0][node];
+        bUE = GD ? A.blk[1][node] : 0;
+        bEU = GD ? A.blk[2][ae] : 0;
+        bEE = GD ? A.blk[3][ae] : 0;
+        k0 = A.cellPtr[node];
+        k1 = A.cellPtr[node + 1];
+#pragma unroll
+        for (int k = 0; k < NR; ++k)
+            for (int i = lane; i < kFusedRowCap; i += 32)
+                sRow[k * kFusedRowCap + i] = 0.f;
+    };
+    enterNode(a);
+    int64_t kp = k0;
+    StageRecords<DIM, ND, NIP, KIND>(A, recs, buf0, kp, k1, lane);
+    int cur = 0;
+    while (true)
+    {
+        // the next pass: the node's next cells, or the first pass of the warp's next node (every node has at least
+        // one pass, possibly empty)
+        int64_t nextNode = a, nextKp = kp + CPP, nextK1 = k1;
+        if (nextKp >= k1)
+        {
+            nextNode = a + nw;
+            if (nextNode < A.nNodes)
+            {
+                nextKp = A.cellPtr[nextNode];
+                nextK1 = A.cellPtr[nextNode + 1];
+            }
+        }
+        float4* now = cur ? buf1 : buf0;
+        float4* next = cur ? buf0 : buf1;
+        if (nextNode < A.nNodes)
+            StageRecords<DIM, ND, NIP, KIND>(A, recs, next, nextKp, nextK1, lane);
+        else
+            asm volatile("cp.async.commit_group;\n" ::: "memory"); // an empty group keeps the count uniform
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this pass's copies (all but the newest group)
+        __syncwarp();
+        PrepRecords<DIM, ND, NIP, KIND>(A, now, kp, k1, lane);
+        __syncwarp();
+        PassBlocks<DIM, ND, NIP, KIND, true>(A, now, nullptr, sRow, kp, k1, lane, bUU, bUE, bEU, bEE);
+        __syncwarp();
+        if (nextNode != a)
+        {
+            // the node's rows are complete
+#pragma unroll
+            for (int k = 0; k < NR; ++k)
+                for (int i = lane; i < len[k]; i += 32)
+                    vals[NG_IDX(rs[k] + i, A.nnz, 57)] = sRow[k * kFusedRowCap + i];
+            __syncwarp();
+            if (nextNode >= A.nNodes)
+                break;
+            a = nextNode;
+            enterNode(a);
+            __syncwarp();
+        }
+        kp = nextKp;
+        cur ^= 1;
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
 // Per-point records of the staged tangent: one thread per (cell, integration point) evaluates PointData once and
@@ -768,8 +908,9 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
         A.blk[k] = c.pairs[pr[k]].dBlk.p;
     }
     const bool staged = c.tangentStaged;
-    // one assembly with W warps per block of the node-row kernel
-    auto assemble = [&](int W) {
+    // one assembly with W warps per block of the node-row kernel; pipe: the double-buffered kernel on a grid of
+    // resident blocks (staged records only)
+    auto assemble = [&](int W, bool pipe) {
         auto run = [&](auto cfg) {
             using C = decltype(cfg);
             constexpr int DIM = C::dim, ND = C::nd, NIP = C::nip, KIND = C::kind;
@@ -789,6 +930,25 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
             }
             auto rows = [&](auto w) {
                 constexpr int WW = decltype(w)::value;
+                if (staged && pipe)
+                {
+                    auto kern = k_tangent_rows_pipe<DIM, ND, NIP, KIND, WW>;
+                    using Sh = FusedShape<DIM, ND, NIP, KIND, true, WW>;
+                    constexpr size_t smem =
+                            static_cast<size_t>(WW) * (2 * Sh::cpp * NIP * Sh::recF4 * 16 + Sh::nr * kFusedRowCap * 4);
+                    if (smem > 48 * 1024)
+                        NG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     static_cast<int>(smem)));
+                    int perSm = 0;
+                    NG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, WW * 32, smem));
+                    const int64_t need = (A.nNodes + WW - 1) / WW;
+                    const unsigned blocks = static_cast<unsigned>(
+                            std::max<int64_t>(1, std::min<int64_t>(need, static_cast<int64_t>(perSm) * c.smCount)));
+                    kern<<<blocks, WW * 32, smem, c.stream>>>(A, recs, vals);
+                    AfterLaunch(c, "k_tangent_rows_pipe");
+                    c.stats.kernel_launches += 1;
+                    return;
+                }
                 const unsigned blocks = static_cast<unsigned>((A.nNodes + WW - 1) / WW);
                 auto launch = [&](auto kern, size_t smem) {
                     if (smem > 48 * 1024)
@@ -821,8 +981,9 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
         else
             run(FCfg<2, 4, 4, NUTO_GPU_MB_LINEAR_ELASTIC>{});
     };
-    // autotuner: the first FP32 tangent of a context (outside any stream capture) assembles once with 2, 4 and 8
-    // warps per block (a warm-up and a timed assembly each; every one writes the same values) and keeps the fastest
+    // autotuner: the first FP32 tangent of a context (outside any stream capture) assembles once with each candidate
+    // shape — 2, 4 and 8 warps per block, and with staged records also the double-buffered kernel with 2 and 4 warps
+    // per block — (a warm-up and a timed assembly each; every one writes the same values) and keeps the fastest
     Tuning& T = c.tuning;
     if (T.tangentWarps == 0)
     {
@@ -832,17 +993,19 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
             T.tangentWarps = 4;
         else if (cs == cudaStreamCaptureStatusNone)
         {
-            const int cand[3] = {2, 4, 8};
+            const int candW[5] = {2, 4, 8, 2, 4};
+            const bool candPipe[5] = {false, false, false, true, true};
+            const int nCand = staged ? 5 : 3;
             cudaEvent_t e0, e1;
             NG_CUDA(cudaEventCreate(&e0));
             NG_CUDA(cudaEventCreate(&e1));
             float best = 0.f;
-            int pick = 4;
-            for (int k = 0; k < 3; ++k)
+            int pick = 1;
+            for (int k = 0; k < nCand; ++k)
             {
-                assemble(cand[k]);
+                assemble(candW[k], candPipe[k]);
                 NG_CUDA(cudaEventRecord(e0, c.stream));
-                assemble(cand[k]);
+                assemble(candW[k], candPipe[k]);
                 NG_CUDA(cudaEventRecord(e1, c.stream));
                 NG_CUDA(cudaEventSynchronize(e1));
                 float ms = 0.f;
@@ -851,15 +1014,16 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
                 if (k == 0 || ms < best)
                 {
                     best = ms;
-                    pick = cand[k];
+                    pick = k;
                 }
             }
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
-            T.tangentWarps = pick;
+            T.tangentWarps = candW[pick];
+            T.tangentPipe = candPipe[pick];
         }
     }
-    assemble(T.tangentWarps ? T.tangentWarps : 4);
+    assemble(T.tangentWarps ? T.tangentWarps : 4, T.tangentPipe);
 }
 
 } // namespace nuto_gpu

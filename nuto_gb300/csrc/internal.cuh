@@ -318,7 +318,8 @@ struct Tuning
 {
     bool enabled = true;             // NUTO_GPU_AUTOTUNE=0 keeps the defaults
     int tangentWarps = 0;            // warps per block of the FP32 tangent's node-row kernel (2, 4, 8)
-    float tangentMs[3] = {0, 0, 0};  // one assembly with 2, 4, 8 warps per block
+    bool tangentPipe = false;        // the double-buffered node-row kernel on a grid of resident blocks
+    float tangentMs[5] = {0, 0, 0, 0, 0}; // one assembly with 2, 4, 8 warps per block; pipelined with 2, 4
     int spmvGroup[4] = {0, 0, 0, 0}; // lanes per node of the fine-level product, per (value, vector) type pair
     float spmvMs[4][3] = {};         // one product with 4, 8, 16 lanes per node
 };

@@ -306,3 +306,26 @@ def test_autotuner_picks_measured_shapes_without_changing_results(monkeypatch):
     assert np.array_equal(res["1"][0], res["0"][0])
     xs = res["0"][1]
     assert np.abs(res["1"][1] - xs).max() <= 1e-4 * np.abs(xs).max()
+
+
+@pytest.mark.parametrize("kind,n", [("hex8gd", 6), ("quad4gd", 12)])
+def test_pipelined_node_rows_bitwise_equal(kind, n, monkeypatch):
+    """The double-buffered node-row kernel (NUTO_GPU_TANGENT=pipelined: a grid of resident blocks walking the nodes,
+    the next pass's records copied while the current one is integrated) adds the same blocks in the same order as the
+    one-node-per-warp kernel: the tangents are equal bit for bit."""
+    _torch()
+    import nuto_gb300
+
+    rng = np.random.default_rng(71)
+    s, (om, layers, P, cons) = _setup(kind, n)
+    u, kappa = _damage_state(kind, s, P, rng)
+    monkeypatch.setenv("NUTO_GPU_AUTOTUNE", "0")
+    g = s.build_gpu()
+    g.history = kappa
+    plain = g.build_matrix(u, nuto_gb300.FP32).cpu().numpy()
+    monkeypatch.setenv("NUTO_GPU_TANGENT", "pipelined")
+    g2 = s.build_gpu()
+    g2.history = kappa
+    piped = g2.build_matrix(u, nuto_gb300.FP32).cpu().numpy()
+    assert g2.autotune_info()["tangent_pipelined"]
+    assert np.array_equal(piped, plain)
