@@ -67,6 +67,8 @@ def parse():
                    help="run only the first N load steps of the 20-step Newton schedule (profiling of small cases)")
     p.add_argument("--workload", default="beam", choices=["beam", "plates", "hex20"])
     p.add_argument("--specimens", type=int, default=128)
+    p.add_argument("--max-newton", type=int, default=None,
+                   help="Newton iterations per load step before a cut-back (beam: 20, hex20: 50)")
     return p.parse_args()
 
 
@@ -206,20 +208,27 @@ def accumulate(t0, dt, k):
     return out
 
 
-def run_steps(g, opts, t_start, t_values, dt=None):
+def run_steps(g, opts, t_start, t_values, dt=None, progress=None, cutbacks=8):
     """Advances the load from t_start through every t in t_values with AdaptiveSolve (time step 1/LOAD_STEPS, cut
     back by halves on NoConvergence as the reference's AdaptiveSolve does). Returns the summed step statistics,
-    failed attempts included (their work was done), the number of cut-backs and the per-load-step Newton counts."""
+    failed attempts included (their work was done), the number of cut-backs and the per-load-step Newton counts.
+    progress: a label; each finished load step then prints one line to stderr. cutbacks: halvings allowed below
+    the load step."""
     from nuto_gb300.adaptive import AdaptiveSolve
 
     dt = dt or 1.0 / LOAD_STEPS
-    ad = AdaptiveSolve(g, opts, dt=dt, dt_max=dt, dt_min=dt / 256)
+    ad = AdaptiveSolve(g, opts, dt=dt, dt_max=dt, dt_min=dt / 2 ** cutbacks)
     t = t_start
     per_step = []
     for tv in t_values:
         n0 = len(ad.stats)
         ad.solve(tv, t)
         per_step.append(sum(st["newton_iterations"] for st in ad.stats[n0:]))
+        if progress:
+            sys.stderr.write("%s: t = %.4f, %d Newton, %d Krylov iterations, %d cut-backs so far\n"
+                             % (progress, tv, per_step[-1], sum(st["krylov_iterations"] for st in ad.stats[n0:]),
+                                ad.cutbacks))
+            sys.stderr.flush()
         t = tv
     agg = {k: 0 for k in AGG_KEYS}
     for st in ad.stats:
@@ -361,7 +370,7 @@ def run_newton(args, s, g, barrier):
 
     n_dofs = g.n_dofs
     t_values = accumulate(0.0, 1.0 / LOAD_STEPS, LOAD_STEPS)[:args.load_steps or LOAD_STEPS]
-    common = dict(newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20, max_krylov=20000,
+    common = dict(newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=args.max_newton or 20, max_krylov=20000,
                   forcing_floor=FORCING_FLOOR)
     opts32 = g.default_options(precision=nuto_gb300.FP32, exact_tangent_below=EXACT_BELOW, **common)
     opts64 = g.default_options(precision=nuto_gb300.FP64, **common)
@@ -533,10 +542,7 @@ def run_ours(args):
     k32 = torch.empty(nnz, dtype=torch.float32, device="cuda")
     f = torch.empty(n_dofs, dtype=torch.float64, device="cuda")
     for _ in range(args.warmup):
-        g.build_matrix(u, nuto_gb300.FP32, out=k32)
-        g.build_vector(u, out=f)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        g.build_system(u, nuto_gb300.FP32, out=k32, f_out=f)
     launches0 = g.stats()["kernel_launches"]
     clocks = ClockSampler(gpu_index(local))
     clocks.start()
@@ -544,22 +550,33 @@ def run_ours(args):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record()
-    for a, b, c in ev:  # the library runs on torch's current stream: the events bracket its kernels
-        a.record()
-        g.build_matrix(u, nuto_gb300.FP32, out=k32)
-        b.record()
-        g.build_vector(u, out=f)
-        c.record()
+    for _ in range(args.steps):  # one step: the tangent and the residual at the state, the residual beside the tangent
+        g.build_system(u, nuto_gb300.FP32, out=k32, f_out=f)
     e1.record()
     barrier()
     clk = clocks.stop()
     launches = g.stats()["kernel_launches"] - launches0
     sec = e0.elapsed_time(e1) / 1e3
-    ms_matrix = [a.elapsed_time(b) for a, b, _ in ev]
-    ms_vector = [b.elapsed_time(c) for _, b, c in ev]
     (work,), sec = aggregate_ranks([n_dofs * args.steps], sec, "cuda")
     value = work / sec
     fp32_check = float(k32.abs().max().item())  # touches the result (non-finite values would show here)
+
+    # the same K steps with the two calls in sequence, each bracketed by events on the library's stream (torch's
+    # current stream): the tangent's and the residual's own launch times (the roofline below), and the gain of
+    # running them side by side
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    for a, b, c in ev:
+        a.record()
+        g.build_matrix(u, nuto_gb300.FP32, out=k32)
+        b.record()
+        g.build_vector(u, out=f)
+        c.record()
+    barrier()
+    ms_matrix = [a.elapsed_time(b) for a, b, _ in ev]
+    ms_vector = [b.elapsed_time(c) for _, b, c in ev]
+    ms_sequential = float(np.mean([a.elapsed_time(c) for a, _, c in ev]))
 
     # the same passes end to end through the C ABI with host buffers: state in from pinned memory, CSR values and
     # residual out to pinned memory, every step
@@ -572,8 +589,7 @@ def run_ours(args):
     h0 = time.perf_counter()
     for _ in range(args.steps):
         ud.copy_(xp, non_blocking=True)
-        g.build_matrix(ud, nuto_gb300.FP32, out=k32)
-        g.build_vector(ud, out=f)
+        g.build_system(ud, nuto_gb300.FP32, out=k32, f_out=f)
         kp.copy_(k32, non_blocking=True)
         fp.copy_(f, non_blocking=True)
         torch.cuda.current_stream().synchronize()
@@ -600,6 +616,10 @@ def run_ours(args):
            "config": beam_config(args.size, n_dofs, nnz, world),
            "precision": "FP32 tangent (law branch decisions in FP64), FP64 residual",
            "ms_matrix_per_step": float(np.mean(ms_matrix)), "ms_vector_per_step": float(np.mean(ms_vector)),
+           "ms_per_step_sequential": ms_sequential,
+           "step_form": "nuto_gpu_build_system: the FP64 residual on a second stream (%s resident blocks per SM) "
+                        "beside the FP32 tangent; ms_matrix/ms_vector_per_step and the rooflines from the same K "
+                        "steps run as two calls in sequence" % os.environ.get("NUTO_GPU_SYSTEM_RES_BLOCKS", "4"),
            "max_abs_tangent_value": fp32_check,
            "roofline": roof,
            "roofline_residual": {"kernel": "k_residual (FP64 internal-force vector)", "bound": "fp64",
@@ -808,7 +828,7 @@ HEX20_STEPS = 5
 
 def run_hex20(args):
     """The large configuration: Hex20 displacements (3x3x3 Gauss) with the local exponential damage law on an n^3
-    cube (80^3: 6.3 M DOFs, 1.09 G nonzeros), its 5 load steps to u_z = 3e-4 from rest on the mixed path (FP32
+    cube (80^3: 6.3 M DOFs, 1.09 G nonzeros), its 5 load steps to u_z = 5e-5 from rest on the mixed path (FP32
     tangent and Krylov, FP64 residual and history) and on the FP64 path, each timed with CUDA events; the two final
     states compared. Not the headline."""
     import torch
@@ -822,7 +842,9 @@ def run_hex20(args):
     s = configs.hex20_local_damage(n, load_steps=HEX20_STEPS)
     g = s.build_gpu(device=0)
     t_values = accumulate(0.0, 1.0 / HEX20_STEPS, HEX20_STEPS)
-    common = dict(newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=20, max_krylov=50000,
+    # local softening localises into one layer of cells in the step where damage starts; Newton needs more
+    # iterations there the finer the mesh (the oracle's exact Newton: 6 at 4^3, 12 at 8^3)
+    common = dict(newton_rtol=1e-8, krylov_rtol=KRYLOV_RTOL, max_newton=args.max_newton or 50, max_krylov=50000,
                   forcing_floor=FORCING_FLOOR)
     runs = {"mixed": g.default_options(precision=nuto_gb300.FP32, exact_tangent_below=EXACT_BELOW, **common),
             "fp64": g.default_options(precision=nuto_gb300.FP64, **common)}
@@ -834,7 +856,7 @@ def run_hex20(args):
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        agg = run_steps(g, o, 0.0, t_values, dt=1.0 / HEX20_STEPS)
+        agg = run_steps(g, o, 0.0, t_values, dt=1.0 / HEX20_STEPS, progress=name, cutbacks=3)
         e1.record()
         torch.cuda.synchronize()
         sec = e0.elapsed_time(e1) / 1e3
@@ -852,7 +874,7 @@ def run_hex20(args):
            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
            "config": {"workload": "hex20_local_damage_%d^3: Hex20 3x3x3 Gauss on the unit cube, MomentumBalance + "
                                   "LocalIsotropicDamage(30000, 0.2, kappa0 1e-4, beta 100, alpha 0.99, k 10), z = 0 "
-                                  "fixed, z = 1 u_z = 3e-4 t, %d load steps from rest" % (n, HEX20_STEPS),
+                                  "fixed, z = 1 u_z = 5e-5 t, %d load steps from rest" % (n, HEX20_STEPS),
                       "n_dofs": int(g.n_dofs), "nnz": int(g.nnz)},
            "runs": out}
     if "fp64" in states:
@@ -860,6 +882,31 @@ def run_hex20(args):
         res["mixed_vs_fp64_path"] = {"max": float(np.abs(a - b).max() / np.abs(b).max()),
                                      "l2": float(np.linalg.norm(a - b) / np.linalg.norm(b))}
         res["speedup_newton_step_mixed_vs_fp64"] = out["fp64"]["newton_step_ms"] / out["mixed"]["newton_step_ms"]
+    # the FP32 tangent (tensor cores: k_tc20_points + k_tangent_tc20 + k_tc20_rows) at the final state of the last
+    # run (damaged points at the fixed face's edges), timed with CUDA events, and its error against the FP64
+    # tangent (element kernel, FP64 law and products) at the same state
+    x_end = torch.as_tensor(g.get_state()[0], device="cuda")
+    k64 = g.build_matrix(x_end, nuto_gb300.FP64)
+    k32 = torch.empty(g.nnz, dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        g.build_matrix(x_end, nuto_gb300.FP32, out=k32)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    e0.record()
+    for _ in range(reps):
+        g.build_matrix(x_end, nuto_gb300.FP32, out=k32)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    err = float((k32.double() - k64).abs().max() / k64.abs().max())
+    tb = tangent_bytes(s, g.nnz, 4)
+    peak, peak_kind = load_peaks()
+    res["tangent_fp32"] = {"kernels": "k_tc20_points + k_tangent_tc20 (tcgen05.mma kind::tf32, three-product split, "
+                                      "accumulators in tensor memory) + k_tc20_rows",
+                           "ms_per_assembly": ms, "assembled_dofs_per_s": g.n_dofs / (ms / 1e3),
+                           "algorithmic_bytes": tb, "hbm_frac": tb / (ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
+                           "max_rel_error_vs_fp64_tangent": err,
+                           "tc_tflops": 2.0 * 128 * 64 * 64 * 3 * s.mesh.num_cells / (ms / 1e3) / 1e12}
     print(json.dumps(res))
 
 

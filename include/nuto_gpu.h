@@ -216,6 +216,12 @@ int nuto_gpu_multigrid_info(const nuto_gpu_ctx* ctx, int* levels, int* graph_act
    times_ms (17 floats): the tangent with 2 / 4 / 8 warps, double-buffered with 2 / 4 warps, then per type pair the
    product with 4 / 8 / 16 lanes (one launch each). */
 int nuto_gpu_autotune_info(const nuto_gpu_ctx* ctx, int* choices, float* times_ms);
+/* Iteration limit of every bounded device wait (no counterpart in the reference; default 4,194,304): the tensor-core
+   tangent of Hex20 cells waits on its MMA completion barrier. A wait that runs out sets NUTO_GPU_ETIMEOUT in the
+   context's status word, the kernel drains its work in flight (with a fixed limit), releases its tensor memory and
+   returns; nuto_gpu_synchronize and nuto_gpu_do_step then return NUTO_GPU_ETIMEOUT and clear the word. A small limit
+   makes the waits run out on purpose (tests). */
+int nuto_gpu_set_spin_limit(nuto_gpu_ctx* ctx, long long iterations);
 
 int nuto_gpu_set_integrand(nuto_gpu_ctx* ctx, const nuto_gpu_integrand* params);
 int nuto_gpu_num_integration_points(const nuto_gpu_ctx* ctx);
@@ -234,6 +240,14 @@ int nuto_gpu_set_cell_scale(nuto_gpu_ctx* ctx, const double* scale);
 int nuto_gpu_build_vector(nuto_gpu_ctx* ctx, const double* d_u, double* d_f);
 /* CSR values of sum over cells of the integrand's Hessian0; d_values is nnz floats (FP32) or doubles (FP64) */
 int nuto_gpu_build_matrix(nuto_gpu_ctx* ctx, const double* d_u, int precision, void* d_values);
+/* Both at one state: the values of nuto_gpu_build_matrix(ctx, d_u, precision, d_values) and the vector of
+   nuto_gpu_build_vector(ctx, d_u, d_f), bitwise the same as the two calls. NewtonRaphson::Solve needs the residual
+   and the derivative at the same x (nuto/math/NewtonRaphson.h:62-94, through TimeDependentProblem::Gradient and
+   Hessian0, nuto/mechanics/tools/TimeDependentProblem.cpp:56-76). The FP64 residual runs on a second stream of the
+   context as a few resident blocks per SM beside the tangent's kernels (its work sits on the FP64 pipe, the
+   tangent's on FP32 issue); both are complete, in the context's stream order, when the call's work is. precision
+   NUTO_GPU_FP32 or NUTO_GPU_FP64. The first call of a context runs the two in sequence. */
+int nuto_gpu_build_system(nuto_gpu_ctx* ctx, const double* d_u, int precision, void* d_values, double* d_f);
 /* The FP32 values of nuto_gpu_build_matrix(ctx, d_u, NUTO_GPU_FP32, d_values), computed without allocating any
    memory: the integration-point records go to a fixed 16 MiB device array inside the library instead of a buffer
    of the context. For callers that must not allocate device memory once set up. Limit: cells x integration points

@@ -92,12 +92,14 @@ SIGNATURES = {
     "nuto_gpu_set_history": (_i, [_vp, _vp]),
     "nuto_gpu_get_history": (_i, [_vp, _vp]),
     "nuto_gpu_set_cell_scale": (_i, [_vp, _vp]),
+    "nuto_gpu_set_spin_limit": (_i, [_vp, ctypes.c_longlong]),
     "nuto_gpu_history_device": (_i, [_vp, _P(_vp)]),
     "nuto_gpu_transpose_values": (_i, [_vp, _i, _vp, _vp]),
     "nuto_gpu_adjoint_history_load": (_i, [_vp, _vp, _vp, _vp]),
     "nuto_gpu_adjoint_step": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nuto_gpu_build_vector": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_build_matrix": (_i, [_vp, _vp, _i, _vp]),
+    "nuto_gpu_build_system": (_i, [_vp, _vp, _i, _vp, _vp]),
     "nuto_gpu_build_matrix_noalloc": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_build_lumped_mass": (_i, [_vp, _d, _vp]),
     "nuto_gpu_eval_ip": (_i, [_vp, _vp, _i, _vp]),

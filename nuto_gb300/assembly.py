@@ -158,6 +158,15 @@ class GpuCellGroup:
         k = np.ascontiguousarray(np.broadcast_to(kappa, (self.mesh.num_cells, self.n_ip)), dtype=np.float64)
         self._call("nuto_gpu_set_history", _ptr(k))
 
+    def set_spin_limit(self, iterations):
+        """Iteration limit of the bounded device waits (a wait that runs out makes synchronize() and do_step() raise
+        with NUTO_GPU_ETIMEOUT)."""
+        self._call("nuto_gpu_set_spin_limit", int(iterations))
+
+    def synchronize(self):
+        """Wait for the context's stream; raises with NUTO_GPU_ETIMEOUT if a bounded device wait gave up."""
+        self._call("nuto_gpu_synchronize")
+
     def set_cell_scale(self, scale):
         """Per-cell factor of the integrand's Young's modulus (None: 1 everywhere)."""
         if scale is None:
@@ -188,6 +197,17 @@ class GpuCellGroup:
         v = out if out is not None else torch.empty(self.nnz, dtype=dt, device=u.device)
         self._call("nuto_gpu_build_matrix", _ptr(u), precision, _ptr(v))
         return v
+
+    def build_system(self, u, precision=FP64, out=None, f_out=None):
+        """(tangent CSR values, residual) at one state through nuto_gpu_build_system: the same values as
+        build_matrix and build_vector, with the FP64 residual running beside the tangent on a second stream."""
+        torch = _torch()
+        u = self._dev(u, torch.float64)
+        dt = torch.float32 if precision == FP32 else torch.float64
+        v = out if out is not None else torch.empty(self.nnz, dtype=dt, device=u.device)
+        f = f_out if f_out is not None else torch.empty(self.n_dofs, dtype=torch.float64, device=u.device)
+        self._call("nuto_gpu_build_system", _ptr(u), precision, _ptr(v), _ptr(f))
+        return v, f
 
     def build_matrix_noalloc(self, u, out=None):
         """FP32 tangent through nuto_gpu_build_matrix_noalloc (records in the library's static device array; the
@@ -321,5 +341,3 @@ class GpuCellGroup:
         check(self.h, self.L.nuto_gpu_get_stats(self.h, ctypes.byref(s)))
         return s.as_dict()
 
-    def synchronize(self):
-        self._call("nuto_gpu_synchronize")

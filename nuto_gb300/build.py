@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(LIB_DIR, VARIANTS["release"][0])
 
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "assemble.cu", "fused.cu", "adjoint.cu", "krylov.cu", "newton.cu", "amg.cu"]
+SOURCES = ["api.cu", "assemble.cu", "fused.cu", "tc20.cu", "adjoint.cu", "krylov.cu", "newton.cu", "amg.cu"]
 
 
 def lib_path(variant="release"):

@@ -596,10 +596,19 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
         c->tuning.tangentWarps = 4; // the double-buffered node-row kernel, not tuned
         c->tuning.tangentPipe = true;
     }
+    // Hex20 FP32 tangent: tensor cores with split TF32 (default), one TF32 product (tf32) or records + row
+    // gather (off)
+    const char* t20 = std::getenv("NUTO_GPU_TC20");
+    c->forceTc20Off = t20 && std::string(t20) == "off";
+    c->tc20Split = t20 && std::string(t20) == "tf32" ? 1 : 3;
     const char* at = std::getenv("NUTO_GPU_AUTOTUNE");
     c->tuning.enabled = !(at && at[0] == '0');
     const char* gr = std::getenv("NUTO_GPU_GMRES_RESTART");
     c->gmresRestart = gr ? std::atoi(gr) : 0;
+    // nuto_gpu_build_system: residual blocks per SM beside the tangent (0: residual and tangent in sequence)
+    const char* sr = std::getenv("NUTO_GPU_SYSTEM_RES_BLOCKS");
+    if (sr)
+        c->sysResBlocks = std::max(0, std::atoi(sr));
     const int rc = Guard(c, [&] {
         NG_CUDA(cudaSetDevice(device));
         NG_CUDA(cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device));
@@ -629,6 +638,14 @@ int nuto_gpu_destroy(nuto_gpu_ctx* ctx)
     int rc = NUTO_GPU_OK;
     if (cudaSetDevice(ctx->device) != cudaSuccess || cudaStreamSynchronize(ctx->stream) != cudaSuccess)
         rc = NUTO_GPU_ECUDA;
+    if (ctx->sideStream && cudaStreamSynchronize(ctx->sideStream) != cudaSuccess)
+        rc = NUTO_GPU_ECUDA;
+    if (ctx->evFork)
+        cudaEventDestroy(ctx->evFork);
+    if (ctx->evJoin)
+        cudaEventDestroy(ctx->evJoin);
+    if (ctx->sideStream)
+        cudaStreamDestroy(ctx->sideStream);
     const bool own = ctx->ownStream;
     cudaStream_t s = ctx->stream;
     delete ctx;
@@ -649,6 +666,8 @@ int nuto_gpu_synchronize(nuto_gpu_ctx* ctx)
 {
     return Guard(ctx, [&] {
         NG_CUDA(cudaStreamSynchronize(ctx->stream));
+        // a bounded device wait that gave up since the last synchronisation
+        NG_CHECK(ReadDeviceStatus(*ctx) == 0, NUTO_GPU_ETIMEOUT, "a bounded device wait gave up");
         return NUTO_GPU_OK;
     });
 }
@@ -930,6 +949,15 @@ int nuto_gpu_set_history(nuto_gpu_ctx* ctx, const double* kappa)
     });
 }
 
+int nuto_gpu_set_spin_limit(nuto_gpu_ctx* ctx, long long iterations)
+{
+    return Guard(ctx, [&] {
+        NG_CHECK(iterations >= 0, NUTO_GPU_EINVAL, "iterations >= 0");
+        ctx->spinLimit = iterations;
+        return NUTO_GPU_OK;
+    });
+}
+
 int nuto_gpu_set_cell_scale(nuto_gpu_ctx* ctx, const double* scale)
 {
     return Guard(ctx, [&] {
@@ -1030,6 +1058,54 @@ int nuto_gpu_build_matrix(nuto_gpu_ctx* ctx, const double* u, int precision, voi
             LaunchTangentExact(*ctx, u, static_cast<double*>(values));
         else
             LaunchTangent(*ctx, u, precision, values);
+        return NUTO_GPU_OK;
+    });
+}
+
+int nuto_gpu_build_system(nuto_gpu_ctx* ctx, const double* u, int precision, void* values, double* f)
+{
+    return Guard(ctx, [&] {
+        RequireReady(*ctx);
+        NG_CHECK(precision == NUTO_GPU_FP32 || precision == NUTO_GPU_FP64, NUTO_GPU_EINVAL, "precision 32 or 64");
+        NG_CHECK(values && f, NUTO_GPU_EINVAL, "values and f");
+        Ctx& c = *ctx;
+        // the first call (lazy set-up of geometry, records and tuning), and contexts that ask for it, run the two
+        // launches in sequence on the context's stream
+        if (c.systemCalls++ == 0 || c.sysResBlocks <= 0)
+        {
+            LaunchTangent(c, u, precision, values);
+            LaunchResidual(c, u, f);
+            return NUTO_GPU_OK;
+        }
+        if (!c.sideStream)
+        {
+            int lo = 0, hi = 0; // numerically: lo >= hi
+            NG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            // the highest priority: whenever an SM frees resources, the residual's few blocks are placed before
+            // the tangent's many, so they reach their slots early and keep them
+            NG_CUDA(cudaStreamCreateWithPriority(&c.sideStream, cudaStreamNonBlocking, hi));
+            NG_CUDA(cudaEventCreateWithFlags(&c.evFork, cudaEventDisableTiming));
+            NG_CUDA(cudaEventCreateWithFlags(&c.evJoin, cudaEventDisableTiming));
+        }
+        // fork: the residual (persistent grid, launched first so that its blocks hold their SM slots) on the side
+        // stream; the tangent on the context's stream; join before anything else runs on the context's stream
+        NG_CUDA(cudaEventRecord(c.evFork, c.stream));
+        NG_CUDA(cudaStreamWaitEvent(c.sideStream, c.evFork, 0));
+        const cudaStream_t main = c.stream;
+        c.stream = c.sideStream;
+        try
+        {
+            LaunchResidual(c, u, f, c.sysResBlocks);
+        }
+        catch (...)
+        {
+            c.stream = main;
+            throw;
+        }
+        c.stream = main;
+        LaunchTangent(c, u, precision, values);
+        NG_CUDA(cudaEventRecord(c.evJoin, c.sideStream));
+        NG_CUDA(cudaStreamWaitEvent(c.stream, c.evJoin, 0));
         return NUTO_GPU_OK;
     });
 }

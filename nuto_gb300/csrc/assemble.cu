@@ -51,45 +51,6 @@ static void DispatchCfg(const Ctx& c, F&& f)
 
 // ---- small device helpers -------------------------------------------------------------------------------
 
-// Engineering strain from the displacement gradient H[c][d] = sum_n u_nc dN_n/dx_d, Voigt order of
-// Nabla::Strain (DifferentialOperators.h:24-90): 2D xx, yy, xy; 3D xx, yy, zz, yz, zx, xy.
-template <typename T, int DIM>
-__device__ __forceinline__ void StrainFromH(const T (&H)[DIM][DIM], T* e)
-{
-    if (DIM == 2)
-    {
-        e[0] = H[0][0];
-        e[1] = H[1][1];
-        e[2] = H[0][1] + H[1][0];
-    }
-    else
-    {
-        e[0] = H[0][0];
-        e[1] = H[1][1];
-        e[2] = H[2][2];
-        e[3] = H[1][2] + H[2][1];
-        e[4] = H[0][2] + H[2][0];
-        e[5] = H[0][1] + H[1][0];
-    }
-}
-
-// B_n^T s for the node with global gradient g (columns of the Voigt strain operator)
-template <typename T, int DIM>
-__device__ __forceinline__ void BtS(const T* g, const T* s, T* out)
-{
-    if (DIM == 2)
-    {
-        out[0] = g[0] * s[0] + g[1] * s[2];
-        out[1] = g[1] * s[1] + g[0] * s[2];
-    }
-    else
-    {
-        out[0] = g[0] * s[0] + g[2] * s[4] + g[1] * s[5];
-        out[1] = g[1] * s[1] + g[2] * s[3] + g[0] * s[5];
-        out[2] = g[2] * s[2] + g[1] * s[3] + g[0] * s[4];
-    }
-}
-
 // LinearElastic stress sigma = C eps (LinearElastic.h:21-24, CalculateC :47-121)
 template <typename T, int DIM>
 __device__ __forceinline__ void ElasticStress(const LawParams& L, const T* e, T* s)
@@ -256,10 +217,12 @@ static CellArgs MakeCellArgs(Ctx& c)
 // ---- FP64 internal-force residual --------------------------------------------------------------------------
 // MomentumBalance::Gradient (MomentumBalance.h:26-35) and GradientDamage::Gradient (GradientDamage.h:70-90)
 // integrated as in Cell::IntegrateGeneric (Cell.h:105-119) and scattered like SimpleAssembler::BuildVector
-// (SimpleAssembler.cpp:38-65); FP64 atomics replace the thread-local vectors.
+// (SimpleAssembler.cpp:38-65).
 // The cell vectors are written planar ([local entry][cell]: the displacement entries node-major, then the eeq
 // entries) and k_gather_cell_vectors sums them per DOF in ascending cell order: the residual is bitwise the same on
 // every run (SimpleAssembler::BuildVector sums thread-local vectors and merges them in a critical section).
+// A block integrates CPB cells per pass and walks the cells with the grid's stride: one pass per block when the grid
+// covers the mesh, or a persistent grid of a few blocks per SM beside the tangent (nuto_gpu_build_system).
 template <int DIM, int ND, int NIP, int KIND>
 __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const double* __restrict__ u,
                                                   double* __restrict__ fcell)
@@ -272,131 +235,134 @@ __global__ void __launch_bounds__(128) k_residual(CellArgs a, LawParams L, const
     __shared__ double sE[GD ? CPB : 1][GD ? ND : 1];
     __shared__ double sIp[CPB][NIP][REC];
     const int64_t n = a.nCells;
-    const int64_t cell0 = static_cast<int64_t>(blockIdx.x) * CPB;
-
-    for (int it = threadIdx.x; it < CPB * ND; it += blockDim.x)
+    for (int64_t cell0 = static_cast<int64_t>(blockIdx.x) * CPB; cell0 < n;
+         cell0 += static_cast<int64_t>(gridDim.x) * CPB)
     {
-        const int cl = it % CPB, nd = it / CPB;
-        const int64_t e = cell0 + cl;
-        if (e >= n)
-            continue;
-        const int64_t g = a.gdofD[NG_IDX(a.connD[static_cast<int64_t>(nd) * n + e], a.nNodesD, 2)];
-#pragma unroll
-        for (int c = 0; c < DIM; ++c)
-            sU[cl][nd][c] = u[NG_IDX(g + c, a.nDofs, 3)];
-        if (GD)
-            sE[cl][nd] = u[NG_IDX(a.gdofE[NG_IDX(a.connE[static_cast<int64_t>(nd) * n + e], a.nNodesE, 4)], a.nDofs, 5)];
-    }
-    __syncthreads();
-
-    for (int it = threadIdx.x; it < CPB * NIP; it += blockDim.x)
-    {
-        const int cl = it % CPB, q = it / CPB;
-        const int64_t e = cell0 + cl;
-        if (e >= n)
-            continue;
-        const int64_t G0 = static_cast<int64_t>(q) * a.geoStride * n + e;
-        const double* G = a.geo64 + NG_IDX(G0, a.geoSize, 6);
-        const double wdj = G[0];
-        // per-cell Young's modulus factor: scales the stress, i.e. the displacement rows
-        const double wdjE = a.escale ? wdj * a.escale[e] : wdj;
-        double H[DIM][DIM];
-#pragma unroll
-        for (int i = 0; i < DIM; ++i)
-#pragma unroll
-            for (int j = 0; j < DIM; ++j)
-                H[i][j] = 0;
-        double eeq = 0, ge[DIM];
-#pragma unroll
-        for (int d = 0; d < DIM; ++d)
-            ge[d] = 0;
-#pragma unroll
-        for (int nd = 0; nd < ND; ++nd)
+        for (int it = threadIdx.x; it < CPB * ND; it += blockDim.x)
         {
-            double g[DIM];
-#pragma unroll
-            for (int d = 0; d < DIM; ++d)
-                g[d] = G[(1 + nd * DIM + d) * n];
+            const int cl = it % CPB, nd = it / CPB;
+            const int64_t e = cell0 + cl;
+            if (e >= n)
+                continue;
+            const int64_t g = a.gdofD[NG_IDX(a.connD[static_cast<int64_t>(nd) * n + e], a.nNodesD, 2)];
 #pragma unroll
             for (int c = 0; c < DIM; ++c)
-#pragma unroll
-                for (int d = 0; d < DIM; ++d)
-                    H[c][d] += sU[cl][nd][c] * g[d];
+                sU[cl][nd][c] = u[NG_IDX(g + c, a.nDofs, 3)];
             if (GD)
-            {
-                const double ev = sE[cl][nd];
-                eeq += a.tabN_D[q * ND + nd] * ev;
+                sE[cl][nd] = u[NG_IDX(a.gdofE[NG_IDX(a.connE[static_cast<int64_t>(nd) * n + e], a.nNodesE, 4)], a.nDofs, 5)];
+        }
+        __syncthreads();
+
+        for (int it = threadIdx.x; it < CPB * NIP; it += blockDim.x)
+        {
+            const int cl = it % CPB, q = it / CPB;
+            const int64_t e = cell0 + cl;
+            if (e >= n)
+                continue;
+            const int64_t G0 = static_cast<int64_t>(q) * a.geoStride * n + e;
+            const double* G = a.geo64 + NG_IDX(G0, a.geoSize, 6);
+            const double wdj = G[0];
+            // per-cell Young's modulus factor: scales the stress, i.e. the displacement rows
+            const double wdjE = a.escale ? wdj * a.escale[e] : wdj;
+            double H[DIM][DIM];
 #pragma unroll
-                for (int d = 0; d < DIM; ++d)
-                    ge[d] += ev * g[d];
-            }
-        }
-        double eps[VD], sig[VD];
-        StrainFromH<double, DIM>(H, eps);
-        const double kh = a.kappa[NG_IDX(e * NIP + q, n * NIP, 7)];
-        if (KIND == NUTO_GPU_MB_LINEAR_ELASTIC)
-            ElasticStress<double, DIM>(L, eps, sig);
-        else if (KIND == NUTO_GPU_MB_LOCAL_DAMAGE)
-        {
-            // LocalIsotropicDamage::Stress with EvolutionImplicit::Kappa (LocalIsotropicDamage.h:52-57, 110-113)
-            const double kap = fmax(MisesValue<double, DIM>(L, eps), kh);
-            LedStress<double, DIM>(L, eps, DamageOmega<double>(L, kap), sig);
-        }
-        else
-        {
-            const double kap = fmax(kh, eeq); // GradientDamage::Kappa (GradientDamage.h:127-130)
-            const double omega = DamageOmega<double>(L, kap);
-            LedStress<double, DIM>(L, eps, omega, sig);
-            const double cg = L.c * InteractionFactor<double>(L, omega) * wdj;
-            sIp[cl][q][VD] = (eeq - MisesValue<double, DIM>(L, eps)) * wdj;
+            for (int i = 0; i < DIM; ++i)
+#pragma unroll
+                for (int j = 0; j < DIM; ++j)
+                    H[i][j] = 0;
+            double eeq = 0, ge[DIM];
 #pragma unroll
             for (int d = 0; d < DIM; ++d)
-                sIp[cl][q][VD + 1 + d] = cg * ge[d];
+                ge[d] = 0;
+#pragma unroll
+            for (int nd = 0; nd < ND; ++nd)
+            {
+                double g[DIM];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    g[d] = G[(1 + nd * DIM + d) * n];
+#pragma unroll
+                for (int c = 0; c < DIM; ++c)
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                        H[c][d] += sU[cl][nd][c] * g[d];
+                if (GD)
+                {
+                    const double ev = sE[cl][nd];
+                    eeq += a.tabN_D[q * ND + nd] * ev;
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                        ge[d] += ev * g[d];
+                }
+            }
+            double eps[VD], sig[VD];
+            StrainFromH<double, DIM>(H, eps);
+            const double kh = a.kappa[NG_IDX(e * NIP + q, n * NIP, 7)];
+            if (KIND == NUTO_GPU_MB_LINEAR_ELASTIC)
+                ElasticStress<double, DIM>(L, eps, sig);
+            else if (KIND == NUTO_GPU_MB_LOCAL_DAMAGE)
+            {
+                // LocalIsotropicDamage::Stress with EvolutionImplicit::Kappa (LocalIsotropicDamage.h:52-57, 110-113)
+                const double kap = fmax(MisesValue<double, DIM>(L, eps), kh);
+                LedStress<double, DIM>(L, eps, DamageOmega<double>(L, kap), sig);
+            }
+            else
+            {
+                const double kap = fmax(kh, eeq); // GradientDamage::Kappa (GradientDamage.h:127-130)
+                const double omega = DamageOmega<double>(L, kap);
+                LedStress<double, DIM>(L, eps, omega, sig);
+                const double cg = L.c * InteractionFactor<double>(L, omega) * wdj;
+                sIp[cl][q][VD] = (eeq - MisesValue<double, DIM>(L, eps)) * wdj;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    sIp[cl][q][VD + 1 + d] = cg * ge[d];
+            }
+#pragma unroll
+            for (int v = 0; v < VD; ++v)
+                sIp[cl][q][v] = sig[v] * wdjE;
         }
-#pragma unroll
-        for (int v = 0; v < VD; ++v)
-            sIp[cl][q][v] = sig[v] * wdjE;
-    }
-    __syncthreads();
+        __syncthreads();
 
-    for (int it = threadIdx.x; it < CPB * ND; it += blockDim.x)
-    {
-        const int cl = it % CPB, nd = it / CPB;
-        const int64_t e = cell0 + cl;
-        if (e >= n)
-            continue;
-        double fu[DIM], fe = 0;
+        for (int it = threadIdx.x; it < CPB * ND; it += blockDim.x)
+        {
+            const int cl = it % CPB, nd = it / CPB;
+            const int64_t e = cell0 + cl;
+            if (e >= n)
+                continue;
+            double fu[DIM], fe = 0;
 #pragma unroll
-        for (int c = 0; c < DIM; ++c)
-            fu[c] = 0;
+            for (int c = 0; c < DIM; ++c)
+                fu[c] = 0;
 #pragma unroll 4
-        for (int q = 0; q < NIP; ++q)
-        {
-            const double* G = a.geo64 + NG_IDX(static_cast<int64_t>(q) * a.geoStride * n + e, a.geoSize, 6);
-            double g[DIM], b[DIM];
-#pragma unroll
-            for (int d = 0; d < DIM; ++d)
-                g[d] = G[(1 + nd * DIM + d) * n];
-            BtS<double, DIM>(g, sIp[cl][q], b);
-#pragma unroll
-            for (int c = 0; c < DIM; ++c)
-                fu[c] += b[c];
-            if (GD)
+            for (int q = 0; q < NIP; ++q)
             {
-                double s = a.tabN_D[q * ND + nd] * sIp[cl][q][VD];
+                const double* G = a.geo64 + NG_IDX(static_cast<int64_t>(q) * a.geoStride * n + e, a.geoSize, 6);
+                double g[DIM], b[DIM];
 #pragma unroll
                 for (int d = 0; d < DIM; ++d)
-                    s += g[d] * sIp[cl][q][VD + 1 + d];
-                fe += s;
-            }
-        }
-        const int64_t nLocal = static_cast<int64_t>(ND) * (DIM + (GD ? 1 : 0));
-        (void)nLocal; // buffer extent for checked builds
+                    g[d] = G[(1 + nd * DIM + d) * n];
+                BtS<double, DIM>(g, sIp[cl][q], b);
 #pragma unroll
-        for (int c = 0; c < DIM; ++c)
-            fcell[NG_IDX((static_cast<int64_t>(nd) * DIM + c) * n + e, nLocal * n, 8)] = fu[c];
-        if (GD)
-            fcell[NG_IDX((static_cast<int64_t>(ND) * DIM + nd) * n + e, nLocal * n, 8)] = fe;
+                for (int c = 0; c < DIM; ++c)
+                    fu[c] += b[c];
+                if (GD)
+                {
+                    double s = a.tabN_D[q * ND + nd] * sIp[cl][q][VD];
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                        s += g[d] * sIp[cl][q][VD + 1 + d];
+                    fe += s;
+                }
+            }
+            const int64_t nLocal = static_cast<int64_t>(ND) * (DIM + (GD ? 1 : 0));
+            (void)nLocal; // buffer extent for checked builds
+#pragma unroll
+            for (int c = 0; c < DIM; ++c)
+                fcell[NG_IDX((static_cast<int64_t>(nd) * DIM + c) * n + e, nLocal * n, 8)] = fu[c];
+            if (GD)
+                fcell[NG_IDX((static_cast<int64_t>(ND) * DIM + nd) * n + e, nLocal * n, 8)] = fe;
+        }
+        __syncthreads(); // the next pass overwrites the shared arrays
     }
 }
 
@@ -433,7 +399,7 @@ void GatherCellVectors(Ctx& c, const Slot& S, int ncomp, int off, int64_t nLocal
     AfterLaunch(c, "k_gather_cell_vectors");
 }
 
-void LaunchResidual(Ctx& c, const double* u, double* f)
+void LaunchResidual(Ctx& c, const double* u, double* f, int blocksPerSm)
 {
     const Slot& D = c.slots[c.prm.disp_slot];
     const bool gd = c.prm.kind == NUTO_GPU_GRADIENT_DAMAGE;
@@ -447,8 +413,11 @@ void LaunchResidual(Ctx& c, const double* u, double* f)
     DispatchCfg(c, [&](auto cfg) {
         using C = decltype(cfg);
         constexpr int CPB = MaxI<1, 128 / MaxI<C::nip, C::nd>::v>::v;
-        const int blocks = static_cast<int>((c.nCells + CPB - 1) / CPB);
-        k_residual<C::dim, C::nd, C::nip, C::kind><<<blocks, 128, 0, c.stream>>>(a, c.law, u, c.dCellVec.p);
+        int64_t blocks = (c.nCells + CPB - 1) / CPB;
+        if (blocksPerSm > 0)
+            blocks = std::min<int64_t>(blocks, static_cast<int64_t>(blocksPerSm) * std::max(c.smCount, 1));
+        k_residual<C::dim, C::nd, C::nip, C::kind><<<static_cast<unsigned>(blocks), 128, 0, c.stream>>>(
+                a, c.law, u, c.dCellVec.p);
     });
     AfterLaunch(c, "k_residual");
     GatherCellVectors(c, D, c.dim, 0, nLocal, f, false);
@@ -1352,6 +1321,9 @@ static void LaunchTangentRows(Ctx& c, const double* u, T* vals)
     c.stats.kernel_launches += 2;
 }
 
+// the allocating set-up of nuto_gpu_build_matrix_noalloc (defined with its static array below)
+static void PrepareNoAlloc(Ctx& c);
+
 template <typename T>
 static void LaunchTangentT(Ctx& c, const double* u, T* vals)
 {
@@ -1359,11 +1331,15 @@ static void LaunchTangentT(Ctx& c, const double* u, T* vals)
     // the rank-1 factors in the row kernel costs more than the FP64 atomics it saves.
     if (sizeof(T) == 4 && RowsSupported(c) && !c.forceAtomicTangent)
     {
-        // linear cells: geometry and law recomputed per node in FP32, no records; otherwise records + row gather
+        // linear cells: node rows from per-point records; Hex20: element matrices on the tensor cores + row
+        // gather; otherwise FP64-law records + row gather
         if (!c.forceRecordTangent && FusedTangentSupported(c))
             LaunchTangentFused(c, u, reinterpret_cast<float*>(vals));
+        else if (!c.forceRecordTangent && Tc20TangentSupported(c))
+            LaunchTangentTc20(c, u, reinterpret_cast<float*>(vals));
         else
             LaunchTangentRows<T>(c, u, vals);
+        PrepareNoAlloc(c);
         return;
     }
     NG_CUDA(cudaMemsetAsync(vals, 0, c.nnz * sizeof(T), c.stream));
@@ -1898,6 +1874,24 @@ static float* StaticRecords(int device)
         g_staticRecordsPtr[device] = static_cast<float*>(p);
     }
     return g_staticRecordsPtr[device];
+}
+
+// Everything of the no-alloc path that may take device memory, done by the first FP32 nuto_gpu_build_matrix of a
+// context (which may allocate): the static array's address on this device, and the two kernels of the path loaded.
+// With lazy module loading (the CUDA default) a kernel's code is loaded, into device memory, at its first launch or
+// attribute query; without this, the first no-alloc call would be that first launch.
+static void PrepareNoAlloc(Ctx& c)
+{
+    if (c.noAllocReady || !c.haveGeo || c.rowsMode != 1)
+        return;
+    StaticRecords(c.device);
+    DispatchCfg(c, [&](auto cfg) {
+        using C = decltype(cfg);
+        cudaFuncAttributes at{};
+        NG_CUDA(cudaFuncGetAttributes(&at, k_tangent<double, C::dim, C::nd, C::nip, C::kind, true, float>));
+        NG_CUDA(cudaFuncGetAttributes(&at, k_tangent_rows<float, C::dim, C::nd, C::nip, C::kind>));
+    });
+    c.noAllocReady = true;
 }
 
 void LaunchTangentNoAlloc(Ctx& c, const double* u, float* vals)

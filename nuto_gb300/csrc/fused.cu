@@ -820,7 +820,7 @@ __global__ void __launch_bounds__(128) k_point_records(FusedArgs A, LawParams L,
 // FP32 coordinates of every cell's nodes relative to its first node (planar [(n * dim + d)][cell]), formed in FP64
 // on the host once per mesh: the Jacobian of the fused tangent then sees differences of the size of the cell
 // instead of FP32 absolute coordinates
-static void BuildRelativeCoordinates(Ctx& c)
+void BuildRelativeCoordinates(Ctx& c)
 {
     const int nge = c.nge, dim = c.dim;
     std::vector<float> rel(static_cast<size_t>(nge) * dim * c.nCells);

@@ -385,8 +385,27 @@ struct Ctx
     int fusedMode = -1;
     bool tangentStaged = true; // per-point records computed once (NUTO_GPU_TANGENT=fused: recomputed per node warp)
     DBuf<float> dRelX;
+    // Hex20 FP32 tangent on the tensor cores: -1 not decided, 0 not applicable, 1 used; split 3 = three TF32
+    // products per contraction (hi.hi + hi.lo + lo.hi, FP32-level accuracy), 1 = one (NUTO_GPU_TC20=tf32);
+    // per-point records and per-cell element matrices ([cell][a][i][b][j], FP32)
+    int tc20Mode = -1;
+    int tc20Split = 3;
+    bool forceTc20Off = false; // NUTO_GPU_TC20=off
+    DBuf<float> dElemMats;
+    // device status word of kernels with bounded waits (0 = fine, else NUTO_GPU_ETIMEOUT), read after a stream
+    // synchronisation; spinLimit bounds every wait loop (iterations)
+    DBuf<int> dStatus;
+    long long spinLimit = 1LL << 22;
     // residual: the cell vectors of the last residual (planar [local entry][cell]) gathered per DOF
     DBuf<double> dCellVec;
+    // nuto_gpu_build_system: the residual on a second stream beside the tangent, as a persistent grid of
+    // sysResBlocks blocks per SM (the FP64 pipe needs few warps), the rest of every SM left to the tangent's
+    // blocks; the first call of a context runs both in sequence (lazy set-up, autotuning)
+    cudaStream_t sideStream = nullptr;
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
+    int sysResBlocks = 4;
+    bool noAllocReady = false; // nuto_gpu_build_matrix_noalloc: address looked up and kernels loaded
+    int64_t systemCalls = 0;
     // adjoint: positions of the transposed entries, per-point partial derivatives
     DBuf<int64_t> dTransPerm;
     DBuf<double> dAdjPart;
@@ -420,12 +439,15 @@ struct Ctx
 // ---- host helpers implemented in the .cu files ----
 void BuildTables(Ctx& c);
 void BuildGeometryCache(Ctx& c);
-void LaunchResidual(Ctx& c, const double* u, double* f);
+void LaunchResidual(Ctx& c, const double* u, double* f, int blocksPerSm = 0); // 0: one block per CPB cells
 void LaunchTangent(Ctx& c, const double* u, int precision, void* values);
 void LaunchTangentExact(Ctx& c, const double* u, double* vals);
 void LaunchTangentNoAlloc(Ctx& c, const double* u, float* values);
 bool FusedTangentSupported(Ctx& c);
 void LaunchTangentFused(Ctx& c, const double* u, float* vals);
+bool Tc20TangentSupported(Ctx& c);
+void LaunchTangentTc20(Ctx& c, const double* u, float* vals);
+int ReadDeviceStatus(Ctx& c); // after a stream synchronisation: the status word (and reset to 0)
 void LaunchHistory(Ctx& c, const double* u);
 void LaunchLumpedMass(Ctx& c, double rho, double* m);
 void LaunchExternalLoad(Ctx& c, const BoundaryGroup& B, const double* p, double* f);
@@ -486,6 +508,45 @@ void LaunchTransposeValues(Ctx& c, int precision, const void* in, void* out);
 void LaunchAdjointHistoryLoad(Ctx& c, const double* u, const double* kbar, double* ubar);
 void LaunchAdjointStep(Ctx& c, const double* u, const double* lam, const double* kbarIn, double* kbarOut,
                        double* gradE, double* gradParams);
+
+// Engineering strain from the displacement gradient H[c][d] = sum_n u_nc dN_n/dx_d, Voigt order of
+// Nabla::Strain (DifferentialOperators.h:24-90): 2D xx, yy, xy; 3D xx, yy, zz, yz, zx, xy.
+template <typename T, int DIM>
+__device__ __forceinline__ void StrainFromH(const T (&H)[DIM][DIM], T* e)
+{
+    if (DIM == 2)
+    {
+        e[0] = H[0][0];
+        e[1] = H[1][1];
+        e[2] = H[0][1] + H[1][0];
+    }
+    else
+    {
+        e[0] = H[0][0];
+        e[1] = H[1][1];
+        e[2] = H[2][2];
+        e[3] = H[1][2] + H[2][1];
+        e[4] = H[0][2] + H[2][0];
+        e[5] = H[0][1] + H[1][0];
+    }
+}
+
+// B_n^T s for the node with global gradient g (columns of the Voigt strain operator)
+template <typename T, int DIM>
+__device__ __forceinline__ void BtS(const T* g, const T* s, T* out)
+{
+    if (DIM == 2)
+    {
+        out[0] = g[0] * s[0] + g[1] * s[2];
+        out[1] = g[1] * s[1] + g[0] * s[2];
+    }
+    else
+    {
+        out[0] = g[0] * s[0] + g[2] * s[4] + g[1] * s[5];
+        out[1] = g[1] * s[1] + g[2] * s[3] + g[0] * s[5];
+        out[2] = g[2] * s[2] + g[1] * s[3] + g[0] * s[4];
+    }
+}
 
 // ------------------------------------------------------------------------------------------------------------
 // Constitutive laws, device side, templated on the arithmetic type. Each cites the reference it restates.

@@ -363,6 +363,12 @@ int DoStep(Ctx& c, double tNew, const nuto_gpu_step_options& o, int* itersOut)
     LaunchHistory(c, w.xs.p);
     NG_CUDA(cudaMemcpyAsync(x, w.xs.p, n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
     NG_CUDA(cudaStreamSynchronize(c.stream));
+    if (ReadDeviceStatus(c) != 0)
+    {
+        finish();
+        c.err = "a bounded device wait gave up";
+        return NUTO_GPU_ETIMEOUT;
+    }
     c.time = tNew;
     finish();
     return NUTO_GPU_OK;

@@ -45,7 +45,7 @@ def hex8_gradient_damage(n, length=4.0, u_end=2e-3, law=None):
     return m, [d, e], P, cons
 
 
-def hex20_local_damage(n, u_end=3e-4):
+def hex20_local_damage(n, u_end=5e-5):
     m = core.Mesh.bricks(n, n, n)
     d = m.add_dof(3, core.HEX20)
     integ = core.Integrand.make(core.MB_LOCAL_DAMAGE, 3, E=30000.0, nu=0.2, damage_application=core.FULL,

@@ -329,3 +329,33 @@ def test_pipelined_node_rows_bitwise_equal(kind, n, monkeypatch):
     piped = g2.build_matrix(u, nuto_gb300.FP32).cpu().numpy()
     assert g2.autotune_info()["tangent_pipelined"]
     assert np.array_equal(piped, plain)
+
+
+@pytest.mark.parametrize("kind,n", [("hex8gd", 8), ("quad4gd", 16), ("quad4", 12)])
+@pytest.mark.parametrize("precision", [32, 64])
+@pytest.mark.parametrize("res_blocks", ["2", "1"])
+def test_build_system_equals_separate_calls(kind, n, precision, res_blocks, monkeypatch):
+    """nuto_gpu_build_system (the residual on a second stream, a persistent grid of a few blocks per SM beside the
+    tangent) gives the values of nuto_gpu_build_matrix and nuto_gpu_build_vector: on its first call (run in
+    sequence) and on the later, concurrent ones, on two states in turn. Bitwise, except the FP64 tangent, whose
+    element kernel adds with FP64 atomics (order-dependent rounding)."""
+    torch = _torch()
+    monkeypatch.setenv("NUTO_GPU_SYSTEM_RES_BLOCKS", res_blocks)
+    s, o = _setup(kind, n)
+    g = s.build_gpu()
+    P = o[2]
+    rng = np.random.default_rng(4)
+    states = [_damage_state(kind, s, P, rng) for _ in range(2)]
+    for k in range(4):
+        u, kappa = states[k % 2]
+        if kappa is not None:
+            g.history = kappa
+        v, f = g.build_system(u, precision)
+        v2 = g.build_matrix(u, precision)
+        f2 = g.build_vector(u)
+        torch.cuda.synchronize()
+        if precision == 32:
+            assert torch.equal(v, v2), k
+        else:
+            assert float((v - v2).abs().max()) <= 1e-13 * float(v2.abs().max()), k
+        assert torch.equal(f, f2), k
