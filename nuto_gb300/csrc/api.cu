@@ -601,6 +601,7 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
     const char* t20 = std::getenv("NUTO_GPU_TC20");
     c->forceTc20Off = t20 && std::string(t20) == "off";
     c->tc20Split = t20 && std::string(t20) == "tf32" ? 1 : 3;
+    c->tc20LawFp64 = t20 && std::string(t20) == "fp64law" ? 1 : 0;
     const char* at = std::getenv("NUTO_GPU_AUTOTUNE");
     c->tuning.enabled = !(at && at[0] == '0');
     const char* gr = std::getenv("NUTO_GPU_GMRES_RESTART");

@@ -391,6 +391,7 @@ struct Ctx
     int tc20Mode = -1;
     int tc20Split = 3;
     bool forceTc20Off = false; // NUTO_GPU_TC20=off
+    int tc20LawFp64 = 0;       // NUTO_GPU_TC20=fp64law: the law of every point in FP64
     DBuf<float> dElemMats;
     // device status word of kernels with bounded waits (0 = fine, else NUTO_GPU_ETIMEOUT), read after a stream
     // synchronisation; spinLimit bounds every wait loop (iterations)

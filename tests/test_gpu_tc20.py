@@ -127,3 +127,26 @@ def test_tc20_wait_gives_up_with_etimeout_and_context_stays_usable():
     v = g.build_matrix(u, nuto_gb300.FP32).double().cpu().numpy()
     g.synchronize()
     assert np.array_equal(v, ref)
+
+
+def test_tc20_at_converged_damaged_states():
+    """After FP64 load steps into the damaged range every loading point has eq = kappa_h (the history update wrote
+    it at that state): the tensor-core tangent must treat those points as loading like the FP64 tangent does, or it
+    loses their rank-1 softening term. 8^3 cells, u_z = 1.5e-4 at t = 1, steps t = 0.2 and 0.4 (damage at the fixed
+    face); the FP32 tangent within 2e-6 of the FP64 tangent after each step."""
+    torch = _torch()
+    import nuto_gb300
+    from nuto_gb300 import configs
+
+    s = configs.hex20_local_damage(8, u_end=1.5e-4, load_steps=5)
+    g = s.build_gpu()
+    o = g.default_options(precision=nuto_gb300.FP64, newton_rtol=1e-10, krylov_rtol=1e-10, forcing=0,
+                          max_newton=40, max_krylov=20000)
+    g.set_state(None, 0.0, True)
+    for t in (0.2, 0.4):
+        g.do_step(t, o)
+        x = torch.as_tensor(g.get_state()[0], device="cuda")
+        k64 = g.build_matrix(x, nuto_gb300.FP64)
+        k32 = g.build_matrix(x, nuto_gb300.FP32).double()
+        assert float((k32 - k64).abs().max()) <= FP32_REL * float(k64.abs().max()), t
+    assert float(np.max(g.history)) > 1e-4  # damaged points present
