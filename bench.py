@@ -631,7 +631,7 @@ def run_ours(args):
     # launch shapes the autotuner chose (first tangent, first Krylov products) with the times it measured, and the
     # gain over the default shapes (4 warps per block, 8 lanes per node)
     tune = g.autotune_info()
-    tms = tune["tangent_ms"] + tune["tangent_pipelined_ms"]
+    tms = tune["tangent_ms"] + tune["tangent_pipelined_ms"] + tune["tangent_cells_ms"]
     if tune["tangent_warps"] and min(tms) > 0:
         tune["tangent_gain_over_default"] = tms[1] / min(tms)
     for k, ms in tune["spmv_ms"].items():

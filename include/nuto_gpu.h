@@ -208,13 +208,14 @@ int nuto_gpu_solver_layout(const nuto_gpu_ctx* ctx, int64_t* padded_values, int6
 int nuto_gpu_multigrid_info(const nuto_gpu_ctx* ctx, int* levels, int* graph_active);
 
 /* Launch shapes chosen by the autotuner (no counterpart in the reference). The first FP32 tangent of a context
-   times its node-row kernel with 2, 4 and 8 warps per block and the double-buffered variant (a grid of resident
-   blocks) with 2 and 4, and the first Krylov product per (value, vector) type pair times the padded-layout kernel
-   with 4, 8 and 16 lanes per node; each keeps the fastest (environment NUTO_GPU_AUTOTUNE=0 keeps the defaults: 4
-   warps, not double-buffered, 8 lanes). choices (6 ints): tangent warps per block, 1 if double-buffered, then the
-   lanes per node for (FP32 values, FP32 vectors), (FP32, FP64), (FP64, FP32), (FP64, FP64); 0 = not tuned yet.
-   times_ms (17 floats): the tangent with 2 / 4 / 8 warps, double-buffered with 2 / 4 warps, then per type pair the
-   product with 4 / 8 / 16 lanes (one launch each). */
+   times its node-row kernel with 2, 4 and 8 warps per block, the double-buffered variant (a grid of resident
+   blocks) with 2 and 4 and the element-matrix form (cell matrices, then a row gather) with 2 and 4, and the first
+   Krylov product per (value, vector) type pair times the padded-layout kernel with 4, 8 and 16 lanes per node; each
+   keeps the fastest (environment NUTO_GPU_AUTOTUNE=0 keeps the defaults: 4 warps, node rows, 8 lanes). choices
+   (6 ints): tangent warps per block, the tangent's form (0 node rows, 1 double-buffered, 2 element matrices), then
+   the lanes per node for (FP32 values, FP32 vectors), (FP32, FP64), (FP64, FP32), (FP64, FP64); 0 = not tuned yet.
+   times_ms (19 floats): the tangent with 2 / 4 / 8 warps, double-buffered with 2 / 4 warps, then per type pair the
+   product with 4 / 8 / 16 lanes (one launch each), then the element-matrix form with 2 / 4 warps. */
 int nuto_gpu_autotune_info(const nuto_gpu_ctx* ctx, int* choices, float* times_ms);
 /* Iteration limit of every bounded device wait (no counterpart in the reference; default 4,194,304): the tensor-core
    tangent of Hex20 cells waits on its MMA completion barrier. A wait that runs out sets NUTO_GPU_ETIMEOUT in the

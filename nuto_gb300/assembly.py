@@ -113,15 +113,18 @@ class GpuCellGroup:
         return lv.value, ga.value
 
     def autotune_info(self):
-        """Launch shapes the autotuner chose and the times it measured: {"tangent_warps": W, "tangent_pipelined": bool,
-        "tangent_ms": [2, 4, 8 warps], "tangent_pipelined_ms": [2, 4 warps], "spmv_lanes": {"f32/f32": G, ...},
+        """Launch shapes the autotuner chose and the times it measured: {"tangent_warps": W, "tangent_form":
+        "node_rows" | "pipelined" | "cell_matrices", "tangent_pipelined": bool, "tangent_ms": [2, 4, 8 warps],
+        "tangent_pipelined_ms": [2, 4 warps], "tangent_cells_ms": [2, 4 warps], "spmv_lanes": {"f32/f32": G, ...},
         "spmv_ms": {"f32/f32": [4, 8, 16 lanes], ...}} (0: not tuned)."""
         ch = np.zeros(6, dtype=np.int32)
-        ms = np.zeros(17, dtype=np.float32)
+        ms = np.zeros(19, dtype=np.float32)
         self._call("nuto_gpu_autotune_info", _ptr(ch), _ptr(ms))
         names = ["f32/f32", "f32/f64", "f64/f32", "f64/f64"]
-        return {"tangent_warps": int(ch[0]), "tangent_pipelined": bool(ch[1]),
+        forms = ["node_rows", "pipelined", "cell_matrices"]
+        return {"tangent_warps": int(ch[0]), "tangent_form": forms[int(ch[1])], "tangent_pipelined": int(ch[1]) == 1,
                 "tangent_ms": [float(v) for v in ms[:3]], "tangent_pipelined_ms": [float(v) for v in ms[3:5]],
+                "tangent_cells_ms": [float(v) for v in ms[17:19]],
                 "spmv_lanes": {k: int(ch[2 + i]) for i, k in enumerate(names)},
                 "spmv_ms": {k: [float(v) for v in ms[5 + 3 * i:8 + 3 * i]] for i, k in enumerate(names)}}
 

@@ -594,7 +594,12 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
     if (tk && std::string(tk) == "pipelined")
     {
         c->tuning.tangentWarps = 4; // the double-buffered node-row kernel, not tuned
-        c->tuning.tangentPipe = true;
+        c->tuning.tangentForm = 1;
+    }
+    if (tk && std::string(tk) == "cells")
+    {
+        c->tuning.tangentWarps = 4; // element matrices + row gather, not tuned
+        c->tuning.tangentForm = 2;
     }
     // Hex20 FP32 tangent: tensor cores with split TF32 (default), one TF32 product (tf32) or records + row
     // gather (off)
@@ -901,7 +906,7 @@ int nuto_gpu_autotune_info(const nuto_gpu_ctx* ctx, int* choices, float* times_m
     if (choices)
     {
         choices[0] = T.tangentWarps;
-        choices[1] = T.tangentPipe ? 1 : 0;
+        choices[1] = T.tangentForm;
         for (int k = 0; k < 4; ++k)
             choices[2 + k] = T.spmvGroup[k];
     }
@@ -912,6 +917,8 @@ int nuto_gpu_autotune_info(const nuto_gpu_ctx* ctx, int* choices, float* times_m
         for (int p = 0; p < 4; ++p)
             for (int k = 0; k < 3; ++k)
                 times_ms[5 + 3 * p + k] = T.spmvMs[p][k];
+        times_ms[17] = T.tangentMs[5];
+        times_ms[18] = T.tangentMs[6];
     }
     return NUTO_GPU_OK;
 }

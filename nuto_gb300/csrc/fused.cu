@@ -815,6 +815,387 @@ __global__ void __launch_bounds__(128) k_point_records(FusedArgs A, LawParams L,
     }
 }
 
+// ---- element-matrix form (NUTO_GPU_TANGENT=cells, an autotuner candidate) ------------------------------------
+// k_point_records as for the staged node rows, then
+//   k_cell_matrices  one warp per cell: the cell's records staged into shared memory; per (point, node) the vectors
+//                    P = B^T sv, gs = (c g' w' k' w grad eeq) . g and Q = B^T tv once; lane (a, b) integrates the
+//                    node-pair blocks (a, b) and (a + ND/2, b) over the points with the node-row kernel's
+//                    expressions, and the cell's element matrix goes to global memory as ND slabs, one per local
+//                    node a: NR rows (a's displacement components, then its eeq row) x NC columns (the
+//                    displacement components of b = 0..ND-1, b-major, then the eeq of b = 0..ND-1);
+//   k_rows_from_cells one warp per displacement node: the slabs of its cells added in ascending cell order into
+//                    shared rows at the ranks of b (a cell's b are distinct nodes: no conflicts), rows stored once.
+// Every node-pair block is integrated once (the node rows form it once per row node) and the per-block sums and their
+// order over the cells are those of the node-row kernel: the values are bitwise the same.
+template <int DIM, int ND, int KIND>
+struct CellSlab
+{
+    static constexpr bool GD = KIND == NUTO_GPU_GRADIENT_DAMAGE;
+    static constexpr int nr = DIM + (GD ? 1 : 0);            // rows per local node
+    static constexpr int nc = ND * DIM + (GD ? ND : 0);       // columns per row
+    static constexpr int size = nr * nc;                      // floats per slab (global)
+    static constexpr int pad = (size + 4 + 3) / 4 * 4;        // floats per slab in shared memory (16-byte rows, banks)
+};
+
+template <int DIM, int ND, int NIP, int KIND, int W>
+__global__ void __launch_bounds__(W * 32) k_cell_matrices(int64_t nCells, const float4* __restrict__ recs,
+                                                          float* __restrict__ em)
+{
+    using Sh = FusedShape<DIM, ND, NIP, KIND, true>;
+    using CS = CellSlab<DIM, ND, KIND>;
+    constexpr bool GD = Sh::GD;
+    constexpr int R4 = Sh::recF4;
+    constexpr int PER_CELL = NIP * R4;
+    constexpr int PAIRS = ND * ND;
+    constexpr int PPL = (PAIRS + 31) / 32; // node pairs per lane
+    extern __shared__ __align__(16) float smC[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int recF = PER_CELL * 4, pqF = GD ? NIP * ND * 8 : 0, emF = ND * CS::pad;
+    float4* sR = reinterpret_cast<float4*>(smC + wid * (recF + pqF + emF));
+    float4* sPQ = sR + PER_CELL;                                   // [NIP][ND][2]: (P, gs), (Q, 0)
+    float* sEM = smC + wid * (recF + pqF + emF) + recF + pqF;      // [ND][pad]
+    const int64_t e = static_cast<int64_t>(blockIdx.x) * W + wid;
+    if (e >= nCells)
+        return; // the whole warp leaves; only warp-level synchronisation follows
+    const float4* src = recs + NG_IDX(e, nCells, 70) * PER_CELL;
+    for (int i = lane; i < PER_CELL; i += 32)
+    {
+        const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(sR + i));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + i) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncwarp();
+    if (GD)
+    {
+        // per (point, node): P = B^T sv and gs as PrepRecords forms them for the row node, Q = B^T tv as PassBlocks
+        for (int it = lane; it < NIP * ND; it += 32)
+        {
+            const int q = it / ND, nd = it % ND;
+            const float4* row = sR + q * R4;
+            const float4 g = row[nd];
+            const float4* S = row + ND;
+            const float4 s1 = S[1], s2 = S[2], s3 = S[3], s4 = S[4];
+            const float sv[6] = {s4.x, s4.y, s4.z, s4.w, s1.w, s2.w};
+            const float tv[6] = {s2.x, s2.y, s2.z, s3.x, s3.y, s3.z};
+            const float3 pa = BtV<DIM>(g.x, g.y, g.z, sv);
+            const float gs = g.x * s1.x + g.y * s1.y + (DIM == 3 ? g.z * s1.z : 0.f);
+            const float3 qb = BtV<DIM>(g.x, g.y, g.z, tv);
+            sPQ[(q * ND + nd) * 2] = F4(pa.x, pa.y, pa.z, gs);
+            sPQ[(q * ND + nd) * 2 + 1] = F4(qb.x, qb.y, qb.z, 0.f);
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int m = 0; m < PPL; ++m)
+    {
+        const int p = lane + 32 * m;
+        if (p >= PAIRS)
+            continue;
+        const int ia = p / ND, b = p % ND;
+        float uu[DIM][DIM], ue[DIM], eu[DIM], ee = 0.f, dg = 0.f;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            ue[k] = eu[k] = 0.f;
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                uu[k][l] = 0.f;
+        }
+#pragma unroll 2
+        for (int q = 0; q < NIP; ++q)
+        {
+            const float4* G = sR + q * R4;
+            const float4* SR = G + ND;
+            const float4 ga = G[ia], gb = G[b];
+            const float4 s0 = SR[0];
+            const float av[3] = {ga.x, ga.y, ga.z}, bv[3] = {gb.x, gb.y, gb.z};
+            float gab = 0.f;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                gab += av[d] * bv[d];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k)
+            {
+                const float lk = s0.x * av[k], mk = s0.y * bv[k];
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    uu[k][l] += lk * bv[l] + mk * av[l];
+            }
+            dg += s0.y * gab;
+            if (GD)
+            {
+                const float4 pa = sPQ[(q * ND + ia) * 2];
+                const float4 qb = sPQ[(q * ND + b) * 2 + 1];
+                const float pv[3] = {pa.x, pa.y, pa.z}, qv[3] = {qb.x, qb.y, qb.z};
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                {
+                    ue[k] += pv[k] * gb.w;
+                    eu[k] -= ga.w * qv[k];
+                }
+                ee += (s0.z * ga.w + pa.w) * gb.w + s0.w * gab;
+            }
+        }
+        float* slab = sEM + ia * CS::pad;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                slab[k * CS::nc + b * DIM + l] = uu[k][l] + (k == l ? dg : 0.f);
+            if (GD)
+                slab[k * CS::nc + ND * DIM + b] = ue[k];
+        }
+        if (GD)
+        {
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                slab[DIM * CS::nc + b * DIM + l] = eu[l];
+            slab[DIM * CS::nc + ND * DIM + b] = ee;
+        }
+    }
+    __syncwarp();
+    // the element matrix, slab after slab, with 16-byte stores (slab sizes are multiples of 4 floats)
+    static_assert(CS::size % 4 == 0, "slabs of whole float4");
+    float4* dst = reinterpret_cast<float4*>(em + NG_IDX(e, nCells, 71) * (ND * CS::size));
+    for (int i = lane; i < ND * CS::size / 4; i += 32)
+    {
+        const int a = i / (CS::size / 4), j = i % (CS::size / 4);
+        dst[i] = *reinterpret_cast<const float4*>(sEM + a * CS::pad + 4 * j);
+    }
+}
+
+template <int DIM, int ND, int NIP, int KIND, int W>
+__global__ void __launch_bounds__(W * 32) k_rows_from_cells(FusedArgs A, const float* __restrict__ em,
+                                                            float* __restrict__ vals)
+{
+    using CS = CellSlab<DIM, ND, KIND>;
+    constexpr bool GD = CS::GD;
+    constexpr int NR = CS::nr, NC = CS::nc, SL = CS::size;
+    constexpr int PER = (SL + 31) / 32; // slab values per lane
+    __shared__ float sRowAll[W][NR * kFusedRowCap];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * W + wid;
+    if (a >= A.nNodes)
+        return; // the whole warp leaves; only warp-level synchronisation follows
+    float* sRow = sRowAll[wid];
+    int64_t rs[NR];
+    int len[NR];
+    const int64_t g0 = A.gdofD[a];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+    {
+        rs[k] = A.rowPtr[NG_IDX(g0 + k, A.nRows, 72)];
+        len[k] = static_cast<int>(A.rowPtr[g0 + k + 1] - rs[k]);
+    }
+    int32_t ae = 0;
+    if (GD)
+    {
+        ae = A.eOf[a];
+        const int64_t ge = A.gdofE[ae];
+        rs[DIM] = A.rowPtr[NG_IDX(ge, A.nRows, 72)];
+        len[DIM] = static_cast<int>(A.rowPtr[ge + 1] - rs[DIM]);
+    }
+    const int32_t bUU = A.blk[0][a];
+    const int32_t bUE = GD ? A.blk[1][a] : 0;
+    const int32_t bEU = GD ? A.blk[2][ae] : 0;
+    const int32_t bEE = GD ? A.blk[3][ae] : 0;
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+        for (int i = lane; i < kFusedRowCap; i += 32)
+            sRow[k * kFusedRowCap + i] = 0.f;
+    const int64_t n = A.nCells;
+    const int64_t k0 = A.cellPtr[a], k1 = A.cellPtr[a + 1];
+    // the slab values of the next cell are loaded while the current one is added
+    float nxt[PER];
+    auto load = [&](int64_t kc, float (&v)[PER]) {
+        const int64_t e = A.cellIdx[kc];
+        const int ia = A.cellLoc[kc];
+        const float* slab = em + (NG_IDX(e, n, 73) * ND + ia) * SL;
+#pragma unroll
+        for (int m = 0; m < PER; ++m)
+        {
+            const int i = lane + 32 * m;
+            v[m] = i < SL ? slab[i] : 0.f;
+        }
+    };
+    if (k0 < k1)
+        load(k0, nxt);
+    for (int64_t kc = k0; kc < k1; ++kc)
+    {
+        float cur[PER];
+#pragma unroll
+        for (int m = 0; m < PER; ++m)
+            cur[m] = nxt[m];
+        const int64_t e = A.cellIdx[kc];
+        const int ia = A.cellLoc[kc];
+        // ranks of b in a's neighbour lists: lane b loads them, the others read them by shuffles
+        int r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+        if (lane < ND)
+        {
+            const int64_t ridx = static_cast<int64_t>(ia * ND + lane) * n + e;
+            r0 = A.rank[0][ridx];
+            if (GD)
+            {
+                r1 = A.rank[1][ridx];
+                r2 = A.rank[2][ridx];
+                r3 = A.rank[3][ridx];
+            }
+        }
+        if (kc + 1 < k1)
+            load(kc + 1, nxt);
+#pragma unroll
+        for (int m = 0; m < PER; ++m)
+        {
+            const int i = lane + 32 * m;
+            const int ic = i < SL ? i : 0;
+            const int row = ic / NC, col = ic % NC;
+            const bool ucol = col < ND * DIM;
+            const int b = ucol ? col / DIM : col - ND * DIM;
+            const int l = ucol ? col % DIM : 0;
+            const int rk0 = __shfl_sync(0xffffffffu, r0, b);
+            int pos;
+            if (GD)
+            {
+                const int rk1 = __shfl_sync(0xffffffffu, r1, b);
+                const int rk2 = __shfl_sync(0xffffffffu, r2, b);
+                const int rk3 = __shfl_sync(0xffffffffu, r3, b);
+                if (row < DIM)
+                    pos = ucol ? bUU + DIM * rk0 + l : bUE + rk1;
+                else
+                    pos = ucol ? bEU + DIM * rk2 + l : bEE + rk3;
+            }
+            else
+                pos = bUU + DIM * rk0 + l;
+            if (i < SL)
+                sRow[row * kFusedRowCap + NG_IDX(pos, kFusedRowCap, 74)] += cur[m];
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+        for (int i = lane; i < len[k]; i += 32)
+            vals[NG_IDX(rs[k] + i, A.nnz, 75)] = sRow[k * kFusedRowCap + i];
+}
+
+// The ranks of one (cell entry of a node, neighbour b) packed into one word (UU | UE << 8 | EU << 16 | EE << 24), in
+// the order of the nodes' cell lists: the row gather of a node then reads the ranks of its cells with contiguous
+// loads instead of byte loads from the planar rank tables. Built once per mesh.
+template <int ND>
+__global__ void k_pack_ranks(FusedArgs A, int64_t nEntries, uint32_t* __restrict__ packed)
+{
+    const int64_t it = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (it >= nEntries * ND)
+        return;
+    const int64_t kc = it / ND;
+    const int b = static_cast<int>(it % ND);
+    const int64_t e = A.cellIdx[kc];
+    const int ia = A.cellLoc[kc];
+    const int64_t ridx = static_cast<int64_t>(ia * ND + b) * A.nCells + e;
+    packed[it] = static_cast<uint32_t>(A.rank[0][ridx]) | static_cast<uint32_t>(A.rank[1][ridx]) << 8 |
+                 static_cast<uint32_t>(A.rank[2][ridx]) << 16 | static_cast<uint32_t>(A.rank[3][ridx]) << 24;
+}
+
+// Row gather of the element-matrix form for slabs of exactly 32 columns (Hex8 gradient damage: 24 displacement
+// columns, 8 eeq columns): lane l owns column l of every slab row, so its neighbour b = l / 3 (or l - 24), and the
+// positions in the displacement rows and in the eeq row are fixed per cell. The slab values and packed ranks of up
+// to 8 cells are loaded before any is added (all loads in flight at once); cells are added in ascending order.
+template <int DIM, int ND, int NIP, int KIND, int W>
+__global__ void __launch_bounds__(W * 32) k_rows_from_cells32(FusedArgs A, const uint32_t* __restrict__ packed,
+                                                              const float* __restrict__ em, float* __restrict__ vals)
+{
+    using CS = CellSlab<DIM, ND, KIND>;
+    constexpr bool GD = CS::GD;
+    constexpr int NR = CS::nr, SL = CS::size;
+    static_assert(CS::nc == 32 && ND == 8, "one slab column per lane, 8 nodes per cell");
+    constexpr int CB = 8; // cells per batch
+    __shared__ float sRowAll[W][NR * kFusedRowCap];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * W + wid;
+    if (a >= A.nNodes)
+        return; // the whole warp leaves; only warp-level synchronisation follows
+    float* sRow = sRowAll[wid];
+    int64_t rs[NR];
+    int len[NR];
+    const int64_t g0 = A.gdofD[a];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+    {
+        rs[k] = A.rowPtr[NG_IDX(g0 + k, A.nRows, 76)];
+        len[k] = static_cast<int>(A.rowPtr[g0 + k + 1] - rs[k]);
+    }
+    int32_t ae = 0;
+    if (GD)
+    {
+        ae = A.eOf[a];
+        const int64_t ge = A.gdofE[ae];
+        rs[DIM] = A.rowPtr[NG_IDX(ge, A.nRows, 76)];
+        len[DIM] = static_cast<int>(A.rowPtr[ge + 1] - rs[DIM]);
+    }
+    const int32_t bUU = A.blk[0][a];
+    const int32_t bUE = GD ? A.blk[1][a] : 0;
+    const int32_t bEU = GD ? A.blk[2][ae] : 0;
+    const int32_t bEE = GD ? A.blk[3][ae] : 0;
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+        for (int i = lane; i < kFusedRowCap; i += 32)
+            sRow[k * kFusedRowCap + i] = 0.f;
+    const bool ucol = lane < ND * DIM;
+    const int myB = ucol ? lane / DIM : lane - ND * DIM;
+    const int myL = ucol ? lane % DIM : 0;
+    const int64_t n = A.nCells; // extent of the checked indices
+    (void)n;
+    const int64_t k0 = A.cellPtr[a], k1 = A.cellPtr[a + 1];
+    for (int64_t kb = k0; kb < k1; kb += CB)
+    {
+        const int nc = static_cast<int>(k1 - kb < CB ? k1 - kb : CB);
+        // packed ranks of the batch: lane l holds (cell slot l / 8, b = l % 8) and (cell slot 4 + l / 8, b)
+        uint32_t pk0 = 0, pk1 = 0;
+        if (lane / ND < nc)
+            pk0 = packed[NG_IDX((kb + lane / ND) * ND + lane % ND, n * ND * ND, 77)];
+        if (4 + lane / ND < nc)
+            pk1 = packed[NG_IDX((kb + 4 + lane / ND) * ND + lane % ND, n * ND * ND, 77)];
+        float v[CB][NR];
+#pragma unroll
+        for (int c = 0; c < CB; ++c)
+        {
+            if (c < nc)
+            {
+                const int64_t kc = kb + c;
+                const float* slab = em + (NG_IDX(A.cellIdx[kc], n, 78) * ND + A.cellLoc[kc]) * SL;
+#pragma unroll
+                for (int r = 0; r < NR; ++r)
+                    v[c][r] = slab[r * 32 + lane];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CB; ++c)
+        {
+            // all lanes take part in the shuffle; cells beyond the batch add nothing
+            const uint32_t w = __shfl_sync(0xffffffffu, c < 4 ? pk0 : pk1, (c & 3) * ND + myB);
+            if (c < nc)
+            {
+                const int r0 = w & 0xff, r1 = (w >> 8) & 0xff, r2 = (w >> 16) & 0xff, r3 = w >> 24;
+                const int posU = ucol ? bUU + DIM * r0 + myL : bUE + r1;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                    sRow[k * kFusedRowCap + NG_IDX(posU, kFusedRowCap, 79)] += v[c][k];
+                if (GD)
+                {
+                    const int posE = ucol ? bEU + DIM * r2 + myL : bEE + r3;
+                    sRow[DIM * kFusedRowCap + NG_IDX(posE, kFusedRowCap, 79)] += v[c][DIM];
+                }
+            }
+            __syncwarp();
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+        for (int i = lane; i < len[k]; i += 32)
+            vals[NG_IDX(rs[k] + i, A.nnz, 75)] = sRow[k * kFusedRowCap + i];
+}
+
 } // namespace
 
 // FP32 coordinates of every cell's nodes relative to its first node (planar [(n * dim + d)][cell]), formed in FP64
@@ -908,9 +1289,9 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
         A.blk[k] = c.pairs[pr[k]].dBlk.p;
     }
     const bool staged = c.tangentStaged;
-    // one assembly with W warps per block of the node-row kernel; pipe: the double-buffered kernel on a grid of
-    // resident blocks (staged records only)
-    auto assemble = [&](int W, bool pipe) {
+    // one assembly with W warps per block; form 0: the node-row kernel, 1: the double-buffered node-row kernel on a
+    // grid of resident blocks, 2: element matrices + row gather (1 and 2 with staged records only)
+    auto assemble = [&](int W, int form) {
         auto run = [&](auto cfg) {
             using C = decltype(cfg);
             constexpr int DIM = C::dim, ND = C::nd, NIP = C::nip, KIND = C::kind;
@@ -930,7 +1311,48 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
             }
             auto rows = [&](auto w) {
                 constexpr int WW = decltype(w)::value;
-                if (staged && pipe)
+                if (staged && form == 2)
+                {
+                    using CS = CellSlab<DIM, ND, KIND>;
+                    const size_t emFloats = static_cast<size_t>(c.nCells) * ND * CS::size;
+                    if (c.dElemMats.n < emFloats)
+                        c.dElemMats.alloc(emFloats);
+                    constexpr int recF = NIP * FusedShape<DIM, ND, NIP, KIND, true>::recF4 * 4;
+                    constexpr int pqF = CS::GD ? NIP * ND * 8 : 0;
+                    constexpr size_t smem = static_cast<size_t>(WW) * (recF + pqF + ND * CS::pad) * sizeof(float);
+                    auto kern = k_cell_matrices<DIM, ND, NIP, KIND, WW>;
+                    if (smem > 48 * 1024)
+                        NG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     static_cast<int>(smem)));
+                    kern<<<static_cast<unsigned>((c.nCells + WW - 1) / WW), WW * 32, smem, c.stream>>>(
+                            c.nCells, recs, c.dElemMats.p);
+                    AfterLaunch(c, "k_cell_matrices");
+                    const unsigned rowBlocks = static_cast<unsigned>((A.nNodes + WW - 1) / WW);
+                    if constexpr (CS::nc == 32 && ND == 8)
+                    {
+                        // packed ranks in cell-list order, once per mesh
+                        const int64_t entries = static_cast<int64_t>(c.nCells) * ND;
+                        if (c.dPackedRanks.n != static_cast<size_t>(entries * ND))
+                        {
+                            c.dPackedRanks.alloc(static_cast<size_t>(entries * ND));
+                            k_pack_ranks<ND><<<static_cast<unsigned>((entries * ND + 255) / 256), 256, 0, c.stream>>>(
+                                    A, entries, c.dPackedRanks.p);
+                            AfterLaunch(c, "k_pack_ranks");
+                        }
+                        k_rows_from_cells32<DIM, ND, NIP, KIND, WW><<<rowBlocks, WW * 32, 0, c.stream>>>(
+                                A, c.dPackedRanks.p, c.dElemMats.p, vals);
+                        AfterLaunch(c, "k_rows_from_cells32");
+                    }
+                    else
+                    {
+                        k_rows_from_cells<DIM, ND, NIP, KIND, WW><<<rowBlocks, WW * 32, 0, c.stream>>>(
+                                A, c.dElemMats.p, vals);
+                        AfterLaunch(c, "k_rows_from_cells");
+                    }
+                    c.stats.kernel_launches += 2;
+                    return;
+                }
+                if (staged && form == 1)
                 {
                     auto kern = k_tangent_rows_pipe<DIM, ND, NIP, KIND, WW>;
                     using Sh = FusedShape<DIM, ND, NIP, KIND, true, WW>;
@@ -982,8 +1404,9 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
             run(FCfg<2, 4, 4, NUTO_GPU_MB_LINEAR_ELASTIC>{});
     };
     // autotuner: the first FP32 tangent of a context (outside any stream capture) assembles once with each candidate
-    // shape — 2, 4 and 8 warps per block, and with staged records also the double-buffered kernel with 2 and 4 warps
-    // per block — (a warm-up and a timed assembly each; every one writes the same values) and keeps the fastest
+    // shape — 2, 4 and 8 warps per block, and with staged records also the double-buffered kernel and the
+    // element-matrix form with 2 and 4 warps per block — (a warm-up and a timed assembly each; every one writes the
+    // same values) and keeps the fastest
     Tuning& T = c.tuning;
     if (T.tangentWarps == 0)
     {
@@ -993,9 +1416,9 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
             T.tangentWarps = 4;
         else if (cs == cudaStreamCaptureStatusNone)
         {
-            const int candW[5] = {2, 4, 8, 2, 4};
-            const bool candPipe[5] = {false, false, false, true, true};
-            const int nCand = staged ? 5 : 3;
+            const int candW[7] = {2, 4, 8, 2, 4, 2, 4};
+            const int candForm[7] = {0, 0, 0, 1, 1, 2, 2};
+            const int nCand = staged ? 7 : 3;
             cudaEvent_t e0, e1;
             NG_CUDA(cudaEventCreate(&e0));
             NG_CUDA(cudaEventCreate(&e1));
@@ -1003,9 +1426,9 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
             int pick = 1;
             for (int k = 0; k < nCand; ++k)
             {
-                assemble(candW[k], candPipe[k]);
+                assemble(candW[k], candForm[k]);
                 NG_CUDA(cudaEventRecord(e0, c.stream));
-                assemble(candW[k], candPipe[k]);
+                assemble(candW[k], candForm[k]);
                 NG_CUDA(cudaEventRecord(e1, c.stream));
                 NG_CUDA(cudaEventSynchronize(e1));
                 float ms = 0.f;
@@ -1020,10 +1443,10 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             T.tangentWarps = candW[pick];
-            T.tangentPipe = candPipe[pick];
+            T.tangentForm = candForm[pick];
         }
     }
-    assemble(T.tangentWarps ? T.tangentWarps : 4, T.tangentPipe);
+    assemble(T.tangentWarps ? T.tangentWarps : 4, staged ? T.tangentForm : 0);
 }
 
 } // namespace nuto_gpu

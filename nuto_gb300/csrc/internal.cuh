@@ -318,8 +318,10 @@ struct Tuning
 {
     bool enabled = true;             // NUTO_GPU_AUTOTUNE=0 keeps the defaults
     int tangentWarps = 0;            // warps per block of the FP32 tangent's node-row kernel (2, 4, 8)
-    bool tangentPipe = false;        // the double-buffered node-row kernel on a grid of resident blocks
-    float tangentMs[5] = {0, 0, 0, 0, 0}; // one assembly with 2, 4, 8 warps per block; pipelined with 2, 4
+    int tangentForm = 0;             // 0 node rows, 1 double-buffered node rows on resident blocks, 2 element
+                                     // matrices + row gather
+    float tangentMs[7] = {0, 0, 0, 0, 0, 0, 0}; // one assembly with 2, 4, 8 warps per block; double-buffered with 2,
+                                                // 4; element matrices with 2, 4
     int spmvGroup[4] = {0, 0, 0, 0}; // lanes per node of the fine-level product, per (value, vector) type pair
     float spmvMs[4][3] = {};         // one product with 4, 8, 16 lanes per node
 };
@@ -393,6 +395,7 @@ struct Ctx
     bool forceTc20Off = false; // NUTO_GPU_TC20=off
     int tc20LawFp64 = 0;       // NUTO_GPU_TC20=fp64law: the law of every point in FP64
     DBuf<float> dElemMats;
+    DBuf<uint32_t> dPackedRanks; // element-matrix form: ranks of (cell entry of a node, b), packed, cell-list order
     // device status word of kernels with bounded waits (0 = fine, else NUTO_GPU_ETIMEOUT), read after a stream
     // synchronisation; spinLimit bounds every wait loop (iterations)
     DBuf<int> dStatus;

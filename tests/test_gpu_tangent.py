@@ -331,6 +331,35 @@ def test_pipelined_node_rows_bitwise_equal(kind, n, monkeypatch):
     assert np.array_equal(piped, plain)
 
 
+@pytest.mark.parametrize("kind,n", [("hex8gd", 6), ("quad4gd", 12), ("quad4", 10)])
+def test_cell_matrix_tangent_bitwise_equal(kind, n, monkeypatch):
+    """The element-matrix form (NUTO_GPU_TANGENT=cells: every node-pair block integrated once into the cell's element
+    matrix, then one warp per node adds the slabs of its cells in ascending cell order) forms each block with the
+    node-row kernel's expressions and adds the blocks in the same order: the tangents are equal bit for bit, and both
+    match the oracle at the FP32 tolerance."""
+    _torch()
+    import nuto_gb300
+
+    rng = np.random.default_rng(72)
+    s, (om, layers, P, cons) = _setup(kind, n)
+    u, kappa = _damage_state(kind, s, P, rng)
+    monkeypatch.setenv("NUTO_GPU_AUTOTUNE", "0")
+    g = s.build_gpu()
+    if kappa is not None:
+        g.history = kappa
+        P.kappa = kappa
+    plain = g.build_matrix(u, nuto_gb300.FP32).cpu().numpy()
+    monkeypatch.setenv("NUTO_GPU_TANGENT", "cells")
+    g2 = s.build_gpu()
+    if kappa is not None:
+        g2.history = kappa
+    cells = g2.build_matrix(u, nuto_gb300.FP32).cpu().numpy()
+    assert g2.autotune_info()["tangent_form"] == "cell_matrices"
+    K = _csr(P, u)
+    assert np.abs(cells - K.data).max() <= FP32_REL * np.abs(K.data).max()
+    assert np.array_equal(cells, plain)
+
+
 @pytest.mark.parametrize("kind,n", [("hex8gd", 8), ("quad4gd", 16), ("quad4", 12)])
 @pytest.mark.parametrize("precision", [32, 64])
 @pytest.mark.parametrize("res_blocks", ["2", "1"])
