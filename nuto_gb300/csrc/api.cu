@@ -596,6 +596,8 @@ int nuto_gpu_create(nuto_gpu_ctx** out, int device, void* stream)
         c->tuning.tangentWarps = 4; // the double-buffered node-row kernel, not tuned
         c->tuning.tangentForm = 1;
     }
+    const char* cr = std::getenv("NUTO_GPU_CELLS_RECORDS");
+    c->cellsLawFused = !(cr && cr[0] == '1');
     if (tk && std::string(tk) == "cells")
     {
         c->tuning.tangentWarps = 4; // element matrices + row gather, not tuned

@@ -1079,6 +1079,230 @@ __global__ void __launch_bounds__(W * 32) k_rows_from_cells(FusedArgs A, const f
             vals[NG_IDX(rs[k] + i, A.nnz, 75)] = sRow[k * kFusedRowCap + i];
 }
 
+// The element matrices with the law evaluated in the same kernel (no records in global memory): a warp takes
+// CPW = 32 / NIP cells; (0) lane (cell, node) stages the node data, (A) lane (cell, point) evaluates PointData into
+// the record layout in shared memory (the values k_point_records writes), (B) the cells one after the other as in
+// k_cell_matrices. Bitwise the same element matrices as k_point_records + k_cell_matrices.
+template <int DIM, int ND, int NIP, int KIND>
+struct CellLawShape
+{
+    using Sh = FusedShape<DIM, ND, NIP, KIND, true>;
+    using CS = CellSlab<DIM, ND, KIND>;
+    static constexpr bool GD = Sh::GD;
+    static constexpr int cpw = 32 / NIP;
+    static constexpr int R4 = Sh::recF4;
+    static constexpr int perCell = NIP * R4; // float4
+    // per warp, in floats: node coordinates and displacements (2 float4 per (cell, node)), eeq in FP64 (2 floats),
+    // the records of the warp's cells, P/Q per (point, node) of one cell, one element matrix
+    static constexpr int nodeF = cpw * ND * 8;
+    static constexpr int eF = GD ? cpw * ND * 2 : 0;
+    static constexpr int recF = cpw * perCell * 4;
+    static constexpr int pqF = GD ? NIP * ND * 8 : 0;
+    static constexpr int emF = ND * CS::pad;
+    static constexpr int perWarp = nodeF + eF + recF + pqF + emF;
+    static constexpr int tabF = NIP * ND * 4 + (NIP + 3) / 4 * 4; // (dN/dxi, N) per point and node, weights
+    static constexpr size_t smem(int W)
+    {
+        return (static_cast<size_t>(W) * perWarp + tabF) * sizeof(float);
+    }
+    static_assert(cpw * ND == 32 && cpw * NIP == 32, "one lane per (cell, node) and per (cell, point)");
+    static_assert(nodeF % 4 == 0 && eF % 4 == 0 && recF % 4 == 0 && pqF % 4 == 0 && emF % 4 == 0, "16-byte regions");
+};
+
+template <int DIM, int ND, int NIP, int KIND, int W>
+__global__ void __launch_bounds__(W * 32) k_cell_matrices_law(FusedArgs A, LawParams L, const double* __restrict__ u,
+                                                              float* __restrict__ em)
+{
+    using LS = CellLawShape<DIM, ND, NIP, KIND>;
+    using CS = CellSlab<DIM, ND, KIND>;
+    constexpr bool GD = LS::GD;
+    constexpr int CPW = LS::cpw, R4 = LS::R4, PER_CELL = LS::perCell;
+    constexpr int PAIRS = ND * ND;
+    constexpr int PPL = (PAIRS + 31) / 32;
+    extern __shared__ __align__(16) float smL[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* sT = reinterpret_cast<float4*>(smL); // [NIP][ND]
+    float* sWq = smL + NIP * ND * 4;             // [NIP]
+    float* base = smL + LS::tabF + wid * LS::perWarp;
+    float4* sX = reinterpret_cast<float4*>(base);                  // [CPW][ND]
+    float4* sU = sX + CPW * ND;                                    // [CPW][ND]
+    double* sE = reinterpret_cast<double*>(base + LS::nodeF);      // [CPW][ND]
+    float4* sR = reinterpret_cast<float4*>(base + LS::nodeF + LS::eF); // [CPW][NIP][R4]
+    float4* sPQ = reinterpret_cast<float4*>(base + LS::nodeF + LS::eF + LS::recF); // [NIP][ND][2]
+    float* sEM = base + LS::nodeF + LS::eF + LS::recF + LS::pqF;   // [ND][pad]
+    for (int i = threadIdx.x; i < NIP * ND; i += blockDim.x)
+    {
+        const int q = i / ND, nd = i % ND;
+        const double* d = A.tabDN + (q * ND + nd) * 3;
+        sT[i] = F4(static_cast<float>(d[0]), static_cast<float>(d[1]), DIM == 3 ? static_cast<float>(d[2]) : 0.f,
+                   static_cast<float>(A.tabN[q * ND + nd]));
+    }
+    for (int i = threadIdx.x; i < NIP; i += blockDim.x)
+        sWq[i] = static_cast<float>(A.tabW[i]);
+    __syncthreads();
+    const int64_t n = A.nCells;
+    const int64_t c0 = (static_cast<int64_t>(blockIdx.x) * W + wid) * CPW;
+    if (c0 >= n)
+        return; // the whole warp leaves; only warp-level synchronisation follows
+    // (0) lane (cell slot, node): the node data, as k_point_records loads them
+    {
+        const int cl = lane / ND, nd = lane % ND;
+        const int64_t e = c0 + cl;
+        if (e < n)
+        {
+            const int32_t nD = static_cast<int32_t>(NG_IDX(A.connD[static_cast<int64_t>(nd) * n + e], A.nNodesD, 80));
+            const int64_t gd = A.gdofD[nD];
+            float x[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+            {
+                x[d] = A.relX[(static_cast<int64_t>(nd) * DIM + d) * n + e];
+                v[d] = static_cast<float>(u[NG_IDX(gd + d, A.nDofs, 81)]);
+            }
+            float ev = 0.f;
+            if (GD)
+            {
+                const int32_t nE =
+                        static_cast<int32_t>(NG_IDX(A.connE[static_cast<int64_t>(nd) * n + e], A.nNodesE, 82));
+                const double e64 = u[NG_IDX(A.gdofE[nE], A.nDofs, 83)];
+                sE[cl * ND + nd] = e64;
+                ev = static_cast<float>(e64);
+            }
+            sX[cl * ND + nd] = F4(x[0], x[1], x[2], ev);
+            sU[cl * ND + nd] = F4(v[0], v[1], v[2], 0.f);
+        }
+    }
+    __syncwarp();
+    // (A) lane (cell slot, point): the law, written in the record layout
+    {
+        const int cl = lane / NIP, q = lane % NIP;
+        const int64_t e = c0 + cl;
+        if (e < n)
+        {
+            PointOut<DIM, ND> o;
+            PointData<DIM, ND, NIP, KIND>(A, L, sT + q * ND, sWq[q], sX + cl * ND, sU + cl * ND,
+                                          GD ? sE + cl * ND : nullptr, q, e, o);
+            float4* r = sR + cl * PER_CELL + q * R4;
+#pragma unroll
+            for (int nd = 0; nd < ND; ++nd)
+                r[nd] = F4(o.g[nd][0], o.g[nd][1], DIM == 3 ? o.g[nd][DIM - 1] : 0.f, sT[q * ND + nd].w);
+            r[ND] = F4(o.s0[0], o.s0[1], o.s0[2], o.s0[3]);
+            if (GD)
+            {
+                r[ND + 1] = F4(o.scge[0], o.scge[1], DIM == 3 ? o.scge[DIM - 1] : 0.f, o.sv[4]);
+                r[ND + 2] = F4(o.tv[0], o.tv[1], o.tv[2], o.sv[5]);
+                r[ND + 3] = F4(o.tv[3], o.tv[4], o.tv[5], 0.f);
+                r[ND + 4] = F4(o.sv[0], o.sv[1], o.sv[2], o.sv[3]);
+            }
+        }
+    }
+    __syncwarp();
+    // (B) the element matrices of the warp's cells, one after the other
+    for (int cl = 0; cl < CPW; ++cl)
+    {
+        const int64_t e = c0 + cl;
+        if (e >= n)
+            break;
+        const float4* rec = sR + cl * PER_CELL;
+        if (GD)
+        {
+            for (int it = lane; it < NIP * ND; it += 32)
+            {
+                const int q = it / ND, nd = it % ND;
+                const float4* row = rec + q * R4;
+                const float4 g = row[nd];
+                const float4* S = row + ND;
+                const float4 s1 = S[1], s2 = S[2], s3 = S[3], s4 = S[4];
+                const float sv[6] = {s4.x, s4.y, s4.z, s4.w, s1.w, s2.w};
+                const float tv[6] = {s2.x, s2.y, s2.z, s3.x, s3.y, s3.z};
+                const float3 pa = BtV<DIM>(g.x, g.y, g.z, sv);
+                const float gs = g.x * s1.x + g.y * s1.y + (DIM == 3 ? g.z * s1.z : 0.f);
+                const float3 qb = BtV<DIM>(g.x, g.y, g.z, tv);
+                sPQ[(q * ND + nd) * 2] = F4(pa.x, pa.y, pa.z, gs);
+                sPQ[(q * ND + nd) * 2 + 1] = F4(qb.x, qb.y, qb.z, 0.f);
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int m = 0; m < PPL; ++m)
+        {
+            const int p = lane + 32 * m;
+            if (p >= PAIRS)
+                continue;
+            const int ia = p / ND, b = p % ND;
+            float uu[DIM][DIM], ue[DIM], eu[DIM], ee = 0.f, dg = 0.f;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k)
+            {
+                ue[k] = eu[k] = 0.f;
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    uu[k][l] = 0.f;
+            }
+#pragma unroll 2
+            for (int q = 0; q < NIP; ++q)
+            {
+                const float4* G = rec + q * R4;
+                const float4* SR = G + ND;
+                const float4 ga = G[ia], gb = G[b];
+                const float4 s0 = SR[0];
+                const float av[3] = {ga.x, ga.y, ga.z}, bv[3] = {gb.x, gb.y, gb.z};
+                float gab = 0.f;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    gab += av[d] * bv[d];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k)
+                {
+                    const float lk = s0.x * av[k], mk = s0.y * bv[k];
+#pragma unroll
+                    for (int l = 0; l < DIM; ++l)
+                        uu[k][l] += lk * bv[l] + mk * av[l];
+                }
+                dg += s0.y * gab;
+                if (GD)
+                {
+                    const float4 pa = sPQ[(q * ND + ia) * 2];
+                    const float4 qb = sPQ[(q * ND + b) * 2 + 1];
+                    const float pv[3] = {pa.x, pa.y, pa.z}, qv[3] = {qb.x, qb.y, qb.z};
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k)
+                    {
+                        ue[k] += pv[k] * gb.w;
+                        eu[k] -= ga.w * qv[k];
+                    }
+                    ee += (s0.z * ga.w + pa.w) * gb.w + s0.w * gab;
+                }
+            }
+            float* slab = sEM + ia * CS::pad;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k)
+            {
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    slab[k * CS::nc + b * DIM + l] = uu[k][l] + (k == l ? dg : 0.f);
+                if (GD)
+                    slab[k * CS::nc + ND * DIM + b] = ue[k];
+            }
+            if (GD)
+            {
+#pragma unroll
+                for (int l = 0; l < DIM; ++l)
+                    slab[DIM * CS::nc + b * DIM + l] = eu[l];
+                slab[DIM * CS::nc + ND * DIM + b] = ee;
+            }
+        }
+        __syncwarp();
+        float4* dst = reinterpret_cast<float4*>(em + NG_IDX(e, n, 84) * (ND * CS::size));
+        for (int i = lane; i < ND * CS::size / 4; i += 32)
+        {
+            const int a = i / (CS::size / 4), j = i % (CS::size / 4);
+            dst[i] = *reinterpret_cast<const float4*>(sEM + a * CS::pad + 4 * j);
+        }
+        __syncwarp(); // sPQ and sEM are rewritten for the next cell
+    }
+}
+
 // The ranks of one (cell entry of a node, neighbour b) packed into one word (UU | UE << 8 | EU << 16 | EE << 24), in
 // the order of the nodes' cell lists: the row gather of a node then reads the ranks of its cells with contiguous
 // loads instead of byte loads from the planar rank tables. Built once per mesh.
@@ -1296,7 +1520,7 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
             using C = decltype(cfg);
             constexpr int DIM = C::dim, ND = C::nd, NIP = C::nip, KIND = C::kind;
             float4* recs = nullptr;
-            if (staged)
+            if (staged && !(form == 2 && c.cellsLawFused))
             {
                 const size_t bytes =
                         static_cast<size_t>(c.nCells) * NIP * FusedShape<DIM, ND, NIP, KIND, true>::recF4 * 16;
@@ -1317,16 +1541,32 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
                     const size_t emFloats = static_cast<size_t>(c.nCells) * ND * CS::size;
                     if (c.dElemMats.n < emFloats)
                         c.dElemMats.alloc(emFloats);
-                    constexpr int recF = NIP * FusedShape<DIM, ND, NIP, KIND, true>::recF4 * 4;
-                    constexpr int pqF = CS::GD ? NIP * ND * 8 : 0;
-                    constexpr size_t smem = static_cast<size_t>(WW) * (recF + pqF + ND * CS::pad) * sizeof(float);
-                    auto kern = k_cell_matrices<DIM, ND, NIP, KIND, WW>;
-                    if (smem > 48 * 1024)
-                        NG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     static_cast<int>(smem)));
-                    kern<<<static_cast<unsigned>((c.nCells + WW - 1) / WW), WW * 32, smem, c.stream>>>(
-                            c.nCells, recs, c.dElemMats.p);
-                    AfterLaunch(c, "k_cell_matrices");
+                    if (c.cellsLawFused)
+                    {
+                        using LS = CellLawShape<DIM, ND, NIP, KIND>;
+                        const size_t smem = LS::smem(WW);
+                        auto kern = k_cell_matrices_law<DIM, ND, NIP, KIND, WW>;
+                        if (smem > 48 * 1024)
+                            NG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         static_cast<int>(smem)));
+                        const int64_t cellsPerBlock = static_cast<int64_t>(WW) * LS::cpw;
+                        kern<<<static_cast<unsigned>((c.nCells + cellsPerBlock - 1) / cellsPerBlock), WW * 32, smem,
+                               c.stream>>>(A, c.law, u, c.dElemMats.p);
+                        AfterLaunch(c, "k_cell_matrices_law");
+                    }
+                    else
+                    {
+                        constexpr int recF = NIP * FusedShape<DIM, ND, NIP, KIND, true>::recF4 * 4;
+                        constexpr int pqF = CS::GD ? NIP * ND * 8 : 0;
+                        constexpr size_t smem = static_cast<size_t>(WW) * (recF + pqF + ND * CS::pad) * sizeof(float);
+                        auto kern = k_cell_matrices<DIM, ND, NIP, KIND, WW>;
+                        if (smem > 48 * 1024)
+                            NG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         static_cast<int>(smem)));
+                        kern<<<static_cast<unsigned>((c.nCells + WW - 1) / WW), WW * 32, smem, c.stream>>>(
+                                c.nCells, recs, c.dElemMats.p);
+                        AfterLaunch(c, "k_cell_matrices");
+                    }
                     const unsigned rowBlocks = static_cast<unsigned>((A.nNodes + WW - 1) / WW);
                     if constexpr (CS::nc == 32 && ND == 8)
                     {

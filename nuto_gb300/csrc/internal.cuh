@@ -395,6 +395,7 @@ struct Ctx
     bool forceTc20Off = false; // NUTO_GPU_TC20=off
     int tc20LawFp64 = 0;       // NUTO_GPU_TC20=fp64law: the law of every point in FP64
     DBuf<float> dElemMats;
+    bool cellsLawFused = true; // element-matrix form: the law in the cell kernel (NUTO_GPU_CELLS_RECORDS=1: records)
     DBuf<uint32_t> dPackedRanks; // element-matrix form: ranks of (cell entry of a node, b), packed, cell-list order
     // device status word of kernels with bounded waits (0 = fine, else NUTO_GPU_ETIMEOUT), read after a stream
     // synchronisation; spinLimit bounds every wait loop (iterations)

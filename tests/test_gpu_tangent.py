@@ -332,14 +332,17 @@ def test_pipelined_node_rows_bitwise_equal(kind, n, monkeypatch):
 
 
 @pytest.mark.parametrize("kind,n", [("hex8gd", 6), ("quad4gd", 12), ("quad4", 10)])
-def test_cell_matrix_tangent_bitwise_equal(kind, n, monkeypatch):
+@pytest.mark.parametrize("records", ["0", "1"])
+def test_cell_matrix_tangent_bitwise_equal(kind, n, records, monkeypatch):
     """The element-matrix form (NUTO_GPU_TANGENT=cells: every node-pair block integrated once into the cell's element
     matrix, then one warp per node adds the slabs of its cells in ascending cell order) forms each block with the
     node-row kernel's expressions and adds the blocks in the same order: the tangents are equal bit for bit, and both
-    match the oracle at the FP32 tolerance."""
+    match the oracle at the FP32 tolerance. With the law evaluated in the cell kernel (default) and from the point
+    records (NUTO_GPU_CELLS_RECORDS=1)."""
     _torch()
     import nuto_gb300
 
+    monkeypatch.setenv("NUTO_GPU_CELLS_RECORDS", records)
     rng = np.random.default_rng(72)
     s, (om, layers, P, cons) = _setup(kind, n)
     u, kappa = _damage_state(kind, s, P, rng)
