@@ -49,7 +49,14 @@ EXACT_BELOW = 1.0e4
 # forcing-term floor of both paths' Newton loops: the last linear solve of a load step leaves a linear residual of
 # about FORCING_FLOOR x the Newton tolerance, so the converged state sits that far below the 1e-8 test
 FORCING_FLOOR = 0.05
-TANGENT_KERNEL = "k_tangent_fused<3,8,8,GD> (FP32 tangent: geometry and law per node warp, rows written once)"
+# the FP32 tangent's kernels per form the autotuner can choose (nuto_gpu_autotune_info)
+TANGENT_KERNELS = {
+    "cell_matrices": "k_cell_matrices_law<3,8,8,GD,W> + k_rows_from_cells32 (law and element matrix per cell, "
+                     "then one warp per node adds its cells' slabs into its rows)",
+    "node_rows": "k_point_records + k_tangent_fused<3,8,8,GD,STAGED,W> (per-point records, one warp per node "
+                 "integrates its node-pair blocks)",
+    "pipelined": "k_point_records + k_tangent_rows_pipe<3,8,8,GD,W> (node rows on resident blocks)",
+}
 
 
 def parse():
@@ -603,8 +610,10 @@ def run_ours(args):
     traffic = load_traffic()
     tb = tangent_bytes(s, nnz, 4)
     asm_s = float(np.mean(ms_matrix)) / 1e3
-    roof = {"kernel": TANGENT_KERNEL, "bound": "hbm", "achieved": tb / asm_s / 1e9, "peak": peak, "unit": "GB/s",
-            "frac": tb / asm_s / 1e9 / peak, "peak_kind": peak_kind, "traffic": traffic.get("k_tangent_fused_bytes_per_launch"),
+    form = g.autotune_info()["tangent_form"]
+    roof = {"kernel": TANGENT_KERNELS[form], "bound": "hbm", "achieved": tb / asm_s / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": tb / asm_s / 1e9 / peak, "peak_kind": peak_kind,
+            "traffic": traffic.get("tangent_%s_bytes_per_launch" % form),
             "algorithmic_bytes_per_launch": tb, "mean_launch_ms": asm_s * 1e3,
             "assembled_dofs_per_s": n_dofs / asm_s}
     rb = residual_bytes(s)

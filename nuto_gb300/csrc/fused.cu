@@ -1098,7 +1098,7 @@ struct CellLawShape
     static constexpr int eF = GD ? cpw * ND * 2 : 0;
     static constexpr int recF = cpw * perCell * 4;
     static constexpr int pqF = GD ? NIP * ND * 8 : 0;
-    static constexpr int emF = ND * CS::pad;
+    static constexpr int emF = 0; // the element matrix is stored from registers
     static constexpr int perWarp = nodeF + eF + recF + pqF + emF;
     static constexpr int tabF = NIP * ND * 4 + (NIP + 3) / 4 * 4; // (dN/dxi, N) per point and node, weights
     static constexpr size_t smem(int W)
@@ -1129,7 +1129,6 @@ __global__ void __launch_bounds__(W * 32) k_cell_matrices_law(FusedArgs A, LawPa
     double* sE = reinterpret_cast<double*>(base + LS::nodeF);      // [CPW][ND]
     float4* sR = reinterpret_cast<float4*>(base + LS::nodeF + LS::eF); // [CPW][NIP][R4]
     float4* sPQ = reinterpret_cast<float4*>(base + LS::nodeF + LS::eF + LS::recF); // [NIP][ND][2]
-    float* sEM = base + LS::nodeF + LS::eF + LS::recF + LS::pqF;   // [ND][pad]
     for (int i = threadIdx.x; i < NIP * ND; i += blockDim.x)
     {
         const int q = i / ND, nd = i % ND;
@@ -1274,7 +1273,9 @@ __global__ void __launch_bounds__(W * 32) k_cell_matrices_law(FusedArgs A, LawPa
                     ee += (s0.z * ga.w + pa.w) * gb.w + s0.w * gab;
                 }
             }
-            float* slab = sEM + ia * CS::pad;
+            // straight from registers to the cell's slab in global memory (a warp's stores of one (k, l) land in
+            // four slab rows of the cell's matrix; L2 merges them into whole sectors before writing back)
+            float* slab = em + (NG_IDX(e, n, 84) * ND + ia) * CS::size;
 #pragma unroll
             for (int k = 0; k < DIM; ++k)
             {
@@ -1292,14 +1293,7 @@ __global__ void __launch_bounds__(W * 32) k_cell_matrices_law(FusedArgs A, LawPa
                 slab[DIM * CS::nc + ND * DIM + b] = ee;
             }
         }
-        __syncwarp();
-        float4* dst = reinterpret_cast<float4*>(em + NG_IDX(e, n, 84) * (ND * CS::size));
-        for (int i = lane; i < ND * CS::size / 4; i += 32)
-        {
-            const int a = i / (CS::size / 4), j = i % (CS::size / 4);
-            dst[i] = *reinterpret_cast<const float4*>(sEM + a * CS::pad + 4 * j);
-        }
-        __syncwarp(); // sPQ and sEM are rewritten for the next cell
+        __syncwarp(); // sPQ is rewritten for the next cell
     }
 }
 
@@ -1323,9 +1317,10 @@ __global__ void k_pack_ranks(FusedArgs A, int64_t nEntries, uint32_t* __restrict
 
 // Row gather of the element-matrix form for slabs of exactly 32 columns (Hex8 gradient damage: 24 displacement
 // columns, 8 eeq columns): lane l owns column l of every slab row, so its neighbour b = l / 3 (or l - 24), and the
-// positions in the displacement rows and in the eeq row are fixed per cell. The slab values and packed ranks of up
-// to 8 cells are loaded before any is added (all loads in flight at once); cells are added in ascending order.
-template <int DIM, int ND, int NIP, int KIND, int W>
+// positions in the displacement rows and in the eeq row are fixed per cell. The slab values and packed ranks of a
+// batch of CB cells are loaded before any is added (all loads in flight at once); cells are added in ascending
+// order.
+template <int DIM, int ND, int NIP, int KIND, int W, int CB>
 __global__ void __launch_bounds__(W * 32) k_rows_from_cells32(FusedArgs A, const uint32_t* __restrict__ packed,
                                                               const float* __restrict__ em, float* __restrict__ vals)
 {
@@ -1333,7 +1328,7 @@ __global__ void __launch_bounds__(W * 32) k_rows_from_cells32(FusedArgs A, const
     constexpr bool GD = CS::GD;
     constexpr int NR = CS::nr, SL = CS::size;
     static_assert(CS::nc == 32 && ND == 8, "one slab column per lane, 8 nodes per cell");
-    constexpr int CB = 8; // cells per batch
+    static_assert(CB == 2 || CB == 4 || CB == 8, "cells per batch");
     __shared__ float sRowAll[W][NR * kFusedRowCap];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t a = static_cast<int64_t>(blockIdx.x) * W + wid;
@@ -1378,7 +1373,7 @@ __global__ void __launch_bounds__(W * 32) k_rows_from_cells32(FusedArgs A, const
         uint32_t pk0 = 0, pk1 = 0;
         if (lane / ND < nc)
             pk0 = packed[NG_IDX((kb + lane / ND) * ND + lane % ND, n * ND * ND, 77)];
-        if (4 + lane / ND < nc)
+        if (CB == 8 && 4 + lane / ND < nc)
             pk1 = packed[NG_IDX((kb + 4 + lane / ND) * ND + lane % ND, n * ND * ND, 77)];
         float v[CB][NR];
 #pragma unroll
@@ -1579,7 +1574,9 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
                                     A, entries, c.dPackedRanks.p);
                             AfterLaunch(c, "k_pack_ranks");
                         }
-                        k_rows_from_cells32<DIM, ND, NIP, KIND, WW><<<rowBlocks, WW * 32, 0, c.stream>>>(
+                        // 4 cells per batch: 64 registers, 32 resident warps per SM (8 cells: 86 registers, 1.14x
+                        // slower; 2 cells: 1.02x slower, measured at 64^3)
+                        k_rows_from_cells32<DIM, ND, NIP, KIND, WW, 4><<<rowBlocks, WW * 32, 0, c.stream>>>(
                                 A, c.dPackedRanks.p, c.dElemMats.p, vals);
                         AfterLaunch(c, "k_rows_from_cells32");
                     }

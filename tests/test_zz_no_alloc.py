@@ -31,14 +31,23 @@ def _state(s, g, seed):
 def _unchanged_memory(fn):
     """Runs fn() and checks that the device memory in use did not change: torch's allocator holds the same
     bytes and cudaMemGetInfo reports the same free memory (nothing was allocated on the device)."""
+    import gc
+
     import torch
 
-    torch.cuda.synchronize()
-    held = torch.cuda.memory_allocated()
-    free0, _ = torch.cuda.mem_get_info()
-    fn()
-    torch.cuda.synchronize()
-    free1, _ = torch.cuda.mem_get_info()
+    # contexts of earlier tests that the garbage collector has not reached yet would free their device memory at an
+    # arbitrary point: collect them first and keep the collector off while measuring
+    gc.collect()
+    gc.disable()
+    try:
+        torch.cuda.synchronize()
+        held = torch.cuda.memory_allocated()
+        free0, _ = torch.cuda.mem_get_info()
+        fn()
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+    finally:
+        gc.enable()
     assert torch.cuda.memory_allocated() == held
     assert free1 == free0
 
