@@ -628,7 +628,7 @@ def run_ours(args):
            "ms_per_step_sequential": ms_sequential,
            "step_form": "nuto_gpu_build_system: the FP64 residual on a second stream (%s resident blocks per SM) "
                         "beside the FP32 tangent; ms_matrix/ms_vector_per_step and the rooflines from the same K "
-                        "steps run as two calls in sequence" % os.environ.get("NUTO_GPU_SYSTEM_RES_BLOCKS", "4"),
+                        "steps run as two calls in sequence" % os.environ.get("NUTO_GPU_SYSTEM_RES_BLOCKS", "6"),
            "max_abs_tangent_value": fp32_check,
            "roofline": roof,
            "roofline_residual": {"kernel": "k_residual (FP64 internal-force vector)", "bound": "fp64",

@@ -408,7 +408,7 @@ struct Ctx
     // blocks; the first call of a context runs both in sequence (lazy set-up, autotuning)
     cudaStream_t sideStream = nullptr;
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
-    int sysResBlocks = 4;
+    int sysResBlocks = 6;
     bool noAllocReady = false; // nuto_gpu_build_matrix_noalloc: address looked up and kernels loaded
     int64_t systemCalls = 0;
     // adjoint: positions of the transposed entries, per-point partial derivatives
