@@ -585,26 +585,32 @@ def run_ours(args):
     ms_vector = [b.elapsed_time(c) for _, b, c in ev]
     ms_sequential = float(np.mean([a.elapsed_time(c) for a, _, c in ev]))
 
-    # the same passes end to end through the C ABI with host buffers: state in from pinned memory, CSR values and
-    # residual out to pinned memory, every step
+    # the same passes end to end through the C ABI with host buffers (nuto_gpu_build_system_host): state in from
+    # pinned memory, CSR values and residual out to pinned memory, every step
     xp = torch.empty(n_dofs, dtype=torch.float64, pin_memory=True)
     xp.numpy()[:] = x_h
     kp = torch.empty(nnz, dtype=torch.float32, pin_memory=True)
     fp = torch.empty(n_dofs, dtype=torch.float64, pin_memory=True)
-    ud = torch.empty(n_dofs, dtype=torch.float64, device="cuda")
+    g.build_system_host(xp, kp, fp, nuto_gb300.FP32)  # allocates the context's host-io buffers (untimed)
     barrier()
     h0 = time.perf_counter()
     for _ in range(args.steps):
-        ud.copy_(xp, non_blocking=True)
-        g.build_system(ud, nuto_gb300.FP32, out=k32, f_out=f)
-        kp.copy_(k32, non_blocking=True)
-        fp.copy_(f, non_blocking=True)
-        torch.cuda.current_stream().synchronize()
+        # state in, tangent values and residual out; the values' copy overlaps the residual
+        g.build_system_host(xp, kp, fp, nuto_gb300.FP32)
     barrier()
     sec_e2e = time.perf_counter() - h0
     (work_e2e,), sec_e2e = aggregate_ranks([n_dofs * args.steps], sec_e2e, "cuda")
+    # the bare copy of the CSR values to pinned host memory, for scale (the floor of the end-to-end pass)
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c0.record()
+    kp.copy_(k32, non_blocking=True)
+    c1.record()
+    torch.cuda.synchronize()
+    d2h_ms = c0.elapsed_time(c1)
     e2e = {"value": work_e2e / sec_e2e, "unit": "DOF/s", "h2d_bytes_per_step": int(n_dofs * 8),
-           "d2h_bytes_per_step": int(nnz * 4 + n_dofs * 8), "ms_per_step": 1e3 * sec_e2e / args.steps}
+           "d2h_bytes_per_step": int(nnz * 4 + n_dofs * 8), "ms_per_step": 1e3 * sec_e2e / args.steps,
+           "call": "nuto_gpu_build_system_host (host buffers, page-locked)",
+           "d2h_values_ms": d2h_ms, "d2h_values_gbs": nnz * 4 / (d2h_ms / 1e3) / 1e9}
 
     peak, peak_kind = load_peaks()
     traffic = load_traffic()

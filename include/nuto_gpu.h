@@ -249,6 +249,13 @@ int nuto_gpu_build_matrix(nuto_gpu_ctx* ctx, const double* d_u, int precision, v
    tangent's on FP32 issue); both are complete, in the context's stream order, when the call's work is. precision
    NUTO_GPU_FP32 or NUTO_GPU_FP64. The first call of a context runs the two in sequence. */
 int nuto_gpu_build_system(nuto_gpu_ctx* ctx, const double* d_u, int precision, void* d_values, double* d_f);
+/* nuto_gpu_build_system with host buffers, the form SimpleAssembler::BuildVector/BuildMatrix return their results in
+   (host Eigen objects, nuto/mechanics/cell/SimpleAssembler.cpp:38-156): h_u (n_dofs doubles) is copied in, the CSR
+   values (nnz floats or doubles) and f (n_dofs doubles) are copied back, and the call returns when they are in host
+   memory. The copy of the values starts as soon as the tangent is done, while the residual still runs. The state and
+   results pass through device buffers of the context (allocated on the first call). Pass page-locked host memory for
+   the copies to run asynchronously; pageable memory works, through the driver's staging. */
+int nuto_gpu_build_system_host(nuto_gpu_ctx* ctx, const double* h_u, int precision, void* h_values, double* h_f);
 /* The FP32 values of nuto_gpu_build_matrix(ctx, d_u, NUTO_GPU_FP32, d_values), computed without allocating any
    memory: the integration-point records go to a fixed 16 MiB device array inside the library instead of a buffer
    of the context. For callers that must not allocate device memory once set up. Limit: cells x integration points

@@ -100,6 +100,7 @@ SIGNATURES = {
     "nuto_gpu_build_vector": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_build_matrix": (_i, [_vp, _vp, _i, _vp]),
     "nuto_gpu_build_system": (_i, [_vp, _vp, _i, _vp, _vp]),
+    "nuto_gpu_build_system_host": (_i, [_vp, _vp, _i, _vp, _vp]),
     "nuto_gpu_build_matrix_noalloc": (_i, [_vp, _vp, _vp]),
     "nuto_gpu_build_lumped_mass": (_i, [_vp, _d, _vp]),
     "nuto_gpu_eval_ip": (_i, [_vp, _vp, _i, _vp]),

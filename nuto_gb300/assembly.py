@@ -212,6 +212,13 @@ class GpuCellGroup:
         self._call("nuto_gpu_build_system", _ptr(u), precision, _ptr(v), _ptr(f))
         return v, f
 
+    def build_system_host(self, u, values, f, precision=FP64):
+        """nuto_gpu_build_system_host: u (host, n_dofs float64), values (host, nnz float32 or float64) and f (host,
+        n_dofs float64) as CPU tensors or numpy arrays, page-locked for asynchronous copies (torch
+        pin_memory=True). Returns when values and f hold the tangent and the residual."""
+        self._call("nuto_gpu_build_system_host", _ptr(u), precision, _ptr(values), _ptr(f))
+        return values, f
+
     def build_matrix_noalloc(self, u, out=None):
         """FP32 tangent through nuto_gpu_build_matrix_noalloc (records in the library's static device array; the
         library allocates nothing). build_matrix(u, FP32) must have run once on this group."""

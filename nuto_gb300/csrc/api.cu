@@ -558,6 +558,20 @@ static int Guard(nuto_gpu_ctx* ctx, F&& f)
     }
 }
 
+// The second stream of nuto_gpu_build_system / _host and its fork and join events, created on first use. The
+// highest priority: whenever an SM frees resources, the residual's few blocks are placed before the tangent's many,
+// so they reach their slots early and keep them.
+static void EnsureSideStream(Ctx& c)
+{
+    if (c.sideStream)
+        return;
+    int lo = 0, hi = 0; // numerically: lo >= hi
+    NG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    NG_CUDA(cudaStreamCreateWithPriority(&c.sideStream, cudaStreamNonBlocking, hi));
+    NG_CUDA(cudaEventCreateWithFlags(&c.evFork, cudaEventDisableTiming));
+    NG_CUDA(cudaEventCreateWithFlags(&c.evJoin, cudaEventDisableTiming));
+}
+
 extern "C" {
 
 int nuto_gpu_version(void)
@@ -1087,16 +1101,7 @@ int nuto_gpu_build_system(nuto_gpu_ctx* ctx, const double* u, int precision, voi
             LaunchResidual(c, u, f);
             return NUTO_GPU_OK;
         }
-        if (!c.sideStream)
-        {
-            int lo = 0, hi = 0; // numerically: lo >= hi
-            NG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-            // the highest priority: whenever an SM frees resources, the residual's few blocks are placed before
-            // the tangent's many, so they reach their slots early and keep them
-            NG_CUDA(cudaStreamCreateWithPriority(&c.sideStream, cudaStreamNonBlocking, hi));
-            NG_CUDA(cudaEventCreateWithFlags(&c.evFork, cudaEventDisableTiming));
-            NG_CUDA(cudaEventCreateWithFlags(&c.evJoin, cudaEventDisableTiming));
-        }
+        EnsureSideStream(c);
         // fork: the residual (persistent grid, launched first so that its blocks hold their SM slots) on the side
         // stream; the tangent on the context's stream; join before anything else runs on the context's stream
         NG_CUDA(cudaEventRecord(c.evFork, c.stream));
@@ -1116,6 +1121,60 @@ int nuto_gpu_build_system(nuto_gpu_ctx* ctx, const double* u, int precision, voi
         LaunchTangent(c, u, precision, values);
         NG_CUDA(cudaEventRecord(c.evJoin, c.sideStream));
         NG_CUDA(cudaStreamWaitEvent(c.stream, c.evJoin, 0));
+        return NUTO_GPU_OK;
+    });
+}
+
+int nuto_gpu_build_system_host(nuto_gpu_ctx* ctx, const double* hU, int precision, void* hValues, double* hF)
+{
+    return Guard(ctx, [&] {
+        RequireReady(*ctx);
+        NG_CHECK(precision == NUTO_GPU_FP32 || precision == NUTO_GPU_FP64, NUTO_GPU_EINVAL, "precision 32 or 64");
+        NG_CHECK(hU && hValues && hF, NUTO_GPU_EINVAL, "host state, values and f");
+        Ctx& c = *ctx;
+        const size_t valBytes = static_cast<size_t>(c.nnz) * (precision == NUTO_GPU_FP32 ? 4 : 8);
+        if (c.dHostIoU.n != static_cast<size_t>(c.nDofs))
+            c.dHostIoU.alloc(static_cast<size_t>(c.nDofs));
+        if (c.dHostIoF.n != static_cast<size_t>(c.nDofs))
+            c.dHostIoF.alloc(static_cast<size_t>(c.nDofs));
+        if (c.dHostIoVals.n < valBytes)
+            c.dHostIoVals.alloc(valBytes);
+        const size_t vecBytes = static_cast<size_t>(c.nDofs) * sizeof(double);
+        NG_CUDA(cudaMemcpyAsync(c.dHostIoU.p, hU, vecBytes, cudaMemcpyHostToDevice, c.stream));
+        if (c.systemCalls++ == 0 || c.sysResBlocks <= 0)
+        {
+            LaunchTangent(c, c.dHostIoU.p, precision, c.dHostIoVals.p);
+            NG_CUDA(cudaMemcpyAsync(hValues, c.dHostIoVals.p, valBytes, cudaMemcpyDeviceToHost, c.stream));
+            LaunchResidual(c, c.dHostIoU.p, c.dHostIoF.p);
+            NG_CUDA(cudaMemcpyAsync(hF, c.dHostIoF.p, vecBytes, cudaMemcpyDeviceToHost, c.stream));
+            NG_CUDA(cudaStreamSynchronize(c.stream));
+            return NUTO_GPU_OK;
+        }
+        EnsureSideStream(c);
+        // the residual and its copy back on the side stream; the tangent and its copy back on the context's stream,
+        // where the copy of the values starts as soon as the tangent is done, while the residual still runs
+        NG_CUDA(cudaEventRecord(c.evFork, c.stream));
+        NG_CUDA(cudaStreamWaitEvent(c.sideStream, c.evFork, 0));
+        const cudaStream_t main = c.stream;
+        c.stream = c.sideStream;
+        try
+        {
+            LaunchResidual(c, c.dHostIoU.p, c.dHostIoF.p, c.sysResBlocks);
+            NG_CUDA(cudaMemcpyAsync(hF, c.dHostIoF.p, vecBytes, cudaMemcpyDeviceToHost, c.stream));
+        }
+        catch (...)
+        {
+            c.stream = main;
+            throw;
+        }
+        c.stream = main;
+        // (the row kernels writing straight into mapped page-locked host memory were measured slower: 5.4 ms per
+        // 64^3 pass against 4.4 ms with this copy)
+        LaunchTangent(c, c.dHostIoU.p, precision, c.dHostIoVals.p);
+        NG_CUDA(cudaMemcpyAsync(hValues, c.dHostIoVals.p, valBytes, cudaMemcpyDeviceToHost, c.stream));
+        NG_CUDA(cudaEventRecord(c.evJoin, c.sideStream));
+        NG_CUDA(cudaStreamWaitEvent(c.stream, c.evJoin, 0));
+        NG_CUDA(cudaStreamSynchronize(c.stream));
         return NUTO_GPU_OK;
     });
 }

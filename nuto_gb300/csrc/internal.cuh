@@ -409,6 +409,9 @@ struct Ctx
     cudaStream_t sideStream = nullptr;
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
     int sysResBlocks = 6;
+    // nuto_gpu_build_system_host: device copies of the caller's host state, values and vector
+    DBuf<double> dHostIoU, dHostIoF;
+    DBuf<unsigned char> dHostIoVals;
     bool noAllocReady = false; // nuto_gpu_build_matrix_noalloc: address looked up and kernels loaded
     int64_t systemCalls = 0;
     // adjoint: positions of the transposed entries, per-point partial derivatives

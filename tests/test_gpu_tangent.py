@@ -391,3 +391,27 @@ def test_build_system_equals_separate_calls(kind, n, precision, res_blocks, monk
         else:
             assert float((v - v2).abs().max()) <= 1e-13 * float(v2.abs().max()), k
         assert torch.equal(f, f2), k
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_build_system_host_equals_device_call(pinned):
+    """nuto_gpu_build_system_host (state in from host memory, values and residual back to host memory, the values'
+    copy overlapping the residual) returns bitwise what nuto_gpu_build_system leaves on the device, on its first
+    (sequential) call and later ones, from page-locked and from pageable host buffers."""
+    torch = _torch()
+    import nuto_gb300
+
+    s, o = _setup("hex8gd", 8)
+    g = s.build_gpu()
+    P = o[2]
+    rng = np.random.default_rng(5)
+    for k in range(3):
+        u, kappa = _damage_state("hex8gd", s, P, rng)
+        g.history = kappa
+        v_dev, f_dev = g.build_system(u, nuto_gb300.FP32)
+        uh = torch.as_tensor(u).pin_memory() if pinned else torch.as_tensor(u)
+        vh = torch.empty(g.nnz, dtype=torch.float32, pin_memory=pinned)
+        fh = torch.empty(g.n_dofs, dtype=torch.float64, pin_memory=pinned)
+        g.build_system_host(uh, vh, fh, nuto_gb300.FP32)
+        assert torch.equal(vh, v_dev.cpu()), k
+        assert torch.equal(fh, f_dev.cpu()), k
