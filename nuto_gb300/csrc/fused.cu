@@ -96,14 +96,175 @@ __device__ __forceinline__ float4 F4(float x, float y, float z, float w)
     return make_float4(x, y, z, w);
 }
 
-// B_n^T v for the node gradient g (Voigt columns; 2D xx yy xy, 3D xx yy zz yz zx xy)
+// B_n^T v for the node gradient g (Voigt columns; 2D xx yy xy, 3D xx yy zz yz zx xy). Every product and sum of
+// the node-pair arithmetic is rounded explicitly (no contraction left to the compiler), so that every kernel and
+// both the scalar and the packed forms below give bitwise the same blocks.
 template <int DIM>
 __device__ __forceinline__ float3 BtV(float gx, float gy, float gz, const float* v)
 {
     if (DIM == 2)
-        return make_float3(gx * v[0] + gy * v[2], gy * v[1] + gx * v[2], 0.f);
-    return make_float3(gx * v[0] + gz * v[4] + gy * v[5], gy * v[1] + gz * v[3] + gx * v[5],
-                       gz * v[2] + gy * v[3] + gx * v[4]);
+        return make_float3(__fmaf_rn(gy, v[2], __fmul_rn(gx, v[0])), __fmaf_rn(gx, v[2], __fmul_rn(gy, v[1])), 0.f);
+    return make_float3(__fmaf_rn(gy, v[5], __fmaf_rn(gz, v[4], __fmul_rn(gx, v[0]))),
+                       __fmaf_rn(gx, v[5], __fmaf_rn(gz, v[3], __fmul_rn(gy, v[1]))),
+                       __fmaf_rn(gx, v[4], __fmaf_rn(gy, v[3], __fmul_rn(gz, v[2]))));
+}
+
+// g . s over DIM components, explicitly rounded
+template <int DIM>
+__device__ __forceinline__ float DotG(float gx, float gy, float gz, float sx, float sy, float sz)
+{
+    float r = __fmaf_rn(gy, sy, __fmul_rn(gx, sx));
+    if (DIM == 3)
+        r = __fmaf_rn(gz, sz, r);
+    return r;
+}
+
+// ---- node-pair block of one integration point --------------------------------------------------------------------
+// lambda w g_a g_b^T + mu w (g_b g_a^T + (g_a . g_b) I), and for gradient damage P_a N_b (disp, eeq), -N_a Q_b^T
+// (eeq, disp) and (w N_a + gs_a) N_b + c g w (g_a . g_b) (eeq, eeq). g: (dN/dX, N) float4; s0 = (lambda w, mu w, w,
+// c g w); pa = (P_a, gs_a); qb = (Q_b, -).
+template <int DIM>
+struct PairAcc
+{
+    float uu[DIM][DIM], ue[DIM], eu[DIM], ee, dg;
+    __device__ __forceinline__ void zero()
+    {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            ue[k] = eu[k] = 0.f;
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                uu[k][l] = 0.f;
+        }
+        ee = dg = 0.f;
+    }
+};
+
+template <int DIM, bool GD>
+__device__ __forceinline__ void PairPoint(const float4& ga, const float4& gb, const float4& s0, const float4& pa,
+                                          const float4& qb, PairAcc<DIM>& c)
+{
+    const float av[3] = {ga.x, ga.y, ga.z}, bv[3] = {gb.x, gb.y, gb.z};
+    const float gab = DotG<DIM>(av[0], av[1], av[2], bv[0], bv[1], bv[2]);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+    {
+        const float lk = __fmul_rn(s0.x, av[k]), mk = __fmul_rn(s0.y, bv[k]);
+#pragma unroll
+        for (int l = 0; l < DIM; ++l)
+            c.uu[k][l] = __fmaf_rn(mk, av[l], __fmaf_rn(lk, bv[l], c.uu[k][l]));
+    }
+    c.dg = __fmaf_rn(s0.y, gab, c.dg);
+    if (GD)
+    {
+        const float pv[3] = {pa.x, pa.y, pa.z}, qv[3] = {qb.x, qb.y, qb.z};
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            c.ue[k] = __fmaf_rn(pv[k], gb.w, c.ue[k]);
+            c.eu[k] = __fmaf_rn(-ga.w, qv[k], c.eu[k]);
+        }
+        c.ee = __fmaf_rn(s0.w, gab, __fmaf_rn(__fmaf_rn(s0.z, ga.w, pa.w), gb.w, c.ee));
+    }
+}
+
+// The same for two blocks (a0, b) and (a1, b) at once in packed FP32 pairs (fma.rn.f32x2 / mul.rn.f32x2: each half
+// rounded as the scalar operation, so the results are bitwise those of PairPoint).
+using F2 = unsigned long long;
+__device__ __forceinline__ F2 Pk(float a, float b)
+{
+    F2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void Unpk(F2 r, float& a, float& b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ F2 Fma2(F2 a, F2 b, F2 c)
+{
+    F2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ F2 Mul2(F2 a, F2 b)
+{
+    F2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+template <int DIM>
+struct PairAcc2
+{
+    F2 uu[DIM][DIM], ue[DIM], eu[DIM], ee, dg;
+    __device__ __forceinline__ void zero()
+    {
+        const F2 z = Pk(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            ue[k] = eu[k] = z;
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                uu[k][l] = z;
+        }
+        ee = dg = z;
+    }
+    // the two blocks' accumulators as scalars
+    __device__ __forceinline__ void split(PairAcc<DIM>& c0, PairAcc<DIM>& c1) const
+    {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            Unpk(ue[k], c0.ue[k], c1.ue[k]);
+            Unpk(eu[k], c0.eu[k], c1.eu[k]);
+#pragma unroll
+            for (int l = 0; l < DIM; ++l)
+                Unpk(uu[k][l], c0.uu[k][l], c1.uu[k][l]);
+        }
+        Unpk(ee, c0.ee, c1.ee);
+        Unpk(dg, c0.dg, c1.dg);
+    }
+};
+
+template <int DIM, bool GD>
+__device__ __forceinline__ void PairPoint2(const float4& ga0, const float4& ga1, const float4& gb, const float4& s0,
+                                           const float4& pa0, const float4& pa1, const float4& qb, PairAcc2<DIM>& c)
+{
+    const F2 A[3] = {Pk(ga0.x, ga1.x), Pk(ga0.y, ga1.y), Pk(ga0.z, ga1.z)};
+    const F2 B[3] = {Pk(gb.x, gb.x), Pk(gb.y, gb.y), Pk(gb.z, gb.z)};
+    const float bv[3] = {gb.x, gb.y, gb.z};
+    F2 gab = Fma2(A[1], B[1], Mul2(A[0], B[0]));
+    if (DIM == 3)
+        gab = Fma2(A[2], B[2], gab);
+    const F2 sx = Pk(s0.x, s0.x);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+    {
+        const F2 lk = Mul2(sx, A[k]);
+        const float m = __fmul_rn(s0.y, bv[k]);
+        const F2 mk = Pk(m, m);
+#pragma unroll
+        for (int l = 0; l < DIM; ++l)
+            c.uu[k][l] = Fma2(mk, A[l], Fma2(lk, B[l], c.uu[k][l]));
+    }
+    c.dg = Fma2(Pk(s0.y, s0.y), gab, c.dg);
+    if (GD)
+    {
+        const F2 P[3] = {Pk(pa0.x, pa1.x), Pk(pa0.y, pa1.y), Pk(pa0.z, pa1.z)};
+        const F2 Q[3] = {Pk(qb.x, qb.x), Pk(qb.y, qb.y), Pk(qb.z, qb.z)};
+        const F2 gbw = Pk(gb.w, gb.w), nga = Pk(-ga0.w, -ga1.w);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+        {
+            c.ue[k] = Fma2(P[k], gbw, c.ue[k]);
+            c.eu[k] = Fma2(nga, Q[k], c.eu[k]);
+        }
+        const F2 t = Fma2(Pk(s0.z, s0.z), Pk(ga0.w, ga1.w), Pk(pa0.w, pa1.w));
+        c.ee = Fma2(Pk(s0.w, s0.w), gab, Fma2(t, gbw, c.ee));
+    }
 }
 
 // Everything the node-pair blocks of one integration point need, in FP32: the node gradients dN/dX, the scalars
@@ -360,7 +521,7 @@ __device__ __forceinline__ void PrepRecords(const FusedArgs& A, float4* sG, int6
             const float4 s1 = S[1], s2 = S[2], s4 = S[4];
             const float sv[6] = {s4.x, s4.y, s4.z, s4.w, s1.w, s2.w};
             const float3 pa = BtV<DIM>(ga.x, ga.y, ga.z, sv);
-            const float gs = ga.x * s1.x + ga.y * s1.y + (DIM == 3 ? ga.z * s1.z : 0.f);
+            const float gs = DotG<DIM>(ga.x, ga.y, ga.z, s1.x, s1.y, s1.z);
             S[1] = F4(pa.x, pa.y, pa.z, gs);
         }
     }
@@ -383,15 +544,8 @@ __device__ __forceinline__ void PassBlocks(const FusedArgs& A, const float4* sG,
     {
         const int cs = lane / ND, b = lane % ND;
         const int64_t kc = kp + cs;
-        float uu[DIM][DIM], ue[DIM], eu[DIM], ee = 0.f, dg = 0.f;
-#pragma unroll
-        for (int k = 0; k < DIM; ++k)
-        {
-            ue[k] = eu[k] = 0.f;
-#pragma unroll
-            for (int l = 0; l < DIM; ++l)
-                uu[k][l] = 0.f;
-        }
+        PairAcc<DIM> acc;
+        acc.zero();
         int r0 = 0, r1 = 0, r2 = 0, r3 = 0;
         bool active = false;
         if (kc < k1)
@@ -415,39 +569,23 @@ __device__ __forceinline__ void PassBlocks(const FusedArgs& A, const float4* sG,
                 const float4* SR = STAGED ? G + ND : sS + (cs * NIP + q) * 5;
                 const float4 ga = G[ia], gb = G[b];
                 const float4 s0 = SR[0];
-                const float av[3] = {ga.x, ga.y, ga.z}, bv[3] = {gb.x, gb.y, gb.z};
-                float gab = 0.f;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d)
-                    gab += av[d] * bv[d];
-                // lambda w g_a g_b^T + mu w (g_b g_a^T + (g_a . g_b) I)
-#pragma unroll
-                for (int k = 0; k < DIM; ++k)
-                {
-                    const float lk = s0.x * av[k], mk = s0.y * bv[k];
-#pragma unroll
-                    for (int l = 0; l < DIM; ++l)
-                        uu[k][l] += lk * bv[l] + mk * av[l];
-                }
-                dg += s0.y * gab;
+                float4 s1 = F4(0.f, 0.f, 0.f, 0.f), qb4 = s1;
                 if (GD)
                 {
-                    const float4 s1 = SR[1];
+                    s1 = SR[1]; // (P_a, gs_a)
                     const float4 t0 = SR[2], t1 = SR[3];
                     const float tv[6] = {t0.x, t0.y, t0.z, t1.x, t1.y, t1.z};
                     const float3 qb = BtV<DIM>(gb.x, gb.y, gb.z, tv); // B_b^T t
-                    const float pv[3] = {s1.x, s1.y, s1.z}, qv[3] = {qb.x, qb.y, qb.z};
-#pragma unroll
-                    for (int k = 0; k < DIM; ++k)
-                    {
-                        ue[k] += pv[k] * gb.w;
-                        eu[k] -= ga.w * qv[k];
-                    }
-                    ee += (s0.z * ga.w + s1.w) * gb.w + s0.w * gab;
+                    qb4 = F4(qb.x, qb.y, qb.z, 0.f);
                 }
+                PairPoint<DIM, GD>(ga, gb, s0, s1, qb4, acc);
             }
             active = true;
         }
+        float(&uu)[DIM][DIM] = acc.uu;
+        float(&ue)[DIM] = acc.ue;
+        float(&eu)[DIM] = acc.eu;
+        const float ee = acc.ee, dg = acc.dg;
         // the cells of a pass can share b: their blocks are added one cell slot after the other (the b of one
         // cell are distinct nodes, so the 8 lanes of a slot write distinct positions); fixed order, no atomics
 #pragma unroll
@@ -614,10 +752,8 @@ __global__ void __launch_bounds__(W * 32, 20 / W)
                         for (int nd = 1; nd < ND; ++nd)
                             gA[d] = nd == ia ? o.g[nd][d] : gA[d];
                     }
-                    float gs = 0.f;
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d)
-                        gs += gA[d] * o.scge[d];
+                    const float gs = DotG<DIM>(gA[0], gA[1], DIM == 3 ? gA[DIM - 1] : 0.f, o.scge[0], o.scge[1],
+                                               DIM == 3 ? o.scge[DIM - 1] : 0.f);
                     const float3 pa = BtV<DIM>(gA[0], gA[1], DIM == 3 ? gA[DIM - 1] : 0.f, o.sv);
                     S[1] = F4(pa.x, pa.y, pa.z, gs);
                     S[2] = F4(o.tv[0], o.tv[1], o.tv[2], 0.f);
@@ -837,6 +973,86 @@ struct CellSlab
     static constexpr int pad = (size + 4 + 3) / 4 * 4;        // floats per slab in shared memory (16-byte rows, banks)
 };
 
+// All node-pair blocks of one cell integrated over its points from the cell's records (rec: NIP rows of R4 float4,
+// the node gradients with N, then the scalars) and the per-(point, node) (P, gs) and Q (sPQ, gradient damage).
+// 8-node cells: lane (a, b) and (a + 4, b) in packed FP32 pairs; otherwise one block per lane. write(a, b, acc) takes
+// each finished block.
+template <int DIM, int ND, int NIP, bool GD, typename Wr>
+__device__ __forceinline__ void CellPairs(const float4* rec, int R4, const float4* sPQ, int lane, Wr&& write)
+{
+    const float4 z4 = F4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (ND == 8)
+    {
+        const int ia0 = lane / ND, ia1 = ia0 + 4, b = lane % ND;
+        PairAcc2<DIM> c2;
+        c2.zero();
+#pragma unroll 2
+        for (int q = 0; q < NIP; ++q)
+        {
+            const float4* G = rec + q * R4;
+            const float4 ga0 = G[ia0], ga1 = G[ia1], gb = G[b], s0 = G[ND];
+            float4 pa0 = z4, pa1 = z4, qb = z4;
+            if (GD)
+            {
+                pa0 = sPQ[(q * ND + ia0) * 2];
+                pa1 = sPQ[(q * ND + ia1) * 2];
+                qb = sPQ[(q * ND + b) * 2 + 1];
+            }
+            PairPoint2<DIM, GD>(ga0, ga1, gb, s0, pa0, pa1, qb, c2);
+        }
+        PairAcc<DIM> c0, c1;
+        c2.split(c0, c1);
+        write(ia0, b, c0);
+        write(ia1, b, c1);
+    }
+    else
+    {
+        for (int p = lane; p < ND * ND; p += 32)
+        {
+            const int ia = p / ND, b = p % ND;
+            PairAcc<DIM> c;
+            c.zero();
+#pragma unroll 2
+            for (int q = 0; q < NIP; ++q)
+            {
+                const float4* G = rec + q * R4;
+                const float4 ga = G[ia], gb = G[b], s0 = G[ND];
+                float4 pa = z4, qb = z4;
+                if (GD)
+                {
+                    pa = sPQ[(q * ND + ia) * 2];
+                    qb = sPQ[(q * ND + b) * 2 + 1];
+                }
+                PairPoint<DIM, GD>(ga, gb, s0, pa, qb, c);
+            }
+            write(ia, b, c);
+        }
+    }
+}
+
+// One finished block into slab a of an element matrix (slab rows of NC columns: the displacement components of b,
+// b-major, then the eeq of b)
+template <int DIM, int ND, bool GD, int NC>
+__device__ __forceinline__ void PutBlock(float* slab, int b, const PairAcc<DIM>& c)
+{
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+    {
+#pragma unroll
+        for (int l = 0; l < DIM; ++l)
+            slab[k * NC + b * DIM + l] = c.uu[k][l] + (k == l ? c.dg : 0.f);
+        if (GD)
+            slab[k * NC + ND * DIM + b] = c.ue[k];
+    }
+    if (GD)
+    {
+#pragma unroll
+        for (int l = 0; l < DIM; ++l)
+            slab[DIM * NC + b * DIM + l] = c.eu[l];
+        slab[DIM * NC + ND * DIM + b] = c.ee;
+    }
+}
+
 template <int DIM, int ND, int NIP, int KIND, int W>
 __global__ void __launch_bounds__(W * 32) k_cell_matrices(int64_t nCells, const float4* __restrict__ recs,
                                                           float* __restrict__ em)
@@ -846,8 +1062,6 @@ __global__ void __launch_bounds__(W * 32) k_cell_matrices(int64_t nCells, const 
     constexpr bool GD = Sh::GD;
     constexpr int R4 = Sh::recF4;
     constexpr int PER_CELL = NIP * R4;
-    constexpr int PAIRS = ND * ND;
-    constexpr int PPL = (PAIRS + 31) / 32; // node pairs per lane
     extern __shared__ __align__(16) float smC[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int recF = PER_CELL * 4, pqF = GD ? NIP * ND * 8 : 0, emF = ND * CS::pad;
@@ -879,82 +1093,16 @@ __global__ void __launch_bounds__(W * 32) k_cell_matrices(int64_t nCells, const 
             const float sv[6] = {s4.x, s4.y, s4.z, s4.w, s1.w, s2.w};
             const float tv[6] = {s2.x, s2.y, s2.z, s3.x, s3.y, s3.z};
             const float3 pa = BtV<DIM>(g.x, g.y, g.z, sv);
-            const float gs = g.x * s1.x + g.y * s1.y + (DIM == 3 ? g.z * s1.z : 0.f);
+            const float gs = DotG<DIM>(g.x, g.y, g.z, s1.x, s1.y, s1.z);
             const float3 qb = BtV<DIM>(g.x, g.y, g.z, tv);
             sPQ[(q * ND + nd) * 2] = F4(pa.x, pa.y, pa.z, gs);
             sPQ[(q * ND + nd) * 2 + 1] = F4(qb.x, qb.y, qb.z, 0.f);
         }
         __syncwarp();
     }
-#pragma unroll
-    for (int m = 0; m < PPL; ++m)
-    {
-        const int p = lane + 32 * m;
-        if (p >= PAIRS)
-            continue;
-        const int ia = p / ND, b = p % ND;
-        float uu[DIM][DIM], ue[DIM], eu[DIM], ee = 0.f, dg = 0.f;
-#pragma unroll
-        for (int k = 0; k < DIM; ++k)
-        {
-            ue[k] = eu[k] = 0.f;
-#pragma unroll
-            for (int l = 0; l < DIM; ++l)
-                uu[k][l] = 0.f;
-        }
-#pragma unroll 2
-        for (int q = 0; q < NIP; ++q)
-        {
-            const float4* G = sR + q * R4;
-            const float4* SR = G + ND;
-            const float4 ga = G[ia], gb = G[b];
-            const float4 s0 = SR[0];
-            const float av[3] = {ga.x, ga.y, ga.z}, bv[3] = {gb.x, gb.y, gb.z};
-            float gab = 0.f;
-#pragma unroll
-            for (int d = 0; d < DIM; ++d)
-                gab += av[d] * bv[d];
-#pragma unroll
-            for (int k = 0; k < DIM; ++k)
-            {
-                const float lk = s0.x * av[k], mk = s0.y * bv[k];
-#pragma unroll
-                for (int l = 0; l < DIM; ++l)
-                    uu[k][l] += lk * bv[l] + mk * av[l];
-            }
-            dg += s0.y * gab;
-            if (GD)
-            {
-                const float4 pa = sPQ[(q * ND + ia) * 2];
-                const float4 qb = sPQ[(q * ND + b) * 2 + 1];
-                const float pv[3] = {pa.x, pa.y, pa.z}, qv[3] = {qb.x, qb.y, qb.z};
-#pragma unroll
-                for (int k = 0; k < DIM; ++k)
-                {
-                    ue[k] += pv[k] * gb.w;
-                    eu[k] -= ga.w * qv[k];
-                }
-                ee += (s0.z * ga.w + pa.w) * gb.w + s0.w * gab;
-            }
-        }
-        float* slab = sEM + ia * CS::pad;
-#pragma unroll
-        for (int k = 0; k < DIM; ++k)
-        {
-#pragma unroll
-            for (int l = 0; l < DIM; ++l)
-                slab[k * CS::nc + b * DIM + l] = uu[k][l] + (k == l ? dg : 0.f);
-            if (GD)
-                slab[k * CS::nc + ND * DIM + b] = ue[k];
-        }
-        if (GD)
-        {
-#pragma unroll
-            for (int l = 0; l < DIM; ++l)
-                slab[DIM * CS::nc + b * DIM + l] = eu[l];
-            slab[DIM * CS::nc + ND * DIM + b] = ee;
-        }
-    }
+    CellPairs<DIM, ND, NIP, GD>(sR, R4, sPQ, lane, [&](int ia, int b, const PairAcc<DIM>& c) {
+        PutBlock<DIM, ND, GD, CS::nc>(sEM + ia * CS::pad, b, c);
+    });
     __syncwarp();
     // the element matrix, slab after slab, with 16-byte stores (slab sizes are multiples of 4 floats)
     static_assert(CS::size % 4 == 0, "slabs of whole float4");
@@ -1117,8 +1265,6 @@ __global__ void __launch_bounds__(W * 32) k_cell_matrices_law(FusedArgs A, LawPa
     using CS = CellSlab<DIM, ND, KIND>;
     constexpr bool GD = LS::GD;
     constexpr int CPW = LS::cpw, R4 = LS::R4, PER_CELL = LS::perCell;
-    constexpr int PAIRS = ND * ND;
-    constexpr int PPL = (PAIRS + 31) / 32;
     extern __shared__ __align__(16) float smL[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* sT = reinterpret_cast<float4*>(smL); // [NIP][ND]
@@ -1215,84 +1361,19 @@ __global__ void __launch_bounds__(W * 32) k_cell_matrices_law(FusedArgs A, LawPa
                 const float sv[6] = {s4.x, s4.y, s4.z, s4.w, s1.w, s2.w};
                 const float tv[6] = {s2.x, s2.y, s2.z, s3.x, s3.y, s3.z};
                 const float3 pa = BtV<DIM>(g.x, g.y, g.z, sv);
-                const float gs = g.x * s1.x + g.y * s1.y + (DIM == 3 ? g.z * s1.z : 0.f);
+                const float gs = DotG<DIM>(g.x, g.y, g.z, s1.x, s1.y, s1.z);
                 const float3 qb = BtV<DIM>(g.x, g.y, g.z, tv);
                 sPQ[(q * ND + nd) * 2] = F4(pa.x, pa.y, pa.z, gs);
                 sPQ[(q * ND + nd) * 2 + 1] = F4(qb.x, qb.y, qb.z, 0.f);
             }
             __syncwarp();
         }
-#pragma unroll
-        for (int m = 0; m < PPL; ++m)
-        {
-            const int p = lane + 32 * m;
-            if (p >= PAIRS)
-                continue;
-            const int ia = p / ND, b = p % ND;
-            float uu[DIM][DIM], ue[DIM], eu[DIM], ee = 0.f, dg = 0.f;
-#pragma unroll
-            for (int k = 0; k < DIM; ++k)
-            {
-                ue[k] = eu[k] = 0.f;
-#pragma unroll
-                for (int l = 0; l < DIM; ++l)
-                    uu[k][l] = 0.f;
-            }
-#pragma unroll 2
-            for (int q = 0; q < NIP; ++q)
-            {
-                const float4* G = rec + q * R4;
-                const float4* SR = G + ND;
-                const float4 ga = G[ia], gb = G[b];
-                const float4 s0 = SR[0];
-                const float av[3] = {ga.x, ga.y, ga.z}, bv[3] = {gb.x, gb.y, gb.z};
-                float gab = 0.f;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d)
-                    gab += av[d] * bv[d];
-#pragma unroll
-                for (int k = 0; k < DIM; ++k)
-                {
-                    const float lk = s0.x * av[k], mk = s0.y * bv[k];
-#pragma unroll
-                    for (int l = 0; l < DIM; ++l)
-                        uu[k][l] += lk * bv[l] + mk * av[l];
-                }
-                dg += s0.y * gab;
-                if (GD)
-                {
-                    const float4 pa = sPQ[(q * ND + ia) * 2];
-                    const float4 qb = sPQ[(q * ND + b) * 2 + 1];
-                    const float pv[3] = {pa.x, pa.y, pa.z}, qv[3] = {qb.x, qb.y, qb.z};
-#pragma unroll
-                    for (int k = 0; k < DIM; ++k)
-                    {
-                        ue[k] += pv[k] * gb.w;
-                        eu[k] -= ga.w * qv[k];
-                    }
-                    ee += (s0.z * ga.w + pa.w) * gb.w + s0.w * gab;
-                }
-            }
-            // straight from registers to the cell's slab in global memory (a warp's stores of one (k, l) land in
-            // four slab rows of the cell's matrix; L2 merges them into whole sectors before writing back)
-            float* slab = em + (NG_IDX(e, n, 84) * ND + ia) * CS::size;
-#pragma unroll
-            for (int k = 0; k < DIM; ++k)
-            {
-#pragma unroll
-                for (int l = 0; l < DIM; ++l)
-                    slab[k * CS::nc + b * DIM + l] = uu[k][l] + (k == l ? dg : 0.f);
-                if (GD)
-                    slab[k * CS::nc + ND * DIM + b] = ue[k];
-            }
-            if (GD)
-            {
-#pragma unroll
-                for (int l = 0; l < DIM; ++l)
-                    slab[DIM * CS::nc + b * DIM + l] = eu[l];
-                slab[DIM * CS::nc + ND * DIM + b] = ee;
-            }
-        }
+        // straight from registers to the cell's slab in global memory (a warp's stores of one (k, l) land in four
+        // slab rows of the cell's matrix; L2 merges them into whole sectors before writing back)
+        float* cellEm = em + NG_IDX(e, n, 84) * (ND * CS::size);
+        CellPairs<DIM, ND, NIP, GD>(rec, R4, sPQ, lane, [&](int ia, int b, const PairAcc<DIM>& c) {
+            PutBlock<DIM, ND, GD, CS::nc>(cellEm + ia * CS::size, b, c);
+        });
         __syncwarp(); // sPQ is rewritten for the next cell
     }
 }
