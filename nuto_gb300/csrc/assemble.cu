@@ -1254,6 +1254,7 @@ static bool RowsSupported(Ctx& c)
         }
         c.dEOf.alloc(eOf.size());
         NG_CUDA(cudaMemcpy(c.dEOf.p, eOf.data(), eOf.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        c.hEOf = eOf;
     }
     c.rowsMode = 1;
     return true;

@@ -36,6 +36,7 @@ constexpr int kFusedRowCap = 128; // values per row buffer: 32 neighbour nodes o
 struct FusedArgs
 {
     int64_t nNodes, nCells, nnz, nRows, nDofs, nNodesD, nNodesE;
+    int64_t nodeBase; // the element-matrix row gathers take nodes nodeBase .. nNodes - 1
     const int32_t* connD; // planar [n][cell]
     const int32_t* connE;
     const int64_t* gdofD; // per node: combined index of component 0
@@ -1124,7 +1125,7 @@ __global__ void __launch_bounds__(W * 32) k_rows_from_cells(FusedArgs A, const f
     constexpr int PER = (SL + 31) / 32; // slab values per lane
     __shared__ float sRowAll[W][NR * kFusedRowCap];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t a = static_cast<int64_t>(blockIdx.x) * W + wid;
+    const int64_t a = A.nodeBase + static_cast<int64_t>(blockIdx.x) * W + wid;
     if (a >= A.nNodes)
         return; // the whole warp leaves; only warp-level synchronisation follows
     float* sRow = sRowAll[wid];
@@ -1412,7 +1413,7 @@ __global__ void __launch_bounds__(W * 32) k_rows_from_cells32(FusedArgs A, const
     static_assert(CB == 2 || CB == 4 || CB == 8, "cells per batch");
     __shared__ float sRowAll[W][NR * kFusedRowCap];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t a = static_cast<int64_t>(blockIdx.x) * W + wid;
+    const int64_t a = A.nodeBase + static_cast<int64_t>(blockIdx.x) * W + wid;
     if (a >= A.nNodes)
         return; // the whole warp leaves; only warp-level synchronisation follows
     float* sRow = sRowAll[wid];
@@ -1643,7 +1644,6 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
                                 c.nCells, recs, c.dElemMats.p);
                         AfterLaunch(c, "k_cell_matrices");
                     }
-                    const unsigned rowBlocks = static_cast<unsigned>((A.nNodes + WW - 1) / WW);
                     if constexpr (CS::nc == 32 && ND == 8)
                     {
                         // packed ranks in cell-list order, once per mesh
@@ -1655,19 +1655,42 @@ void LaunchTangentFused(Ctx& c, const double* u, float* vals)
                                     A, entries, c.dPackedRanks.p);
                             AfterLaunch(c, "k_pack_ranks");
                         }
-                        // 4 cells per batch: 64 registers, 32 resident warps per SM (8 cells: 86 registers, 1.14x
-                        // slower; 2 cells: 1.02x slower, measured at 64^3)
-                        k_rows_from_cells32<DIM, ND, NIP, KIND, WW, 4><<<rowBlocks, WW * 32, 0, c.stream>>>(
-                                A, c.dPackedRanks.p, c.dElemMats.p, vals);
-                        AfterLaunch(c, "k_rows_from_cells32");
                     }
-                    else
+                    // the row gather, in node chunks when a caller hooks into them (each chunk's rows are complete
+                    // when its launch is)
+                    const int chunks = c.rowChunks > 1 && c.onRowChunk ? c.rowChunks : 1;
+                    for (int ch = 0; ch < chunks; ++ch)
                     {
-                        k_rows_from_cells<DIM, ND, NIP, KIND, WW><<<rowBlocks, WW * 32, 0, c.stream>>>(
-                                A, c.dElemMats.p, vals);
-                        AfterLaunch(c, "k_rows_from_cells");
+                        FusedArgs Ac = A;
+                        Ac.nodeBase = A.nNodes * ch / chunks;
+                        Ac.nNodes = A.nNodes * (ch + 1) / chunks;
+                        const int64_t nodes = Ac.nNodes - Ac.nodeBase;
+                        const unsigned rowBlocks = static_cast<unsigned>((nodes + WW - 1) / WW);
+                        if (rowBlocks > 0)
+                        {
+                            if constexpr (CS::nc == 32 && ND == 8)
+                            {
+                                // 4 cells per batch: 64 registers, 32 resident warps per SM (8 cells: 86 registers,
+                                // 1.14x slower; 2 cells: 1.02x slower, measured at 64^3)
+                                k_rows_from_cells32<DIM, ND, NIP, KIND, WW, 4><<<rowBlocks, WW * 32, 0, c.stream>>>(
+                                        Ac, c.dPackedRanks.p, c.dElemMats.p, vals);
+                                AfterLaunch(c, "k_rows_from_cells32");
+                            }
+                            else
+                            {
+                                k_rows_from_cells<DIM, ND, NIP, KIND, WW><<<rowBlocks, WW * 32, 0, c.stream>>>(
+                                        Ac, c.dElemMats.p, vals);
+                                AfterLaunch(c, "k_rows_from_cells");
+                            }
+                            c.stats.kernel_launches += 1;
+                        }
+                        if (chunks > 1)
+                        {
+                            c.onRowChunk(Ac.nodeBase, Ac.nNodes);
+                            c.rowChunksDone++;
+                        }
                     }
-                    c.stats.kernel_launches += 2;
+                    c.stats.kernel_launches += 1;
                     return;
                 }
                 if (staged && form == 1)

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -412,6 +413,16 @@ struct Ctx
     // nuto_gpu_build_system_host: device copies of the caller's host state, values and vector
     DBuf<double> dHostIoU, dHostIoF;
     DBuf<unsigned char> dHostIoVals;
+    // the element-matrix form's row gather in node chunks, with a hook after each chunk (nuto_gpu_build_system_host
+    // copies each chunk's values to the host while the next chunks run); 0 or 1: one launch
+    int rowChunks = 0;
+    std::function<void(int64_t, int64_t)> onRowChunk;
+    int rowChunksDone = 0;
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t evCopy = nullptr;
+    std::vector<cudaEvent_t> evChunks;
+    std::vector<int32_t> hEOf; // displacement node -> eeq node (gradient damage, row-gather set-ups)
+    int rowsContig = -1;       // -1 not checked; 1: consecutive nodes have consecutive rows (and eeq rows)
     bool noAllocReady = false; // nuto_gpu_build_matrix_noalloc: address looked up and kernels loaded
     int64_t systemCalls = 0;
     // adjoint: positions of the transposed entries, per-point partial derivatives
