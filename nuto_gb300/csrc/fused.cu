@@ -3,10 +3,17 @@
 // (nuto/mechanics/integrands/GradientDamage.h:92-120) for Quad4 and Hex8 cells, written straight into the CSR values
 // without atomics in global memory.
 //
-// One warp per displacement node a assembles the complete CSR rows of a (and of its eeq node). The cells around a
-// are taken a pass of CPP = 32 / NIP at a time; per pass the warp needs, for every point of the pass's cells, the
-// node gradients dN/dX and the law's scalars and vectors (PointData):
-//   staged (default): k_point_records evaluates PointData once per (cell, point) into per-cell contiguous records
+// Two forms, chosen by the autotuner on a context's first FP32 tangent (the values are bitwise the same):
+//
+// Element matrices (k_cell_matrices_law + k_rows_from_cells32 / k_rows_from_cells; the faster form on the 64^3
+// beam): a warp evaluates the law of 4 cells' points into shared memory and integrates every node-pair block of each
+// cell once (two blocks per lane in packed FP32 pairs), writing the cell's element matrix; then one warp per
+// displacement node adds the matrix slabs of its cells in ascending cell order into its rows and stores them once.
+//
+// Node rows: one warp per displacement node a assembles the complete CSR rows of a (and of its eeq node). The cells
+// around a are taken a pass of CPP = 32 / NIP at a time; per pass the warp needs, for every point of the pass's
+// cells, the node gradients dN/dX and the law's scalars and vectors (PointData):
+//   staged: k_point_records evaluates PointData once per (cell, point) into per-cell contiguous records
 //       (13 float4 per point for Hex8 gradient damage); the node warp copies a pass's records into shared memory
 //       with 16-byte asynchronous copies;
 //   fused (NUTO_GPU_TANGENT=fused): (0) lane (cell, node) loads the node's coordinates relative to the cell's first
@@ -14,7 +21,8 @@
 //       then evaluated by every warp whose node the cell holds, up to 8 times).
 // Then (B) lane (cell, neighbour b) integrates the node-pair block (a, b) over the points in registers and adds it
 // into the warp's shared copy of a's rows at the rank of b, one cell slot after the other (fixed order: the values
-// are bitwise reproducible). At the end the rows are stored once, coalesced.
+// are bitwise reproducible). At the end the rows are stored once, coalesced. Both forms integrate a block with the
+// same explicitly rounded operations (PairPoint, PairPoint2).
 //
 // Branch decisions of the law are the FP64 kernels' (k_residual, k_tangent<double>): the nonlocal equivalent
 // strain at a point is formed in FP32 with an error bound, and where the bound does not separate it from the
